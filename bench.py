@@ -1,0 +1,307 @@
+"""Benchmark: rays/s and solves/s of the radiation solve on one GB300.
+
+Workload (default): the orchard triangle mesh — 200 trees on a 20 x 10 grid at
+5 m, 5,000 equilateral 3 cm triangular leaves per tree in ellipsoidal crowns
+(1.0 M triangles), 3 bands (PAR rho .08 tau .05, NIR rho .45 tau .40, LW eps .96
+with leaf T ~ N(25, 2^2) C), sun at zenith 30 deg, 100 direct and 200 diffuse
+(15 x 15 = 225) rays per primitive, scattering depth 5.  Synthetic, seeded
+(seed 0).  One step = one full runBand (direct + primary diffuse + 5 scattering
+passes) over the resident scene.
+
+Arms:
+  (default)          libhrt on cuda:0; `value` = device-resident rays/s, `e2e` =
+                     rays/s through the C ABI with host buffers (geometry upload,
+                     BVH build, material upload, solve, flux download every step).
+  --impl reference   the reference algorithm on the host cores (the CPU oracle,
+                     OpenMP, all threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "rays/s and solves/s (batched/served vs plain, 1 GB300) at <=1e-4 flux err; p50/p99"
+UNIT = "rays/s"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def orchard_model(leaves_per_tree=5000, nx=20, ny=10, mode="device", device=0):
+    from helios_gb300 import scenes
+    from helios_gb300.radiation import Context, RadiationModel
+
+    sc = scenes.orchard(nx=nx, ny=ny, leaves_per_tree=leaves_per_tree, side=0.03, seed=0)
+    ctx = Context()
+    ctx.addScene(sc)
+    n = sc.n
+    rng = np.random.default_rng(0)
+    uu = np.arange(n)
+    ctx.setPrimitiveData(uu, "reflectivity_PAR", np.full(n, 0.08))
+    ctx.setPrimitiveData(uu, "transmissivity_PAR", np.full(n, 0.05))
+    ctx.setPrimitiveData(uu, "reflectivity_NIR", np.full(n, 0.45))
+    ctx.setPrimitiveData(uu, "transmissivity_NIR", np.full(n, 0.40))
+    ctx.setPrimitiveData(uu, "emissivity_LW", np.full(n, 0.96))
+    ctx.setPrimitiveData(uu, "temperature", 273.15 + rng.normal(25.0, 2.0, n))
+    rad = RadiationModel(ctx, device=device, mode=mode)
+    sun = rad.addCollimatedRadiationSource(scenes.sun_direction(30.0, 0.0))
+    for b in ("PAR", "NIR", "LW"):
+        rad.addRadiationBand(b)
+        rad.setDirectRayCount(b, 100)
+        rad.setDiffuseRayCount(b, 200)
+        rad.setScatteringDepth(b, 5)
+    rad.disableEmission("PAR")
+    rad.disableEmission("NIR")
+    rad.setSourceFlux(sun, "PAR", 500.0)
+    rad.setSourceFlux(sun, "NIR", 450.0)
+    rad.setDiffuseRadiationFlux("PAR", 50.0)
+    rad.setDiffuseRadiationFlux("NIR", 45.0)
+    rad.setDiffuseRadiationFlux("LW", 350.0)
+    return rad, sc
+
+
+BANDS = ["LW", "NIR", "PAR"]
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, nm in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def cpu_sample(rad, seconds_hint=15.0, threads=0, prim_limit=None):
+    """The CPU oracle (the reference algorithm restated, FP64, OpenMP) on the first
+    prim_limit primitives of the same workload; returns (rays/s, cores, sample text, t)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle
+    from helpers import oracle_solve
+
+    oracle.build()
+    T, ty, ts = rad.geometry_arrays()
+    sc = oracle.OracleScene(T, ty, ts)
+    desc = rad.solve_description(BANDS, seed=1)
+    cores = threads or os.cpu_count()
+    if prim_limit is None:
+        # calibrate: a small sample, then scale to ~seconds_hint
+        t0 = time.perf_counter()
+        _, st = sc.run_band(oracle_solve(desc), threads=cores, prim_limit=200)
+        dt = max(time.perf_counter() - t0, 1e-3)
+        prim_limit = int(min(T.shape[0], max(200, 200 * seconds_hint / dt)))
+    t0 = time.perf_counter()
+    _, st = sc.run_band(oracle_solve(desc), threads=cores, prim_limit=prim_limit)
+    dt = time.perf_counter() - t0
+    return st["rays"] / dt, cores, prim_limit, dt, st
+
+
+def run_reference(args):
+    rad, sc = orchard_model()
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    times, rays = [], 0
+    plim = None
+    for i in range(args.warmup + args.steps):
+        rps, cores, plim, dt, st = cpu_sample(rad, seconds_hint=args.ref_seconds, prim_limit=plim)
+        if i >= args.warmup:
+            times.append(dt)
+            rays += st["rays"]
+    val = rays / sum(times)
+    sample = (f"oracle runBand restricted to rays launched from the first {plim} of {sc.n} primitives "
+              f"(all passes, all bands), {cores} threads")
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 geometry / f64 sums",
+            "data": "synthetic (seeded)", "config": {"workload": "orchard-1M-triangles-3band", "primitives": sc.n},
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+
+    from helios_gb300 import _hrt
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    rad, sc = orchard_model(device=local)
+    stream = torch.cuda.Stream(device=local)
+    rad.ctx.set_stream(stream.cuda_stream)
+    rad.setSeed(1234 + rank)
+    t_setup = time.perf_counter()
+    rad.updateGeometry()
+    desc = rad.solve_description(BANDS)
+    ctx = rad.ctx
+    # first solve uploads materials, sources, emissivity and temperature
+    ctx.run_band(desc, out=False)
+    resident = {k: desc[k] for k in ("band_launch", "source_flux", "diffuse_flux", "diffuse_ext", "diffuse_norm",
+                                     "diffuse_peak", "prague", "direct_rays", "diffuse_rays", "depth",
+                                     "emission", "seed")}
+    resident["nsources"] = len(desc["sources"])
+    setup_s = time.perf_counter() - t_setup
+    for _ in range(args.warmup):
+        ctx.run_band(resident, out=False)
+    rays_per_step = ctx.last_stats()["rays"]
+    # traversal statistics (untimed): node visits and primitive tests per ray
+    ctx.set_measure(1)
+    ctx.run_band(resident, out=False)
+    stats = ctx.get_measure()
+    ctx.set_measure(2)  # time each trace-kernel launch in the timed region
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            ctx.run_band(resident, out=False)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    meas = ctx.get_measure()
+    ctx.set_measure(0)
+    ms_t = torch.tensor([ms], device=f"cuda:{local}")
+    if world > 1:
+        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    # end to end through the C ABI with host buffers
+    T, ty, ts = rad.geometry_arrays()
+    full = dict(desc)
+    h2d = T.nbytes + ty.nbytes + ts.nbytes + desc["rho"].nbytes + desc["tau"].nbytes + desc["eps"].nbytes + \
+        desc["temperature"].nbytes
+    d2h = sc.n * len(BANDS) * 4
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.update_geometry(T, ty, ts)
+        ctx.build_accel()
+        flux = ctx.run_band(full, out=True)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if rank != 0:
+        return
+    hbm, peak_kind = peaks()
+    # algorithmic bytes of the diffuse kernel (dominant): per ray 64 B per node visit,
+    # 48 B per primitive test, origin record 64 B, per-band gather 4 B on hits and 8 B accumulate
+    n_launch = max(stats["diffuse_launches"] + stats["direct_launches"], 1)
+    alg_bytes_total = 64.0 * stats["node_visits"] + 48.0 * stats["prim_tests"] + rays_per_step * (64 + 4 * 3)
+    diff_ms = meas["diffuse_ms"] / max(meas["diffuse_launches"], 1)
+    diff_share = meas["diffuse_ms"] / max(meas["diffuse_ms"] + meas["direct_ms"], 1e-9)
+    bytes_per_launch = alg_bytes_total / n_launch
+    achieved = bytes_per_launch / (diff_ms * 1e-3) / 1e9
+    rps = rays_per_step * world / (ms * 1e-3)
+    cpu = None
+    if not args.no_cpu:
+        crps, cores, plim, dt, st = cpu_sample(rad, seconds_hint=args.ref_seconds)
+        cpu = {"value": crps, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"CPU oracle runBand, rays launched from the first {plim} of {sc.n} primitives, {dt:.1f} s"}
+    line = {
+        "metric": METRIC, "value": rps, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 geometry / f64 sums", "data": "synthetic (seeded, seed 0)",
+        "config": {"workload": "orchard-1M-triangles-3band", "primitives": sc.n, "bands": BANDS,
+                   "direct_rays": 100, "diffuse_rays": 225, "scattering_depth": 5,
+                   "rays_per_step": rays_per_step, "solves_per_s": 1e3 / ms * world,
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "working set (BVH 64 MB + records 128 MB + buffers) larger than the 129 MB L2; no flush",
+                   "setup_s": setup_s},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_kind": peak_kind, "traffic": None, "kernel": "k_diffuse",
+                     "kernel_ms": diff_ms, "kernel_share": diff_share,
+                     "node_visits_per_ray": stats["node_visits"] / max(rays_per_step, 1),
+                     "prim_tests_per_ray": stats["prim_tests"] / max(rays_per_step, 1)},
+        "clocks": clk.summary(),
+        "e2e": {"value": rays_per_step / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s},
+        "gpu_launches": None,
+        "cpu_baseline": cpu,
+    }
+    line["gpu_launches"] = int(ctx.last_stats()["kernels"]) * args.steps
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="hrt", choices=["hrt", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ref-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

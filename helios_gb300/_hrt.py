@@ -1,0 +1,362 @@
+"""ctypes binding of libhrt's C ABI (include/hrt.h).
+
+The library is the product: there is no CPU fallback.  ``load()`` raises if
+the shared object is missing, and every call that returns a non-zero code
+raises ``HrtError`` with the context's error text.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libhrt.so")
+
+HRT_OK, HRT_EINVAL, HRT_ECUDA, HRT_ENOMEM, HRT_EDEVICE, HRT_EUNSUPPORTED = 0, -1, -2, -3, -4, -5
+
+# Every function the header declares; the CPU test suite checks they are exported.
+EXPORTS = [
+    "hrt_create", "hrt_destroy", "hrt_last_error", "hrt_set_stream", "hrt_update_geometry", "hrt_build_accel",
+    "hrt_update_materials", "hrt_update_sources", "hrt_upload_source_fluxes", "hrt_launch_direct",
+    "hrt_launch_diffuse", "hrt_get_results", "hrt_zero_radiation_buffers", "hrt_zero_scatter_buffers",
+    "hrt_copy_scatter_to_radiation", "hrt_upload_radiation_out", "hrt_query_memory", "hrt_backend_name",
+    "hrt_run_band", "hrt_last_stats", "hrt_device_status", "hrt_trace_rays", "hrt_gen_rays", "hrt_get_bvh",
+    "hrt_source_rotation", "hrt_set_measure", "hrt_get_measure",
+]
+
+
+class HrtError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"hrt error {code}: {msg}")
+        self.code = code
+
+
+class Geometry(C.Structure):
+    _fields_ = [("n", C.c_int32), ("transform", C.c_void_p), ("type", C.c_void_p), ("twosided", C.c_void_p),
+                ("nbbox", C.c_int32), ("bbox_vertices", C.c_void_p), ("periodic_x", C.c_float),
+                ("periodic_y", C.c_float)]
+
+
+class Source(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("position", C.c_float * 3), ("width", C.c_float * 2),
+                ("rotation", C.c_float * 3)]
+
+
+class Launch(C.Structure):
+    _fields_ = [("launch_offset", C.c_uint32), ("launch_count", C.c_uint32), ("rays_per_primitive", C.c_uint32),
+                ("random_seed", C.c_uint32), ("pass_id", C.c_uint32), ("nbands_global", C.c_uint32),
+                ("nbands_launch", C.c_uint32), ("band_launch_flag", C.c_void_p), ("launch_face", C.c_uint32),
+                ("diffuse_flux", C.c_void_p), ("diffuse_extinction", C.c_void_p), ("diffuse_peak_dir", C.c_void_p),
+                ("diffuse_dist_norm", C.c_void_p), ("sky_radiance_params", C.c_void_p),
+                ("radiation_out_top", C.c_void_p), ("radiation_out_bottom", C.c_void_p)]
+
+
+class BandSolve(C.Structure):
+    _fields_ = [("nbands_global", C.c_int32), ("band_launch", C.c_void_p), ("nsources", C.c_int32),
+                ("sources", C.c_void_p), ("source_flux", C.c_void_p), ("rho", C.c_void_p), ("tau", C.c_void_p),
+                ("diffuse_flux", C.c_void_p), ("diffuse_extinction", C.c_void_p), ("diffuse_peak_dir", C.c_void_p),
+                ("diffuse_dist_norm", C.c_void_p), ("sky_radiance_params", C.c_void_p),
+                ("direct_rays", C.c_void_p), ("diffuse_rays", C.c_void_p), ("scattering_depth", C.c_void_p),
+                ("emission", C.c_void_p), ("emissivity", C.c_void_p), ("temperature", C.c_void_p),
+                ("seed", C.c_uint32)]
+
+
+_lib = None
+VP = C.c_void_p
+
+
+def load(path: str | None = None):
+    """Load libhrt.so (build it first with helios_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"libhrt.so not found at {p}; run helios_gb300.build.build() (nvcc, sm_103a)")
+    lib = C.CDLL(p)
+    sig = {
+        "hrt_create": (C.c_int, [C.POINTER(VP), C.c_int]),
+        "hrt_destroy": (C.c_int, [VP]),
+        "hrt_last_error": (C.c_char_p, [VP]),
+        "hrt_set_stream": (C.c_int, [VP, VP]),
+        "hrt_update_geometry": (C.c_int, [VP, C.POINTER(Geometry)]),
+        "hrt_build_accel": (C.c_int, [VP]),
+        "hrt_update_materials": (C.c_int, [VP, C.c_int32, C.c_int32, C.c_int32, VP, VP]),
+        "hrt_update_sources": (C.c_int, [VP, C.c_int32, VP]),
+        "hrt_upload_source_fluxes": (C.c_int, [VP, VP, C.c_size_t]),
+        "hrt_launch_direct": (C.c_int, [VP, C.POINTER(Launch)]),
+        "hrt_launch_diffuse": (C.c_int, [VP, C.POINTER(Launch)]),
+        "hrt_get_results": (C.c_int, [VP, VP, VP, VP, VP, VP]),
+        "hrt_zero_radiation_buffers": (C.c_int, [VP, C.c_size_t]),
+        "hrt_zero_scatter_buffers": (C.c_int, [VP]),
+        "hrt_copy_scatter_to_radiation": (C.c_int, [VP]),
+        "hrt_upload_radiation_out": (C.c_int, [VP, VP, VP, C.c_size_t]),
+        "hrt_query_memory": (C.c_int, [VP, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+        "hrt_backend_name": (C.c_char_p, []),
+        "hrt_run_band": (C.c_int, [VP, C.POINTER(BandSolve), VP]),
+        "hrt_last_stats": (C.c_int, [VP, VP, C.c_int]),
+        "hrt_device_status": (C.c_int, [VP, C.POINTER(C.c_uint32), C.c_int]),
+        "hrt_trace_rays": (C.c_int, [VP, C.c_int64, VP, VP, C.c_float, C.c_float, C.c_int, VP, VP, VP]),
+        "hrt_gen_rays": (C.c_int, [VP, C.c_int, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, VP, VP, VP]),
+        "hrt_get_bvh": (C.c_int, [VP, VP, VP, VP]),
+        "hrt_source_rotation": (None, [VP, VP]),
+        "hrt_set_measure": (C.c_int, [VP, C.c_int]),
+        "hrt_get_measure": (C.c_int, [VP, VP, C.c_int]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def f32(a, shape=None):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a.reshape(shape) if shape is not None else a
+
+
+def source_rotation(rot) -> np.ndarray:
+    r = np.ascontiguousarray(rot, np.float32)
+    out = np.zeros(9, np.float32)
+    load().hrt_source_rotation(ptr(r), ptr(out))
+    return out
+
+
+class Context:
+    """An hrt_context: one device, one stream, device-resident scene and buffers."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.hrt_create(C.byref(h), device)
+        if rc != HRT_OK:
+            raise HrtError(rc, "hrt_create failed (no CUDA device?)")
+        self.h = h
+        self.n = 0
+        self._keep = []
+
+    def check(self, rc):
+        if rc != HRT_OK:
+            raise HrtError(rc, self.lib.hrt_last_error(self.h).decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.hrt_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int | None):
+        self.check(self.lib.hrt_set_stream(self.h, stream_handle))
+
+    # -------------------------------------------------------------- geometry
+    def update_geometry(self, T, ptype, twosided, bbox_verts=None, periodic=(0.0, 0.0)):
+        T = f32(T).reshape(-1, 16)
+        ty = np.ascontiguousarray(ptype, np.uint32)
+        ts = np.ascontiguousarray(twosided, np.int8)
+        bb = None if bbox_verts is None else f32(bbox_verts).reshape(-1, 4, 3)
+        g = Geometry(T.shape[0], ptr(T), ptr(ty), ptr(ts), 0 if bb is None else bb.shape[0], ptr(bb),
+                     float(periodic[0]), float(periodic[1]))
+        self.check(self.lib.hrt_update_geometry(self.h, C.byref(g)))
+        self.n = T.shape[0]
+
+    def build_accel(self):
+        self.check(self.lib.hrt_build_accel(self.h))
+
+    def update_materials(self, rho, tau, nsources, nbands_global):
+        rho, tau = f32(rho), f32(tau)
+        self.check(self.lib.hrt_update_materials(self.h, nsources, self.n, nbands_global, ptr(rho), ptr(tau)))
+
+    @staticmethod
+    def make_sources(sources):
+        arr = (Source * max(len(sources), 1))()
+        for i, s in enumerate(sources):
+            arr[i].type = int(s.get("type", 0))
+            for k in range(3):
+                arr[i].position[k] = float(s["position"][k])
+                arr[i].rotation[k] = float(s.get("rotation", (0, 0, 0))[k])
+            w = s.get("width", (0.0, 0.0))
+            arr[i].width[0] = float(w[0])
+            arr[i].width[1] = float(w[1])
+        return arr
+
+    def update_sources(self, sources):
+        arr = self.make_sources(sources)
+        self.check(self.lib.hrt_update_sources(self.h, len(sources), arr))
+
+    def upload_source_fluxes(self, fluxes):
+        f = f32(fluxes).ravel()
+        self.check(self.lib.hrt_upload_source_fluxes(self.h, ptr(f), f.size))
+
+    def zero_radiation_buffers(self, nb):
+        self.check(self.lib.hrt_zero_radiation_buffers(self.h, nb))
+
+    def zero_scatter_buffers(self):
+        self.check(self.lib.hrt_zero_scatter_buffers(self.h))
+
+    def copy_scatter_to_radiation(self):
+        self.check(self.lib.hrt_copy_scatter_to_radiation(self.h))
+
+    def upload_radiation_out(self, top, bottom):
+        t, b = f32(top).ravel(), f32(bottom).ravel()
+        self.check(self.lib.hrt_upload_radiation_out(self.h, ptr(t), ptr(b), t.size))
+
+    def _launch(self, p: dict) -> Launch:
+        keep = []
+
+        def a(key, dt):
+            v = p.get(key)
+            if v is None:
+                return None
+            arr = np.ascontiguousarray(v, dt).ravel()
+            keep.append(arr)
+            return ptr(arr)
+
+        L = Launch()
+        L.launch_offset = int(p.get("launch_offset", 0))
+        L.launch_count = int(p.get("launch_count", self.n))
+        L.rays_per_primitive = int(p["rays_per_primitive"])
+        L.random_seed = int(p.get("random_seed", 0)) & 0xFFFFFFFF
+        L.pass_id = int(p.get("pass_id", 0))
+        L.nbands_global = int(p["nbands_global"])
+        L.nbands_launch = int(p["nbands_launch"])
+        L.band_launch_flag = a("band_launch_flag", np.uint8)
+        L.launch_face = int(p.get("launch_face", 1))
+        L.diffuse_flux = a("diffuse_flux", np.float32)
+        L.diffuse_extinction = a("diffuse_extinction", np.float32)
+        L.diffuse_peak_dir = a("diffuse_peak_dir", np.float32)
+        L.diffuse_dist_norm = a("diffuse_dist_norm", np.float32)
+        L.sky_radiance_params = a("sky_radiance_params", np.float32)
+        L.radiation_out_top = a("radiation_out_top", np.float32)
+        L.radiation_out_bottom = a("radiation_out_bottom", np.float32)
+        self._keep = keep
+        return L
+
+    def launch_direct(self, **p):
+        L = self._launch(p)
+        self.check(self.lib.hrt_launch_direct(self.h, C.byref(L)))
+
+    def launch_diffuse(self, **p):
+        L = self._launch(p)
+        self.check(self.lib.hrt_launch_diffuse(self.h, C.byref(L)))
+
+    def get_results(self, nb):
+        m = self.n * nb
+        out = {k: np.zeros(m, np.float32) for k in ("radiation_in", "radiation_out_top", "radiation_out_bottom",
+                                                     "scatter_buff_top", "scatter_buff_bottom")}
+        self.check(self.lib.hrt_get_results(self.h, ptr(out["radiation_in"]), ptr(out["radiation_out_top"]),
+                                            ptr(out["radiation_out_bottom"]), ptr(out["scatter_buff_top"]),
+                                            ptr(out["scatter_buff_bottom"])))
+        return out
+
+    # -------------------------------------------------------------- whole solve
+    def band_solve(self, solve: dict):
+        """Build an hrt_band_solve from the same dict the oracle takes; returns (struct, keepalive)."""
+        keep = []
+
+        def a(key, dt):
+            v = solve.get(key)
+            if v is None:
+                return None
+            arr = np.ascontiguousarray(v, dt).ravel()
+            keep.append(arr)
+            return ptr(arr)
+
+        s = BandSolve()
+        bl = np.ascontiguousarray(solve["band_launch"], np.uint8)
+        keep.append(bl)
+        s.nbands_global = bl.size
+        s.band_launch = ptr(bl)
+        srcs = solve.get("sources")
+        if srcs is not None:
+            arr = self.make_sources(srcs)
+            keep.append(arr)
+            s.sources = C.cast(arr, C.c_void_p)
+            s.nsources = len(srcs)
+        else:
+            s.sources = None
+            s.nsources = int(solve.get("nsources", 0))
+        s.source_flux = a("source_flux", np.float32)
+        s.rho = a("rho", np.float32)
+        s.tau = a("tau", np.float32)
+        s.diffuse_flux = a("diffuse_flux", np.float32)
+        s.diffuse_extinction = a("diffuse_ext", np.float32)
+        s.diffuse_peak_dir = a("diffuse_peak", np.float32)
+        s.diffuse_dist_norm = a("diffuse_norm", np.float32)
+        s.sky_radiance_params = a("prague", np.float32)
+        s.direct_rays = a("direct_rays", np.int32)
+        s.diffuse_rays = a("diffuse_rays", np.int32)
+        s.scattering_depth = a("depth", np.int32)
+        s.emission = a("emission", np.uint8)
+        s.emissivity = a("eps", np.float32)
+        s.temperature = a("temperature", np.float32)
+        s.seed = int(solve.get("seed", 0)) & 0xFFFFFFFF
+        return s, keep
+
+    def run_band(self, solve: dict, out: bool = True):
+        s, keep = self.band_solve(solve)
+        bl = int(np.count_nonzero(np.asarray(solve["band_launch"])))
+        flux = np.zeros((self.n, bl), np.float32) if out else None
+        self.check(self.lib.hrt_run_band(self.h, C.byref(s), ptr(flux)))
+        return flux
+
+    def last_stats(self):
+        st = np.zeros(2, np.uint64)
+        self.check(self.lib.hrt_last_stats(self.h, ptr(st), 2))
+        return {"rays": int(st[0]), "kernels": int(st[1])}
+
+    # -------------------------------------------------------------- inspection
+    def trace_rays(self, o, d, tmin=1e-4, tmax=1e38, anyhit=False):
+        o, d = f32(o).reshape(-1, 3), f32(d).reshape(-1, 3)
+        n = o.shape[0]
+        hit = np.zeros(n, np.int32)
+        t = np.zeros(n, np.float32)
+        face = np.zeros(n, np.int32)
+        self.check(self.lib.hrt_trace_rays(self.h, n, ptr(o), ptr(d), tmin, tmax, int(anyhit), ptr(hit), ptr(t),
+                                           ptr(face)))
+        return hit, t, face
+
+    def gen_rays(self, kind, seed, pass_id, rpp, face=1, direction=(0.0, 0.0, 1.0)):
+        dimx = max(int(np.sqrt(np.float32(rpp))), 1)
+        nr = dimx * (rpp // dimx)
+        o = np.zeros((self.n * nr, 3), np.float32)
+        d = np.zeros((self.n * nr, 3), np.float32)
+        dv = f32(direction)
+        self.check(self.lib.hrt_gen_rays(self.h, kind, seed, pass_id, rpp, face, ptr(dv), ptr(o), ptr(d)))
+        return o, d
+
+    def bvh(self):
+        n = self.n
+        codes = np.zeros(n, np.uint64)
+        perm = np.zeros(n, np.uint32)
+        nodes = np.zeros((max(n - 1, 1), 16), np.uint32)
+        self.check(self.lib.hrt_get_bvh(self.h, ptr(codes), ptr(perm), ptr(nodes)))
+        return codes, perm, nodes
+
+    def set_measure(self, flags: int):
+        self.check(self.lib.hrt_set_measure(self.h, int(flags)))
+
+    def get_measure(self):
+        out = np.zeros(8, np.float64)
+        self.check(self.lib.hrt_get_measure(self.h, ptr(out), 8))
+        return {"direct_launches": int(out[0]), "direct_ms": float(out[1]), "diffuse_launches": int(out[2]),
+                "diffuse_ms": float(out[3]), "node_visits": int(out[4]), "prim_tests": int(out[5])}
+
+    def device_status(self, reset=True):
+        st = C.c_uint32()
+        self.check(self.lib.hrt_device_status(self.h, C.byref(st), int(reset)))
+        return st.value

@@ -1,0 +1,886 @@
+// hrt_api.cu -- context, C ABI (include/hrt.h) and the device-resident runBand.
+//
+// The granular entry points keep the semantics of the reference backend
+// (plugins/radiation/src/backends/OptiX8Backend.cpp): launches ACCUMULATE into
+// radiation_in / scatter buffers, zero/copy/upload calls do what their
+// RayTracingBackend virtuals document.  hrt_run_band() executes the pass
+// sequence of RadiationModel::runBand (src/RadiationModel.cpp:3470-4663)
+// without returning to the host between passes.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/hrt.h"
+#include "hrt_device.cuh"
+#include "hrt_internal.h"
+
+using namespace hrt;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = bytes ? bytes : 16;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    template <class T>
+    T *as() const {
+        return (T *)p;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    ~DevBuf() { release(); }
+};
+
+}  // namespace
+
+struct hrt_context {
+    int device = 0;
+    int sms = 152;
+    cudaStream_t own = nullptr, stream = nullptr;
+    std::string err;
+    // geometry
+    int n = 0, nbbox = 0;
+    float px = 0.f, py = 0.f;
+    bool have_geometry = false, built = false;
+    std::vector<int8_t> h_twosided;
+    DevBuf T, type, twosided, bbox, rec, rgen, nodes, codes, perm, bvh_scratch;
+    // materials and sources
+    int mS = 0, mN = 0, mB = 0;
+    DevBuf rho, tau, src, src_flux;
+    int S = 0;
+    size_t src_flux_count = 0;
+    std::vector<float> h_src_flux;
+    // radiation buffers
+    int Bl = 0;
+    DevBuf rin, stop, sbot, otop, obot, ftop, fbot, Gd, Gt, Gb, flags, sky, fin, status, counter, emis, emis_eps, emis_T;
+    size_t emis_eps_count = 0, emis_T_count = 0;
+    DevBuf io_a, io_b, io_c;  // staging for inspection calls
+    uint64_t last_rays = 0, last_kernels = 0;
+    // measurement: bit 0 counts traversal work, bit 1 times trace launches
+    int measure = 0;
+    DevBuf visits;
+    struct Timed {
+        int kind;  // 0 direct, 1 diffuse
+        cudaEvent_t a, b;
+    };
+    std::vector<Timed> timed;
+    double meas[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+namespace {
+
+int fail(hrt_context *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+#define CU(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e__ = (call);                                                                  \
+        if (e__ != cudaSuccess)                                                                    \
+            return fail(ctx, e__ == cudaErrorMemoryAllocation ? HRT_ENOMEM : HRT_ECUDA,            \
+                        std::string("CUDA error in ") + #call + ": " + cudaGetErrorString(e__));   \
+    } while (0)
+
+TraceScene scene_of(hrt_context *ctx) {
+    TraceScene sc;
+    sc.rec = ctx->rec.as<float4>();
+    sc.nodes = ctx->nodes.as<float4>();
+    sc.rgen = ctx->rgen.as<float4>();
+    sc.bbox = ctx->nbbox ? ctx->bbox.as<float4>() : nullptr;
+    sc.n = ctx->n;
+    sc.nbbox = ctx->nbbox;
+    sc.periodic_x = ctx->px;
+    sc.periodic_y = ctx->py;
+    sc.twosided = ctx->twosided.as<int8_t>();
+    sc.status = ctx->status.as<uint32_t>();
+    sc.rays = ctx->counter.as<unsigned long long>();
+    sc.visits = (ctx->measure & 1) ? ctx->visits.as<unsigned long long>() : nullptr;
+    return sc;
+}
+
+int max_blocks(hrt_context *ctx) { return ctx->sms * 8; }
+
+// Launch a trace kernel, bracketed by CUDA events when timing is on.
+template <class F>
+cudaError_t timed_launch(hrt_context *ctx, int kind, F &&launch) {
+    if (!(ctx->measure & 2)) return launch();
+    hrt_context::Timed t{kind, nullptr, nullptr};
+    cudaError_t e = cudaEventCreate(&t.a);
+    if (e == cudaSuccess) e = cudaEventCreate(&t.b);
+    if (e != cudaSuccess) return e;
+    cudaEventRecord(t.a, ctx->stream);
+    e = launch();
+    cudaEventRecord(t.b, ctx->stream);
+    ctx->timed.push_back(t);
+    return e;
+}
+
+// Fold finished timings into ctx->meas ([0] direct launches, [1] direct ms, [2] diffuse launches, [3] diffuse ms).
+void collect_timings(hrt_context *ctx) {
+    for (auto &t : ctx->timed) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(t.b) == cudaSuccess && cudaEventElapsedTime(&ms, t.a, t.b) == cudaSuccess) {
+            ctx->meas[t.kind == 0 ? 0 : 2] += 1.0;
+            ctx->meas[t.kind == 0 ? 1 : 3] += ms;
+        }
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    ctx->timed.clear();
+}
+
+// rotation about x, y, z (reference d_makeTransformMatrix, OptiX8DeviceCode.cu:191-201)
+void rotation3(const float r[3], float out[9]) {
+    double sx = std::sin((double)r[0]), cx = std::cos((double)r[0]);
+    double sy = std::sin((double)r[1]), cy = std::cos((double)r[1]);
+    double sz = std::sin((double)r[2]), cz = std::cos((double)r[2]);
+    double m[9] = {cz * cy, cz * sy * sx - sz * cx, cz * sy * cx + sz * sx,
+                   sz * cy, sz * sy * sx + cz * cx, sz * sy * cx - cz * sx,
+                   -sy,     cy * sx,                cy * cx};
+    for (int i = 0; i < 9; ++i) out[i] = (float)m[i];
+}
+
+int check_built(hrt_context *ctx) {
+    if (!ctx->built)
+        return fail(ctx, HRT_EINVAL,
+                    "No acceleration structure. Call hrt_update_geometry() and hrt_build_accel() before launching rays.");
+    return HRT_OK;
+}
+
+int sync_and_status(hrt_context *ctx) {
+    CU(cudaStreamSynchronize(ctx->stream));
+    uint32_t st = 0;
+    CU(cudaMemcpy(&st, ctx->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (st) {
+        CU(cudaMemsetAsync(ctx->status.p, 0, sizeof(uint32_t), ctx->stream));
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "device error word 0x%x (%s%s%s)", st, (st & ERR_STACK) ? "traversal stack overflow " : "",
+                      (st & ERR_WRAP) ? "periodic wrap limit " : "", (st & ERR_BOUNDS) ? "index out of range" : "");
+        return fail(ctx, HRT_EDEVICE, buf);
+    }
+    return HRT_OK;
+}
+
+// Radiation buffers for n x Bl values.
+int ensure_buffers(hrt_context *ctx, int Bl) {
+    size_t m = (size_t)std::max(ctx->n, 1) * (size_t)std::max(Bl, 1);
+    CU(ctx->rin.ensure(m * sizeof(double)));
+    CU(ctx->stop.ensure(m * sizeof(double)));
+    CU(ctx->sbot.ensure(m * sizeof(double)));
+    CU(ctx->otop.ensure(m * sizeof(float)));
+    CU(ctx->obot.ensure(m * sizeof(float)));
+    CU(ctx->ftop.ensure(m * sizeof(double)));
+    CU(ctx->fbot.ensure(m * sizeof(double)));
+    CU(ctx->Gt.ensure(m * sizeof(double)));
+    CU(ctx->Gb.ensure(m * sizeof(double)));
+    CU(ctx->fin.ensure(m * sizeof(float)));
+    return HRT_OK;
+}
+
+// Device copy of the per-launch sky parameters: [flux Bl][K Bl][norm Bl][peak 3Bl][prague 4Bl].
+int upload_sky(hrt_context *ctx, int Bl, const float *flux, const float *K, const float *norm, const float *peak,
+               const float *prague, SkyParams *sp) {
+    size_t Bn = (size_t)std::max(Bl, 1);
+    std::vector<float> h(10 * Bn, 0.f);
+    for (int b = 0; b < Bl; ++b) {
+        h[b] = flux ? flux[b] : 0.f;
+        h[Bn + b] = K ? K[b] : 0.f;
+        h[2 * Bn + b] = norm ? norm[b] : 1.f;
+        for (int k = 0; k < 3; ++k) h[3 * Bn + 3 * b + k] = peak ? peak[3 * b + k] : (k == 2 ? 1.f : 0.f);
+        for (int k = 0; k < 4; ++k) h[6 * Bn + 4 * b + k] = prague ? prague[4 * b + k] : 0.f;
+    }
+    CU(ctx->sky.ensure(h.size() * sizeof(float)));
+    CU(cudaMemcpyAsync(ctx->sky.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    float *d = ctx->sky.as<float>();
+    sp->flux = d;
+    sp->K = d + Bn;
+    sp->knorm = d + 2 * Bn;
+    sp->peak = d + 3 * Bn;
+    sp->prague = d + 6 * Bn;
+    return HRT_OK;
+}
+
+int upload_flags(hrt_context *ctx, int Bg, const uint8_t *flags) {
+    CU(ctx->flags.ensure((size_t)std::max(Bg, 1)));
+    CU(cudaMemcpyAsync(ctx->flags.p, flags, (size_t)Bg, cudaMemcpyHostToDevice, ctx->stream));
+    return HRT_OK;
+}
+
+void strata(uint32_t rpp, int *dimx, int *dimy) {
+    int dx = (int)std::sqrt((float)rpp);
+    *dimx = dx;
+    *dimy = dx > 0 ? (int)(rpp / (uint32_t)dx) : 1;
+}
+
+// Direct pass + epilogue (__raygen__direct / __miss__direct).
+int direct_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp, uint32_t seed, uint32_t pass, int Bg,
+                int Bc, int Bl) {
+    int dimx, dimy;
+    strata(rpp, &dimx, &dimy);
+    if (dimx * dimy == 0 || count == 0 || ctx->S == 0) return HRT_OK;
+    if (ctx->mS < ctx->S || ctx->mN != ctx->n)
+        return fail(ctx, HRT_EINVAL, "materials do not match the geometry/sources; call hrt_update_materials()");
+    if (ctx->src_flux_count < (size_t)ctx->S * Bl)
+        return fail(ctx, HRT_EINVAL, "source fluxes not uploaded for every source and launched band");
+    size_t ng = (size_t)ctx->n * ctx->S * 2;
+    CU(ctx->Gd.ensure(ng * sizeof(double)));
+    CU(cudaMemsetAsync(ctx->Gd.p, 0, ng * sizeof(double), ctx->stream));
+    DirectParams P;
+    P.sc = scene_of(ctx);
+    P.src = ctx->src.as<SourceDev>();
+    P.S = ctx->S;
+    P.dimx = dimx;
+    P.dimy = dimy;
+    P.seed = seed;
+    P.pass = pass;
+    P.offset = offset;
+    P.count = count;
+    P.G = ctx->Gd.as<double>();
+    CU(timed_launch(ctx, 0, [&] {
+        return (ctx->measure & 1) ? launch_direct_stats(P, max_blocks(ctx), ctx->stream)
+                                  : launch_direct(P, max_blocks(ctx), ctx->stream);
+    }));
+    EpilogueParams E{};
+    E.n = ctx->n;
+    E.Bc = Bc;
+    E.Bl = Bl;
+    E.Bg = Bg;
+    E.S = ctx->S;
+    E.flags = ctx->flags.as<uint8_t>();
+    E.rho = ctx->rho.as<float>();
+    E.tau = ctx->tau.as<float>();
+    E.rin = ctx->rin.as<double>();
+    E.stop = ctx->stop.as<double>();
+    E.sbot = ctx->sbot.as<double>();
+    E.Gd = ctx->Gd.as<double>();
+    E.src_flux = ctx->src_flux.as<float>();
+    CU(launch_epilogue_direct(E, ctx->stream));
+    ctx->last_kernels += 2;
+    return HRT_OK;
+}
+
+// Diffuse pass over one or both faces + epilogue (__raygen__diffuse, __closesthit__diffuse, __miss__diffuse).
+int diffuse_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp, uint32_t seed, uint32_t pass, int faces,
+                 int Bg, int Bc, int Bl, const SkyParams &sky) {
+    int dimx, dimy;
+    strata(rpp, &dimx, &dimy);
+    if (dimx * dimy == 0 || count == 0 || Bc == 0) return HRT_OK;
+    if (ctx->mS < 1 || ctx->mN != ctx->n)
+        return fail(ctx, HRT_EINVAL, "materials do not match the geometry; call hrt_update_materials()");
+    if (Bc > 16) return fail(ctx, HRT_EUNSUPPORTED, "at most 16 bands can be launched together");
+    size_t m = (size_t)ctx->n * Bl;
+    CU(cudaMemsetAsync(ctx->Gt.p, 0, m * sizeof(double), ctx->stream));
+    CU(cudaMemsetAsync(ctx->Gb.p, 0, m * sizeof(double), ctx->stream));
+    DiffuseParams P;
+    P.sc = scene_of(ctx);
+    P.dimx = dimx;
+    P.dimy = dimy;
+    P.seed = seed;
+    P.pass = pass;
+    P.offset = offset;
+    P.count = count;
+    P.faces = faces;
+    P.Bc = Bc;
+    P.Bl = Bl;
+    P.otop = ctx->otop.as<float>();
+    P.obot = ctx->obot.as<float>();
+    P.sky = sky;
+    P.Gt = ctx->Gt.as<double>();
+    P.Gb = ctx->Gb.as<double>();
+    CU(timed_launch(ctx, 1, [&] {
+        return (ctx->measure & 1) ? launch_diffuse_stats(P, max_blocks(ctx), ctx->stream)
+                                  : launch_diffuse(P, max_blocks(ctx), ctx->stream);
+    }));
+    EpilogueParams E{};
+    E.n = ctx->n;
+    E.Bc = Bc;
+    E.Bl = Bl;
+    E.Bg = Bg;
+    E.S = 1;
+    E.flags = ctx->flags.as<uint8_t>();
+    E.rho = ctx->rho.as<float>();
+    E.tau = ctx->tau.as<float>();
+    E.rin = ctx->rin.as<double>();
+    E.stop = ctx->stop.as<double>();
+    E.sbot = ctx->sbot.as<double>();
+    E.Gt = ctx->Gt.as<double>();
+    E.Gb = ctx->Gb.as<double>();
+    E.strength = 1.0 / (double)(dimx * dimy);
+    CU(launch_epilogue_diffuse(E, ctx->stream));
+    ctx->last_kernels += 2;
+    return HRT_OK;
+}
+
+int count_flags(int Bg, const uint8_t *f) {
+    int c = 0;
+    for (int b = 0; b < Bg; ++b) c += f[b] ? 1 : 0;
+    return c;
+}
+
+}  // namespace
+
+// ============================================================== C ABI ===
+extern "C" {
+
+const char *hrt_backend_name(void) { return "GB300 sm_103a (hrt)"; }
+
+int hrt_create(hrt_context **out, int device) {
+    if (!out) return HRT_EINVAL;
+    *out = nullptr;
+    hrt_context *ctx = new hrt_context();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return HRT_ECUDA;
+    }
+    cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return HRT_ECUDA;
+    }
+    ctx->stream = ctx->own;
+    if (ctx->status.ensure(sizeof(uint32_t)) != cudaSuccess || ctx->counter.ensure(sizeof(unsigned long long)) != cudaSuccess) {
+        cudaStreamDestroy(ctx->own);
+        delete ctx;
+        return HRT_ENOMEM;
+    }
+    cudaMemset(ctx->status.p, 0, sizeof(uint32_t));
+    cudaMemset(ctx->counter.p, 0, sizeof(unsigned long long));
+    *out = ctx;
+    return HRT_OK;
+}
+
+int hrt_destroy(hrt_context *ctx) {
+    if (!ctx) return HRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->own) cudaStreamDestroy(ctx->own);
+    delete ctx;
+    return HRT_OK;
+}
+
+const char *hrt_last_error(const hrt_context *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int hrt_set_stream(hrt_context *ctx, void *stream) {
+    if (!ctx) return HRT_EINVAL;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own;
+    return HRT_OK;
+}
+
+int hrt_update_geometry(hrt_context *ctx, const hrt_geometry *g) {
+    if (!ctx || !g) return HRT_EINVAL;
+    if (g->n < 0) return fail(ctx, HRT_EINVAL, "negative primitive count");
+    if (g->n > 0 && (!g->transform || !g->type || !g->twosided))
+        return fail(ctx, HRT_EINVAL, "null geometry array");
+    if (!(g->nbbox == 0 || g->nbbox == 2 || g->nbbox == 4) || (g->nbbox > 0 && !g->bbox_vertices))
+        return fail(ctx, HRT_EINVAL, "periodic walls must be 0, 2 or 4 quads");
+    for (int i = 0; i < g->n; ++i)
+        if (g->type[i] > 4) return fail(ctx, HRT_EUNSUPPORTED, "unsupported primitive type " + std::to_string(g->type[i]));
+    CU(cudaSetDevice(ctx->device));
+    size_t n = (size_t)g->n;
+    CU(ctx->T.ensure(std::max<size_t>(n, 1) * 16 * sizeof(float)));
+    CU(ctx->type.ensure(std::max<size_t>(n, 1) * sizeof(uint32_t)));
+    CU(ctx->twosided.ensure(std::max<size_t>(n, 1)));
+    if (n) {
+        CU(cudaMemcpyAsync(ctx->T.p, g->transform, n * 16 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        CU(cudaMemcpyAsync(ctx->type.p, g->type, n * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
+        CU(cudaMemcpyAsync(ctx->twosided.p, g->twosided, n, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    ctx->h_twosided.assign(g->twosided, g->twosided + n);
+    ctx->nbbox = g->nbbox;
+    ctx->px = g->periodic_x;
+    ctx->py = g->periodic_y;
+    if (g->nbbox) {
+        std::vector<float4> q((size_t)g->nbbox * 4);
+        for (int i = 0; i < g->nbbox * 4; ++i)
+            q[i] = make_float4(g->bbox_vertices[3 * i], g->bbox_vertices[3 * i + 1], g->bbox_vertices[3 * i + 2], 0.f);
+        CU(ctx->bbox.ensure(q.size() * sizeof(float4)));
+        CU(cudaMemcpyAsync(ctx->bbox.p, q.data(), q.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    ctx->n = g->n;
+    ctx->have_geometry = true;
+    ctx->built = false;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_build_accel(hrt_context *ctx) {
+    if (!ctx) return HRT_EINVAL;
+    if (!ctx->have_geometry) return fail(ctx, HRT_EINVAL, "hrt_update_geometry() has not been called");
+    CU(cudaSetDevice(ctx->device));
+    int n = ctx->n;
+    if (n == 0) {
+        ctx->built = true;
+        return HRT_OK;
+    }
+    size_t nn = (size_t)n, ni = (size_t)std::max(n - 1, 1);
+    CU(ctx->rec.ensure(nn * 4 * sizeof(float4)));
+    CU(ctx->rgen.ensure(nn * 4 * sizeof(float4)));
+    CU(ctx->nodes.ensure(ni * 4 * sizeof(float4)));
+    CU(ctx->codes.ensure(nn * sizeof(uint64_t)));
+    CU(ctx->perm.ensure(nn * sizeof(uint32_t)));
+    CU(ctx->bvh_scratch.ensure(bvh_scratch_bytes(n)));
+    BvhBuffers b;
+    bvh_carve(b, ctx->bvh_scratch.p, n);
+    b.rec = ctx->rec.as<float4>();
+    b.rgen = ctx->rgen.as<float4>();
+    b.nodes = ctx->nodes.as<float4>();
+    b.codes = ctx->codes.as<uint64_t>();
+    b.perm = ctx->perm.as<uint32_t>();
+    b.status = ctx->status.as<uint32_t>();
+    CU(bvh_build(ctx->T.as<float>(), ctx->type.as<uint32_t>(), n, b, ctx->stream));
+    int r = sync_and_status(ctx);
+    if (r) return r;
+    ctx->built = true;
+    return HRT_OK;
+}
+
+int hrt_update_materials(hrt_context *ctx, int32_t nsources, int32_t nprims, int32_t nbands_global, const float *rho,
+                         const float *tau) {
+    if (!ctx || nsources < 0 || nprims < 0 || nbands_global < 0) return HRT_EINVAL;
+    size_t m = (size_t)nsources * nprims * nbands_global;
+    if (m && (!rho || !tau)) return fail(ctx, HRT_EINVAL, "null material array");
+    CU(cudaSetDevice(ctx->device));
+    CU(ctx->rho.ensure(std::max<size_t>(m, 1) * sizeof(float)));
+    CU(ctx->tau.ensure(std::max<size_t>(m, 1) * sizeof(float)));
+    if (m) {
+        CU(cudaMemcpyAsync(ctx->rho.p, rho, m * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        CU(cudaMemcpyAsync(ctx->tau.p, tau, m * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    ctx->mS = nsources;
+    ctx->mN = nprims;
+    ctx->mB = nbands_global;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_update_sources(hrt_context *ctx, int32_t nsources, const hrt_source *sources) {
+    if (!ctx || nsources < 0 || (nsources > 0 && !sources)) return HRT_EINVAL;
+    if (nsources > 256) return fail(ctx, HRT_EINVAL, "A maximum of 256 radiation sources are allowed.");
+    CU(cudaSetDevice(ctx->device));
+    std::vector<SourceDev> h((size_t)std::max(nsources, 1));
+    for (int k = 0; k < nsources; ++k) {
+        if (sources[k].type > 4) return fail(ctx, HRT_EINVAL, "unknown source type");
+        SourceDev &s = h[k];
+        s.type = (int)sources[k].type;
+        for (int i = 0; i < 3; ++i) s.pos[i] = sources[k].position[i];
+        s.w0 = sources[k].width[0];
+        s.w1 = sources[k].width[1];
+        rotation3(sources[k].rotation, s.R);
+    }
+    CU(ctx->src.ensure(h.size() * sizeof(SourceDev)));
+    CU(cudaMemcpyAsync(ctx->src.p, h.data(), h.size() * sizeof(SourceDev), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->S = nsources;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_upload_source_fluxes(hrt_context *ctx, const float *fluxes, size_t count) {
+    if (!ctx || (count && !fluxes)) return HRT_EINVAL;
+    CU(cudaSetDevice(ctx->device));
+    CU(ctx->src_flux.ensure(std::max<size_t>(count, 1) * sizeof(float)));
+    if (count) CU(cudaMemcpyAsync(ctx->src_flux.p, fluxes, count * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->src_flux_count = count;
+    ctx->h_src_flux.assign(fluxes, fluxes + count);
+    CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_zero_radiation_buffers(hrt_context *ctx, size_t launch_band_count) {
+    if (!ctx) return HRT_EINVAL;
+    if (ctx->n == 0 || launch_band_count == 0) return HRT_OK;
+    if ((int)launch_band_count > ctx->mB)
+        return fail(ctx, HRT_EINVAL, "launch_band_count exceeds the band count of the materials; call hrt_update_materials() first");
+    CU(cudaSetDevice(ctx->device));
+    int r = ensure_buffers(ctx, (int)launch_band_count);
+    if (r) return r;
+    size_t m = (size_t)ctx->n * launch_band_count;
+    CU(cudaMemsetAsync(ctx->rin.p, 0, m * sizeof(double), ctx->stream));
+    CU(cudaMemsetAsync(ctx->stop.p, 0, m * sizeof(double), ctx->stream));
+    CU(cudaMemsetAsync(ctx->sbot.p, 0, m * sizeof(double), ctx->stream));
+    CU(cudaMemsetAsync(ctx->otop.p, 0, m * sizeof(float), ctx->stream));
+    CU(cudaMemsetAsync(ctx->obot.p, 0, m * sizeof(float), ctx->stream));
+    ctx->Bl = (int)launch_band_count;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_zero_scatter_buffers(hrt_context *ctx) {
+    if (!ctx) return HRT_EINVAL;
+    if (ctx->n == 0 || ctx->Bl == 0) return HRT_OK;
+    size_t m = (size_t)ctx->n * ctx->Bl;
+    CU(cudaMemsetAsync(ctx->stop.p, 0, m * sizeof(double), ctx->stream));
+    CU(cudaMemsetAsync(ctx->sbot.p, 0, m * sizeof(double), ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_copy_scatter_to_radiation(hrt_context *ctx) {
+    if (!ctx) return HRT_EINVAL;
+    if (ctx->n == 0 || ctx->Bl == 0) return HRT_OK;
+    size_t m = (size_t)ctx->n * ctx->Bl;
+    CU(launch_to_float(ctx->stop.as<double>(), ctx->otop.as<float>(), m, ctx->stream));
+    CU(launch_to_float(ctx->sbot.as<double>(), ctx->obot.as<float>(), m, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_upload_radiation_out(hrt_context *ctx, const float *top, const float *bottom, size_t count) {
+    if (!ctx) return HRT_EINVAL;
+    size_t m = (size_t)ctx->n * ctx->Bl;
+    if (count > m) return fail(ctx, HRT_EINVAL, "radiation_out larger than Nprims x Nbands_launch");
+    if (top && count) CU(cudaMemcpyAsync(ctx->otop.p, top, count * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    if (bottom && count) CU(cudaMemcpyAsync(ctx->obot.p, bottom, count * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_get_results(hrt_context *ctx, float *radiation_in, float *out_top, float *out_bottom, float *scatter_top,
+                    float *scatter_bottom) {
+    if (!ctx) return HRT_EINVAL;
+    size_t m = (size_t)ctx->n * ctx->Bl;
+    if (m == 0) return HRT_OK;
+    auto dl_double = [&](DevBuf &src, float *dst) -> int {
+        if (!dst) return HRT_OK;
+        CU(launch_to_float(src.as<double>(), ctx->fin.as<float>(), m, ctx->stream));
+        CU(cudaMemcpyAsync(dst, ctx->fin.p, m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaStreamSynchronize(ctx->stream));
+        return HRT_OK;
+    };
+    int r;
+    if ((r = dl_double(ctx->rin, radiation_in))) return r;
+    if ((r = dl_double(ctx->stop, scatter_top))) return r;
+    if ((r = dl_double(ctx->sbot, scatter_bottom))) return r;
+    if (out_top) CU(cudaMemcpyAsync(out_top, ctx->otop.p, m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    if (out_bottom) CU(cudaMemcpyAsync(out_bottom, ctx->obot.p, m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_launch_direct(hrt_context *ctx, const hrt_launch *p) {
+    if (!ctx || !p) return HRT_EINVAL;
+    int r = check_built(ctx);
+    if (r) return r;
+    if (!p->band_launch_flag) return fail(ctx, HRT_EINVAL, "null band_launch_flag");
+    if (p->launch_offset + (uint64_t)p->launch_count > (uint64_t)ctx->n)
+        return fail(ctx, HRT_EINVAL, "launch range exceeds the primitive count");
+    int Bg = (int)p->nbands_global, Bl = (int)p->nbands_launch;
+    int Bc = count_flags(Bg, p->band_launch_flag);
+    if (Bl != ctx->Bl) return fail(ctx, HRT_EINVAL, "nbands_launch differs from the last hrt_zero_radiation_buffers()");
+    if (Bg > ctx->mB) return fail(ctx, HRT_EINVAL, "nbands_global exceeds the band count of the materials");
+    if ((r = upload_flags(ctx, Bg, p->band_launch_flag))) return r;
+    CU(cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), ctx->stream));
+    if ((r = direct_pass(ctx, p->launch_offset, p->launch_count, p->rays_per_primitive, p->random_seed, p->pass_id, Bg, Bc, Bl)))
+        return r;
+    return sync_and_status(ctx);
+}
+
+int hrt_launch_diffuse(hrt_context *ctx, const hrt_launch *p) {
+    if (!ctx || !p) return HRT_EINVAL;
+    int r = check_built(ctx);
+    if (r) return r;
+    if (!p->band_launch_flag) return fail(ctx, HRT_EINVAL, "null band_launch_flag");
+    if (p->launch_offset + (uint64_t)p->launch_count > (uint64_t)ctx->n)
+        return fail(ctx, HRT_EINVAL, "launch range exceeds the primitive count");
+    int Bg = (int)p->nbands_global, Bl = (int)p->nbands_launch;
+    if (Bl != ctx->Bl) return fail(ctx, HRT_EINVAL, "nbands_launch differs from the last hrt_zero_radiation_buffers()");
+    if (Bg > ctx->mB) return fail(ctx, HRT_EINVAL, "nbands_global exceeds the band count of the materials");
+    size_t m = (size_t)ctx->n * Bl;
+    // OptiX8Backend.cpp:887-898: radiation_out is uploaded before the launch when given.
+    if (p->radiation_out_top) CU(cudaMemcpyAsync(ctx->otop.p, p->radiation_out_top, m * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    if (p->radiation_out_bottom) CU(cudaMemcpyAsync(ctx->obot.p, p->radiation_out_bottom, m * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    if (p->rays_per_primitive == 0 || p->launch_count == 0) return sync_and_status(ctx);
+    int Bc = count_flags(Bg, p->band_launch_flag);
+    if ((r = upload_flags(ctx, Bg, p->band_launch_flag))) return r;
+    SkyParams sky;
+    if ((r = upload_sky(ctx, Bl, p->diffuse_flux, p->diffuse_extinction, p->diffuse_dist_norm, p->diffuse_peak_dir,
+                        p->sky_radiance_params, &sky)))
+        return r;
+    CU(cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), ctx->stream));
+    int faces = (p->launch_face == 1) ? 1 : 2;
+    if ((r = diffuse_pass(ctx, p->launch_offset, p->launch_count, p->rays_per_primitive, p->random_seed, p->pass_id,
+                          faces, Bg, Bc, Bl, sky)))
+        return r;
+    return sync_and_status(ctx);
+}
+
+int hrt_query_memory(hrt_context *ctx, size_t *free_bytes, size_t *total_bytes) {
+    if (!ctx) return HRT_EINVAL;
+    CU(cudaSetDevice(ctx->device));
+    size_t f = 0, t = 0;
+    CU(cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
+    return HRT_OK;
+}
+
+// ------------------------------------------------------------ runBand ----
+int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
+    if (!ctx || !s) return HRT_EINVAL;
+    int r = check_built(ctx);
+    if (r) return r;
+    CU(cudaSetDevice(ctx->device));
+    const int n = ctx->n, Bg = s->nbands_global;
+    if (!s->band_launch || Bg <= 0) return fail(ctx, HRT_EINVAL, "no bands");
+    const int Bl = count_flags(Bg, s->band_launch);
+    if (Bl == 0) return fail(ctx, HRT_EINVAL, "no band is launched");
+    if (Bl > 16) return fail(ctx, HRT_EUNSUPPORTED, "at most 16 bands per runBand");
+    if (!s->direct_rays || !s->diffuse_rays || !s->scattering_depth || !s->emission || !s->diffuse_flux)
+        return fail(ctx, HRT_EINVAL, "null per-band array");
+    ctx->last_kernels = 0;
+    // materials / sources: NULL keeps what is resident on the device
+    if (s->rho || s->tau) {
+        if (!s->rho || !s->tau) return fail(ctx, HRT_EINVAL, "rho and tau must be given together");
+        if ((r = hrt_update_materials(ctx, std::max(s->nsources, 1), n, Bg, s->rho, s->tau))) return r;
+    }
+    if (s->sources) {
+        if ((r = hrt_update_sources(ctx, s->nsources, s->sources))) return r;
+    }
+    if (s->source_flux && s->nsources > 0) {
+        if ((r = hrt_upload_source_fluxes(ctx, s->source_flux, (size_t)s->nsources * Bl))) return r;
+    }
+    if (ctx->mN != n || ctx->mB < Bg || ctx->mS < 1) return fail(ctx, HRT_EINVAL, "materials do not match the scene");
+    const int S = ctx->S;
+    bool rundirect = false;
+    if (ctx->h_src_flux.size() < (size_t)S * Bl)
+        return fail(ctx, HRT_EINVAL, "source fluxes not set for every source and launched band");
+    for (size_t i = 0; i < (size_t)S * Bl; ++i) rundirect = rundirect || ctx->h_src_flux[i] > 0.f;
+    bool scattering = false, diffuse = false, emission = false;
+    int dirN = 0, difN = 0, depth = 0;
+    for (int b = 0; b < Bl; ++b) {
+        scattering = scattering || s->scattering_depth[b] > 0;
+        diffuse = diffuse || s->diffuse_flux[b] > 0.f;
+        emission = emission || s->emission[b];
+        dirN = std::max(dirN, s->direct_rays[b]);
+        difN = std::max(difN, s->diffuse_rays[b]);
+        depth = std::max(depth, s->scattering_depth[b]);
+    }
+    if ((r = ensure_buffers(ctx, Bl))) return r;
+    ctx->Bl = Bl;
+    const size_t m = (size_t)n * Bl;
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemsetAsync(ctx->rin.p, 0, m * sizeof(double), st));
+    CU(cudaMemsetAsync(ctx->stop.p, 0, m * sizeof(double), st));
+    CU(cudaMemsetAsync(ctx->sbot.p, 0, m * sizeof(double), st));
+    CU(cudaMemsetAsync(ctx->ftop.p, 0, m * sizeof(double), st));
+    CU(cudaMemsetAsync(ctx->fbot.p, 0, m * sizeof(double), st));
+    CU(cudaMemsetAsync(ctx->otop.p, 0, m * sizeof(float), st));
+    CU(cudaMemsetAsync(ctx->obot.p, 0, m * sizeof(float), st));
+    CU(cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), st));
+    std::vector<uint8_t> flags(s->band_launch, s->band_launch + Bg);
+    if ((r = upload_flags(ctx, Bg, flags.data()))) return r;
+    if (emission) {
+        // per-band flags and depths (small, every call); emissivity and temperature when given,
+        // else the arrays resident from an earlier call are used
+        if (Bl > 15) return fail(ctx, HRT_EUNSUPPORTED, "emission supports at most 15 launched bands");
+        CU(ctx->emis.ensure(128));
+        CU(cudaMemcpyAsync(ctx->emis.p, s->emission, (size_t)Bl, cudaMemcpyHostToDevice, st));
+        CU(cudaMemcpyAsync(ctx->emis.as<char>() + 64, s->scattering_depth, (size_t)Bl * 4, cudaMemcpyHostToDevice, st));
+        if (s->emissivity) {
+            CU(ctx->emis_eps.ensure(m * sizeof(float)));
+            CU(cudaMemcpyAsync(ctx->emis_eps.p, s->emissivity, m * sizeof(float), cudaMemcpyHostToDevice, st));
+            ctx->emis_eps_count = m;
+        }
+        if (s->temperature) {
+            CU(ctx->emis_T.ensure((size_t)n * sizeof(float)));
+            CU(cudaMemcpyAsync(ctx->emis_T.p, s->temperature, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, st));
+            ctx->emis_T_count = (size_t)n;
+        }
+        if (ctx->emis_eps_count != m || ctx->emis_T_count != (size_t)n)
+            return fail(ctx, HRT_EINVAL, "emission needs emissivity [n*Bl] and temperature [n]");
+    }
+    // ---- direct
+    if (S > 0 && rundirect && dirN > 0) {
+        if ((r = direct_pass(ctx, 0, (uint32_t)n, (uint32_t)dirN, s->seed, 0u, Bg, Bl, Bl))) return r;
+    }
+    // ---- scattered direct energy becomes the outgoing flux (one-sided prims fold top+bottom)
+    if (scattering && rundirect) {
+        CU(launch_fold_onesided(n, Bl, ctx->twosided.as<int8_t>(), ctx->stop.as<double>(), ctx->sbot.as<double>(),
+                                ctx->ftop.as<double>(), ctx->fbot.as<double>(), st));
+        CU(cudaMemsetAsync(ctx->stop.p, 0, m * sizeof(double), st));
+        CU(cudaMemsetAsync(ctx->sbot.p, 0, m * sizeof(double), st));
+        ctx->last_kernels += 1;
+    }
+    uint32_t rpp_d = 0;
+    {
+        double c = std::ceil(std::sqrt((double)difN));
+        rpp_d = (uint32_t)(c * c);
+    }
+    SkyParams sky;
+    if ((r = upload_sky(ctx, Bl, s->diffuse_flux, s->diffuse_extinction, s->diffuse_dist_norm, s->diffuse_peak_dir,
+                        s->sky_radiance_params, &sky)))
+        return r;
+    if (emission || diffuse) {
+        if (emission) {
+            CU(launch_emission(n, Bl, ctx->emis.as<uint8_t>(), (const int32_t *)(ctx->emis.as<char>() + 64),
+                               ctx->emis_eps.as<float>(), ctx->emis_T.as<float>(), ctx->twosided.as<int8_t>(),
+                               ctx->ftop.as<double>(), ctx->fbot.as<double>(), st));
+            ctx->last_kernels += 1;
+        }
+        CU(launch_to_float(ctx->ftop.as<double>(), ctx->otop.as<float>(), m, st));
+        CU(launch_to_float(ctx->fbot.as<double>(), ctx->obot.as<float>(), m, st));
+        ctx->last_kernels += 2;
+        if ((r = diffuse_pass(ctx, 0, (uint32_t)n, rpp_d, s->seed, 1u, 3, Bg, Bl, Bl, sky))) return r;
+    } else if (scattering && rundirect) {
+        CU(launch_to_float(ctx->ftop.as<double>(), ctx->otop.as<float>(), m, st));
+        CU(launch_to_float(ctx->fbot.as<double>(), ctx->obot.as<float>(), m, st));
+        ctx->last_kernels += 2;
+    }
+    if (scattering && (emission || diffuse) && !rundirect) {
+        CU(launch_to_float(ctx->stop.as<double>(), ctx->otop.as<float>(), m, st));
+        CU(launch_to_float(ctx->sbot.as<double>(), ctx->obot.as<float>(), m, st));
+        CU(cudaMemsetAsync(ctx->stop.p, 0, m * sizeof(double), st));
+        CU(cudaMemsetAsync(ctx->sbot.p, 0, m * sizeof(double), st));
+        ctx->last_kernels += 2;
+    }
+    if (scattering && (emission || diffuse || rundirect)) {
+        std::vector<float> zero((size_t)Bl, 0.f);
+        SkyParams sky0;
+        {
+            // zero diffuse flux for the scattering iterations (RadiationModel.cpp:4237-4240)
+            CU(cudaMemsetAsync((void *)sky.flux, 0, (size_t)Bl * sizeof(float), st));
+            sky0 = sky;
+        }
+        std::vector<uint8_t> sflags = flags;
+        for (int it = 0; it < depth; ++it) {
+            int b = -1;
+            for (int bg = 0; bg < Bg; ++bg) {
+                if (!sflags[bg]) continue;
+                ++b;
+                if (it + 1 > s->scattering_depth[b]) sflags[bg] = 0;
+            }
+            if ((r = upload_flags(ctx, Bg, sflags.data()))) return r;
+            if (it > 0 || (emission && rundirect)) {
+                CU(launch_to_float(ctx->stop.as<double>(), ctx->otop.as<float>(), m, st));
+                CU(launch_to_float(ctx->sbot.as<double>(), ctx->obot.as<float>(), m, st));
+                ctx->last_kernels += 2;
+            }
+            CU(cudaMemsetAsync(ctx->stop.p, 0, m * sizeof(double), st));
+            CU(cudaMemsetAsync(ctx->sbot.p, 0, m * sizeof(double), st));
+            int Bc = count_flags(Bg, sflags.data());
+            if ((r = diffuse_pass(ctx, 0, (uint32_t)n, rpp_d, s->seed, 2u + (uint32_t)it, 3, Bg, Bc, Bl, sky0))) return r;
+        }
+    }
+    CU(launch_final_flux(m, ctx->rin.as<double>(), ctx->stop.as<double>(), ctx->sbot.as<double>(), ctx->fin.as<float>(), st));
+    ctx->last_kernels += 1;
+    if (flux_out) CU(cudaMemcpyAsync(flux_out, ctx->fin.p, m * sizeof(float), cudaMemcpyDeviceToHost, st));
+    unsigned long long rays = 0;
+    CU(cudaMemcpyAsync(&rays, ctx->counter.p, sizeof(rays), cudaMemcpyDeviceToHost, st));
+    r = sync_and_status(ctx);
+    ctx->last_rays = rays;
+    return r;
+}
+
+int hrt_last_stats(const hrt_context *ctx, uint64_t *stats, int count) {
+    if (!ctx || !stats) return HRT_EINVAL;
+    if (count > 0) stats[0] = ctx->last_rays;
+    if (count > 1) stats[1] = ctx->last_kernels;
+    return HRT_OK;
+}
+
+int hrt_device_status(hrt_context *ctx, uint32_t *status, int reset) {
+    if (!ctx || !status) return HRT_EINVAL;
+    CU(cudaStreamSynchronize(ctx->stream));
+    CU(cudaMemcpy(status, ctx->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (reset) CU(cudaMemset(ctx->status.p, 0, sizeof(uint32_t)));
+    return HRT_OK;
+}
+
+// ------------------------------------------------------------ inspection --
+int hrt_trace_rays(hrt_context *ctx, int64_t nrays, const float *origins, const float *dirs, float tmin, float tmax,
+                   int anyhit, int32_t *hit, float *t, int32_t *face) {
+    if (!ctx || nrays < 0 || (nrays && (!origins || !dirs || !hit || !t || !face))) return HRT_EINVAL;
+    int r = check_built(ctx);
+    if (r) return r;
+    size_t nr = (size_t)nrays;
+    CU(ctx->io_a.ensure(std::max<size_t>(nr, 1) * 24));
+    CU(ctx->io_b.ensure(std::max<size_t>(nr, 1) * 12));
+    float *dO = ctx->io_a.as<float>(), *dD = dO + 3 * nr;
+    int32_t *dH = ctx->io_b.as<int32_t>();
+    float *dT = (float *)(dH + nr);
+    int32_t *dF = (int32_t *)(dT + nr);
+    CU(cudaMemcpyAsync(dO, origins, nr * 12, cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(dD, dirs, nr * 12, cudaMemcpyHostToDevice, ctx->stream));
+    CU(launch_trace_rays(scene_of(ctx), nrays, dO, dD, tmin, tmax, anyhit, dH, dT, dF, ctx->stream));
+    CU(cudaMemcpyAsync(hit, dH, nr * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaMemcpyAsync(t, dT, nr * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaMemcpyAsync(face, dF, nr * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    return sync_and_status(ctx);
+}
+
+int hrt_gen_rays(hrt_context *ctx, int kind, uint32_t seed, uint32_t pass, int32_t rpp, int32_t face,
+                 const float *direction, float *origins, float *dirs) {
+    if (!ctx || rpp < 0 || !origins || !dirs) return HRT_EINVAL;
+    int r = check_built(ctx);
+    if (r) return r;
+    int dimx, dimy;
+    strata((uint32_t)rpp, &dimx, &dimy);
+    if (dimx < 1) {
+        dimx = 1;
+        dimy = rpp;
+    }
+    size_t nr = (size_t)ctx->n * dimx * dimy;
+    CU(ctx->io_a.ensure(std::max<size_t>(nr, 1) * 24));
+    float *dO = ctx->io_a.as<float>(), *dD = dO + 3 * nr;
+    float dx = direction ? direction[0] : 0.f, dy = direction ? direction[1] : 0.f, dz = direction ? direction[2] : 1.f;
+    CU(launch_gen_rays(scene_of(ctx), kind, seed, pass, dimx, dimy, face, dx, dy, dz, dO, dD, ctx->stream));
+    CU(cudaMemcpyAsync(origins, dO, nr * 12, cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaMemcpyAsync(dirs, dD, nr * 12, cudaMemcpyDeviceToHost, ctx->stream));
+    return sync_and_status(ctx);
+}
+
+int hrt_get_bvh(hrt_context *ctx, uint64_t *codes, uint32_t *perm, uint32_t *nodes) {
+    if (!ctx) return HRT_EINVAL;
+    int r = check_built(ctx);
+    if (r) return r;
+    size_t n = (size_t)ctx->n, ni = (size_t)std::max(ctx->n - 1, 1);
+    if (n == 0) return HRT_OK;
+    if (codes) CU(cudaMemcpy(codes, ctx->codes.p, n * 8, cudaMemcpyDeviceToHost));
+    if (perm) CU(cudaMemcpy(perm, ctx->perm.p, n * 4, cudaMemcpyDeviceToHost));
+    if (nodes) CU(cudaMemcpy(nodes, ctx->nodes.p, ni * 64, cudaMemcpyDeviceToHost));
+    return HRT_OK;
+}
+
+void hrt_source_rotation(const float rotation[3], float out[9]) { rotation3(rotation, out); }
+
+int hrt_set_measure(hrt_context *ctx, int flags) {
+    if (!ctx) return HRT_EINVAL;
+    CU(cudaSetDevice(ctx->device));
+    CU(ctx->visits.ensure(2 * sizeof(unsigned long long)));
+    CU(cudaStreamSynchronize(ctx->stream));
+    collect_timings(ctx);
+    CU(cudaMemset(ctx->visits.p, 0, 2 * sizeof(unsigned long long)));
+    for (double &m : ctx->meas) m = 0.0;
+    ctx->measure = flags;
+    return HRT_OK;
+}
+
+int hrt_get_measure(hrt_context *ctx, double *out, int count) {
+    if (!ctx || !out) return HRT_EINVAL;
+    CU(cudaStreamSynchronize(ctx->stream));
+    collect_timings(ctx);
+    unsigned long long v[2] = {0, 0};
+    if (ctx->visits.p) CU(cudaMemcpy(v, ctx->visits.p, sizeof v, cudaMemcpyDeviceToHost));
+    ctx->meas[4] = (double)v[0];
+    ctx->meas[5] = (double)v[1];
+    for (int i = 0; i < count && i < 8; ++i) out[i] = ctx->meas[i];
+    return HRT_OK;
+}
+
+}  // extern "C"

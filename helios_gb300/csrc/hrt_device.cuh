@@ -1,0 +1,359 @@
+// hrt_device.cuh -- device-side building blocks of the GB300 radiation engine.
+//
+// Arithmetic contract: all FP32 geometry (ray generation, primitive records,
+// bounding boxes, Morton codes, slab and primitive tests) is written as plain
+// IEEE-754 single-precision +, -, *, / and sqrt sequences and this library is
+// compiled with --fmad=false (no contraction), -prec-div=true and
+// -prec-sqrt=true.  The same sequences evaluated on the host give bit-identical
+// results, which is what lets the device LBVH be checked bit-for-bit against a
+// host build and lets hit IDs be compared exactly.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hrt {
+
+// Primitive type codes (RayTracingTypes.h:45 of the reference radiation plugin).
+enum : uint32_t { PT_PATCH = 0, PT_TRI = 1, PT_DISK = 2, PT_TILE = 3, PT_VOXEL = 4, PT_BBOX = 5 };
+
+// Error bits of the per-context device status word.
+enum : uint32_t { ERR_STACK = 1u, ERR_WRAP = 2u, ERR_TIMEOUT = 4u, ERR_BOUNDS = 8u };
+
+constexpr int kStack = 64;           // traversal stack entries per ray
+constexpr int32_t kEmptyChild = ~0x7FFFFFFF;
+
+struct f3 {
+    float x, y, z;
+};
+__host__ __device__ __forceinline__ f3 mk(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 sub(f3 a, f3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ f3 add(f3 a, f3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ f3 scl(f3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ f3 normalize(f3 a) {
+    float l = sqrtf(dot(a, a));
+    return mk(a.x / l, a.y / l, a.z / l);
+}
+__device__ __forceinline__ float get(f3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+__device__ __forceinline__ f3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
+
+// T . (px, py, 0, 1) for a row-major 4x4 transform.
+__device__ __forceinline__ f3 xform(const float *T, float px, float py) {
+    return mk((T[0] * px + T[1] * py) + T[3], (T[4] * px + T[5] * py) + T[7],
+              (T[8] * px + T[9] * py) + T[11]);
+}
+
+// ------------------------------------------------------------------ Philox ---
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
+struct u4 {
+    uint32_t a, b, c, d;
+};
+__device__ __forceinline__ u4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                     uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+    }
+    return u4{c0, c1, c2, c3};
+}
+__device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+// cos(2*pi*u), sin(2*pi*u) for u in [0,1): reduction to [0, pi/4] and Taylor
+// polynomials (coefficients 1/k!) evaluated in a fixed order.
+__device__ __forceinline__ void sincos2pi(float u, float *c_out, float *s_out) {
+    float x = u * 4.0f;
+    int q = (int)x;
+    float f = x - (float)q;
+    bool swap = f > 0.5f;
+    float g = swap ? (1.0f - f) : f;
+    float a = g * 1.57079632679489662f;
+    float a2 = a * a;
+    float s = a + a * a2 * (-1.66666666666666667e-1f +
+                            a2 * (8.33333333333333333e-3f +
+                                  a2 * (-1.98412698412698413e-4f + a2 * 2.75573192239858907e-6f)));
+    float c = 1.0f + a2 * (-0.5f + a2 * (4.16666666666666667e-2f +
+                                         a2 * (-1.38888888888888889e-3f +
+                                               a2 * (2.48015873015873016e-5f +
+                                                     a2 * -2.75573192239858907e-7f))));
+    float c0 = swap ? s : c;
+    float s0 = swap ? c : s;
+    q &= 3;
+    if (q == 0) {
+        *c_out = c0;
+        *s_out = s0;
+    } else if (q == 1) {
+        *c_out = -s0;
+        *s_out = c0;
+    } else if (q == 2) {
+        *c_out = -c0;
+        *s_out = -s0;
+    } else {
+        *c_out = s0;
+        *s_out = -c0;
+    }
+}
+
+// Orthonormal basis about unit n (Duff et al., JCGT 6(1), 2017).
+__device__ __forceinline__ void onb(f3 n, f3 *t1, f3 *t2) {
+    float sign = copysignf(1.0f, n.z);
+    float a = -1.0f / (sign + n.z);
+    float b = n.x * n.y * a;
+    *t1 = mk(1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+    *t2 = mk(b, sign + n.y * n.y * a, -n.y);
+}
+
+// Cosine-weighted stratified direction about n (stratum (ti, pi) of dimx x dimy).
+__device__ __forceinline__ f3 diffuse_dir(f3 n, int ti, int pi, int dimx, int dimy, float j0, float j1) {
+    float Rt = ((float)ti + j0) / (float)dimx;
+    float Rp = ((float)pi + j1) / (float)dimy;
+    float st = sqrtf(Rt);
+    float ct = sqrtf(1.0f - Rt);
+    float cp, sp;
+    sincos2pi(Rp, &cp, &sp);
+    float lx = st * cp, ly = st * sp;
+    f3 t1, t2;
+    onb(n, &t1, &t2);
+    return mk((t1.x * lx + t2.x * ly) + n.x * ct, (t1.y * lx + t2.y * ly) + n.y * ct,
+              (t1.z * lx + t2.z * ly) + n.z * ct);
+}
+
+// ------------------------------------------------------------------ records ---
+// Intersection record (64 B, BVH leaf order):
+//   r0 = (p0.xyz, type bits)  r1 = (p1.xyz, original index bits)
+//   r2 = (p2.xyz, 0)          r3 = (p3.xyz, 0)
+// patch/bbox: 4 corners; triangle: v0,v1,v2 (r3 = v2); disk: centre, unit normal, (radius,0,0);
+// voxel: lo, hi.
+// Ray-origin record (64 B, original order):
+//   g0 = (P.xyz, type bits) g1 = (A.xyz, twosided bits) g2 = (B.xyz, 0) g3 = (N.xyz, 0)
+// with sample point P + u*A + v*B and unit normal N.
+
+__device__ __forceinline__ void make_records(const float *T, uint32_t type, float4 rec[4], float4 g[4],
+                                             f3 *lo, f3 *hi) {
+    f3 p0, p1, p2, p3;
+    uint32_t rt = type;
+    if (type == PT_TRI) {
+        p0 = xform(T, 0.f, 0.f);
+        p1 = xform(T, 0.f, 1.f);
+        p2 = xform(T, 1.f, 1.f);
+        p3 = p2;
+    } else if (type == PT_DISK) {
+        p0 = xform(T, 0.f, 0.f);
+        f3 ax = mk(T[0], T[4], T[8]), ay = mk(T[1], T[5], T[9]);
+        p1 = normalize(cross(ax, ay));
+        p2 = mk(sqrtf(dot(ax, ax)), 0.f, 0.f);
+        p3 = p0;
+    } else if (type == PT_VOXEL) {
+        f3 c = mk(T[3], T[7], T[11]);
+        f3 h = mk(fabsf(T[0]) * 0.5f, fabsf(T[5]) * 0.5f, fabsf(T[10]) * 0.5f);
+        p0 = sub(c, h);
+        p1 = add(c, h);
+        p2 = p0;
+        p3 = p1;
+    } else {
+        rt = PT_PATCH;
+        p0 = xform(T, -0.5f, -0.5f);
+        p1 = xform(T, 0.5f, -0.5f);
+        p2 = xform(T, 0.5f, 0.5f);
+        p3 = xform(T, -0.5f, 0.5f);
+    }
+    rec[0] = make_float4(p0.x, p0.y, p0.z, __uint_as_float(rt));
+    rec[1] = make_float4(p1.x, p1.y, p1.z, 0.f);
+    rec[2] = make_float4(p2.x, p2.y, p2.z, 0.f);
+    rec[3] = make_float4(p3.x, p3.y, p3.z, 0.f);
+    // bounds
+    if (rt == PT_DISK) {
+        float rad = p2.x;
+        f3 n = p1;
+        float ex = rad * sqrtf(fmaxf(0.f, 1.0f - n.x * n.x));
+        float ey = rad * sqrtf(fmaxf(0.f, 1.0f - n.y * n.y));
+        float ez = rad * sqrtf(fmaxf(0.f, 1.0f - n.z * n.z));
+        *lo = mk(p0.x - ex, p0.y - ey, p0.z - ez);
+        *hi = mk(p0.x + ex, p0.y + ey, p0.z + ez);
+    } else {
+        f3 v[4] = {p0, p1, p2, p3};
+        int nv = (rt == PT_TRI) ? 3 : (rt == PT_VOXEL ? 2 : 4);
+        f3 a = v[0], b = v[0];
+        for (int i = 1; i < nv; ++i) {
+            a = mk(fminf(a.x, v[i].x), fminf(a.y, v[i].y), fminf(a.z, v[i].z));
+            b = mk(fmaxf(b.x, v[i].x), fmaxf(b.y, v[i].y), fmaxf(b.z, v[i].z));
+        }
+        *lo = a;
+        *hi = b;
+    }
+    // origin-sampling record
+    f3 A = mk(T[0], T[4], T[8]), B = mk(T[1], T[5], T[9]), P, N;
+    if (type == PT_TRI) {
+        P = mk(T[3], T[7], T[11]);
+        N = normalize(cross(B, A));
+    } else {
+        P = xform(T, -0.5f, -0.5f);
+        N = normalize(cross(A, B));
+    }
+    g[0] = make_float4(P.x, P.y, P.z, __uint_as_float(type));
+    g[1] = make_float4(A.x, A.y, A.z, 0.f);
+    g[2] = make_float4(B.x, B.y, B.z, 0.f);
+    g[3] = make_float4(N.x, N.y, N.z, 0.f);
+}
+
+__device__ __forceinline__ f3 sample_point(const float4 g[4], uint32_t type, float u, float v) {
+    f3 P = xyz(g[0]), A = xyz(g[1]), B = xyz(g[2]);
+    if (type == PT_TRI) {
+        float a = u < v ? u : v, b = u < v ? v : u;
+        return mk((P.x + a * A.x) + b * B.x, (P.y + a * A.y) + b * B.y, (P.z + a * A.z) + b * B.z);
+    }
+    return mk((P.x + u * A.x) + v * B.x, (P.y + u * A.y) + v * B.y, (P.z + u * A.z) + v * B.z);
+}
+
+// Leaf-box padding: each face moves out by (|x| + extent) * 2^-20.
+__device__ __forceinline__ float pad_lo(float x, float ext) { return x - (fabsf(x) + ext) * 9.5367431640625e-07f; }
+__device__ __forceinline__ float pad_hi(float x, float ext) { return x + (fabsf(x) + ext) * 9.5367431640625e-07f; }
+
+// ------------------------------------------------------------------ tests ---
+struct WT {
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+__device__ __forceinline__ WT wt_setup(f3 d) {
+    WT w;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    w.kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
+    w.kx = (w.kz == 2) ? 0 : w.kz + 1;
+    w.ky = (w.kx == 2) ? 0 : w.kx + 1;
+    float dz = get(d, w.kz);
+    if (dz < 0.f) {
+        int t = w.kx;
+        w.kx = w.ky;
+        w.ky = t;
+    }
+    w.Sx = get(d, w.kx) / dz;
+    w.Sy = get(d, w.ky) / dz;
+    w.Sz = 1.0f / dz;
+    return w;
+}
+
+__device__ __forceinline__ float edgef(float px, float py, float qx, float qy) {
+    float e = px * qy - py * qx;
+    if (e == 0.f) e = (float)((double)px * (double)qy - (double)py * (double)qx);
+    return e;
+}
+
+// Watertight polygon test (Woop, Benthin, Wald, JCGT 2(1), 2013) for triangles (n=3)
+// and planar convex quads (n=4).  face = 1 when dot(d, n) < 0.
+template <int NV>
+__device__ __forceinline__ bool poly_hit(const WT &w, f3 o, float tmin, const f3 *v, float tmax, float *t_out,
+                                         int *face_out) {
+    float px[NV], py[NV], pz[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        f3 a = sub(v[i], o);
+        float az = get(a, w.kz);
+        px[i] = get(a, w.kx) - w.Sx * az;
+        py[i] = get(a, w.ky) - w.Sy * az;
+        pz[i] = w.Sz * az;
+    }
+    float e[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        int j = (i + 1 == NV) ? 0 : i + 1;
+        e[i] = edgef(px[i], py[i], px[j], py[j]);
+    }
+    bool anyneg = false, anypos = false;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        anyneg = anyneg || (e[i] < 0.f);
+        anypos = anypos || (e[i] > 0.f);
+    }
+    if (anyneg && anypos) return false;
+    float e20 = (NV == 3) ? e[NV - 1] : edgef(px[2], py[2], px[0], py[0]);
+    float det = (e[1] + e20) + e[0];
+    if (det == 0.f) return false;
+    float T = (e[1] * pz[0] + e20 * pz[1]) + e[0] * pz[2];
+    float t = T / det;
+    if (!(t >= tmin) || !(t <= tmax)) return false;
+    *t_out = t;
+    // det < 0 <=> dot(d, n) < 0 for n = (v1-v0) x (v2-v0): the ray meets the top face
+    *face_out = (det < 0.f) ? 1 : 0;
+    return true;
+}
+
+__device__ __forceinline__ float safe_inv(float d) {
+    if (fabsf(d) < 1e-30f) d = copysignf(1e-30f, d);
+    return 1.0f / d;
+}
+
+__device__ __forceinline__ bool slab(f3 o, f3 inv, f3 lo, f3 hi, float tmin, float tmax, float *tnear) {
+    float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
+    float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
+    float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
+    float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+    float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax));
+    *tnear = tn;
+    return tn <= tf;
+}
+
+// Disk: plane hit inside the radius (reference OptiX 6 primitiveIntersection.cu:236-300).
+__device__ __forceinline__ bool disk_hit(f3 o, f3 d, float tmin, f3 c, f3 n, float rad, float tmax, float *t_out,
+                                         int *face_out) {
+    float nd = dot(d, n);
+    if (nd == 0.f) return false;
+    float t = dot(sub(c, o), n) / nd;
+    if (!(t >= tmin) || !(t <= tmax)) return false;
+    f3 h = sub(add(o, scl(d, t)), c);
+    if (dot(h, h) > rad * rad) return false;
+    *t_out = t;
+    *face_out = (nd < 0.f) ? 1 : 0;
+    return true;
+}
+
+// Voxel: no hit when the origin is inside (reference OptiX 6 primitiveIntersection.cu:330-374).
+__device__ __forceinline__ bool voxel_hit(f3 o, f3 inv, float tmin, f3 lo, f3 hi, float tmax, float *t_out,
+                                          int *face_out) {
+    if (o.x >= lo.x && o.x <= hi.x && o.y >= lo.y && o.y <= hi.y && o.z >= lo.z && o.z <= hi.z) return false;
+    float tn;
+    if (!slab(o, inv, lo, hi, tmin, tmax, &tn)) return false;
+    if (!(tn > 1e-5f)) return false;
+    *t_out = tn;
+    *face_out = 1;
+    return true;
+}
+
+// Test record `slot`; on success returns t, face and the original primitive index.
+__device__ __forceinline__ bool rec_hit(const float4 *__restrict__ rec, uint32_t slot, const WT &w, f3 o, f3 d,
+                                        f3 inv, float tmin, float tmax, float *t, int *face, uint32_t *orig) {
+    const float4 *r = rec + 4 * (size_t)slot;
+    float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2);
+    uint32_t type = __float_as_uint(r0.w);
+    *orig = __float_as_uint(r1.w);
+    bool ok;
+    if (type == PT_TRI) {
+        f3 v[3] = {xyz(r0), xyz(r1), xyz(r2)};
+        ok = poly_hit<3>(w, o, tmin, v, tmax, t, face);
+    } else if (type == PT_PATCH) {
+        float4 r3 = __ldg(r + 3);
+        f3 v[4] = {xyz(r0), xyz(r1), xyz(r2), xyz(r3)};
+        ok = poly_hit<4>(w, o, tmin, v, tmax, t, face);
+    } else if (type == PT_DISK) {
+        ok = disk_hit(o, d, tmin, xyz(r0), xyz(r1), r2.x, tmax, t, face);
+    } else if (type == PT_VOXEL) {
+        ok = voxel_hit(o, inv, tmin, xyz(r0), xyz(r1), tmax, t, face);
+    } else {
+        ok = false;
+    }
+    return ok;
+}
+
+}  // namespace hrt

@@ -1,0 +1,128 @@
+// hrt_internal.h -- structures shared by the CUDA translation units of libhrt.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hrt {
+
+// Scene as the trace kernels see it.
+struct TraceScene {
+    const float4 *rec;    // [n*4] intersection records, BVH leaf order
+    const float4 *nodes;  // [max(n-1,1)*4] BVH2 nodes
+    const float4 *rgen;   // [n*4] ray-origin records, original order
+    const float4 *bbox;   // [nbbox*4] periodic wall corners (xyz, w unused)
+    int n;
+    int nbbox;
+    float periodic_x, periodic_y;
+    const int8_t *twosided; // [n] two-sided flags
+    uint32_t *status;     // device error word (ERR_* bits)
+    unsigned long long *rays; // traced-ray counter
+    unsigned long long *visits; // [2] node visits, primitive tests (statistics launches only)
+};
+
+// Radiation source in device form (rotation pre-expanded to a 3x3 matrix on the host).
+struct SourceDev {
+    int type;             // 0 collimated, 1 sphere, 2 sun sphere, 3 rectangle, 4 disk
+    float pos[3];
+    float w0, w1;
+    float R[9];
+};
+
+struct DirectParams {
+    TraceScene sc;
+    const SourceDev *src;
+    int S;
+    int dimx, dimy;
+    uint32_t seed, pass;
+    uint32_t offset, count;   // primitive range
+    double *G;                // [n*S*2] sums of strength of unoccluded rays, [p][s][face]
+};
+
+struct SkyParams {
+    const float *flux;     // [Bc] diffuse flux per compacted band
+    const float *K;        // [Bc] power-law exponent (0 = off)
+    const float *knorm;    // [Bc]
+    const float *peak;     // [Bc*3]
+    const float *prague;   // [Bc*4]
+};
+
+struct DiffuseParams {
+    TraceScene sc;
+    int dimx, dimy;
+    uint32_t seed, pass;
+    uint32_t offset, count;
+    int faces;                // bit 0: launch top face (1), bit 1: launch bottom face (0)
+    int Bc;                   // compacted (launched) band count
+    int Bl;                   // buffer stride
+    const float *otop, *obot; // radiation_out [n*Bl]
+    SkyParams sky;
+    double *Gt, *Gb;          // [n*Bl] sums of incoming values per origin face
+};
+
+// ---------------------------------------------------------------- BVH build
+struct BvhBuffers {
+    float4 *rec;        // out: sorted records [n*4]
+    float4 *rgen;       // out: origin records [n*4]
+    float4 *nodes;      // out: packed nodes [max(n-1,1)*4]
+    uint64_t *codes;    // out: sorted Morton codes [n]
+    uint32_t *perm;     // out: sorted slot -> original index [n]
+    // scratch
+    float4 *rec_tmp;    // [n*4]
+    float *aabb;        // [n*6]
+    float *leafbox;     // [n*6]
+    float *nodebox;     // [(n-1)*6]
+    float *bounds;      // [16]
+    float *partial;     // [nparts*12]
+    uint64_t *keys_alt; // [n]
+    uint32_t *vals_alt; // [n]
+    uint32_t *hist;     // [256*nblk]
+    uint32_t *offs;     // [256*nblk]
+    uint32_t *scan_tmp; // [scan scratch]
+    int32_t *child;     // [2*(n-1)]
+    int32_t *parent_int;// [n-1]
+    int32_t *parent_leaf;// [n]
+    uint32_t *flags;    // [n-1]
+    uint32_t *status;   // device error word
+};
+size_t bvh_scratch_bytes(int n);
+void bvh_carve(BvhBuffers &b, void *scratch, int n);
+cudaError_t bvh_build(const float *T, const uint32_t *type, int n, BvhBuffers &b, cudaStream_t s);
+constexpr int kSortTile = 2048;
+
+// ---------------------------------------------------------------- passes
+cudaError_t launch_direct(const DirectParams &p, int max_blocks, cudaStream_t s);
+cudaError_t launch_diffuse(const DiffuseParams &p, int max_blocks, cudaStream_t s);
+// Same launches with per-ray node-visit / primitive-test counting into sc.visits.
+cudaError_t launch_direct_stats(const DirectParams &p, int max_blocks, cudaStream_t s);
+cudaError_t launch_diffuse_stats(const DiffuseParams &p, int max_blocks, cudaStream_t s);
+cudaError_t launch_trace_rays(const TraceScene &sc, int64_t nrays, const float *o, const float *d, float tmin,
+                              float tmax, int anyhit, int32_t *hit, float *t, int32_t *face, cudaStream_t s);
+cudaError_t launch_gen_rays(const TraceScene &sc, int kind, uint32_t seed, uint32_t pass, int dimx, int dimy,
+                            int face, float dx, float dy, float dz, float *o, float *d, cudaStream_t s);
+
+// Epilogues: fold per-face sums into radiation_in / scatter buffers.
+struct EpilogueParams {
+    int n, Bc, Bl, Bg, S, nsrc_mat;
+    const uint8_t *flags;      // [Bg] band flags of this launch (device)
+    const float *rho, *tau;    // [Smat*n*Bg]
+    double *rin, *stop, *sbot; // [n*Bl]
+    const double *Gt, *Gb;     // diffuse: [n*Bl]
+    const double *Gd;          // direct: [n*S*2]
+    const float *src_flux;     // direct: [S*Bl]
+    double strength;           // diffuse: 1/(dimx*dimy)
+};
+cudaError_t launch_epilogue_direct(const EpilogueParams &p, cudaStream_t s);
+cudaError_t launch_epilogue_diffuse(const EpilogueParams &p, cudaStream_t s);
+
+// Buffer bookkeeping (OptiX8Backend.cpp:1168-1250 semantics).
+cudaError_t launch_to_float(const double *a, float *out, size_t n, cudaStream_t s);
+cudaError_t launch_fold_onesided(int n, int Bl, const int8_t *twosided, const double *stop, const double *sbot,
+                                 double *ftop, double *fbot, cudaStream_t s);
+cudaError_t launch_emission(int n, int Bl, const uint8_t *emission, const int32_t *depth, const float *eps,
+                            const float *temperature, const int8_t *twosided, double *ftop, double *fbot,
+                            cudaStream_t s);
+cudaError_t launch_final_flux(size_t nb, const double *rin, const double *stop, const double *sbot, float *out,
+                              cudaStream_t s);
+
+}  // namespace hrt

@@ -1,0 +1,592 @@
+"""Host-side mirror of the reference radiation plugin's user API over libhrt.
+
+``Context`` holds the part of ``helios::Context`` the radiation solve reads
+(primitive transforms, types, two-sided flags, primitive and global data);
+``RadiationModel`` keeps the method names, argument meaning, defaults and error
+behaviour of ``helios::RadiationModel`` (plugins/radiation/include/RadiationModel.h)
+for the radiation path: bands, sources, ray counts, scattering depth,
+``updateGeometry`` and ``runBand``, whose results land in the primitive data
+``radiation_flux_<band>``.
+
+``runBand`` has two execution modes:
+  * ``"device"`` (default): one ``hrt_run_band`` call, all passes on the GPU;
+  * ``"backend"``: the pass sequence of ``RadiationModel::runBand``
+    (src/RadiationModel.cpp:3470-4663) issued call by call through the
+    RayTracingBackend-shaped entry points (launchDirectRays, getRadiationResults,
+    uploadRadiationOut, ...), exactly as the reference drives a backend.
+Both give the same numbers for the same seed.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _hrt, scenes
+
+SIGMA = 5.6703744e-8  # RadiationModel.h:2210
+
+
+class HeliosRuntimeError(RuntimeError):
+    """Raised where the reference calls helios_runtime_error (core/include/global.h:102)."""
+
+
+class Context:
+    """Primitive store: transforms, types, two-sided flags, primitive data."""
+
+    def __init__(self):
+        self._chunks = []  # (T [k,16] float32, type [k] uint32, area [k] float64)
+        self._n = 0
+        self._cache = None
+        self.primitive_data: dict[str, dict[int, object]] = {}
+        self.bulk_data: dict[str, np.ndarray] = {}
+        self.global_data: dict[str, object] = {}
+
+    # --------------------------------------------------------------- geometry
+    def _add_many(self, T, ptype, area):
+        T = np.asarray(T, np.float32).reshape(-1, 16)
+        k = T.shape[0]
+        self._chunks.append((T, np.broadcast_to(np.asarray(ptype, np.uint32), (k,)).copy(),
+                             np.broadcast_to(np.asarray(area, np.float64), (k,)).copy()))
+        first = self._n
+        self._n += k
+        self._cache = None
+        return first
+
+    def _add(self, T, ptype, area):
+        return self._add_many(T, ptype, area)
+
+    def addPatch(self, center=(0, 0, 0), size=(1, 1), rotation=(0.0, 0.0)):
+        """rotation = (elevation, azimuth) radians, as SphericalCoord(1, elevation, azimuth)."""
+        if size[0] < 1e-6 or size[1] < 1e-6:
+            raise HeliosRuntimeError("ERROR (Context::addPatch): Size of patch must be greater than 1e-6 "
+                                     "to avoid numerical precision issues.")
+        T = scenes.helios_patch_T(center, size, rotation[0], rotation[1])
+        return self._add(T, scenes.PATCH, size[0] * size[1])
+
+    def addTriangle(self, v0, v1, v2):
+        T = scenes.triangle_T(v0, v1, v2)[0]
+        a = 0.5 * np.linalg.norm(np.cross(np.subtract(v1, v0), np.subtract(v2, v0)))
+        return self._add(T, scenes.TRIANGLE, a)
+
+    def addTile(self, center=(0, 0, 0), size=(1, 1), rotation=(0.0, 0.0), div=(1, 1)):
+        s = scenes.tile_grid(center, size, div, twosided=1)
+        return [self._add(T, scenes.PATCH, a) for T, a in zip(s.T, s.area)]
+
+    def addDisk(self, center, radius, normal=(0, 0, 1)):
+        T = scenes.disks(np.asarray(center, np.float64)[None], radius, np.asarray(normal, np.float64)[None])[0]
+        return self._add(T, scenes.DISK, math.pi * radius * radius)
+
+    def addVoxel(self, center, size):
+        T = scenes.voxel_T(np.asarray(center, np.float64)[None], size)[0]
+        return self._add(T, scenes.VOXEL, 2 * (size[0] * size[1] + size[1] * size[2] + size[0] * size[2]))
+
+    def addPrimitives(self, T, ptype, area=None, twosided=None):
+        """Bulk add (synthetic scenes): returns the new UUIDs."""
+        T = np.asarray(T, np.float32).reshape(-1, 16)
+        first = self._add_many(T, ptype, 1.0 if area is None else area)
+        uuids = np.arange(first, first + T.shape[0])
+        if twosided is not None:
+            self.setPrimitiveData(uuids, "twosided_flag", np.broadcast_to(np.asarray(twosided, np.float64), uuids.shape))
+        return uuids
+
+    def addScene(self, sc: "scenes.Scene"):
+        return self.addPrimitives(sc.T, sc.ptype, sc.area, sc.twosided)
+
+    def getPrimitiveCount(self):
+        return self._n
+
+    def getAllUUIDs(self):
+        return list(range(self._n))
+
+    def getPrimitiveArea(self, uuid):
+        return float(self.arrays()[2][uuid])
+
+    def arrays(self):
+        if self._cache is None:
+            if self._chunks:
+                T = np.concatenate([c[0] for c in self._chunks])
+                ty = np.concatenate([c[1] for c in self._chunks])
+                area = np.concatenate([c[2] for c in self._chunks])
+                self._chunks = [(T, ty, area)]
+            else:
+                T, ty, area = np.zeros((0, 16), np.float32), np.zeros(0, np.uint32), np.zeros(0)
+            self._cache = (T, ty, area)
+        return self._cache
+
+    def getDomainBoundingBox(self):
+        """x, y, z bounds over all primitive vertices (Context::getDomainBoundingBox)."""
+        T, ty, _ = self.arrays()
+        if T.shape[0] == 0:
+            return (0.0, 0.0), (0.0, 0.0), (0.0, 0.0)
+        lo = np.full(3, np.inf)
+        hi = np.full(3, -np.inf)
+        ax, ay, c = T[:, [0, 4, 8]].astype(np.float64), T[:, [1, 5, 9]].astype(np.float64), T[:, [3, 7, 11]].astype(np.float64)
+        corners = {scenes.PATCH: ((-0.5, -0.5), (0.5, -0.5), (0.5, 0.5), (-0.5, 0.5)),
+                   scenes.TILE: ((-0.5, -0.5), (0.5, -0.5), (0.5, 0.5), (-0.5, 0.5)),
+                   scenes.TRIANGLE: ((0, 0), (0, 1), (1, 1))}
+        for t, cs in corners.items():
+            m = ty == t
+            for cx, cy in cs:
+                p = ax[m] * cx + ay[m] * cy + c[m]
+                if p.size:
+                    lo = np.minimum(lo, p.min(0))
+                    hi = np.maximum(hi, p.max(0))
+        m = ty == scenes.DISK
+        if m.any():
+            r = np.linalg.norm(ax[m], axis=1)[:, None]
+            lo = np.minimum(lo, (c[m] - r).min(0))
+            hi = np.maximum(hi, (c[m] + r).max(0))
+        m = ty == scenes.VOXEL
+        if m.any():
+            h = 0.5 * np.abs(np.stack([T[m, 0], T[m, 5], T[m, 10]], 1))
+            lo = np.minimum(lo, (c[m] - h).min(0))
+            hi = np.maximum(hi, (c[m] + h).max(0))
+        return (lo[0], hi[0]), (lo[1], hi[1]), (lo[2], hi[2])
+
+    # --------------------------------------------------------------- data
+    def setPrimitiveData(self, uuid, label, value):
+        if np.ndim(uuid) > 0:
+            uuids = np.asarray(uuid).ravel()
+            vals = np.broadcast_to(np.asarray(value), uuids.shape)
+            arr = self._bulk(label, vals.dtype)
+            arr[uuids] = vals
+            return
+        d = self.primitive_data.setdefault(label, {})
+        d[int(uuid)] = value
+        if label in self.bulk_data:
+            self._bulk(label, np.asarray(value).dtype)[int(uuid)] = value
+
+    def _bulk(self, label, dtype):
+        n = self._n
+        arr = self.bulk_data.get(label)
+        if arr is None or arr.shape[0] < n:
+            new = np.full(n, np.nan, np.float64)
+            if arr is not None:
+                new[: arr.shape[0]] = arr
+            for k, v in self.primitive_data.get(label, {}).items():
+                new[k] = v
+            self.bulk_data[label] = arr = new
+        return arr
+
+    def doesPrimitiveDataExist(self, uuid, label):
+        if label in self.bulk_data and uuid < self.bulk_data[label].shape[0]:
+            return not np.isnan(self.bulk_data[label][uuid])
+        return uuid in self.primitive_data.get(label, {})
+
+    def getPrimitiveData(self, uuid, label):
+        if label in self.bulk_data and uuid < self.bulk_data[label].shape[0]:
+            v = self.bulk_data[label][uuid]
+            if not np.isnan(v):
+                return float(v)
+        d = self.primitive_data.get(label, {})
+        if uuid not in d:
+            raise HeliosRuntimeError(f"ERROR (Context::getPrimitiveData): Primitive data {label} does not exist "
+                                     f"for primitive {uuid}.")
+        return d[uuid]
+
+    def primitive_array(self, label, default):
+        """Dense float64 view of a primitive-data label with a default for missing entries."""
+        n = self._n
+        out = np.full(n, float(default))
+        if label in self.bulk_data:
+            a = self.bulk_data[label][:n]
+            m = ~np.isnan(a)
+            out[: a.shape[0]][m] = a[m]
+        for k, v in self.primitive_data.get(label, {}).items():
+            if k < n:
+                out[k] = float(v)
+        return out
+
+    def setGlobalData(self, label, value):
+        self.global_data[label] = value
+
+    def getGlobalData(self, label):
+        return self.global_data[label]
+
+
+class _Band:
+    def __init__(self):
+        self.directRayCount = 100       # RadiationModel.cpp:40
+        self.diffuseRayCount = 1000     # RadiationModel.cpp:41
+        self.diffuseFlux = -1.0         # RadiationModel.cpp:43
+        self.scatteringDepth = 0        # RadiationModel.cpp:46
+        self.emissionFlag = True        # RadiationModel.h:549
+        self.diffuseExtinction = 0.0
+        self.diffusePeakDir = (0.0, 0.0, 1.0)
+        self.diffuseDistNorm = 1.0
+
+
+class RadiationModel:
+    def __init__(self, context: Context, device: int = 0, mode: str = "device"):
+        self.context = context
+        self.device = device
+        self._ctx = None
+        self.mode = mode
+        self.bands: dict[str, _Band] = {}
+        self.sources: list[dict] = []
+        self.periodic = (0.0, 0.0)
+        self.seed = 0
+        self.auto_seed = True
+        self.message_flag = True
+        self._geom_n = -1
+        self.rho_default, self.tau_default, self.eps_default = 0.0, 0.0, 1.0
+        self.temperature_default = 300.0
+        self.last_stats = {}
+
+    @property
+    def ctx(self) -> "_hrt.Context":
+        """The device context, created on first use (initialize(), RayTracingBackend.h:54)."""
+        if self._ctx is None:
+            self._ctx = _hrt.Context(self.device)
+        return self._ctx
+
+    # --------------------------------------------------------------- config
+    def disableMessages(self):
+        self.message_flag = False
+
+    def setSeed(self, seed: int):
+        """Fix the Philox key of the next runBand calls (the reference seeds from the clock)."""
+        self.seed = int(seed) & 0xFFFFFFFF
+        self.auto_seed = False
+
+    def addRadiationBand(self, label, wavelength_min=None, wavelength_max=None):
+        if label in self.bands:
+            raise HeliosRuntimeError(f"ERROR (RadiationModel::addRadiationBand): Radiation band {label} has already "
+                                     "been added.")
+        self.bands[label] = _Band()
+        for s in self.sources:
+            s["fluxes"].setdefault(label, -1.0)
+
+    def doesBandExist(self, label):
+        return label in self.bands
+
+    def _band(self, label, fn):
+        if label not in self.bands:
+            raise HeliosRuntimeError(f"ERROR (RadiationModel::{fn}): Cannot {fn} for band '{label}' because it "
+                                     "is not a valid band.")
+        return self.bands[label]
+
+    def disableEmission(self, label):
+        self._band(label, "disableEmission").emissionFlag = False
+
+    def enableEmission(self, label):
+        self._band(label, "enableEmission").emissionFlag = True
+
+    def setDirectRayCount(self, label, n):
+        self._band(label, "setDirectRayCount").directRayCount = int(n)
+
+    def setDiffuseRayCount(self, label, n):
+        self._band(label, "setDiffuseRayCount").diffuseRayCount = int(n)
+
+    def setScatteringDepth(self, label, depth):
+        if depth < 0:
+            raise HeliosRuntimeError("ERROR (RadiationModel::setScatteringDepth): scattering depth must be >= 0.")
+        self._band(label, "setScatteringDepth").scatteringDepth = int(depth)
+
+    def setDiffuseRadiationFlux(self, label, flux):
+        self._band(label, "setDiffuseRadiationFlux").diffuseFlux = float(flux)
+
+    def setDiffuseRadiationExtinctionCoeff(self, label, K, peak_direction):
+        """Power-law sky fd = psi^-K normalised over the hemisphere (RadiationModel.cpp:185-217)."""
+        b = self._band(label, "setDiffuseRadiationExtinctionCoeff")
+        d = np.asarray(peak_direction, np.float64)
+        d = d / np.linalg.norm(d)
+        N = 100
+        th = 0.5 * math.pi / N * (0.5 + np.arange(N))
+        ph = 2.0 * math.pi / N * (0.5 + np.arange(N))
+        TH, PH = np.meshgrid(th, ph, indexing="ij")
+        el = 0.5 * math.pi - TH  # sphere2cart(elevation, azimuth) convention
+        v = np.stack([np.cos(el) * np.sin(PH), np.cos(el) * np.cos(PH), np.sin(el)], -1)
+        psi = np.arccos(np.clip(v @ d, -1.0, 1.0))
+        fd = np.where(psi < math.pi / 180.0, (math.pi / 180.0) ** (-K), psi ** (-K))
+        norm = float((fd * np.cos(TH) * np.sin(TH) * math.pi / (N * N)).sum())
+        b.diffuseExtinction = float(K)
+        b.diffusePeakDir = tuple(d)
+        b.diffuseDistNorm = 1.0 / norm
+
+    def _add_source(self, src):
+        if len(self.sources) >= 256:
+            raise HeliosRuntimeError("ERROR (RadiationModel): A maximum of 256 radiation sources are allowed.")
+        src["fluxes"] = {b: -1.0 for b in self.bands}
+        self.sources.append(src)
+        return len(self.sources) - 1
+
+    def addCollimatedRadiationSource(self, direction=(0.0, 0.0, 1.0)):
+        d = np.asarray(direction, np.float64)
+        if np.linalg.norm(d) == 0:
+            raise HeliosRuntimeError("ERROR (RadiationModel::addCollimatedRadiationSource): Invalid collimated "
+                                     "source direction. Direction vector should not have length of zero.")
+        return self._add_source({"type": 0, "position": tuple(d), "width": (0.0, 0.0), "rotation": (0, 0, 0)})
+
+    def addSunSphereRadiationSource(self, direction=(0.0, 0.0, 1.0)):
+        d = np.asarray(direction, np.float64)
+        d = 150e9 * d / np.linalg.norm(d)
+        return self._add_source({"type": 2, "position": tuple(d), "width": (2 * 695.5e6, 0.0), "rotation": (0, 0, 0)})
+
+    def addSphereRadiationSource(self, position, radius):
+        return self._add_source({"type": 1, "position": tuple(position), "width": (2 * radius, 0.0),
+                                 "rotation": (0, 0, 0)})
+
+    def addRectangleRadiationSource(self, position, size, rotation):
+        return self._add_source({"type": 3, "position": tuple(position), "width": tuple(size),
+                                 "rotation": tuple(rotation)})
+
+    def addDiskRadiationSource(self, position, radius, rotation):
+        return self._add_source({"type": 4, "position": tuple(position), "width": (radius, 0.0),
+                                 "rotation": tuple(rotation)})
+
+    def setSourceFlux(self, source, label, flux):
+        self._band(label, "setSourceFlux")
+        if source >= len(self.sources):
+            raise HeliosRuntimeError("ERROR (RadiationModel::setSourceFlux): Source ID out of bounds.")
+        self.sources[source]["fluxes"][label] = float(flux)
+
+    def getSourceFlux(self, source, label):
+        f = self.sources[source]["fluxes"].get(label, -1.0)
+        return 0.0 if f < 0 else f  # RadiationModel.cpp:1226-1230
+
+    def getDiffuseFlux(self, label):
+        f = self.bands[label].diffuseFlux
+        return f if f >= 0 else 0.0  # RadiationModel.cpp:1312-1330
+
+    def enforcePeriodicBoundary(self, boundary):
+        px, py = self.periodic
+        if boundary == "x":
+            px = 1.0
+        elif boundary == "y":
+            py = 1.0
+        elif boundary == "xy":
+            px = py = 1.0
+        else:
+            print(f"WARNING (RadiationModel::enforcePeriodicBoundary()): unknown boundary of '{boundary}'. "
+                  "Possible choices are x, y, or xy.")
+        self.periodic = (px, py)
+        self._geom_n = -1
+
+    # --------------------------------------------------------------- geometry
+    def _bbox_faces(self):
+        px, py = self.periodic
+        if px != 1 and py != 1:
+            return None
+        (x0, x1), (y0, y1), (z0, z1) = self.context.getDomainBoundingBox()
+        x0, x1, y0, y1, z0, z1 = (np.float32(v) for v in (x0 - 1e-5, x1 + 1e-5, y0 - 1e-5, y1 + 1e-5, z0 - 1e-5,
+                                                            z1 + 1e-5))
+        faces = []
+        if px == 1:  # RadiationModel.cpp:6046-6063
+            faces.append([(x0, y0, z0), (x0, y1, z0), (x0, y1, z1), (x0, y0, z1)])
+            faces.append([(x1, y0, z0), (x1, y1, z0), (x1, y1, z1), (x1, y0, z1)])
+        if py == 1:
+            faces.append([(x0, y0, z0), (x1, y0, z0), (x1, y0, z1), (x0, y0, z1)])
+            faces.append([(x0, y1, z0), (x1, y1, z0), (x1, y1, z1), (x0, y1, z1)])
+        return np.asarray(faces, np.float32)
+
+    def geometry_arrays(self):
+        T, ty, area = self.context.arrays()
+        ts = self.context.primitive_array("twosided_flag", 1).astype(np.int8)
+        keep = (area > 0) | (ty == scenes.TILE)  # zero-area primitives are skipped (RadiationModel.cpp:5813-5824)
+        if not keep.all():
+            raise HeliosRuntimeError("zero-area primitives are not supported by this mirror")
+        return T, ty, ts
+
+    def updateGeometry(self):
+        T, ty, ts = self.geometry_arrays()
+        self._ts = ts
+        self.ctx.update_geometry(T, ty, ts, self._bbox_faces(), self.periodic)
+        self.ctx.build_accel()
+        self._geom_n = T.shape[0]
+
+    # --------------------------------------------------------------- solve
+    def _materials(self, band_labels, S):
+        """rho/tau [S][N][Bg] and eps [N][Bl] following updateRadiativeProperties (RadiationModel.cpp:2850-2880)."""
+        n = self.context.getPrimitiveCount()
+        all_bands = sorted(self.bands)
+        Bg = len(all_bands)
+        rho = np.zeros((n, Bg))
+        tau = np.zeros((n, Bg))
+        eps_l = np.ones((n, len(band_labels)))
+        for bi, b in enumerate(all_bands):
+            band = self.bands[b]
+            r = self.context.primitive_array("reflectivity_" + b, self.rho_default)
+            t = self.context.primitive_array("transmissivity_" + b, self.tau_default)
+            e = self.context.primitive_array("emissivity_" + b, self.eps_default)
+            if band.emissionFlag:
+                m1 = (e != 1.0) & (r == 0) & (t == 0)
+                r = np.where(m1, 1.0 - e, r)
+                bad = ~m1 & (np.abs(e + t + r - 1.0) > 1e-6) & (e > 0)
+                if bad.any():
+                    raise HeliosRuntimeError(f"ERROR (RadiationModel): emissivity, transmissivity, and reflectivity "
+                                             f"must sum to 1 to ensure energy conservation. Band {b}. It is also "
+                                             "possible that you forgot to disable emission for this band.")
+                m3 = ~m1 & (band.scatteringDepth == 0) & (e != 1.0)
+                e = np.where(m3, 1.0, e)
+                r = np.where(m3, 0.0, r)
+                t = np.where(m3, 0.0, t)
+            elif (t + r > 1.0 + 1e-6).any():
+                raise HeliosRuntimeError("ERROR (RadiationModel): transmissivity and reflectivity cannot sum to "
+                                         "greater than 1 ensure energy conservation.")
+            rho[:, bi] = r
+            tau[:, bi] = t
+            if b in band_labels:
+                eps_l[:, band_labels.index(b)] = e
+        rho = np.broadcast_to(rho, (S, n, Bg)).astype(np.float32)
+        tau = np.broadcast_to(tau, (S, n, Bg)).astype(np.float32)
+        return rho, tau, eps_l.astype(np.float32)
+
+    def solve_description(self, labels, seed=None):
+        """The band set of one runBand call as plain arrays (shared with the oracle)."""
+        if isinstance(labels, str):
+            labels = [labels]
+        for b in labels:
+            if b not in self.bands:
+                raise HeliosRuntimeError(f"ERROR (RadiationModel::runBand): Cannot run band {b} because it is not a "
+                                         "valid band. Use addRadiationBand() function to add the band.")
+        all_bands = sorted(self.bands)  # std::map order (RadiationModel.cpp:3520-3527)
+        band_labels = [b for b in all_bands if b in labels]
+        if not self.sources:
+            self.addCollimatedRadiationSource()
+        S = len(self.sources)
+        rho, tau, eps = self._materials(band_labels, S)
+        n = self.context.getPrimitiveCount()
+        temp = self.context.primitive_array("temperature", self.temperature_default)
+        temp = np.where(temp < 0, self.temperature_default, temp).astype(np.float32)
+        sflux = np.array([[self.getSourceFlux(s, b) for b in band_labels] for s in range(S)], np.float32)
+        B = [self.bands[b] for b in band_labels]
+        desc = {
+            "band_labels": band_labels,
+            "band_launch": np.array([1 if b in band_labels else 0 for b in all_bands], np.uint8),
+            "sources": [dict(s) for s in self.sources],
+            "source_flux": sflux,
+            "rho": rho, "tau": tau,
+            "diffuse_flux": np.array([self.getDiffuseFlux(b) for b in band_labels], np.float32),
+            "diffuse_ext": np.array([x.diffuseExtinction for x in B], np.float32),
+            "diffuse_norm": np.array([x.diffuseDistNorm for x in B], np.float32),
+            "diffuse_peak": np.array([x.diffusePeakDir for x in B], np.float32),
+            "prague": np.zeros((len(B), 4), np.float32),
+            "direct_rays": np.array([x.directRayCount for x in B], np.int32),
+            "diffuse_rays": np.array([x.diffuseRayCount for x in B], np.int32),
+            "depth": np.array([x.scatteringDepth for x in B], np.int32),
+            "emission": np.array([1 if x.emissionFlag else 0 for x in B], np.uint8),
+            "eps": eps, "temperature": temp,
+            "seed": self.seed if seed is None else seed,
+            "n": n,
+        }
+        return desc
+
+    def runBand(self, labels):
+        if isinstance(labels, str):
+            labels = [labels]
+        for b in self.bands:
+            self.context.setGlobalData("emission_enabled_" + b, 1 if self.bands[b].emissionFlag else 0)
+        if self.context.getPrimitiveCount() == 0:
+            print("WARNING (RadiationModel::runBand): No geometry was added to the context. There is nothing to "
+                  "simulate...exiting.")
+            return
+        if self._geom_n != self.context.getPrimitiveCount():
+            self.updateGeometry()
+        desc = self.solve_description(labels)
+        if self.mode == "backend":
+            flux = run_band_through_backend(self.ctx, desc, self._ts)
+        else:
+            flux = self.ctx.run_band(desc)
+            self.last_stats = self.ctx.last_stats()
+        n = desc["n"]
+        uu = np.arange(n)
+        for i, b in enumerate(desc["band_labels"]):
+            self.context.setPrimitiveData(uu, "radiation_flux_" + b, flux[:, i].astype(np.float64))
+        if self.auto_seed:
+            self.seed = (self.seed + 0x9E3779B9) & 0xFFFFFFFF
+        return flux
+
+    def getTotalAbsorbedFlux(self):
+        """Per-primitive sum over bands of radiation_flux_<band> times area (RadiationModel.cpp:4686-4708)."""
+        n = self.context.getPrimitiveCount()
+        _, _, area = self.context.arrays()
+        tot = np.zeros(n)
+        for b in self.bands:
+            lab = "radiation_flux_" + b
+            if lab in self.context.bulk_data:
+                tot += np.nan_to_num(self.context.bulk_data[lab][:n]) * area
+        return tot
+
+
+def run_band_through_backend(ctx: "_hrt.Context", d: dict, twosided: np.ndarray) -> np.ndarray:
+    """RadiationModel::runBand's pass sequence through the backend entry points
+    (src/RadiationModel.cpp:3779-4356 and 4628-4663)."""
+    n = d["n"]
+    flags = d["band_launch"]
+    Bg = flags.size
+    Bl = int(flags.sum())
+    S = len(d["sources"])
+    ctx.update_materials(d["rho"], d["tau"], S, Bg)
+    ctx.update_sources(d["sources"])
+    scattering = bool((d["depth"] > 0).any())
+    diffuse = bool((d["diffuse_flux"] > 0).any())
+    emission = bool(d["emission"].any())
+    dirN, difN, depth = int(d["direct_rays"].max()), int(d["diffuse_rays"].max()), int(d["depth"].max())
+    seed = d["seed"]
+    ctx.zero_radiation_buffers(Bl)
+    rundirect = bool((d["source_flux"] > 0).any())
+    ctx.upload_source_fluxes(d["source_flux"])
+    common = dict(launch_offset=0, launch_count=n, random_seed=seed, nbands_global=Bg, nbands_launch=Bl)
+    if S > 0 and rundirect:
+        ctx.launch_direct(rays_per_primitive=dirN, pass_id=0, band_launch_flag=flags, **common)
+    ftop = np.zeros((n, Bl), np.float32)
+    fbot = np.zeros((n, Bl), np.float32)
+    if scattering and rundirect:
+        res = ctx.get_results(Bl)
+        ftop = res["scatter_buff_top"].reshape(n, Bl).copy()
+        fbot = res["scatter_buff_bottom"].reshape(n, Bl).copy()
+        one = twosided == 0
+        tot = ftop[one] + fbot[one]
+        ftop[one] = tot
+        fbot[one] = tot
+        ctx.upload_radiation_out(ftop, fbot)
+        ctx.zero_scatter_buffers()
+    sky = dict(diffuse_extinction=d["diffuse_ext"], diffuse_peak_dir=d["diffuse_peak"],
+               diffuse_dist_norm=d["diffuse_norm"], sky_radiance_params=d["prague"])
+    rpp = int(math.ceil(math.sqrt(difN))) ** 2
+    if emission or diffuse:
+        if emission:
+            for b in range(Bl):
+                if not d["emission"][b]:
+                    continue
+                e = d["eps"][:, b].copy()
+                if d["depth"][b] == 0:
+                    e[e != 1.0] = 1.0
+                T = d["temperature"].astype(np.float64)
+                out = ((SIGMA_F32 * e).astype(np.float64) * (T * T * T * T)).astype(np.float32)
+                ftop[:, b] += out
+                fbot[twosided != 0, b] += out[twosided != 0]
+        for face in (1, 0):
+            ctx.launch_diffuse(rays_per_primitive=rpp, pass_id=1, band_launch_flag=flags, launch_face=face,
+                               diffuse_flux=d["diffuse_flux"], radiation_out_top=ftop, radiation_out_bottom=fbot,
+                               **sky, **common)
+    if scattering and (emission or diffuse) and not rundirect:
+        ctx.copy_scatter_to_radiation()
+        ctx.zero_scatter_buffers()
+    if scattering and (emission or diffuse or rundirect):
+        zero = np.zeros(Bl, np.float32)
+        sflags = flags.copy()
+        for it in range(depth):
+            b = -1
+            for bg in range(Bg):
+                if not sflags[bg]:
+                    continue
+                b += 1
+                if it + 1 > d["depth"][b]:
+                    sflags[bg] = 0
+            if it > 0 or (emission and rundirect):
+                ctx.copy_scatter_to_radiation()
+            ctx.zero_scatter_buffers()
+            res = ctx.get_results(Bl)
+            for face in (1, 0):
+                ctx.launch_diffuse(rays_per_primitive=rpp, pass_id=2 + it, band_launch_flag=sflags, launch_face=face,
+                                   diffuse_flux=zero, radiation_out_top=res["radiation_out_top"],
+                                   radiation_out_bottom=res["radiation_out_bottom"], **sky, **common)
+    res = ctx.get_results(Bl)
+    flux = (res["radiation_in"] + res["scatter_buff_top"] + res["scatter_buff_bottom"]).reshape(n, Bl)
+    return flux
+
+
+SIGMA_F32 = np.float32(SIGMA)

@@ -1,0 +1,232 @@
+"""Seeded synthetic scenes for the radiation solve.
+
+Every generator returns plain numpy arrays in the layout the reference's
+``RadiationModel::buildGeometryData`` hands to a ray-tracing backend
+(``plugins/radiation/src/RadiationModel.cpp:5808-6148``): one row-major 4x4
+FP32 transform per primitive (the Context's ``getPrimitiveTransformationMatrix``
+convention), a primitive type code and a two-sided flag.
+
+Canonical shapes (``plugins/radiation/src/optix8/OptiX8DeviceCode.cu:369-489``):
+  * patch / tile: the square [-0.5, 0.5]^2 in the local xy plane;
+  * triangle: vertices (0,0,0), (0,1,0), (1,1,0);
+  * disk: the unit disk in the local xy plane;
+  * voxel: the cube [-0.5, 0.5]^3.
+
+The random streams are numpy PCG64 generators seeded by the caller (seed 0 for
+the benchmark workloads), never Helios's ``Context::randu``.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+PATCH, TRIANGLE, DISK, TILE, VOXEL = 0, 1, 2, 3, 4
+
+
+@dataclass
+class Scene:
+    T: np.ndarray                 # [n, 16] float32
+    ptype: np.ndarray             # [n] uint32
+    twosided: np.ndarray          # [n] int8
+    area: np.ndarray              # [n] float64 (one face)
+    groups: dict = field(default_factory=dict)   # name -> index array
+    bbox_verts: np.ndarray | None = None         # periodic walls [nb, 4, 3]
+    periodic: tuple = (0.0, 0.0)
+
+    @property
+    def n(self) -> int:
+        return int(self.T.shape[0])
+
+
+def _rot(axis: str, a: float) -> np.ndarray:
+    c, s = math.cos(a), math.sin(a)
+    if axis == "x":
+        return np.array([[1, 0, 0], [0, c, -s], [0, s, c]])
+    if axis == "y":
+        return np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])
+    return np.array([[c, -s, 0], [s, c, 0], [0, 0, 1]])
+
+
+def helios_patch_T(center, size, elevation=0.0, azimuth=0.0) -> np.ndarray:
+    """Transform of ``Context::addPatch(center, size, SphericalCoord(1, elevation, azimuth))``:
+    scale, rotate(-elevation, x), rotate(-azimuth, z), translate
+    (``core/src/Context_primitive.cpp:36-56``)."""
+    M = np.diag([float(size[0]), float(size[1]), 1.0])
+    if elevation != 0:
+        M = _rot("x", -elevation) @ M
+    if azimuth != 0:
+        M = _rot("z", -azimuth) @ M
+    T = np.eye(4)
+    T[:3, :3] = M
+    T[:3, 3] = center
+    return T.reshape(16).astype(np.float32)
+
+
+def frame_T(center, sx, sy, normal, spin) -> np.ndarray:
+    """Vectorised patch transforms: local x/y axes scaled by (sx, sy), local z = unit normal."""
+    normal = np.asarray(normal, np.float64)
+    normal = normal / np.linalg.norm(normal, axis=-1, keepdims=True)
+    helper = np.where(np.abs(normal[..., 2:3]) < 0.9, np.array([0.0, 0.0, 1.0]), np.array([1.0, 0.0, 0.0]))
+    ex = np.cross(helper, normal)
+    ex /= np.linalg.norm(ex, axis=-1, keepdims=True)
+    ey = np.cross(normal, ex)
+    c, s = np.cos(spin)[..., None], np.sin(spin)[..., None]
+    ex, ey = c * ex + s * ey, -s * ex + c * ey
+    n = normal.shape[0]
+    T = np.zeros((n, 4, 4))
+    T[:, :3, 0] = ex * np.asarray(sx).reshape(-1, 1)
+    T[:, :3, 1] = ey * np.asarray(sy).reshape(-1, 1)
+    T[:, :3, 2] = normal
+    T[:, :3, 3] = center
+    T[:, 3, 3] = 1.0
+    return T.reshape(n, 16).astype(np.float32)
+
+
+def triangle_T(v0, v1, v2) -> np.ndarray:
+    """Transforms mapping the canonical triangle (0,0,0),(0,1,0),(1,1,0) onto (v0, v1, v2)
+    (the mapping ``Triangle::makeTransformationMatrix`` solves for,
+    ``core/src/Context_primitive.cpp:1327``)."""
+    v0, v1, v2 = (np.asarray(v, np.float64).reshape(-1, 3) for v in (v0, v1, v2))
+    n = v0.shape[0]
+    nrm = np.cross(v1 - v0, v2 - v0)
+    nrm /= np.maximum(np.linalg.norm(nrm, axis=-1, keepdims=True), 1e-30)
+    T = np.zeros((n, 4, 4))
+    T[:, :3, 0] = v2 - v1
+    T[:, :3, 1] = v1 - v0
+    T[:, :3, 2] = nrm
+    T[:, :3, 3] = v0
+    T[:, 3, 3] = 1.0
+    return T.reshape(n, 16).astype(np.float32)
+
+
+def uniform_sphere(rng, n) -> np.ndarray:
+    z = rng.uniform(-1.0, 1.0, n)
+    phi = rng.uniform(0.0, 2.0 * math.pi, n)
+    r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+    return np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=-1)
+
+
+def _concat(parts):
+    T = np.concatenate([p[0] for p in parts]).astype(np.float32)
+    ty = np.concatenate([np.full(p[0].shape[0], p[1], np.uint32) for p in parts])
+    ts = np.concatenate([np.full(p[0].shape[0], p[2], np.int8) for p in parts])
+    area = np.concatenate([p[3] for p in parts])
+    return T, ty, ts, area
+
+
+def homogeneous_canopy(n_leaves=20000, leaf=0.1, domain=10.0, zlo=1.0, zhi=3.0, seed=0, ground_div=1,
+                       ground_margin=0.0) -> Scene:
+    """One-sided ground (one patch, or a ground_div x ground_div tile) + two-sided square
+    leaves with a spherical leaf-angle distribution, centres uniform in [0,domain]^2 x [zlo,zhi].
+    ground_margin extends the ground past the leaf domain on every side (so that leaves
+    overhanging the edge still have ground below them)."""
+    rng = np.random.default_rng(seed)
+    gs = domain + 2.0 * ground_margin
+    if ground_div == 1:
+        ground = helios_patch_T((0.5 * domain, 0.5 * domain, 0.0), (gs, gs))[None, :]
+    else:
+        ground = tile_grid((0.5 * domain, 0.5 * domain, 0.0), (gs, gs), (ground_div, ground_div)).T
+    ng = ground.shape[0]
+    c = np.stack([rng.uniform(0, domain, n_leaves), rng.uniform(0, domain, n_leaves),
+                  rng.uniform(zlo, zhi, n_leaves)], axis=-1)
+    nrm = uniform_sphere(rng, n_leaves)
+    spin = rng.uniform(0, 2 * math.pi, n_leaves)
+    leaves = frame_T(c, np.full(n_leaves, leaf), np.full(n_leaves, leaf), nrm, spin)
+    T, ty, ts, area = _concat([(ground, PATCH, 0, np.full(ng, gs * gs / ng)),
+                               (leaves, PATCH, 1, np.full(n_leaves, leaf * leaf))])
+    return Scene(T, ty, ts, area, {"ground": np.arange(ng), "leaves": np.arange(ng, ng + n_leaves)})
+
+
+def orchard(nx=20, ny=10, spacing=5.0, leaves_per_tree=5000, side=0.03, radii=(1.5, 1.5, 2.0),
+            centre_z=3.0, seed=0, ground=False) -> Scene:
+    """Equilateral triangular leaves uniform in ellipsoidal crowns on a regular grid."""
+    rng = np.random.default_rng(seed)
+    ntree = nx * ny
+    n = ntree * leaves_per_tree
+    # uniform points in the unit ball
+    d = uniform_sphere(rng, n) * (rng.uniform(0, 1, n) ** (1.0 / 3.0))[:, None]
+    tx = (np.arange(ntree) % nx) * spacing
+    ty_ = (np.arange(ntree) // nx) * spacing
+    tid = np.repeat(np.arange(ntree), leaves_per_tree)
+    c = np.stack([tx[tid] + radii[0] * d[:, 0], ty_[tid] + radii[1] * d[:, 1], centre_z + radii[2] * d[:, 2]], -1)
+    nrm = uniform_sphere(rng, n)
+    spin = rng.uniform(0, 2 * math.pi, n)
+    # equilateral triangle of side `side` centred at c in the plane normal to nrm
+    helper = np.where(np.abs(nrm[:, 2:3]) < 0.9, np.array([0.0, 0.0, 1.0]), np.array([1.0, 0.0, 0.0]))
+    ex = np.cross(helper, nrm)
+    ex /= np.linalg.norm(ex, axis=-1, keepdims=True)
+    ey = np.cross(nrm, ex)
+    R = side / math.sqrt(3.0)
+    verts = []
+    for k in range(3):
+        a = spin + 2.0 * math.pi * k / 3.0
+        verts.append(c + R * (np.cos(a)[:, None] * ex + np.sin(a)[:, None] * ey))
+    T = triangle_T(verts[0], verts[1], verts[2])
+    area = np.full(n, math.sqrt(3.0) / 4.0 * side * side)
+    parts = [(T, TRIANGLE, 1, area)]
+    groups = {"leaves": np.arange(n)}
+    if ground:
+        gx, gy = nx * spacing, ny * spacing
+        g = helios_patch_T((0.5 * gx - 0.5 * spacing, 0.5 * gy - 0.5 * spacing, 0.0), (gx, gy))[None, :]
+        parts.append((g, PATCH, 0, np.array([gx * gy])))
+        groups["ground"] = np.array([n])
+    Tm, tym, tsm, aream = _concat(parts)
+    return Scene(Tm, tym, tsm, aream, groups)
+
+
+def parallel_rectangles(a=1.0, b=2.0, c=0.5) -> Scene:
+    """Two one-sided a x b rectangles facing each other at distance c
+    (reference selfTest "Black/Gray Parallel Rectangles")."""
+    T0 = helios_patch_T((0, 0, 0), (a, b))
+    T1 = helios_patch_T((0, 0, c), (a, b), elevation=math.pi, azimuth=0.0)
+    T = np.stack([T0, T1])
+    return Scene(T, np.zeros(2, np.uint32), np.zeros(2, np.int8), np.full(2, a * b))
+
+
+def common_edge_squares() -> Scene:
+    """Horizontal unit square and a vertical one sharing an edge
+    (reference selfTest "90 Degree Common-Edge Squares")."""
+    T0 = helios_patch_T((0, 0, 0), (1, 1))
+    T1 = helios_patch_T((0.5, 0, 0.5), (1, 1), elevation=0.5 * math.pi, azimuth=-0.5 * math.pi)
+    T = np.stack([T0, T1])
+    return Scene(T, np.zeros(2, np.uint32), np.zeros(2, np.int8), np.ones(2))
+
+
+def tile_grid(center=(0.0, 0.0, 0.0), size=(10.0, 10.0), div=(40, 40), twosided=0) -> Scene:
+    """A horizontal tile split into div[0] x div[1] patches (``Context::addTile``)."""
+    nx, ny = div
+    dx, dy = size[0] / nx, size[1] / ny
+    xs = center[0] - 0.5 * size[0] + (np.arange(nx) + 0.5) * dx
+    ys = center[1] - 0.5 * size[1] + (np.arange(ny) + 0.5) * dy
+    X, Y = np.meshgrid(xs, ys, indexing="xy")
+    T = np.stack([helios_patch_T((x, y, center[2]), (dx, dy)) for x, y in zip(X.ravel(), Y.ravel())])
+    n = T.shape[0]
+    return Scene(T, np.zeros(n, np.uint32), np.full(n, twosided, np.int8), np.full(n, dx * dy))
+
+
+def disks(centers, radius, normals) -> np.ndarray:
+    """Transforms of disks (unit disk scaled by radius) with the given normals."""
+    n = centers.shape[0]
+    spin = np.zeros(n)
+    return frame_T(centers, np.full(n, radius), np.full(n, radius), normals, spin)
+
+
+def voxel_T(centers, size) -> np.ndarray:
+    n = centers.shape[0]
+    T = np.zeros((n, 4, 4))
+    T[:, 0, 0] = size[0]
+    T[:, 1, 1] = size[1]
+    T[:, 2, 2] = size[2]
+    T[:, :3, 3] = centers
+    T[:, 3, 3] = 1.0
+    return T.reshape(n, 16).astype(np.float32)
+
+
+def sun_direction(zenith_deg: float, azimuth_deg: float) -> np.ndarray:
+    """Unit vector toward the sun, Helios ``sphere2cart`` convention (azimuth from +y toward +x,
+    ``core/src/global.cpp:833``)."""
+    el = math.radians(90.0 - zenith_deg)
+    az = math.radians(azimuth_deg)
+    return np.array([math.cos(el) * math.sin(az), math.cos(el) * math.cos(az), math.sin(el)], np.float32)

@@ -1,0 +1,181 @@
+/* hrt.h -- C ABI of libhrt, the GB300 (sm_103a) radiation-transfer engine.
+ *
+ * This is the drop-in boundary for the Helios radiation plugin.  The reference
+ * talks to its ray tracers only through the abstract class
+ * helios::RayTracingBackend (plugins/radiation/include/RayTracingBackend.h:42-317);
+ * each entry point below replaces one of its virtuals, named in the comment
+ * with the file:line of the declaration.  A C++ adapter that implements that
+ * class on top of these functions lives in helios_gb300/backend/.
+ *
+ * Conventions
+ *   - All pointers passed in are HOST pointers unless a name says otherwise;
+ *     sizes are element counts.  The library copies inputs to device memory it
+ *     owns; results are copied back into caller-provided host arrays.
+ *   - Every function returns HRT_OK (0) or a negative HRT_E* code; the text of
+ *     the last error of a context is returned by hrt_last_error().  The C++
+ *     adapter turns a non-zero code into helios::helios_runtime_error, which is
+ *     how the reference reports backend failures (core/include/global.h:102).
+ *   - Radiation buffers are indexed [primitive * Nbands_launch + band_launch],
+ *     materials [source * Nprims * Nbands_global + prim * Nbands_global + band]
+ *     (plugins/radiation/include/BufferIndexing.h:216-252).
+ *   - A context is used by one host thread at a time.  Calls are synchronous
+ *     unless stated otherwise, as the reference backends are
+ *     (OptiX8Backend.cpp:866,998).
+ */
+#ifndef HRT_H
+#define HRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HRT_OK 0
+#define HRT_EINVAL -1      /* bad argument or call order */
+#define HRT_ECUDA -2       /* CUDA runtime error */
+#define HRT_ENOMEM -3      /* device allocation failed */
+#define HRT_EDEVICE -4     /* device-side error word set (stack overflow, wrap limit) */
+#define HRT_EUNSUPPORTED -5
+
+typedef struct hrt_context hrt_context;
+
+/* Geometry, the subset of helios::RayTracingGeometry (RayTracingTypes.h:40-155)
+ * that the radiation solve reads.  Primitive types: 0 patch, 1 triangle, 2 disk,
+ * 3 tile (traced as a patch), 4 voxel.  Periodic walls are the reference's
+ * "bbox" primitives (type 5), passed separately as world-space quads. */
+typedef struct {
+    int32_t n;                    /* primitive_count */
+    const float *transform;       /* [n*16] row-major 4x4 (transform_matrices) */
+    const uint32_t *type;         /* [n] primitive_types */
+    const int8_t *twosided;       /* [n] twosided_flags: 0 one-sided, 1 two-sided, 2, 3 (skip) */
+    int32_t nbbox;                /* bbox_count: 0, 2 or 4 periodic walls */
+    const float *bbox_vertices;   /* [nbbox*4*3] wall corners (bboxes.vertices) */
+    float periodic_x, periodic_y; /* periodic_flag */
+} hrt_geometry;
+
+/* helios::RayTracingSource (RayTracingTypes.h:189-196) without the flux vectors,
+ * which travel through hrt_upload_source_fluxes(). */
+typedef struct {
+    uint32_t type;        /* 0 collimated, 1 sphere, 2 sun sphere, 3 rectangle, 4 disk */
+    float position[3];    /* direction toward the source (collimated) or centre */
+    float width[2];       /* diameter / rectangle sides */
+    float rotation[3];    /* Euler angles (rectangle and disk sources) */
+} hrt_source;
+
+/* helios::RayTracingLaunchParams (RayTracingTypes.h:201-250), radiation fields. */
+typedef struct {
+    uint32_t launch_offset;             /* first primitive */
+    uint32_t launch_count;              /* number of primitives */
+    uint32_t rays_per_primitive;        /* split into floor(sqrt(n)) x (n / floor(sqrt(n))) strata */
+    uint32_t random_seed;               /* Philox key word 0 */
+    uint32_t pass_id;                   /* Philox key word 1 (0 direct, 1 primary diffuse, 2+s scatter s) */
+    uint32_t nbands_global;
+    uint32_t nbands_launch;             /* buffer stride */
+    const uint8_t *band_launch_flag;    /* [nbands_global] */
+    uint32_t launch_face;               /* diffuse: 1 top, 0 bottom */
+    const float *diffuse_flux;          /* [nbands_launch] */
+    const float *diffuse_extinction;    /* [nbands_launch] power-law K, or NULL */
+    const float *diffuse_peak_dir;      /* [nbands_launch*3] or NULL */
+    const float *diffuse_dist_norm;     /* [nbands_launch] or NULL */
+    const float *sky_radiance_params;   /* [nbands_launch*4] Prague parameters, or NULL */
+    const float *radiation_out_top;     /* [n*nbands_launch] uploaded before a diffuse launch, or NULL */
+    const float *radiation_out_bottom;  /* [n*nbands_launch] or NULL */
+} hrt_launch;
+
+/* One whole RadiationModel::runBand() (RadiationModel.cpp:3470-4663) executed on
+ * the device: direct pass, emission source term, primary diffuse pass and the
+ * scattering iterations, with every intermediate buffer kept in HBM. */
+typedef struct {
+    int32_t nbands_global;
+    const uint8_t *band_launch;         /* [nbands_global] bands run by this call */
+    int32_t nsources;
+    const hrt_source *sources;          /* [nsources], or NULL to keep the sources already set */
+    const float *source_flux;           /* [nsources*Bl], or NULL to keep the fluxes already set */
+    const float *rho, *tau;             /* [nsources*n*nbands_global], or NULL to keep the materials already set */
+    const float *diffuse_flux;          /* [Bl] */
+    const float *diffuse_extinction;    /* [Bl] or NULL */
+    const float *diffuse_peak_dir;      /* [Bl*3] or NULL */
+    const float *diffuse_dist_norm;     /* [Bl] or NULL */
+    const float *sky_radiance_params;   /* [Bl*4] or NULL */
+    const int32_t *direct_rays;         /* [Bl] directRayCount per band */
+    const int32_t *diffuse_rays;        /* [Bl] diffuseRayCount per band */
+    const int32_t *scattering_depth;    /* [Bl] */
+    const uint8_t *emission;            /* [Bl] emission flag per band */
+    const float *emissivity;            /* [n*Bl], or NULL to reuse the array of an earlier call */
+    const float *temperature;           /* [n] kelvin, or NULL to reuse the array of an earlier call */
+    uint32_t seed;
+} hrt_band_solve;
+
+/* ---- lifecycle: RayTracingBackend::initialize / shutdown (RayTracingBackend.h:54,61) */
+int hrt_create(hrt_context **out, int device);
+int hrt_destroy(hrt_context *ctx);
+const char *hrt_last_error(const hrt_context *ctx);
+/* Run all work of this context on `stream` (a cudaStream_t), or NULL for the
+ * context's own stream. */
+int hrt_set_stream(hrt_context *ctx, void *stream);
+
+/* ---- RayTracingBackend::updateGeometry (RayTracingBackend.h:73) */
+int hrt_update_geometry(hrt_context *ctx, const hrt_geometry *g);
+/* ---- RayTracingBackend::buildAccelerationStructure (RayTracingBackend.h:81) */
+int hrt_build_accel(hrt_context *ctx);
+/* ---- RayTracingBackend::updateMaterials (RayTracingBackend.h:90) */
+int hrt_update_materials(hrt_context *ctx, int32_t nsources, int32_t nprims, int32_t nbands_global,
+                         const float *rho, const float *tau);
+/* ---- RayTracingBackend::updateSources (RayTracingBackend.h:99) */
+int hrt_update_sources(hrt_context *ctx, int32_t nsources, const hrt_source *sources);
+/* ---- RayTracingBackend::uploadSourceFluxes (RayTracingBackend.h:247) [source*Bl + band] */
+int hrt_upload_source_fluxes(hrt_context *ctx, const float *fluxes, size_t count);
+/* ---- RayTracingBackend::launchDirectRays (RayTracingBackend.h:139) */
+int hrt_launch_direct(hrt_context *ctx, const hrt_launch *p);
+/* ---- RayTracingBackend::launchDiffuseRays (RayTracingBackend.h:146) */
+int hrt_launch_diffuse(hrt_context *ctx, const hrt_launch *p);
+/* ---- RayTracingBackend::getRadiationResults (RayTracingBackend.h:171): any pointer may be NULL */
+int hrt_get_results(hrt_context *ctx, float *radiation_in, float *radiation_out_top, float *radiation_out_bottom,
+                    float *scatter_top, float *scatter_bottom);
+/* ---- RayTracingBackend::zeroRadiationBuffers (RayTracingBackend.h:194) */
+int hrt_zero_radiation_buffers(hrt_context *ctx, size_t launch_band_count);
+/* ---- RayTracingBackend::zeroScatterBuffers (RayTracingBackend.h:199) */
+int hrt_zero_scatter_buffers(hrt_context *ctx);
+/* ---- RayTracingBackend::copyScatterToRadiation (RayTracingBackend.h:218) */
+int hrt_copy_scatter_to_radiation(hrt_context *ctx);
+/* ---- RayTracingBackend::uploadRadiationOut (RayTracingBackend.h:228) */
+int hrt_upload_radiation_out(hrt_context *ctx, const float *top, const float *bottom, size_t count);
+/* ---- RayTracingBackend::queryGPUMemory (RayTracingBackend.h:263) */
+int hrt_query_memory(hrt_context *ctx, size_t *free_bytes, size_t *total_bytes);
+/* ---- RayTracingBackend::getBackendName (RayTracingBackend.h:270) */
+const char *hrt_backend_name(void);
+
+/* ---- whole runBand on the device (RadiationModel::runBand, RadiationModel.cpp:3470-4663).
+ * flux_out: host [n*Bl] = radiation_in + scatter_top + scatter_bottom
+ * (RadiationModel.cpp:4652), or NULL to leave the result on the device. */
+int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out);
+/* Statistics of the last hrt_run_band: [0] rays traced, [1] kernels launched. */
+int hrt_last_stats(const hrt_context *ctx, uint64_t *stats, int count);
+/* Device status word (HRT error bits) accumulated since the last reset. */
+int hrt_device_status(hrt_context *ctx, uint32_t *status, int reset);
+
+/* ---- inspection (tests): closest/any hit for explicit rays, the ray set of one
+ * pass, and the device-built BVH (same layout as the host build). */
+int hrt_trace_rays(hrt_context *ctx, int64_t nrays, const float *origins, const float *dirs, float tmin, float tmax,
+                   int anyhit, int32_t *hit, float *t, int32_t *face);
+int hrt_gen_rays(hrt_context *ctx, int kind, uint32_t seed, uint32_t pass, int32_t rays_per_primitive, int32_t face,
+                 const float *direction, float *origins, float *dirs);
+int hrt_get_bvh(hrt_context *ctx, uint64_t *codes, uint32_t *perm, uint32_t *nodes);
+/* Measurement controls (no counterpart in the reference; used by the benchmark).
+ * flags bit 0: run the statistics variants of the trace kernels, which count BVH
+ * node visits and primitive tests; bit 1: time every trace-kernel launch with CUDA
+ * events on the context's stream.  Setting flags also resets the accumulators.
+ * hrt_get_measure: [0] direct launches, [1] direct ms, [2] diffuse launches,
+ * [3] diffuse ms, [4] node visits, [5] primitive tests. */
+int hrt_set_measure(hrt_context *ctx, int flags);
+int hrt_get_measure(hrt_context *ctx, double *out, int count);
+/* Rotation matrix (row-major 3x3) that rect/disk sources use, from Euler angles
+ * (same convention as the reference's d_makeTransformMatrix, OptiX8DeviceCode.cu:191-201). */
+void hrt_source_rotation(const float rotation[3], float out[9]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HRT_H */

@@ -1,0 +1,1304 @@
+// hrt_oracle.cpp -- CPU FP64 oracle for the Helios radiation-transfer hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  Nothing in the product (helios_gb300/) links, loads
+// or calls this file; only tests/, __graft_entry__.smoke() (as the checker) and
+// bench.py's cpu_baseline / --impl reference legs use it.
+//
+// What it restates (reference = PlantSimulationLab/Helios, plugin "radiation"):
+//   * ray generation          src/optix8/OptiX8DeviceCode.cu:1210-1465 (__raygen__direct)
+//                              src/optix8/OptiX8DeviceCode.cu:1471-1658 (__raygen__diffuse)
+//   * primitive intersection   src/optix8/OptiX8DeviceCode.cu:320-490  (__intersection__patch,
+//                              kept as the "reference formula" mode) plus the watertight
+//                              test (Woop, Benthin, Wald, JCGT 2013) used by the GPU build
+//   * energy deposition        src/optix8/OptiX8DeviceCode.cu:514-596  (__miss__direct)
+//                              src/optix8/OptiX8DeviceCode.cu:598-671  (__miss__diffuse)
+//                              src/optix8/OptiX8DeviceCode.cu:930-1001 (__closesthit__diffuse)
+//                              src/optix8/OptiX8DeviceCode.cu:148-164  (sky distribution)
+//   * buffer bookkeeping       src/backends/OptiX8Backend.cpp:1168-1250
+//   * pass orchestration       src/RadiationModel.cpp:3470-4663 (runBand)
+//   * emission source term     src/RadiationModel.cpp:4041-4137 (sigma*eps*T^4)
+//
+// Arithmetic contract: every FP32 operation on the geometric path (ray generation,
+// bounding boxes, Morton codes, slab and primitive tests) is written as a plain
+// sequence of IEEE-754 single-precision +, -, *, / and sqrt, compiled with
+// -ffp-contract=off.  The CUDA kernels compile the same sequences with
+// --fmad=false, so both sides produce bit-identical rays, BVHs and hit IDs.
+// Energy sums are FP64 here (the "FP64 oracle").
+//
+// Random numbers: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), keyed by
+// (seed, pass) with counter (ray, primitive, face|source<<1, 0).  The reference
+// uses TEA16 + LCG seeded from the wall clock (RadiationModel.cpp:3961), so its
+// ray sets are not reproducible; parity with the reference is statistical.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// ---------------------------------------------------------------- vectors ---
+struct V3 {
+    float x, y, z;
+};
+inline V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+inline V3 vsub(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 vadd(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 vscale(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+inline float vdot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+inline V3 vcross(V3 a, V3 b) {
+    return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+inline V3 vnormalize(V3 a) {
+    float l = std::sqrt(vdot(a, a));
+    return v3(a.x / l, a.y / l, a.z / l);
+}
+inline float vget(V3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+
+// T . (px, py, 0, 1) for a row-major 4x4 transform, fixed evaluation order.
+inline V3 xform(const float *T, float px, float py) {
+    return v3((T[0] * px + T[1] * py) + T[3], (T[4] * px + T[5] * py) + T[7],
+              (T[8] * px + T[9] * py) + T[11]);
+}
+
+// ---------------------------------------------------------------- Philox ---
+struct U4 {
+    uint32_t v[4];
+};
+inline U4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        uint32_t n1 = (uint32_t)p1;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        uint32_t n3 = (uint32_t)p0;
+        c0 = n0;
+        c1 = n1;
+        c2 = n2;
+        c3 = n3;
+    }
+    return U4{{c0, c1, c2, c3}};
+}
+inline float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+// cos(2*pi*u), sin(2*pi*u) for u in [0,1): quadrant/octant reduction and
+// Taylor polynomials on [0, pi/4] (coefficients are 1/k!), evaluated in a fixed order.
+inline void sincos2pi(float u, float *c_out, float *s_out) {
+    float x = u * 4.0f;
+    int q = (int)x;
+    float f = x - (float)q;
+    bool swap = f > 0.5f;
+    float g = swap ? (1.0f - f) : f;
+    float a = g * 1.57079632679489662f;
+    float a2 = a * a;
+    float s = a + a * a2 * (-1.66666666666666667e-1f +
+                            a2 * (8.33333333333333333e-3f +
+                                  a2 * (-1.98412698412698413e-4f + a2 * 2.75573192239858907e-6f)));
+    float c = 1.0f + a2 * (-0.5f + a2 * (4.16666666666666667e-2f +
+                                         a2 * (-1.38888888888888889e-3f +
+                                               a2 * (2.48015873015873016e-5f +
+                                                     a2 * -2.75573192239858907e-7f))));
+    float c0 = swap ? s : c;
+    float s0 = swap ? c : s;
+    q &= 3;
+    if (q == 0) {
+        *c_out = c0;
+        *s_out = s0;
+    } else if (q == 1) {
+        *c_out = -s0;
+        *s_out = c0;
+    } else if (q == 2) {
+        *c_out = -c0;
+        *s_out = -s0;
+    } else {
+        *c_out = s0;
+        *s_out = -c0;
+    }
+}
+
+// Orthonormal basis around unit n (Duff, Burgess, Christensen, Hery, Kensler,
+// Liani, Villemin: "Building an Orthonormal Basis, Revisited", JCGT 6(1), 2017).
+inline void onb(V3 n, V3 *t1, V3 *t2) {
+    float sign = std::copysign(1.0f, n.z);
+    float a = -1.0f / (sign + n.z);
+    float b = n.x * n.y * a;
+    *t1 = v3(1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+    *t2 = v3(b, sign + n.y * n.y * a, -n.y);
+}
+
+// ---------------------------------------------------------------- records ---
+// Primitive types (RayTracingTypes.h:45): 0 patch, 1 triangle, 2 disk, 3 tile, 4 voxel, 5 bbox face.
+enum { PT_PATCH = 0, PT_TRI = 1, PT_DISK = 2, PT_TILE = 3, PT_VOXEL = 4, PT_BBOX = 5 };
+
+struct Rec {        // intersection record, one per primitive
+    V3 p[4];        // patch/bbox: 4 corners; triangle: v0,v1,v2; disk: centre, normal(unit), (r,0,0)
+    int type;       // voxel: p[0]=lo, p[1]=hi
+};
+struct RGen {       // ray-origin sampling record
+    V3 P, A, B, N;  // point = P + u*A + v*B ; N = unit normal
+};
+
+Rec make_rec(const float *T, int type) {
+    Rec r{};
+    r.type = type;
+    if (type == PT_TRI) {
+        r.p[0] = xform(T, 0.f, 0.f);
+        r.p[1] = xform(T, 0.f, 1.f);
+        r.p[2] = xform(T, 1.f, 1.f);
+        r.p[3] = r.p[2];
+    } else if (type == PT_DISK) {
+        // unit disk in the canonical xy plane; T scales it (OptiX 6 primitiveIntersection.cu:236-300)
+        r.p[0] = xform(T, 0.f, 0.f);
+        V3 ax = v3(T[0], T[4], T[8]);
+        V3 ay = v3(T[1], T[5], T[9]);
+        r.p[1] = vnormalize(vcross(ax, ay));
+        r.p[2] = v3(std::sqrt(vdot(ax, ax)), 0.f, 0.f);
+        r.p[3] = r.p[0];
+    } else if (type == PT_VOXEL) {
+        // axis-aligned box: canonical [-0.5,0.5]^3 scaled/translated by T (diagonal part only)
+        V3 c = v3(T[3], T[7], T[11]);
+        V3 h = v3(std::fabs(T[0]) * 0.5f, std::fabs(T[5]) * 0.5f, std::fabs(T[10]) * 0.5f);
+        r.p[0] = vsub(c, h);
+        r.p[1] = vadd(c, h);
+        r.p[2] = r.p[0];
+        r.p[3] = r.p[1];
+    } else {  // patch, tile
+        r.type = PT_PATCH;
+        r.p[0] = xform(T, -0.5f, -0.5f);
+        r.p[1] = xform(T, 0.5f, -0.5f);
+        r.p[2] = xform(T, 0.5f, 0.5f);
+        r.p[3] = xform(T, -0.5f, 0.5f);
+    }
+    return r;
+}
+
+RGen make_rgen(const float *T, int type) {
+    RGen g{};
+    g.A = v3(T[0], T[4], T[8]);
+    g.B = v3(T[1], T[5], T[9]);
+    if (type == PT_TRI) {
+        g.P = v3(T[3], T[7], T[11]);
+        g.N = vnormalize(vcross(g.B, g.A));  // = normalize(cross(v1-v0, v2-v0))
+    } else {
+        g.P = xform(T, -0.5f, -0.5f);
+        g.N = vnormalize(vcross(g.A, g.B));
+    }
+    return g;
+}
+
+void rec_bounds(const Rec &r, V3 *lo, V3 *hi) {
+    if (r.type == PT_DISK) {
+        V3 c = r.p[0], n = r.p[1];
+        float rad = r.p[2].x;
+        // extent of a disk of radius rad with normal n along axis k: rad*sqrt(1-n_k^2)
+        float ex = rad * std::sqrt(std::fmax(0.f, 1.0f - n.x * n.x));
+        float ey = rad * std::sqrt(std::fmax(0.f, 1.0f - n.y * n.y));
+        float ez = rad * std::sqrt(std::fmax(0.f, 1.0f - n.z * n.z));
+        *lo = v3(c.x - ex, c.y - ey, c.z - ez);
+        *hi = v3(c.x + ex, c.y + ey, c.z + ez);
+        return;
+    }
+    int nv = (r.type == PT_TRI) ? 3 : (r.type == PT_VOXEL ? 2 : 4);
+    V3 a = r.p[0], b = r.p[0];
+    for (int i = 1; i < nv; ++i) {
+        a = v3(std::fmin(a.x, r.p[i].x), std::fmin(a.y, r.p[i].y), std::fmin(a.z, r.p[i].z));
+        b = v3(std::fmax(b.x, r.p[i].x), std::fmax(b.y, r.p[i].y), std::fmax(b.z, r.p[i].z));
+    }
+    *lo = a;
+    *hi = b;
+}
+
+// ---------------------------------------------------------------- rays -----
+struct Ray {
+    V3 o, d;
+    float tmin, tmax;
+};
+struct Hit {
+    float t;
+    int32_t prim;  // original primitive index, -1 = miss
+    int32_t face;  // 1 = ray hit the top (front) face, 0 = bottom
+};
+
+// Per-ray precomputation for the watertight test.
+struct WT {
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+inline WT wt_setup(V3 d) {
+    WT w;
+    float ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
+    w.kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
+    w.kx = (w.kz + 1) % 3;
+    w.ky = (w.kx + 1) % 3;
+    if (vget(d, w.kz) < 0.f) std::swap(w.kx, w.ky);
+    float dz = vget(d, w.kz);
+    w.Sx = vget(d, w.kx) / dz;
+    w.Sy = vget(d, w.ky) / dz;
+    w.Sz = 1.0f / dz;
+    return w;
+}
+
+// 2-D edge function e(P,Q) = Px*Qy - Py*Qx with an FP64 recompute when it is exactly 0.
+inline float edgef(float px, float py, float qx, float qy) {
+    float e = px * qy - py * qx;
+    if (e == 0.f) e = (float)((double)px * (double)qy - (double)py * (double)qx);
+    return e;
+}
+
+// Watertight polygon test (triangle: n=3, planar convex quad: n=4).  Returns t or -1.
+// face: 1 when the ray arrives on the side the geometric normal points to is *not*
+// the side it comes from, i.e. dot(d, n) < 0 (top face), matching the reference's
+// face attribute (OptiX8DeviceCode.cu:421,485).
+inline bool poly_hit(const WT &w, const Ray &ray, const V3 *v, int n, float tmax, float *t_out,
+                     int *face_out) {
+    float px[4], py[4], pz[4];
+    for (int i = 0; i < n; ++i) {
+        V3 a = vsub(v[i], ray.o);
+        float az = vget(a, w.kz);
+        px[i] = vget(a, w.kx) - w.Sx * az;
+        py[i] = vget(a, w.ky) - w.Sy * az;
+        pz[i] = w.Sz * az;
+    }
+    float e[4];
+    for (int i = 0; i < n; ++i) {
+        int j = (i + 1 == n) ? 0 : i + 1;
+        e[i] = edgef(px[i], py[i], px[j], py[j]);
+    }
+    bool anyneg = false, anypos = false;
+    for (int i = 0; i < n; ++i) {
+        anyneg = anyneg || (e[i] < 0.f);
+        anypos = anypos || (e[i] > 0.f);
+    }
+    if (anyneg && anypos) return false;
+    // barycentric weights of triangle (v0, v1, v2): w0 = e(v1,v2), w1 = e(v2,v0), w2 = e(v0,v1)
+    float e20 = (n == 3) ? e[2] : edgef(px[2], py[2], px[0], py[0]);
+    float det = (e[1] + e20) + e[0];
+    if (det == 0.f) return false;
+    float T = (e[1] * pz[0] + e20 * pz[1]) + e[0] * pz[2];
+    float t = T / det;
+    if (!(t >= ray.tmin) || !(t <= tmax)) return false;
+    *t_out = t;
+    // det < 0 <=> dot(d, n) < 0 for n = (v1-v0) x (v2-v0): the ray meets the top face
+    *face_out = (det < 0.f) ? 1 : 0;
+    return true;
+}
+
+// Disk (OptiX 6 primitiveIntersection.cu:236-300 semantics: plane hit inside radius).
+inline bool disk_hit(const Ray &ray, const Rec &r, float tmax, float *t_out, int *face_out) {
+    V3 c = r.p[0], n = r.p[1];
+    float rad = r.p[2].x;
+    float nd = vdot(ray.d, n);
+    if (nd == 0.f) return false;
+    float t = vdot(vsub(c, ray.o), n) / nd;
+    if (!(t >= ray.tmin) || !(t <= tmax)) return false;
+    V3 h = vsub(vadd(ray.o, vscale(ray.d, t)), c);
+    if (vdot(h, h) > rad * rad) return false;
+    *t_out = t;
+    *face_out = (nd < 0.f) ? 1 : 0;
+    return true;
+}
+
+// Slab test against an axis-aligned box; used for voxels and BVH nodes.
+inline bool slab(const V3 &o, const V3 &inv, V3 lo, V3 hi, float tmin, float tmax, float *tnear) {
+    float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
+    float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
+    float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
+    float tn = std::fmax(std::fmax(std::fmin(t0x, t1x), std::fmin(t0y, t1y)),
+                         std::fmax(std::fmin(t0z, t1z), tmin));
+    float tf = std::fmin(std::fmin(std::fmax(t0x, t1x), std::fmax(t0y, t1y)),
+                         std::fmin(std::fmax(t0z, t1z), tmax));
+    *tnear = tn;
+    return tn <= tf;
+}
+inline float safe_inv(float d) {
+    if (std::fabs(d) < 1e-30f) d = std::copysign(1e-30f, d);
+    return 1.0f / d;
+}
+
+// Voxel: a ray whose origin lies inside the box does not hit it (OptiX 6
+// primitiveIntersection.cu:330-374); otherwise the entry distance is the hit.
+inline bool voxel_hit(const Ray &ray, const V3 &inv, const Rec &r, float tmax, float *t_out,
+                      int *face_out) {
+    V3 lo = r.p[0], hi = r.p[1];
+    V3 o = ray.o;
+    if (o.x >= lo.x && o.x <= hi.x && o.y >= lo.y && o.y <= hi.y && o.z >= lo.z && o.z <= hi.z)
+        return false;
+    float tn;
+    if (!slab(o, inv, lo, hi, ray.tmin, tmax, &tn)) return false;
+    if (!(tn > 1e-5f)) return false;
+    *t_out = tn;
+    *face_out = 1;
+    return true;
+}
+
+inline bool prim_hit(const WT &w, const Ray &ray, const V3 &inv, const Rec &r, float tmax,
+                     float *t, int *face) {
+    switch (r.type) {
+        case PT_TRI:
+            return poly_hit(w, ray, r.p, 3, tmax, t, face);
+        case PT_PATCH:
+        case PT_BBOX:
+            return poly_hit(w, ray, r.p, 4, tmax, t, face);
+        case PT_DISK:
+            return disk_hit(ray, r, tmax, t, face);
+        case PT_VOXEL:
+            return voxel_hit(ray, inv, r, tmax, t, face);
+    }
+    return false;
+}
+
+// Reference intersection formulas, restated from OptiX8DeviceCode.cu:369-489
+// (patch: plane + local (u,v) in [-0.5,0.5]^2; triangle: Shirley/Cramer form).
+inline bool prim_hit_reference(const Ray &ray, const float *T, int type, float tmax, float *t_out,
+                               int *face_out) {
+    V3 o = ray.o, d = ray.d;
+    if (type == PT_PATCH || type == PT_TILE) {
+        V3 n = v3(T[2], T[6], T[10]);
+        float nd = vdot(d, n);
+        if (std::fabs(nd) < 1e-8f) return false;
+        V3 c = v3(T[3], T[7], T[11]);
+        float t = vdot(vsub(c, o), n) / nd;
+        if (t < ray.tmin || t > tmax) return false;
+        V3 hl = vsub(vadd(o, vscale(d, t)), c);
+        V3 lx = v3(T[0], T[4], T[8]), ly = v3(T[1], T[5], T[9]);
+        float lx2 = vdot(lx, lx), ly2 = vdot(ly, ly);
+        if (lx2 < 1e-12f || ly2 < 1e-12f) return false;
+        float u = vdot(hl, lx) / lx2, v = vdot(hl, ly) / ly2;
+        if (u < -0.5f || u > 0.5f || v < -0.5f || v > 0.5f) return false;
+        *t_out = t;
+        *face_out = (nd < 0.f) ? 1 : 0;
+        return true;
+    }
+    if (type != PT_TRI) return false;
+    V3 v0 = v3(T[3], T[7], T[11]);
+    V3 v1 = v3(T[1] + T[3], T[5] + T[7], T[9] + T[11]);
+    V3 v2 = v3(T[0] + T[1] + T[3], T[4] + T[5] + T[7], T[8] + T[9] + T[11]);
+    float a = v0.x - v1.x, b = v0.x - v2.x, c = d.x, dd = v0.x - o.x;
+    float e = v0.y - v1.y, f = v0.y - v2.y, g = d.y, h = v0.y - o.y;
+    float i = v0.z - v1.z, j = v0.z - v2.z, k = d.z, l = v0.z - o.z;
+    float m = f * k - g * j, nn = h * k - g * l, p = f * l - h * j;
+    float q = g * i - e * k, s = e * j - f * i;
+    float den = a * m + b * q + c * s;
+    if (std::fabs(den) < 1e-12f) return false;
+    float inv = 1.f / den;
+    float beta = (dd * m - b * nn - c * p) * inv;
+    if (beta < 0.f) return false;
+    float r = e * l - h * i;
+    float gamma = (a * nn + dd * q + c * r) * inv;
+    if (gamma < 0.f || beta + gamma > 1.f) return false;
+    float t = (a * p - b * r + dd * s) * inv;
+    if (t < ray.tmin || t > tmax) return false;
+    V3 nrm = vcross(vsub(v1, v0), vsub(v2, v0));
+    *t_out = t;
+    *face_out = (vdot(d, nrm) < 0.f) ? 1 : 0;
+    return true;
+}
+
+// ---------------------------------------------------------------- LBVH -----
+inline uint64_t expand21(uint32_t v) {
+    uint64_t x = v & 0x1FFFFFu;
+    x = (x | (x << 32)) & 0x1F00000000FFFFull;
+    x = (x | (x << 16)) & 0x1F0000FF0000FFull;
+    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+inline uint32_t quant21(float c, float lo, float scale) {
+    float q = (c - lo) * scale;
+    if (!(q > 0.f)) q = 0.f;
+    if (q > 2097151.0f) q = 2097151.0f;
+    return (uint32_t)q;
+}
+inline int clz64(uint64_t x) { return x ? __builtin_clzll(x) : 64; }
+inline int clz32(uint32_t x) { return x ? __builtin_clz(x) : 32; }
+
+// Leaf bounds padding: each face moves out by (|x| + extent) * 2^-20 so that the
+// FP32 slab test never rejects a box holding an accepted primitive hit.
+inline float pad_lo(float x, float ext) { return x - (std::fabs(x) + ext) * 9.5367431640625e-07f; }
+inline float pad_hi(float x, float ext) { return x + (std::fabs(x) + ext) * 9.5367431640625e-07f; }
+
+struct Node {       // BVH2 node: both child boxes + child references
+    float b[12];    // c0.lo.xyz, c0.hi.xyz, c1.lo.xyz, c1.hi.xyz
+    int32_t c[2];   // >= 0: internal node; < 0: ~leaf (sorted primitive slot)
+};
+
+struct Scene {
+    int n = 0;
+    std::vector<float> T;
+    std::vector<uint32_t> type;
+    std::vector<int8_t> twosided;
+    std::vector<Rec> rec;       // original order
+    std::vector<RGen> rgen;     // original order
+    // BVH
+    std::vector<uint64_t> codes;    // sorted Morton codes
+    std::vector<uint32_t> perm;     // sorted slot -> original primitive
+    std::vector<Node> nodes;        // n-1 internal nodes (1 for n == 1)
+    std::vector<float> leaf_lo, leaf_hi;  // padded leaf boxes, sorted order (3 each)
+    float scene_lo[3], scene_hi[3], extent;
+    // periodic boundary (bbox faces appended after the n real primitives)
+    int nbbox = 0;
+    float periodic[2] = {0, 0};
+    std::vector<Rec> bbox;
+};
+
+void build_bvh(Scene &s) {
+    const int n = s.n;
+    std::vector<V3> lo(n), hi(n), cen(n);
+    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float blo[3] = {INFINITY, INFINITY, INFINITY}, bhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = 0; i < n; ++i) {
+        rec_bounds(s.rec[i], &lo[i], &hi[i]);
+        cen[i] = v3((lo[i].x + hi[i].x) * 0.5f, (lo[i].y + hi[i].y) * 0.5f, (lo[i].z + hi[i].z) * 0.5f);
+        for (int k = 0; k < 3; ++k) {
+            clo[k] = std::fmin(clo[k], vget(cen[i], k));
+            chi[k] = std::fmax(chi[k], vget(cen[i], k));
+            blo[k] = std::fmin(blo[k], vget(lo[i], k));
+            bhi[k] = std::fmax(bhi[k], vget(hi[i], k));
+        }
+    }
+    float ext = 0.f;
+    for (int k = 0; k < 3; ++k) {
+        s.scene_lo[k] = blo[k];
+        s.scene_hi[k] = bhi[k];
+        ext = std::fmax(ext, bhi[k] - blo[k]);
+    }
+    s.extent = ext;
+    float scale[3];
+    for (int k = 0; k < 3; ++k) {
+        float e = chi[k] - clo[k];
+        scale[k] = (e > 0.f) ? (2097152.0f / e) : 0.f;
+    }
+    std::vector<std::pair<uint64_t, uint32_t>> kv(n);
+    for (int i = 0; i < n; ++i) {
+        uint64_t code = (expand21(quant21(cen[i].x, clo[0], scale[0])) << 2) |
+                        (expand21(quant21(cen[i].y, clo[1], scale[1])) << 1) |
+                        expand21(quant21(cen[i].z, clo[2], scale[2]));
+        kv[i] = {code, (uint32_t)i};
+    }
+    std::sort(kv.begin(), kv.end());
+    s.codes.resize(n);
+    s.perm.resize(n);
+    s.leaf_lo.resize(3 * (size_t)n);
+    s.leaf_hi.resize(3 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        s.codes[i] = kv[i].first;
+        s.perm[i] = kv[i].second;
+        V3 a = lo[kv[i].second], b = hi[kv[i].second];
+        s.leaf_lo[3 * i + 0] = pad_lo(a.x, ext);
+        s.leaf_lo[3 * i + 1] = pad_lo(a.y, ext);
+        s.leaf_lo[3 * i + 2] = pad_lo(a.z, ext);
+        s.leaf_hi[3 * i + 0] = pad_hi(b.x, ext);
+        s.leaf_hi[3 * i + 1] = pad_hi(b.y, ext);
+        s.leaf_hi[3 * i + 2] = pad_hi(b.z, ext);
+    }
+    // Karras 2012 ("Maximizing parallelism in the construction of BVHs, octrees
+    // and k-d trees", HPG 2012) hierarchy over the sorted codes.
+    const int ni = std::max(n - 1, 1);
+    s.nodes.assign(ni, Node{});
+    std::vector<int32_t> parent_internal(ni, -1), parent_leaf(n, -1);
+    auto delta = [&](int i, int j) -> int {
+        if (j < 0 || j > n - 1) return -1;
+        uint64_t a = s.codes[i], b = s.codes[j];
+        if (a == b) return 64 + clz32((uint32_t)i ^ (uint32_t)j);
+        return clz64(a ^ b);
+    };
+    if (n == 1) {
+        Node &nd = s.nodes[0];
+        nd.c[0] = ~0;
+        nd.c[1] = ~0x7FFFFFFF;  // empty sentinel (box never hit)
+        parent_leaf[0] = 0;
+    } else {
+        for (int i = 0; i < n - 1; ++i) {
+            int dsgn = (delta(i, i + 1) - delta(i, i - 1)) >= 0 ? 1 : -1;
+            int dmin = delta(i, i - dsgn);
+            int lmax = 2;
+            while (delta(i, i + lmax * dsgn) > dmin) lmax *= 2;
+            int l = 0;
+            for (int t = lmax / 2; t >= 1; t /= 2)
+                if (delta(i, i + (l + t) * dsgn) > dmin) l += t;
+            int j = i + l * dsgn;
+            int dnode = delta(i, j);
+            int sp = 0;
+            int t = l;
+            do {
+                t = (t + 1) >> 1;
+                if (delta(i, i + (sp + t) * dsgn) > dnode) sp += t;
+            } while (t > 1);
+            int gamma = i + sp * dsgn + std::min(dsgn, 0);
+            int lo_i = std::min(i, j), hi_i = std::max(i, j);
+            Node &nd = s.nodes[i];
+            if (lo_i == gamma) {
+                nd.c[0] = ~gamma;
+                parent_leaf[gamma] = i;
+            } else {
+                nd.c[0] = gamma;
+                parent_internal[gamma] = i;
+            }
+            if (hi_i == gamma + 1) {
+                nd.c[1] = ~(gamma + 1);
+                parent_leaf[gamma + 1] = i;
+            } else {
+                nd.c[1] = gamma + 1;
+                parent_internal[gamma + 1] = i;
+            }
+        }
+    }
+    // Bottom-up refit: a node's box is the exact min/max union of its children.
+    std::vector<float> nlo(3 * (size_t)ni), nhi(3 * (size_t)ni);
+    std::vector<int> done(ni, 0);
+    auto child_box = [&](int32_t c, float *blo_, float *bhi_) {
+        if (c == ~0x7FFFFFFF) {
+            for (int k = 0; k < 3; ++k) {
+                blo_[k] = INFINITY;
+                bhi_[k] = -INFINITY;
+            }
+        } else if (c < 0) {
+            for (int k = 0; k < 3; ++k) {
+                blo_[k] = s.leaf_lo[3 * (size_t)(~c) + k];
+                bhi_[k] = s.leaf_hi[3 * (size_t)(~c) + k];
+            }
+        } else {
+            for (int k = 0; k < 3; ++k) {
+                blo_[k] = nlo[3 * (size_t)c + k];
+                bhi_[k] = nhi[3 * (size_t)c + k];
+            }
+        }
+    };
+    std::vector<int> order;
+    order.reserve(ni);
+    // post-order via explicit stack
+    {
+        std::vector<std::pair<int, int>> st;
+        st.push_back({0, 0});
+        while (!st.empty()) {
+            auto &top = st.back();
+            int nd = top.first;
+            if (top.second < 2) {
+                int32_t c = s.nodes[nd].c[top.second++];
+                if (c >= 0) st.push_back({c, 0});
+            } else {
+                order.push_back(nd);
+                st.pop_back();
+            }
+        }
+    }
+    for (int nd : order) {
+        float a0[3], b0[3], a1[3], b1[3];
+        child_box(s.nodes[nd].c[0], a0, b0);
+        child_box(s.nodes[nd].c[1], a1, b1);
+        for (int k = 0; k < 3; ++k) {
+            s.nodes[nd].b[k] = a0[k];
+            s.nodes[nd].b[3 + k] = b0[k];
+            s.nodes[nd].b[6 + k] = a1[k];
+            s.nodes[nd].b[9 + k] = b1[k];
+            nlo[3 * (size_t)nd + k] = std::fmin(a0[k], a1[k]);
+            nhi[3 * (size_t)nd + k] = std::fmax(b0[k], b1[k]);
+        }
+    }
+    (void)parent_internal;
+    (void)parent_leaf;
+    (void)done;
+}
+
+// Closest hit.  Ties in t go to the smaller original primitive index.
+struct TraceStats {
+    uint64_t nodes = 0, prims = 0;
+};
+inline bool better(float t, int32_t p, float bt, int32_t bp) {
+    return t < bt || (t == bt && (uint32_t)p < (uint32_t)bp);
+}
+
+Hit trace_bvh(const Scene &s, const Ray &ray, bool anyhit, TraceStats *st) {
+    Hit h{ray.tmax, -1, 0};
+    if (s.n == 0) return h;
+    WT w = wt_setup(ray.d);
+    V3 inv = v3(safe_inv(ray.d.x), safe_inv(ray.d.y), safe_inv(ray.d.z));
+    int32_t stack[128];
+    int sp = 0;
+    int32_t cur = 0;
+    float best = ray.tmax;
+    for (;;) {
+        const Node &nd = s.nodes[cur];
+        if (st) st->nodes++;
+        float tn0, tn1;
+        bool h0 = slab(ray.o, inv, v3(nd.b[0], nd.b[1], nd.b[2]), v3(nd.b[3], nd.b[4], nd.b[5]),
+                       ray.tmin, best, &tn0);
+        bool h1 = slab(ray.o, inv, v3(nd.b[6], nd.b[7], nd.b[8]), v3(nd.b[9], nd.b[10], nd.b[11]),
+                       ray.tmin, best, &tn1);
+        int32_t c0 = nd.c[0], c1 = nd.c[1];
+        // leaves are tested immediately, internal children are traversed near-first
+        int32_t next[2];
+        int nn = 0;
+        for (int k = 0; k < 2; ++k) {
+            bool hk = k == 0 ? h0 : h1;
+            int32_t ck = k == 0 ? c0 : c1;
+            if (!hk) continue;
+            if (ck < 0) {
+                if (ck == ~0x7FFFFFFF) continue;
+                uint32_t slot = (uint32_t)(~ck);
+                int32_t p = (int32_t)s.perm[slot];
+                if (st) st->prims++;
+                float t;
+                int face;
+                if (prim_hit(w, ray, inv, s.rec[p], best, &t, &face)) {
+                    if (h.prim < 0 || better(t, p, h.t, h.prim)) {
+                        h.t = t;
+                        h.prim = p;
+                        h.face = face;
+                        best = t;
+                    }
+                    if (anyhit) return h;
+                }
+            } else {
+                next[nn++] = ck;
+            }
+        }
+        if (nn == 2) {
+            bool swap01 = tn1 < tn0;
+            int32_t nearc = swap01 ? next[1] : next[0];
+            int32_t farc = swap01 ? next[0] : next[1];
+            stack[sp++] = farc;
+            cur = nearc;
+        } else if (nn == 1) {
+            cur = next[0];
+        } else {
+            if (sp == 0) break;
+            cur = stack[--sp];
+        }
+    }
+    return h;
+}
+
+Hit trace_brute(const Scene &s, const Ray &ray, bool reference_formula) {
+    Hit h{ray.tmax, -1, 0};
+    WT w = wt_setup(ray.d);
+    V3 inv = v3(safe_inv(ray.d.x), safe_inv(ray.d.y), safe_inv(ray.d.z));
+    for (int p = 0; p < s.n; ++p) {
+        float t;
+        int face;
+        bool ok = reference_formula
+                      ? prim_hit_reference(ray, &s.T[16 * (size_t)p], (int)s.type[p], ray.tmax, &t, &face)
+                      : prim_hit(w, ray, inv, s.rec[p], ray.tmax, &t, &face);
+        if (ok && (h.prim < 0 || better(t, p, h.t, h.prim))) {
+            h.t = t;
+            h.prim = p;
+            h.face = face;
+        }
+    }
+    return h;
+}
+
+// Periodic walls: closest of the bbox faces (tested separately from the BVH).
+inline bool bbox_closest(const Scene &s, const Ray &ray, float tmax, float *t_out, int *which) {
+    if (s.nbbox == 0) return false;
+    WT w = wt_setup(ray.d);
+    bool any = false;
+    float best = tmax;
+    for (int b = 0; b < s.nbbox; ++b) {
+        float t;
+        int face;
+        if (poly_hit(w, ray, s.bbox[b].p, 4, best, &t, &face)) {
+            if (!any || t < best) {
+                best = t;
+                *which = b;
+                any = true;
+            }
+        }
+    }
+    *t_out = best;
+    return any;
+}
+
+// Full trace with periodic wrapping (<= 10 wraps, OptiX8DeviceCode.cu:1440-1459, 763-789).
+Hit trace_full(const Scene &s, Ray ray, bool anyhit, TraceStats *st) {
+    for (int wrap = 0; wrap < 10; ++wrap) {
+        Hit h = trace_bvh(s, ray, anyhit && s.nbbox == 0, st);
+        if (s.nbbox == 0) return h;
+        float tb;
+        int which = -1;
+        float lim = (h.prim >= 0) ? h.t : ray.tmax;
+        if (!bbox_closest(s, ray, lim, &tb, &which) || (h.prim >= 0 && !(tb < h.t))) return h;
+        // wrap to the opposite wall
+        V3 hp = vadd(ray.o, vscale(ray.d, tb));
+        bool xwall = (s.periodic[0] == 1.f) && which < 2;
+        if (xwall) {
+            float width = s.bbox[1].p[0].x - s.bbox[0].p[0].x;
+            hp.x = hp.x + ((which == 0) ? width : -width);
+        } else {
+            int ybase = (s.periodic[0] == 1.f) ? 2 : 0;
+            float width = s.bbox[ybase + 1].p[0].y - s.bbox[ybase].p[0].y;
+            hp.y = hp.y + ((which == ybase) ? width : -width);
+        }
+        ray.o = hp;
+    }
+    return Hit{ray.tmax, -1, 0};
+}
+
+// ---------------------------------------------------------------- sources ---
+struct Source {
+    int type;        // 0 collimated, 1 sphere, 2 sun sphere, 3 rectangle, 4 disk
+    V3 pos;          // direction (collimated) or centre
+    float w0, w1;    // width / diameter
+    float R[9];      // rotation matrix (row-major) for rect / disk sources
+};
+
+// Sample origin on primitive p: (u, v) are the two uniform numbers.
+inline V3 sample_point(const RGen &g, int type, float u, float v) {
+    if (type == PT_TRI) {
+        float a = u < v ? u : v, b = u < v ? v : u;  // sorted (OptiX8DeviceCode.cu:1288-1289)
+        return v3((g.P.x + a * g.A.x) + b * g.B.x, (g.P.y + a * g.A.y) + b * g.B.y,
+                  (g.P.z + a * g.A.z) + b * g.B.z);
+    }
+    return v3((g.P.x + u * g.A.x) + v * g.B.x, (g.P.y + u * g.A.y) + v * g.B.y,
+              (g.P.z + u * g.A.z) + v * g.B.z);
+}
+
+// Direction (and tmax, FP64 strength) of a direct ray towards source `src`
+// (OptiX8DeviceCode.cu:1329-1415).  Returns false if the source emits away.
+inline bool direct_dir(const Source &src, V3 org, V3 nrm, uint32_t rx, uint32_t ry, double inv_nr,
+                       V3 *dir, float *tmax, double *strength) {
+    if (src.type == 0) {
+        V3 d = vnormalize(src.pos);
+        *dir = d;
+        *tmax = 1e38f;
+        *strength = inv_nr * (double)std::fabs(vdot(nrm, d));
+        return true;
+    }
+    if (src.type == 1 || src.type == 2) {
+        float ct = 1.0f - 2.0f * u01(rx);
+        float st = std::sqrt(std::fmax(0.f, 1.0f - ct * ct));
+        float cp, sp;
+        sincos2pi(u01(ry), &cp, &sp);
+        float r = 0.5f * src.w0;
+        V3 pt = v3(r * st * cp, r * st * sp, r * ct);
+        V3 d = vsub(vadd(pt, src.pos), org);
+        float dist = std::sqrt(vdot(d, d));
+        d = vnormalize(d);
+        double acc = 0.0;
+        const int N = 10;
+        for (int j = 0; j < N; ++j) {
+            float cpj, spj;
+            sincos2pi(((float)j + 0.5f) / (float)N, &cpj, &spj);
+            for (int i = 0; i < N; ++i) {
+                float cti = 1.0f - 2.0f * ((float)i + 0.5f) / (float)N;
+                float sti = std::sqrt(std::fmax(0.f, 1.0f - cti * cti));
+                V3 l = v3(sti * cpj, sti * spj, cti);
+                if (vdot(l, d) < 0.f) {
+                    acc += inv_nr * (double)std::fabs(vdot(nrm, d)) * (double)std::fabs(vdot(l, d)) /
+                           ((double)dist * (double)dist) / (double)(N * N) * (double)src.w0 *
+                           (double)src.w0;
+                }
+            }
+        }
+        *dir = d;
+        *tmax = dist;
+        *strength = acc;
+        return true;
+    }
+    if (src.type == 3 || src.type == 4) {
+        V3 pt;
+        if (src.type == 3) {
+            pt = v3(src.w0 * (-0.5f + u01(rx)), src.w1 * (-0.5f + u01(ry)), 0.f);
+        } else {
+            // concentric square-to-disk map (Shirley & Chiu 1997)
+            float sx = -1.0f + 2.0f * u01(rx), sy = -1.0f + 2.0f * u01(ry);
+            float r, ph;  // ph in units of pi/4
+            if (sx > -sy) {
+                if (sx > sy) { r = sx; ph = sy / sx; }
+                else { r = sy; ph = 2.0f - sx / sy; }
+            } else {
+                if (sx < sy) { r = -sx; ph = 4.0f + sy / sx; }
+                else { r = -sy; ph = (sy != 0.f) ? 6.0f - sx / sy : 0.f; }
+            }
+            float frac = ph * 0.125f;
+            if (frac < 0.f) frac = frac + 1.0f;
+            float c, s;
+            sincos2pi(frac, &c, &s);
+            pt = v3(src.w0 * r * c, src.w0 * r * s, 0.f);
+        }
+        const float *R = src.R;
+        V3 q = v3((R[0] * pt.x + R[1] * pt.y) + R[2] * pt.z, (R[3] * pt.x + R[4] * pt.y) + R[5] * pt.z,
+                  (R[6] * pt.x + R[7] * pt.y) + R[8] * pt.z);
+        V3 ldir = v3(R[2], R[5], R[8]);
+        V3 d = vsub(vadd(q, src.pos), org);
+        if (vdot(d, ldir) > 0.f) return false;
+        float dist = std::sqrt(vdot(d, d));
+        d = vnormalize(d);
+        double area = (src.type == 3) ? (double)src.w0 * (double)src.w1 / M_PI
+                                      : (double)src.w0 * (double)src.w0;
+        *strength = inv_nr * (double)std::fabs(vdot(nrm, d)) * (double)std::fabs(vdot(ldir, d)) /
+                    ((double)dist * (double)dist) * area;
+        *dir = d;
+        *tmax = dist;
+        return true;
+    }
+    return false;
+}
+
+// Diffuse (cosine-weighted, stratified) direction about normal n.
+inline V3 diffuse_dir(V3 n, int ti, int pi, int dimx, int dimy, float j0, float j1) {
+    float Rt = ((float)ti + j0) / (float)dimx;
+    float Rp = ((float)pi + j1) / (float)dimy;
+    float st = std::sqrt(Rt);
+    float ct = std::sqrt(1.0f - Rt);
+    float cp, sp;
+    sincos2pi(Rp, &cp, &sp);
+    float lx = st * cp, ly = st * sp;
+    V3 t1, t2;
+    onb(n, &t1, &t2);
+    return v3((t1.x * lx + t2.x * ly) + n.x * ct, (t1.y * lx + t2.y * ly) + n.y * ct,
+              (t1.z * lx + t2.z * ly) + n.z * ct);
+}
+
+// Sky angular distribution (OptiX8DeviceCode.cu:148-164).
+inline double sky_fd(V3 dir, V3 peak, float K, float knorm, const float *prague) {
+    if (K > 0.f) {
+        double c = std::max(-1.0, std::min(1.0, (double)vdot(peak, dir)));
+        double psi = std::max(std::acos(c), M_PI / 180.0);
+        return std::pow(psi, -(double)K) * (double)knorm;
+    }
+    if (prague[3] > 0.f) {
+        double c = std::max(-1.0, std::min(1.0, (double)vdot(dir, peak)));
+        double gamma = std::acos(c) * 180.0 / M_PI;
+        double cth = std::max((double)dir.z, 0.0);
+        double pat = (1.0 + prague[0] * std::exp(-gamma / prague[1])) * (1.0 + (prague[2] - 1.0) * (1.0 - cth));
+        return pat * prague[3] * M_PI;
+    }
+    return 1.0;
+}
+
+}  // namespace
+
+// ==================================================================== C API ===
+extern "C" {
+
+typedef struct {
+    int32_t n;                // primitives
+    const float *T;           // n*16 row-major transforms
+    const uint32_t *type;     // n (0 patch, 1 triangle, 2 disk, 3 tile, 4 voxel)
+    const int8_t *twosided;   // n (0 one-sided, 1 two-sided, 2 transparent, 3 skip)
+    int32_t nbbox;            // periodic walls (0, 2 or 4)
+    const float *bbox_verts;  // nbbox*4*3 world-space corners
+    float periodic_x, periodic_y;
+} orc_geometry;
+
+typedef struct {
+    int32_t nbands_global;
+    const uint8_t *band_launch;   // [nbands_global]
+    int32_t nsources;
+    const int32_t *source_type;   // [S]
+    const float *source_pos;      // [S*3]
+    const float *source_width;    // [S*2]
+    const float *source_rot;      // [S*9] rotation matrices (row-major) for rect/disk
+    const float *source_flux;     // [S*Bl]
+    const float *rho;             // [S*n*Bg]
+    const float *tau;             // [S*n*Bg]
+    const float *diffuse_flux;    // [Bl]
+    const float *diffuse_ext;     // [Bl] power-law K (0 = off)
+    const float *diffuse_norm;    // [Bl]
+    const float *diffuse_peak;    // [Bl*3]
+    const float *prague;          // [Bl*4]
+    const int32_t *direct_rays;   // [Bl]
+    const int32_t *diffuse_rays;  // [Bl]
+    const int32_t *depth;         // [Bl]
+    const uint8_t *emission;      // [Bl]
+    const float *eps;             // [n*Bl] emissivity (after RadiationModel's rules)
+    const float *temperature;     // [n] K
+    uint32_t seed;
+    int32_t threads;              // OpenMP threads (<=0: all)
+    int32_t prim_limit;           // >0: launch rays only from the first prim_limit primitives (timing samples)
+} orc_solve;
+
+void *orc_scene_create(const orc_geometry *g) {
+    Scene *s = new Scene();
+    s->n = g->n;
+    s->T.assign(g->T, g->T + 16 * (size_t)g->n);
+    s->type.assign(g->type, g->type + g->n);
+    s->twosided.assign(g->twosided, g->twosided + g->n);
+    s->rec.resize(g->n);
+    s->rgen.resize(g->n);
+    for (int i = 0; i < g->n; ++i) {
+        s->rec[i] = make_rec(&s->T[16 * (size_t)i], (int)s->type[i]);
+        s->rgen[i] = make_rgen(&s->T[16 * (size_t)i], (int)s->type[i]);
+    }
+    s->nbbox = g->nbbox;
+    s->periodic[0] = g->periodic_x;
+    s->periodic[1] = g->periodic_y;
+    for (int b = 0; b < g->nbbox; ++b) {
+        Rec r{};
+        r.type = PT_BBOX;
+        for (int v = 0; v < 4; ++v)
+            r.p[v] = v3(g->bbox_verts[12 * b + 3 * v], g->bbox_verts[12 * b + 3 * v + 1],
+                        g->bbox_verts[12 * b + 3 * v + 2]);
+        s->bbox.push_back(r);
+    }
+    if (s->n > 0) build_bvh(*s);
+    return s;
+}
+
+void orc_scene_destroy(void *h) { delete (Scene *)h; }
+
+// Philox4x32-10 block (for known-answer tests).
+void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    U4 u = philox(ctr[0], ctr[1], ctr[2], ctr[3], key[0], key[1]);
+    for (int i = 0; i < 4; ++i) out[i] = u.v[i];
+}
+
+// sincos2pi for a batch (tests of the polynomial against libm).
+void orc_sincos2pi(int64_t n, const float *u, float *c, float *s) {
+    for (int64_t i = 0; i < n; ++i) sincos2pi(u[i], &c[i], &s[i]);
+}
+
+// Export the host-built BVH for bit-exact comparison with the device build.
+// nodes: (n-1) * 16 words: 12 float box words then child0, child1, 0, 0.
+int orc_scene_bvh(void *h, uint64_t *codes, uint32_t *perm, uint32_t *nodes) {
+    Scene *s = (Scene *)h;
+    if (s->n == 0) return 0;
+    std::memcpy(codes, s->codes.data(), sizeof(uint64_t) * s->n);
+    std::memcpy(perm, s->perm.data(), sizeof(uint32_t) * s->n);
+    for (size_t i = 0; i < s->nodes.size(); ++i) {
+        std::memcpy(&nodes[16 * i], s->nodes[i].b, 48);
+        nodes[16 * i + 12] = (uint32_t)s->nodes[i].c[0];
+        nodes[16 * i + 13] = (uint32_t)s->nodes[i].c[1];
+        nodes[16 * i + 14] = 0;
+        nodes[16 * i + 15] = 0;
+    }
+    return (int)s->nodes.size();
+}
+
+// Closest hit for explicit rays.  mode 0: BVH + watertight; 1: brute force + watertight;
+// 2: brute force + reference formulas; 3: BVH any-hit.  counters (may be null):
+// [0] node visits, [1] primitive tests (BVH modes only).
+int orc_trace(void *h, int64_t nrays, const float *o, const float *d, float tmin, float tmax, int mode,
+              int32_t *hit, float *t, int32_t *face, uint64_t *counters, int threads) {
+    Scene *s = (Scene *)h;
+    uint64_t cn = 0, cp = 0;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : cn, cp)
+    for (int64_t i = 0; i < nrays; ++i) {
+        Ray r{v3(o[3 * i], o[3 * i + 1], o[3 * i + 2]), v3(d[3 * i], d[3 * i + 1], d[3 * i + 2]), tmin, tmax};
+        Hit hh;
+        TraceStats st;
+        if (mode == 0 || mode == 3) hh = trace_bvh(*s, r, mode == 3, &st);
+        else hh = trace_brute(*s, r, mode == 2);
+        hit[i] = hh.prim;
+        if (t) t[i] = hh.t;
+        if (face) face[i] = hh.face;
+        cn += st.nodes;
+        cp += st.prims;
+    }
+    if (counters) {
+        counters[0] = cn;
+        counters[1] = cp;
+    }
+    return 0;
+}
+
+// Generate the ray set of one pass, for hit-ID parity.
+// kind 0: direct rays toward collimated direction dir3 (one per stratum, rpp rays per prim);
+// kind 1: diffuse rays (top face, rpp rays per prim).  Outputs n*rpp rays (origin, dir).
+int orc_gen_rays(void *h, int kind, uint32_t seed, uint32_t pass, int32_t rpp, int32_t face,
+                 const float *dir3, float *o, float *d) {
+    Scene *s = (Scene *)h;
+    int dimx = (int)std::sqrt((float)rpp);
+    if (dimx < 1) dimx = 1;
+    int dimy = rpp / dimx;
+    int nr = dimx * dimy;
+    for (int p = 0; p < s->n; ++p) {
+        const RGen &g = s->rgen[p];
+        for (int r = 0; r < nr; ++r) {
+            U4 u = philox((uint32_t)r, (uint32_t)p, (uint32_t)face, 0u, seed, pass);
+            V3 org, dir;
+            if (kind == 0) {
+                int xi = r % dimx, yi = r / dimx;
+                float uu = u01(u.v[0]), vv = u01(u.v[1]);
+                if (s->type[p] != PT_TRI) {
+                    uu = ((float)xi + uu) / (float)dimx;
+                    vv = ((float)yi + vv) / (float)dimy;
+                }
+                org = sample_point(g, (int)s->type[p], uu, vv);
+                dir = vnormalize(v3(dir3[0], dir3[1], dir3[2]));
+            } else {
+                int ti = r % dimx, pi = r / dimx;
+                dir = diffuse_dir(g.N, ti, pi, dimx, dimy, u01(u.v[0]), u01(u.v[1]));
+                if (face == 0) dir = v3(-dir.x, -dir.y, -dir.z);
+                org = sample_point(g, (int)s->type[p], u01(u.v[2]), u01(u.v[3]));
+            }
+            size_t k = (size_t)p * nr + r;
+            o[3 * k] = org.x;
+            o[3 * k + 1] = org.y;
+            o[3 * k + 2] = org.z;
+            d[3 * k] = dir.x;
+            d[3 * k + 1] = dir.y;
+            d[3 * k + 2] = dir.z;
+        }
+    }
+    return nr;
+}
+
+// --------------------------------------------------------------- runBand ---
+// Restatement of RadiationModel::runBand (RadiationModel.cpp:3470-4663) driving the
+// OptiX8 device-program semantics, with FP64 buffers.  flux_out: [n*Bl] =
+// radiation_in + scatter_top + scatter_bottom (RadiationModel.cpp:4652).
+// stats (may be null): [0] rays traced, [1] BVH node visits, [2] primitive tests, [3] hits.
+int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats) {
+    Scene *s = (Scene *)h;
+    const int n = s->n;
+    const int Bg = q->nbands_global;
+    int Bl = 0;
+    for (int b = 0; b < Bg; ++b) Bl += q->band_launch[b] ? 1 : 0;
+    const int S = q->nsources;
+#ifdef _OPENMP
+    if (q->threads > 0) omp_set_num_threads(q->threads);
+#endif
+    std::vector<double> rin((size_t)n * Bl, 0.0), otop((size_t)n * Bl, 0.0), obot((size_t)n * Bl, 0.0),
+        stop((size_t)n * Bl, 0.0), sbot((size_t)n * Bl, 0.0);
+    std::vector<Source> src(S);
+    for (int k = 0; k < S; ++k) {
+        src[k].type = q->source_type[k];
+        src[k].pos = v3(q->source_pos[3 * k], q->source_pos[3 * k + 1], q->source_pos[3 * k + 2]);
+        src[k].w0 = q->source_width[2 * k];
+        src[k].w1 = q->source_width[2 * k + 1];
+        for (int i = 0; i < 9; ++i) src[k].R[i] = q->source_rot ? q->source_rot[9 * k + i] : (i % 4 == 0 ? 1.f : 0.f);
+    }
+    bool rundirect = false;
+    for (int k = 0; k < S; ++k)
+        for (int b = 0; b < Bl; ++b)
+            if (q->source_flux[k * Bl + b] > 0.f) rundirect = true;
+    bool scattering = false, diffuse = false, emission = false;
+    int dirN = 0, difN = 0, depth = 0;
+    for (int b = 0; b < Bl; ++b) {
+        scattering = scattering || q->depth[b] > 0;
+        diffuse = diffuse || q->diffuse_flux[b] > 0.f;
+        emission = emission || q->emission[b];
+        dirN = std::max(dirN, q->direct_rays[b]);
+        difN = std::max(difN, q->diffuse_rays[b]);
+        depth = std::max(depth, q->depth[b]);
+    }
+    uint64_t n_rays = 0, n_nodes = 0, n_prims = 0, n_hits = 0;
+    const int nl = (q->prim_limit > 0 && q->prim_limit < n) ? q->prim_limit : n;
+    auto matidx = [&](int srcid, int p, int bg) { return ((size_t)srcid * n + p) * Bg + bg; };
+
+    // ---- direct pass (OptiX8Backend::launchDirectRays + __raygen__direct + __miss__direct)
+    if (S > 0 && rundirect && dirN > 0) {
+        int dimx = (int)std::sqrt((float)dirN);
+        int dimy = dimx > 0 ? dirN / dimx : 1;
+        double inv_nr = 1.0 / (double)(dimx * dimy);
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : n_rays, n_nodes, n_prims, n_hits)
+        for (int p = 0; p < nl; ++p) {
+            const RGen &g = s->rgen[p];
+            int ts = s->twosided[p];
+            std::vector<double> d_in(Bl, 0.0), d_top(Bl, 0.0), d_bot(Bl, 0.0);
+            for (int r = 0; r < dimx * dimy; ++r) {
+                int xi = r % dimx, yi = r / dimx;
+                for (int k = 0; k < S; ++k) {
+                    U4 u = philox((uint32_t)r, (uint32_t)p, (uint32_t)(k << 1), 0u, q->seed, 0u);
+                    float uu = u01(u.v[0]), vv = u01(u.v[1]);
+                    if (s->type[p] != PT_TRI) {
+                        uu = ((float)xi + uu) / (float)dimx;
+                        vv = ((float)yi + vv) / (float)dimy;
+                    }
+                    V3 org = sample_point(g, (int)s->type[p], uu, vv);
+                    V3 dir;
+                    float tmax;
+                    double strength;
+                    if (!direct_dir(src[k], org, g.N, u.v[2], u.v[3], inv_nr, &dir, &tmax, &strength)) continue;
+                    bool face = vdot(dir, g.N) > 0.f;
+                    if (!face && ts == 0) continue;
+                    if (ts == 3) continue;
+                    TraceStats st;
+                    Hit hh = trace_full(*s, Ray{org, dir, 1e-4f, tmax}, true, &st);
+                    n_rays++;
+                    n_nodes += st.nodes;
+                    n_prims += st.prims;
+                    if (hh.prim >= 0) {
+                        n_hits++;
+                        continue;
+                    }
+                    int b = -1;
+                    for (int bg = 0; bg < Bg; ++bg) {
+                        if (!q->band_launch[bg]) continue;
+                        ++b;
+                        float rho = q->rho[matidx(k, p, bg)], tau = q->tau[matidx(k, p, bg)];
+                        double str = strength * (double)q->source_flux[k * Bl + b];
+                        d_in[b] += str * (1.0 - rho - tau);
+                        if (rho > 0.f || tau > 0.f) {
+                            if (face) {
+                                d_top[b] += str * rho;
+                                d_bot[b] += str * tau;
+                            } else {
+                                d_bot[b] += str * rho;
+                                d_top[b] += str * tau;
+                            }
+                        }
+                    }
+                }
+            }
+            for (int b = 0; b < Bl; ++b) {
+                rin[(size_t)p * Bl + b] += d_in[b];
+                stop[(size_t)p * Bl + b] += d_top[b];
+                sbot[(size_t)p * Bl + b] += d_bot[b];
+            }
+        }
+    }
+
+    // ---- diffuse launch (OptiX8Backend::launchDiffuseRays + __raygen__diffuse +
+    //      __closesthit__diffuse / __miss__diffuse); flags = launched-band mask
+    auto diffuse_pass = [&](int face, uint32_t pass, const std::vector<uint8_t> &flags,
+                            const std::vector<float> &dflux) {
+        int rpp = (int)std::ceil(std::sqrt((double)difN));
+        rpp = rpp * rpp;
+        if (rpp == 0 || n == 0) return;
+        int dimx = (int)std::sqrt((float)rpp);
+        int dimy = dimx > 0 ? rpp / dimx : 1;
+        double strength = 1.0 / (double)(dimx * dimy);
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : n_rays, n_nodes, n_prims, n_hits)
+        for (int p = 0; p < nl; ++p) {
+            int ts = s->twosided[p];
+            if (face == 0 && ts == 0) continue;
+            if (face == 1 && ts == 3) continue;
+            if (face == 0 && ts != 1) continue;
+            const RGen &g = s->rgen[p];
+            std::vector<double> d_in(Bl, 0.0), d_top(Bl, 0.0), d_bot(Bl, 0.0);
+            for (int r = 0; r < dimx * dimy; ++r) {
+                int ti = r % dimx, pi = r / dimx;
+                U4 u = philox((uint32_t)r, (uint32_t)p, (uint32_t)face, 0u, q->seed, pass);
+                V3 dir = diffuse_dir(g.N, ti, pi, dimx, dimy, u01(u.v[0]), u01(u.v[1]));
+                if (face == 0) dir = v3(-dir.x, -dir.y, -dir.z);
+                V3 org = sample_point(g, (int)s->type[p], u01(u.v[2]), u01(u.v[3]));
+                TraceStats st;
+                Hit hh = trace_full(*s, Ray{org, dir, 1e-4f, 1e38f}, false, &st);
+                n_rays++;
+                n_nodes += st.nodes;
+                n_prims += st.prims;
+                if (hh.prim >= 0) n_hits++;
+                int b = -1;
+                for (int bg = 0; bg < Bg; ++bg) {
+                    if (!flags[bg]) continue;
+                    ++b;
+                    double val;
+                    if (hh.prim >= 0) {
+                        size_t ih = (size_t)hh.prim * Bl + b;
+                        val = (hh.face ? otop[ih] : obot[ih]) * strength;
+                        if (val == 0.0) continue;
+                    } else {
+                        if (!(dflux[b] > 0.f)) continue;
+                        V3 pk = q->diffuse_peak ? v3(q->diffuse_peak[3 * b], q->diffuse_peak[3 * b + 1], q->diffuse_peak[3 * b + 2])
+                                                : v3(0.f, 0.f, 1.f);
+                        float K = q->diffuse_ext ? q->diffuse_ext[b] : 0.f;
+                        float kn = q->diffuse_norm ? q->diffuse_norm[b] : 1.f;
+                        float zero4[4] = {0, 0, 0, 0};
+                        const float *pr = q->prague ? &q->prague[4 * b] : zero4;
+                        val = sky_fd(dir, pk, K, kn, pr) * (double)dflux[b] * strength;
+                    }
+                    float rho = q->rho[matidx(0, p, bg)], tau = q->tau[matidx(0, p, bg)];
+                    d_in[b] += val * (1.0 - rho - tau);
+                    if (rho > 0.f || tau > 0.f) {
+                        if (face) {
+                            d_top[b] += val * rho;
+                            d_bot[b] += val * tau;
+                        } else {
+                            d_bot[b] += val * rho;
+                            d_top[b] += val * tau;
+                        }
+                    }
+                }
+            }
+            for (int b = 0; b < Bl; ++b) {
+                rin[(size_t)p * Bl + b] += d_in[b];
+                stop[(size_t)p * Bl + b] += d_top[b];
+                sbot[(size_t)p * Bl + b] += d_bot[b];
+            }
+        }
+    };
+
+    std::vector<uint8_t> flags(q->band_launch, q->band_launch + Bg);
+    std::vector<float> dflux(q->diffuse_flux, q->diffuse_flux + Bl);
+    std::vector<double> ftop((size_t)n * Bl, 0.0), fbot((size_t)n * Bl, 0.0);
+    if (scattering && rundirect) {
+        ftop = stop;
+        fbot = sbot;
+        for (int p = 0; p < n; ++p) {
+            if (s->twosided[p] != 0) continue;
+            for (int b = 0; b < Bl; ++b) {
+                size_t i = (size_t)p * Bl + b;
+                double tot = ftop[i] + fbot[i];
+                ftop[i] = tot;
+                fbot[i] = tot;
+            }
+        }
+        otop = ftop;
+        obot = fbot;
+        std::fill(stop.begin(), stop.end(), 0.0);
+        std::fill(sbot.begin(), sbot.end(), 0.0);
+    }
+    if (emission || diffuse) {
+        if (emission) {
+            const float sigma = 5.6703744e-8f;
+            for (int b = 0; b < Bl; ++b) {
+                if (!q->emission[b]) continue;
+                for (int p = 0; p < n; ++p) {
+                    float eps = q->eps[(size_t)p * Bl + b];
+                    if (q->depth[b] == 0 && eps != 1.f) eps = 1.f;
+                    double T = (double)q->temperature[p];
+                    float out = (float)((double)(sigma * eps) * (T * T * T * T));
+                    size_t i = (size_t)p * Bl + b;
+                    ftop[i] += out;
+                    if (s->twosided[p] != 0) fbot[i] += out;
+                }
+            }
+        }
+        otop = ftop;
+        obot = fbot;
+        diffuse_pass(1, 1u, flags, dflux);
+        diffuse_pass(0, 1u, flags, dflux);
+    }
+    if (scattering && (emission || diffuse) && !rundirect) {
+        otop = stop;
+        obot = sbot;
+        std::fill(stop.begin(), stop.end(), 0.0);
+        std::fill(sbot.begin(), sbot.end(), 0.0);
+    }
+    if (scattering && (emission || diffuse || rundirect)) {
+        std::fill(dflux.begin(), dflux.end(), 0.f);
+        std::vector<uint8_t> sflags = flags;
+        for (int it = 0; it < depth; ++it) {
+            int b = -1;
+            for (int bg = 0; bg < Bg; ++bg) {
+                if (!sflags[bg]) continue;
+                ++b;
+                if (it + 1 > q->depth[b]) sflags[bg] = 0;
+            }
+            if (it > 0 || (emission && rundirect)) {
+                otop = stop;
+                obot = sbot;
+            }
+            std::fill(stop.begin(), stop.end(), 0.0);
+            std::fill(sbot.begin(), sbot.end(), 0.0);
+            diffuse_pass(1, 2u + (uint32_t)it, sflags, dflux);
+            diffuse_pass(0, 2u + (uint32_t)it, sflags, dflux);
+        }
+    }
+    for (size_t i = 0; i < (size_t)n * Bl; ++i) flux_out[i] = rin[i] + stop[i] + sbot[i];
+    if (stats) {
+        stats[0] = n_rays;
+        stats[1] = n_nodes;
+        stats[2] = n_prims;
+        stats[3] = n_hits;
+    }
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,213 @@
+"""ctypes front end of the CPU FP64 oracle (test infrastructure only).
+
+Only tests/, ``__graft_entry__.smoke()`` (as the checker) and bench.py's CPU
+baseline legs import this module.  The product path never does.
+
+The oracle restates the reference's radiation solve (PlantSimulationLab/Helios,
+``plugins/radiation``): ray generation and energy deposition of
+``src/optix8/OptiX8DeviceCode.cu`` and the pass orchestration of
+``RadiationModel::runBand`` (``src/RadiationModel.cpp:3470-4663``).  See
+``hrt_oracle.cpp`` for line-level citations.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libhrt_oracle.so")
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle shared library with its Makefile (gcc, OpenMP)."""
+    src = os.path.join(_HERE, "hrt_oracle.cpp")
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+class _Geometry(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32),
+        ("T", C.c_void_p),
+        ("type", C.c_void_p),
+        ("twosided", C.c_void_p),
+        ("nbbox", C.c_int32),
+        ("bbox_verts", C.c_void_p),
+        ("periodic_x", C.c_float),
+        ("periodic_y", C.c_float),
+    ]
+
+
+class _Solve(C.Structure):
+    _fields_ = [
+        ("nbands_global", C.c_int32),
+        ("band_launch", C.c_void_p),
+        ("nsources", C.c_int32),
+        ("source_type", C.c_void_p),
+        ("source_pos", C.c_void_p),
+        ("source_width", C.c_void_p),
+        ("source_rot", C.c_void_p),
+        ("source_flux", C.c_void_p),
+        ("rho", C.c_void_p),
+        ("tau", C.c_void_p),
+        ("diffuse_flux", C.c_void_p),
+        ("diffuse_ext", C.c_void_p),
+        ("diffuse_norm", C.c_void_p),
+        ("diffuse_peak", C.c_void_p),
+        ("prague", C.c_void_p),
+        ("direct_rays", C.c_void_p),
+        ("diffuse_rays", C.c_void_p),
+        ("depth", C.c_void_p),
+        ("emission", C.c_void_p),
+        ("eps", C.c_void_p),
+        ("temperature", C.c_void_p),
+        ("seed", C.c_uint32),
+        ("threads", C.c_int32),
+        ("prim_limit", C.c_int32),
+    ]
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        _lib.orc_scene_create.restype = C.c_void_p
+        _lib.orc_scene_create.argtypes = [C.POINTER(_Geometry)]
+        _lib.orc_scene_destroy.argtypes = [C.c_void_p]
+        _lib.orc_scene_bvh.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_trace.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_float, C.c_float,
+                                   C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        _lib.orc_gen_rays.argtypes = [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32,
+                                      C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_run_band.argtypes = [C.c_void_p, C.POINTER(_Solve), C.c_void_p, C.c_void_p]
+        _lib.orc_philox.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_sincos2pi.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class OracleScene:
+    """Host scene: primitive records, the host LBVH twin and the FP64 solver."""
+
+    def __init__(self, T, ptype, twosided, bbox_verts=None, periodic=(0.0, 0.0)):
+        lib = _load()
+        self.T = np.ascontiguousarray(T, dtype=np.float32).reshape(-1, 16)
+        self.n = self.T.shape[0]
+        self.type = np.ascontiguousarray(ptype, dtype=np.uint32)
+        self.twosided = np.ascontiguousarray(twosided, dtype=np.int8)
+        self.bbox = None if bbox_verts is None else np.ascontiguousarray(bbox_verts, dtype=np.float32)
+        g = _Geometry(self.n, _ptr(self.T), _ptr(self.type), _ptr(self.twosided),
+                      0 if self.bbox is None else self.bbox.shape[0], _ptr(self.bbox),
+                      float(periodic[0]), float(periodic[1]))
+        self._h = lib.orc_scene_create(C.byref(g))
+
+    def close(self):
+        if self._h:
+            _load().orc_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def bvh(self):
+        n = self.n
+        codes = np.zeros(n, np.uint64)
+        perm = np.zeros(n, np.uint32)
+        nodes = np.zeros((max(n - 1, 1), 16), np.uint32)
+        _load().orc_scene_bvh(self._h, _ptr(codes), _ptr(perm), _ptr(nodes))
+        return codes, perm, nodes
+
+    def trace(self, o, d, mode=0, tmin=1e-4, tmax=1e38, threads=0):
+        """mode 0: BVH closest hit; 1: brute force; 2: brute force, reference formulas; 3: BVH any hit."""
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        nr = o.shape[0]
+        hit = np.zeros(nr, np.int32)
+        t = np.zeros(nr, np.float32)
+        face = np.zeros(nr, np.int32)
+        cnt = np.zeros(2, np.uint64)
+        _load().orc_trace(self._h, nr, _ptr(o), _ptr(d), tmin, tmax, mode, _ptr(hit), _ptr(t), _ptr(face),
+                          _ptr(cnt), threads)
+        return hit, t, face, cnt
+
+    def gen_rays(self, kind, seed, pass_id, rpp, face=1, direction=(0.0, 0.0, 1.0)):
+        dimx = max(int(np.sqrt(np.float32(rpp))), 1)
+        nr = dimx * (rpp // dimx)
+        o = np.zeros((self.n * nr, 3), np.float32)
+        d = np.zeros((self.n * nr, 3), np.float32)
+        dir3 = np.asarray(direction, np.float32)
+        _load().orc_gen_rays(self._h, kind, seed, pass_id, rpp, face, _ptr(dir3), _ptr(o), _ptr(d))
+        return o, d
+
+    def run_band(self, solve: dict, threads=0, prim_limit=0):
+        """Solve one runBand call; returns (flux [n, Bl] float64, stats dict)."""
+        keep = []
+
+        def arr(key, dtype, default=None):
+            v = solve.get(key, default)
+            if v is None:
+                return None
+            a = np.ascontiguousarray(v, dtype=dtype)
+            keep.append(a)
+            return a
+
+        band_launch = arr("band_launch", np.uint8)
+        bl = int(band_launch.sum())
+        s = _Solve()
+        s.nbands_global = band_launch.shape[0]
+        s.band_launch = _ptr(band_launch)
+        src_type = arr("source_type", np.int32)
+        s.nsources = 0 if src_type is None else src_type.shape[0]
+        s.source_type = _ptr(src_type)
+        s.source_pos = _ptr(arr("source_pos", np.float32))
+        s.source_width = _ptr(arr("source_width", np.float32))
+        s.source_rot = _ptr(arr("source_rot", np.float32))
+        s.source_flux = _ptr(arr("source_flux", np.float32))
+        s.rho = _ptr(arr("rho", np.float32))
+        s.tau = _ptr(arr("tau", np.float32))
+        s.diffuse_flux = _ptr(arr("diffuse_flux", np.float32))
+        s.diffuse_ext = _ptr(arr("diffuse_ext", np.float32))
+        s.diffuse_norm = _ptr(arr("diffuse_norm", np.float32))
+        s.diffuse_peak = _ptr(arr("diffuse_peak", np.float32))
+        s.prague = _ptr(arr("prague", np.float32))
+        s.direct_rays = _ptr(arr("direct_rays", np.int32))
+        s.diffuse_rays = _ptr(arr("diffuse_rays", np.int32))
+        s.depth = _ptr(arr("depth", np.int32))
+        s.emission = _ptr(arr("emission", np.uint8))
+        s.eps = _ptr(arr("eps", np.float32))
+        s.temperature = _ptr(arr("temperature", np.float32))
+        s.seed = int(solve.get("seed", 0)) & 0xFFFFFFFF
+        s.threads = int(threads)
+        s.prim_limit = int(prim_limit)
+        flux = np.zeros((self.n, bl), np.float64)
+        stats = np.zeros(4, np.uint64)
+        _load().orc_run_band(self._h, C.byref(s), _ptr(flux), _ptr(stats))
+        return flux, {"rays": int(stats[0]), "nodes": int(stats[1]), "prims": int(stats[2]),
+                      "hits": int(stats[3])}
+
+
+def philox(ctr, key):
+    c = np.ascontiguousarray(ctr, np.uint32)
+    k = np.ascontiguousarray(key, np.uint32)
+    out = np.zeros(4, np.uint32)
+    _load().orc_philox(_ptr(c), _ptr(k), _ptr(out))
+    return out
+
+
+def sincos2pi(u):
+    u = np.ascontiguousarray(u, np.float32)
+    c = np.zeros_like(u)
+    s = np.zeros_like(u)
+    _load().orc_sincos2pi(u.size, _ptr(u), _ptr(c), _ptr(s))
+    return c, s

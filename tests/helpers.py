@@ -1,0 +1,63 @@
+"""Shared helpers: run one runBand through the oracle or the GPU engine."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def rotation_np(r):
+    """Row-major 3x3 rotation of rect/disk sources (same formula as hrt_source_rotation)."""
+    sx, cx = math.sin(r[0]), math.cos(r[0])
+    sy, cy = math.sin(r[1]), math.cos(r[1])
+    sz, cz = math.sin(r[2]), math.cos(r[2])
+    return np.array([cz * cy, cz * sy * sx - sz * cx, cz * sy * cx + sz * sx,
+                     sz * cy, sz * sy * sx + cz * cx, sz * sy * cx - cz * sx,
+                     -sy, cy * sx, cy * cx], np.float32)
+
+
+def oracle_solve(desc: dict, rotation=rotation_np) -> dict:
+    """Convert a RadiationModel.solve_description() dict to the oracle's solve dict."""
+    srcs = desc["sources"]
+    d = {k: desc[k] for k in ("band_launch", "source_flux", "rho", "tau", "diffuse_flux", "diffuse_ext",
+                              "diffuse_norm", "diffuse_peak", "prague", "direct_rays", "diffuse_rays", "depth",
+                              "emission", "eps", "temperature", "seed")}
+    d["source_type"] = np.array([s["type"] for s in srcs], np.int32)
+    d["source_pos"] = np.array([s["position"] for s in srcs], np.float32)
+    d["source_width"] = np.array([s["width"] for s in srcs], np.float32)
+    d["source_rot"] = np.stack([rotation(s.get("rotation", (0, 0, 0))) for s in srcs]).astype(np.float32)
+    return d
+
+
+def oracle_scene_for(rad, oracle_mod):
+    T, ty, ts = rad.geometry_arrays()
+    bb = rad._bbox_faces()
+    return oracle_mod.OracleScene(T, ty, ts, bb, rad.periodic)
+
+
+def run_oracle(rad, labels, oracle_mod, scene=None, seed=None, threads=0):
+    """Flux [n, Bl] (float64) of one runBand computed by the FP64 oracle."""
+    desc = rad.solve_description(labels, seed=seed)
+    sc = scene or oracle_scene_for(rad, oracle_mod)
+    flux, stats = sc.run_band(oracle_solve(desc), threads=threads)
+    return flux, stats
+
+
+def beer_diffuse(lai, n=50):
+    """Hemispherical integral of canopy interception under isotropic sky (selfTest.cpp:1453-1462)."""
+    dth = 0.5 * math.pi / n
+    acc = 0.0
+    for i in range(n):
+        th = (i + 0.5) * dth
+        acc += 2.0 * (1.0 - math.exp(-0.5 * lai / math.cos(th))) * math.cos(th) * math.sin(th) * dth
+    return acc
+
+
+def view_factor_parallel(a, b, c):
+    """F12 of two directly opposed a x b rectangles at distance c (selfTest.cpp:685-686)."""
+    X, Y = a / c, b / c
+    X2, Y2 = X * X, Y * Y
+    return 2.0 / (math.pi * X * Y) * (math.log(math.sqrt((1 + X2) * (1 + Y2) / (1 + X2 + Y2)))
+                                      + X * math.sqrt(1 + Y2) * math.atan(X / math.sqrt(1 + Y2))
+                                      + Y * math.sqrt(1 + X2) * math.atan(Y / math.sqrt(1 + X2))
+                                      - X * math.atan(X) - Y * math.atan(Y))

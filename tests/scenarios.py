@@ -1,0 +1,237 @@
+"""Known-answer radiation scenarios restated from the reference's own tests
+(plugins/radiation/tests/selfTest.cpp).  Each builds a Context + RadiationModel
+exactly as the reference test does and returns (name, value, expected, tol)
+checks; ``run(rad, labels, seed)`` executes one runBand on some engine (the
+oracle on CPU or libhrt on the GPU) and returns the flux array [n, Bl]."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from helios_gb300 import scenes
+from helios_gb300.radiation import SIGMA, Context, RadiationModel
+
+from helpers import beer_diffuse, view_factor_parallel
+
+
+def _ensemble(run, rad, labels, k, seed0=11):
+    acc = None
+    for i in range(k):
+        f = np.asarray(run(rad, labels, seed0 + 7919 * i), np.float64)
+        acc = f if acc is None else acc + f
+    return acc / k
+
+
+def simple_direct(run):
+    """selfTest.cpp:518-545"""
+    ctx = Context()
+    p = ctx.addPatch((0, 0, 0), (1, 1))
+    ctx.setPrimitiveData(p, "twosided_flag", 0)
+    ctx.setPrimitiveData(p, "reflectivity_SW", 0.0)
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("SW")
+    rad.disableEmission("SW")
+    sun = rad.addCollimatedRadiationSource((0, 0, 1))
+    rad.setSourceFlux(sun, "SW", 1000.0)
+    rad.setDirectRayCount("SW", 10000)
+    rad.setScatteringDepth("SW", 0)
+    f = run(rad, ["SW"], 3)
+    return [("simple_direct", float(f[0, 0]), 1000.0, 0.01)]
+
+
+def black_parallel_rectangles(run, ensemble=8, rays=50000):
+    """selfTest.cpp:670-729"""
+    a, b, c = 1.0, 2.0, 0.5
+    F12 = view_factor_parallel(a, b, c)
+    ctx = Context()
+    p0 = ctx.addPatch((0, 0, 0), (a, b))
+    p1 = ctx.addPatch((0, 0, c), (a, b), (math.pi, 0.0))
+    ctx.setPrimitiveData(p0, "twosided_flag", 0)
+    ctx.setPrimitiveData(p1, "twosided_flag", 0)
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("SW")
+    rad.disableEmission("SW")
+    rad.setDiffuseRayCount("SW", rays)
+    rad.setDiffuseRadiationFlux("SW", 1.0)
+    rad.setScatteringDepth("SW", 0)
+    f = _ensemble(run, rad, ["SW"], ensemble)
+    return [("black_rect_0", f[0, 0], 1 - F12, 0.005), ("black_rect_1", f[1, 0], 1 - F12, 0.005)]
+
+
+def gray_parallel_rectangles(run, ensemble=4, rays=100000):
+    """selfTest.cpp:731-807 (emission + 5 scattering iterations)."""
+    eps, rho, T0, T1 = 0.6, 0.4, 300.0, 300.0
+    a, b, c = 1.0, 2.0, 0.5
+    F12 = view_factor_parallel(a, b, c)
+    s = SIGMA
+    ex0 = (eps * (1 / eps - 1) * F12 * s * (T1 ** 4 - F12 * T0 ** 4) + s * (T0 ** 4 - F12 * T1 ** 4)) / (
+        1 / eps - (1 / eps - 1) * F12 * eps * (1 / eps - 1) * F12) - eps * s * T0 ** 4
+    ex1 = abs(eps * ((1 / eps - 1) * F12 * (ex0 + eps * s * T0 ** 4) + s * (T1 ** 4 - F12 * T0 ** 4)) - eps * s * T1 ** 4)
+    ex0 = abs(ex0)
+    ctx = Context()
+    ctx.addPatch((0, 0, 0), (a, b))
+    ctx.addPatch((0, 0, c), (a, b), (math.pi, 0.0))
+    for p, T in ((0, T0), (1, T1)):
+        ctx.setPrimitiveData(p, "temperature", T)
+        ctx.setPrimitiveData(p, "emissivity_LW", eps)
+        ctx.setPrimitiveData(p, "reflectivity_LW", rho)
+        ctx.setPrimitiveData(p, "twosided_flag", 0)
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("LW")
+    rad.setDirectRayCount("LW", rays)
+    rad.setDiffuseRayCount("LW", rays)
+    rad.setDiffuseRadiationFlux("LW", 0.0)
+    rad.setScatteringDepth("LW", 5)
+    f = _ensemble(run, rad, ["LW"], ensemble)
+    return [("gray_rect_0", f[0, 0], ex0, 0.005), ("gray_rect_1", f[1, 0], ex1, 0.005)]
+
+
+def common_edge_squares(run, ensemble=4, ndiff=100000, ndir=5000):
+    """selfTest.cpp:585-668: LW view factor 0.2 and one SW scattering bounce."""
+    Qs = 1000.0
+    ctx = Context()
+    u0 = ctx.addPatch((0, 0, 0), (1, 1))
+    u1 = ctx.addPatch((0.5, 0, 0.5), (1, 1), (0.5 * math.pi, -0.5 * math.pi))
+    ctx.setPrimitiveData(u0, "twosided_flag", 0)
+    ctx.setPrimitiveData(u1, "twosided_flag", 0)
+    ctx.setPrimitiveData(0, "temperature", 300.0)
+    ctx.setPrimitiveData(1, "temperature", 0.0)
+    ctx.setPrimitiveData(0, "reflectivity_SW", 0.3)
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("LW")
+    rad.setDirectRayCount("LW", ndiff)
+    rad.setDiffuseRayCount("LW", ndiff)
+    rad.setScatteringDepth("LW", 0)
+    sun = rad.addCollimatedRadiationSource((0, 0, 1))
+    rad.addRadiationBand("SW")
+    rad.disableEmission("SW")
+    rad.setDirectRayCount("SW", ndir)
+    rad.setDiffuseRayCount("SW", ndir)
+    rad.setScatteringDepth("SW", 1)
+    rad.setSourceFlux(sun, "SW", Qs)
+    f = _ensemble(run, rad, ["LW", "SW"], ensemble)
+    lw, sw = 0, 1  # std::map order: LW < SW
+    return [("edge_sw_0", f[0, sw], 0.7 * Qs, 0.005), ("edge_sw_1", f[1, sw], 0.3 * 0.2 * Qs, 0.005),
+            ("edge_lw_0", f[0, lw], 0.0, 0.0), ("edge_lw_1", f[1, lw], SIGMA * 300.0 ** 4 * 0.2, 0.005)]
+
+
+def second_law_box(run, rays=50000, eps=0.8):
+    """selfTest.cpp:1061-1132: closed isothermal box, absorbed flux = eps*sigma*T^4."""
+    ctx = Context()
+    L, nd = 10.0, 5
+    h = L / nd
+    faces = []
+    for i in range(nd):
+        for j in range(nd):
+            u, v = -0.5 * L + (i + 0.5) * h, -0.5 * L + (j + 0.5) * h
+            # inward normals: floor +z, ceiling -z, walls toward the centre
+            faces.append(((u, v, 0.0), (0.0, 0.0)))
+            faces.append(((u, v, L), (math.pi, 0.0)))
+    for T, n in _walls(L, nd):
+        ctx.addPrimitives(T[None], scenes.PATCH, h * h)
+    for c, rot in faces:
+        ctx.addPatch(c, (h, h), rot)
+    nprim = ctx.getPrimitiveCount()
+    uu = np.arange(nprim)
+    ctx.setPrimitiveData(uu, "twosided_flag", np.zeros(nprim))
+    ctx.setPrimitiveData(uu, "emissivity_LW", np.full(nprim, eps))
+    ctx.setPrimitiveData(uu, "reflectivity_LW", np.full(nprim, 1 - eps))
+    ctx.setPrimitiveData(uu, "temperature", np.full(nprim, 300.0))
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("LW")
+    rad.setDiffuseRayCount("LW", rays)
+    rad.setDiffuseRadiationFlux("LW", 0.0)
+    rad.setScatteringDepth("LW", 5)
+    f = run(rad, ["LW"], 5)[:, 0]
+    ref = eps * SIGMA * 300.0 ** 4
+    err = float(np.mean(np.abs(f - ref) / ref))
+    return [("second_law_mean_rel_err", err, 0.0, 0.005)]
+
+
+def _walls(L, nd):
+    """Inward-facing wall patches of a box [-L/2, L/2]^2 x [0, L]."""
+    h = L / nd
+    out = []
+    for i in range(nd):
+        for j in range(nd):
+            u = -0.5 * L + (i + 0.5) * h
+            z = (j + 0.5) * h
+            for normal, centre in (((1, 0, 0), (-0.5 * L, u, z)), ((-1, 0, 0), (0.5 * L, u, z)),
+                                   ((0, 1, 0), (u, -0.5 * L, z)), ((0, -1, 0), (u, 0.5 * L, z))):
+                T = scenes.frame_T(np.array([centre], np.float64), [h], [h], np.array([normal], np.float64),
+                                   np.zeros(1))[0]
+                out.append((T, normal))
+    return out
+
+
+def canopy_beer(run, n_leaves=10000, lai=2.0, zenith=30.0, periodic=True, ndir=100, ndiff=300, ground_div=20,
+                leaf=0.1):
+    """Beer's-law interception of a homogeneous canopy with spherical leaf angles
+    (selfTest.cpp:1372-1468 and the periodic-boundary variant :1625-1717).  The ground
+    extends half a leaf diagonal past the leaf domain so that every downward ray ends on
+    it; LAI and interception are taken over the ground area."""
+    dom = math.sqrt(n_leaves * leaf * leaf / lai)
+    margin = leaf * math.sqrt(0.5)
+    sc = scenes.homogeneous_canopy(n_leaves=n_leaves, leaf=leaf, domain=dom, zlo=0.5 * leaf, zhi=3.0, seed=0,
+                                   ground_div=ground_div, ground_margin=margin)
+    ctx = Context()
+    ctx.addScene(sc)
+    rad = RadiationModel(ctx)
+    if periodic:
+        rad.enforcePeriodicBoundary("xy")
+    th = math.radians(zenith)
+    rad.addRadiationBand("direct")
+    rad.disableEmission("direct")
+    rad.setDirectRayCount("direct", ndir)
+    sun = rad.addCollimatedRadiationSource(scenes.sun_direction(zenith, 0.0))
+    rad.setSourceFlux(sun, "direct", 1.0 / math.cos(th))
+    rad.addRadiationBand("diffuse")
+    rad.disableEmission("diffuse")
+    rad.setDiffuseRayCount("diffuse", ndiff)
+    rad.setDiffuseRadiationFlux("diffuse", 1.0)
+    fd = run(rad, ["direct"], 21)[:, 0]
+    fdf = run(rad, ["diffuse"], 22)[:, 0]
+    leaves = sc.groups["leaves"]
+    g = sc.groups["ground"]
+    area_g = float(sc.area[g].sum())
+    lai_eff = n_leaves * leaf * leaf / area_g
+    leaf_dir = float((fd[leaves] * sc.area[leaves]).sum() / area_g)
+    leaf_dif = float((fdf[leaves] * sc.area[leaves]).sum() / area_g)
+    gd = float((fd[g] * sc.area[g]).sum() / area_g)
+    gdf = float((fdf[g] * sc.area[g]).sum() / area_g)
+    beer_dir = 1.0 - math.exp(-0.5 * lai_eff / math.cos(th))
+    beer_dif = beer_diffuse(lai_eff)
+    return [("canopy_ground_direct", 1.0 - gd, beer_dir, 0.01),
+            ("canopy_leaf_direct", leaf_dir, beer_dir, 0.01),
+            ("canopy_ground_diffuse", 1.0 - gdf, beer_dif, 0.01),
+            ("canopy_leaf_diffuse", leaf_dif, beer_dif, 0.01)]
+
+
+def launch_batching(run):
+    """selfTest.cpp:9889-9925: every primitive of a 40x40 tile gets 1000 W/m^2 +- 2%."""
+    ctx = Context()
+    uu = ctx.addTile((0, 0, 0), (10, 10), (0.0, 0.0), (40, 40))
+    ctx.setPrimitiveData(np.asarray(uu), "twosided_flag", np.zeros(len(uu)))
+    ctx.setPrimitiveData(np.asarray(uu), "reflectivity_SW", np.zeros(len(uu)))
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("SW")
+    rad.disableEmission("SW")
+    sun = rad.addCollimatedRadiationSource((0, 0, 1))
+    rad.setSourceFlux(sun, "SW", 1000.0)
+    rad.setDirectRayCount("SW", 100)
+    rad.setScatteringDepth("SW", 0)
+    f = run(rad, ["SW"], 9)[:, 0]
+    return [("batch_min", float(f.min()), 1000.0, 0.02), ("batch_max", float(f.max()), 1000.0, 0.02)]
+
+
+def check(results, abs_tol_names=()):
+    bad = []
+    for name, val, exp, tol in results:
+        if name.startswith("canopy") or name in abs_tol_names or exp == 0.0:
+            err = abs(val - exp)
+        else:
+            err = abs(val - exp) / abs(exp)
+        if not err <= tol:
+            bad.append(f"{name}: got {val:.6g}, expected {exp:.6g}, err {err:.3g} > {tol}")
+    return bad

@@ -1,0 +1,284 @@
+"""GPU parity: libhrt (sm_103a) against the CPU oracle through the C ABI.
+
+Bit-exact: device LBVH vs host build, generated ray sets, hit IDs / distances /
+faces.  Flux: per-primitive relative error <= 1e-4 against the FP64 oracle on
+the same seeded ray set (FP32 geometry, FP64 accumulation on both sides).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from helios_gb300 import _hrt, scenes
+from helios_gb300.radiation import Context, RadiationModel
+
+import scenarios
+from helpers import oracle_solve, oracle_scene_for, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+FLUX_RTOL = 1e-4  # spec tolerance: per-primitive relative flux error vs the FP64 oracle
+
+
+def _mixed(seed=1, n_leaf=3000, n_tri=3000, leaf=0.3):
+    a = scenes.homogeneous_canopy(n_leaves=n_leaf, leaf=leaf, domain=5, seed=seed)
+    b = scenes.orchard(nx=1, ny=1, leaves_per_tree=n_tri, side=leaf, seed=seed + 1)
+    return (np.concatenate([a.T, b.T]), np.concatenate([a.ptype, b.ptype]), np.concatenate([a.twosided, b.twosided]))
+
+
+@pytest.fixture(scope="module")
+def gpu(hrt_lib):
+    return _hrt.Context(0)
+
+
+def _flux_close(got, ref, rtol=FLUX_RTOL):
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    floor = 1e-3 * max(float(np.abs(ref).mean()), 1e-30)
+    err = np.abs(got - ref) / np.maximum(np.abs(ref), floor)
+    return float(err.max()), err
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 17, 4096, 6000])
+def test_bvh_bit_exact(gpu, oracle_mod, n):
+    T, ty, ts = _mixed(seed=n)
+    T, ty, ts = T[:n], ty[:n], ts[:n]
+    gpu.update_geometry(T, ty, ts)
+    gpu.build_accel()
+    c1, p1, n1 = gpu.bvh()
+    c2, p2, n2 = oracle_mod.OracleScene(T, ty, ts).bvh()
+    assert np.array_equal(c1, c2)
+    assert np.array_equal(p1, p2)
+    assert np.array_equal(n1[:, 12:14], n2[:, 12:14])
+    assert np.array_equal(n1[:, :12].view(np.float32), n2[:, :12].view(np.float32))
+
+
+@pytest.mark.parametrize("kind,face", [(0, 1), (1, 1), (1, 0)])
+def test_ray_sets_bit_exact(gpu, oracle_mod, kind, face):
+    T, ty, ts = _mixed(seed=4, n_leaf=500, n_tri=500)
+    gpu.update_geometry(T, ty, ts)
+    gpu.build_accel()
+    sc = oracle_mod.OracleScene(T, ty, ts)
+    sun = scenes.sun_direction(30, 0)
+    o1, d1 = gpu.gen_rays(kind, 1234, 7, 100 if kind == 0 else 324, face, sun)
+    o2, d2 = sc.gen_rays(kind, 1234, 7, 100 if kind == 0 else 324, face, sun)
+    assert np.array_equal(o1, o2)
+    assert np.array_equal(d1, d2)
+
+
+@pytest.mark.parametrize("anyhit", [False, True])
+def test_hit_ids_exact(gpu, oracle_mod, anyhit):
+    T, ty, ts = _mixed(seed=9)
+    gpu.update_geometry(T, ty, ts)
+    gpu.build_accel()
+    sc = oracle_mod.OracleScene(T, ty, ts)
+    rng = np.random.default_rng(2)
+    n = 200000
+    o = np.stack([rng.uniform(-1, 6, n), rng.uniform(-1, 6, n), rng.uniform(0, 6, n)], 1).astype(np.float32)
+    d = rng.normal(size=(n, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    h1, t1, f1 = gpu.trace_rays(o, d, anyhit=anyhit)
+    h2, t2, f2, _ = sc.trace(o, d, mode=3 if anyhit else 0)
+    if anyhit:
+        assert np.array_equal(h1 >= 0, h2 >= 0)
+    else:
+        assert np.array_equal(h1, h2)
+        assert np.array_equal(t1[h1 >= 0], t2[h2 >= 0])
+        assert np.array_equal(f1, f2)
+    assert gpu.device_status() == 0
+
+
+def _canopy_model(n_leaves=2000, depth=3, periodic=False, mode="device"):
+    sc = scenes.homogeneous_canopy(n_leaves=n_leaves, leaf=0.1, domain=math.sqrt(n_leaves * 0.01 / 2.0), seed=0)
+    ctx = Context()
+    ctx.addScene(sc)
+    ctx.setPrimitiveData(sc.groups["leaves"], "reflectivity_SW", np.full(n_leaves, 0.10))
+    ctx.setPrimitiveData(sc.groups["leaves"], "transmissivity_SW", np.full(n_leaves, 0.05))
+    rad = RadiationModel(ctx, mode=mode)
+    if periodic:
+        rad.enforcePeriodicBoundary("xy")
+    rad.addRadiationBand("SW")
+    rad.disableEmission("SW")
+    sun = rad.addCollimatedRadiationSource(scenes.sun_direction(30, 0))
+    rad.setSourceFlux(sun, "SW", 1000.0)
+    rad.setDiffuseRadiationFlux("SW", 100.0)
+    rad.setDirectRayCount("SW", 100)
+    rad.setDiffuseRayCount("SW", 300)
+    rad.setScatteringDepth("SW", depth)
+    return rad
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_canopy_flux_vs_oracle(oracle_mod, periodic):
+    rad = _canopy_model(periodic=periodic)
+    rad.setSeed(77)
+    got = rad.runBand("SW")
+    ref, st = run_oracle(rad, ["SW"], oracle_mod, seed=77)
+    worst, _ = _flux_close(got, ref)
+    assert worst <= FLUX_RTOL, worst
+    assert rad.last_stats["rays"] == st["rays"]
+
+
+def test_backend_sequence_matches_device_solve(oracle_mod):
+    a = _canopy_model(mode="device")
+    b = _canopy_model(mode="backend")
+    a.setSeed(5)
+    b.setSeed(5)
+    fa = a.runBand("SW")
+    fb = b.runBand("SW")
+    worst, _ = _flux_close(fb, fa, 1e-5)
+    assert worst <= 1e-5, worst
+
+
+def _orchard_model(trees=(2, 1), leaves=1500, mode="device"):
+    sc = scenes.orchard(nx=trees[0], ny=trees[1], leaves_per_tree=leaves, side=0.05, seed=0, ground=True)
+    ctx = Context()
+    ctx.addScene(sc)
+    n = sc.n
+    lv = sc.groups["leaves"]
+    rng = np.random.default_rng(0)
+    ctx.setPrimitiveData(lv, "reflectivity_PAR", np.full(lv.size, 0.08))
+    ctx.setPrimitiveData(lv, "transmissivity_PAR", np.full(lv.size, 0.05))
+    ctx.setPrimitiveData(lv, "reflectivity_NIR", np.full(lv.size, 0.45))
+    ctx.setPrimitiveData(lv, "transmissivity_NIR", np.full(lv.size, 0.40))
+    ctx.setPrimitiveData(lv, "emissivity_LW", np.full(lv.size, 0.96))
+    ctx.setPrimitiveData(np.arange(n), "temperature", 273.15 + rng.normal(25.0, 2.0, n))
+    rad = RadiationModel(ctx, mode=mode)
+    sun = rad.addCollimatedRadiationSource(scenes.sun_direction(30, 0))
+    for b in ("PAR", "NIR", "LW"):
+        rad.addRadiationBand(b)
+        rad.setDirectRayCount(b, 100)
+        rad.setDiffuseRayCount(b, 200)
+        rad.setScatteringDepth(b, 5)
+    for b in ("PAR", "NIR"):
+        rad.disableEmission(b)
+        rad.setDiffuseRadiationFlux(b, 100.0)
+    rad.setSourceFlux(sun, "PAR", 500.0)
+    rad.setSourceFlux(sun, "NIR", 450.0)
+    return rad
+
+
+def test_orchard_three_bands_vs_oracle(oracle_mod):
+    rad = _orchard_model()
+    rad.setSeed(3)
+    got = rad.runBand(["PAR", "NIR", "LW"])
+    ref, st = run_oracle(rad, ["PAR", "NIR", "LW"], oracle_mod, seed=3)
+    worst, _ = _flux_close(got, ref)
+    assert worst <= FLUX_RTOL, worst
+
+
+def test_orchard_backend_sequence(oracle_mod):
+    a, b = _orchard_model(), _orchard_model(mode="backend")
+    a.setSeed(8)
+    b.setSeed(8)
+    fa = a.runBand(["PAR", "NIR", "LW"])
+    fb = b.runBand(["PAR", "NIR", "LW"])
+    worst, _ = _flux_close(fb, fa, 1e-5)
+    assert worst <= 1e-5, worst
+
+
+def test_mixed_depth_band_compaction(oracle_mod):
+    """Bands with different scattering depths run together: the launched-band
+    compaction of the reference's scattering loop (RadiationModel.cpp:4250-4276)."""
+    rad = _orchard_model(leaves=800)
+    rad.setScatteringDepth("PAR", 1)
+    rad.setScatteringDepth("NIR", 3)
+    rad.setScatteringDepth("LW", 2)
+    rad.setSeed(13)
+    got = rad.runBand(["PAR", "NIR", "LW"])
+    ref, _ = run_oracle(rad, ["PAR", "NIR", "LW"], oracle_mod, seed=13)
+    worst, _ = _flux_close(got, ref)
+    assert worst <= FLUX_RTOL, worst
+
+
+def test_sources_all_types(oracle_mod):
+    """Sphere, sun-sphere, rectangle and disk sources (OptiX8DeviceCode.cu:1341-1415)."""
+    ctx = Context()
+    ctx.addScene(scenes.homogeneous_canopy(n_leaves=400, leaf=0.2, domain=3, seed=2))
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("SW")
+    rad.disableEmission("SW")
+    s = [rad.addSphereRadiationSource((1.0, 1.0, 6.0), 0.5),
+         rad.addSunSphereRadiationSource(scenes.sun_direction(40, 30)),
+         rad.addRectangleRadiationSource((2.0, 1.0, 5.0), (1.0, 2.0), (0.1, 0.2, 0.3)),
+         rad.addDiskRadiationSource((0.5, 2.0, 5.5), 0.7, (0.0, 0.3, 0.0))]
+    for k, f in zip(s, (300.0, 800.0, 150.0, 120.0)):
+        rad.setSourceFlux(k, "SW", f)
+    rad.setDirectRayCount("SW", 64)
+    rad.setScatteringDepth("SW", 0)
+    rad.setSeed(21)
+    got = rad.runBand("SW")
+    desc = rad.solve_description(["SW"])
+    sc = oracle_scene_for(rad, oracle_mod)
+    ref, _ = sc.run_band(oracle_solve(desc, rotation=_hrt.source_rotation))
+    worst, _ = _flux_close(got, ref)
+    assert worst <= FLUX_RTOL, worst
+
+
+@pytest.mark.parametrize("name", ["simple_direct", "black_parallel_rectangles", "gray_parallel_rectangles",
+                                  "common_edge_squares", "launch_batching", "second_law_box"])
+def test_known_answers_on_gpu(name):
+    def run(rad, labels, seed):
+        rad.setSeed(seed)
+        return rad.runBand(labels)
+    res = getattr(scenarios, name)(run)
+    assert not scenarios.check(res), scenarios.check(res)
+
+
+def test_canopy_beer_reference_size():
+    """The reference's periodic canopy test at its own size: 20 x 20 m, LAI 2, 5 cm
+    leaves (160,000 patches), 1000 direct / 5000 diffuse rays (selfTest.cpp:1625-1717)."""
+    def run(rad, labels, seed):
+        rad.setSeed(seed)
+        return rad.runBand(labels)
+    res = scenarios.canopy_beer(run, n_leaves=160000, leaf=0.05, ndir=1000, ndiff=5000, ground_div=100)
+    assert not scenarios.check(res), scenarios.check(res)
+
+
+def test_errors_and_edge_cases(gpu):
+    with pytest.raises(_hrt.HrtError):
+        gpu.update_geometry(np.zeros((1, 16), np.float32), [7], [1])  # unsupported primitive type
+    g2 = _hrt.Context(0)
+    with pytest.raises(_hrt.HrtError):
+        g2.trace_rays(np.zeros((1, 3)), np.ones((1, 3)))  # no acceleration structure yet
+    g2.update_geometry(np.zeros((0, 16), np.float32), np.zeros(0), np.zeros(0))
+    g2.build_accel()
+    h, t, f = g2.trace_rays(np.zeros((4, 3)), np.ones((4, 3)))
+    assert (h == -1).all()
+    # a zero diffuse ray count is a no-op launch (OptiX8Backend.cpp:968-970)
+    ctx = Context()
+    ctx.addPatch((0, 0, 0), (1, 1))
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("SW")
+    rad.disableEmission("SW")
+    rad.setDiffuseRadiationFlux("SW", 10.0)
+    rad.setDiffuseRayCount("SW", 0)
+    f = rad.runBand("SW")
+    assert f.shape == (1, 1) and f[0, 0] == 0.0
+
+
+def test_determinism_and_energy_bound():
+    rad = _canopy_model(n_leaves=4000, depth=3)
+    rad.setSeed(99)
+    f1 = rad.runBand("SW").astype(np.float64)
+    rad.setSeed(99)
+    f2 = rad.runBand("SW").astype(np.float64)
+    np.testing.assert_allclose(f1, f2, rtol=1e-6, atol=1e-6)
+    T, ty, area = rad.context.arrays()
+    absorbed = float((f1[:, 0] * area).sum())
+    dom = math.sqrt(4000 * 0.01 / 2.0)
+    incident = (1000.0 * math.cos(math.radians(30)) + 100.0) * dom * dom
+    assert absorbed <= incident * 1.01
+
+
+def test_traversal_counts_match_oracle(gpu, oracle_mod):
+    """The statistics kernels count the same node visits as the host traversal of the same BVH."""
+    rad = _canopy_model(n_leaves=1500, depth=0)
+    rad.setSeed(4)
+    rad.ctx.set_measure(1)
+    rad.runBand("SW")
+    m = rad.ctx.get_measure()
+    rad.ctx.set_measure(0)
+    _, st = run_oracle(rad, ["SW"], oracle_mod, seed=4)
+    assert m["node_visits"] == st["nodes"]
+    assert m["prim_tests"] == st["prims"]
