@@ -155,7 +155,7 @@ def cpu_sample(rad, seconds_hint=15.0, threads=0, prim_limit=None):
 
 
 def run_reference(args):
-    rad, sc = orchard_model()
+    rad, sc = orchard_model(nx=args.trees[0], ny=args.trees[1])
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -172,7 +172,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 geometry / f64 sums",
-            "data": "synthetic (seeded)", "config": {"workload": "orchard-1M-triangles-3band", "primitives": sc.n},
+            "data": "synthetic (seeded)", "config": {"workload": f"orchard-{sc.n}-triangles-3band", "primitives": sc.n},
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -191,7 +191,7 @@ def run_gpu(args):
 
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    rad, sc = orchard_model(device=local)
+    rad, sc = orchard_model(nx=args.trees[0], ny=args.trees[1], device=local)
     stream = torch.cuda.Stream(device=local)
     rad.ctx.set_stream(stream.cuda_stream)
     rad.setSeed(1234 + rank)
@@ -267,7 +267,7 @@ def run_gpu(args):
         "metric": METRIC, "value": rps, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 geometry / f64 sums", "data": "synthetic (seeded, seed 0)",
-        "config": {"workload": "orchard-1M-triangles-3band", "primitives": sc.n, "bands": BANDS,
+        "config": {"workload": f"orchard-{sc.n}-triangles-3band", "primitives": sc.n, "bands": BANDS,
                    "direct_rays": 100, "diffuse_rays": 225, "scattering_depth": 5,
                    "rays_per_step": rays_per_step, "solves_per_s": 1e3 / ms * world,
                    "parallelism": "replicas" if world > 1 else "single",
@@ -296,6 +296,7 @@ def main():
     ap.add_argument("--impl", default="hrt", choices=["hrt", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
+    ap.add_argument("--trees", type=int, nargs=2, default=(20, 10), help="orchard grid (default 20 x 10 = 1M leaves)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

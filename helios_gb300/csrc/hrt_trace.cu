@@ -24,9 +24,10 @@ constexpr int kBlock = 256;
 
 struct Hit {
     float t;
-    uint32_t prim;  // original index, 0xFFFFFFFF = miss
+    uint32_t prim;  // original index, 0xFFFFFFFF = miss, kLost = dropped after the wrap limit
     int face;
 };
+constexpr uint32_t kLost = 0xFFFFFFFEu;
 
 __device__ __forceinline__ void raise(uint32_t *status, uint32_t bit) {
     if (status) atomicOr(status, bit);
@@ -155,8 +156,9 @@ __device__ Hit trace_full(const TraceScene &sc, f3 o, f3 d, float tmin, float tm
         }
         o = hp;
     }
-    raise(sc.status, ERR_WRAP);
-    return Hit{tmax, 0xFFFFFFFFu, 0};
+    // The tenth trace ended on a wall again: the reference's loop stops there and no
+    // miss or closest-hit program deposits anything for this ray.
+    return Hit{tmax, kLost, 0};
 }
 
 __device__ __forceinline__ void load_rgen(const TraceScene &sc, uint32_t p, float4 g[4]) {
@@ -408,7 +410,9 @@ __global__ void __launch_bounds__(kBlock) k_diffuse(const DiffuseParams P) {
             if (face == 0) dir = mk(-dir.x, -dir.y, -dir.z);
             f3 org = sample_point(g, type, u01(u.c), u01(u.d));
             Hit h = trace_full<STATS>(P.sc, org, dir, 1e-4f, 1e38f, false, &nv, &np);
-            if (h.prim != 0xFFFFFFFFu) {
+            if (h.prim == kLost) {
+                // dropped ray: no deposit
+            } else if (h.prim != 0xFFFFFFFFu) {
                 const float *src = (h.face ? P.otop : P.obot) + (size_t)h.prim * P.Bl;
 #pragma unroll
                 for (int j = 0; j < NB; ++j)

@@ -741,7 +741,9 @@ Hit trace_full(const Scene &s, Ray ray, bool anyhit, TraceStats *st) {
         }
         ray.o = hp;
     }
-    return Hit{ray.tmax, -1, 0};
+    // The tenth trace ended on a wall again: the reference's loop stops and neither a miss
+    // nor a closest-hit program deposits energy for this ray (OptiX8DeviceCode.cu:1616-1653).
+    return Hit{ray.tmax, -2, 0};
 }
 
 // ---------------------------------------------------------------- sources ---
@@ -1123,10 +1125,8 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
                     n_rays++;
                     n_nodes += st.nodes;
                     n_prims += st.prims;
-                    if (hh.prim >= 0) {
-                        n_hits++;
-                        continue;
-                    }
+                    if (hh.prim >= 0) n_hits++;
+                    if (hh.prim != -1) continue;  // occluded, or dropped at the wrap limit
                     int b = -1;
                     for (int bg = 0; bg < Bg; ++bg) {
                         if (!q->band_launch[bg]) continue;
@@ -1184,6 +1184,7 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
                 n_nodes += st.nodes;
                 n_prims += st.prims;
                 if (hh.prim >= 0) n_hits++;
+                if (hh.prim == -2) continue;  // dropped at the wrap limit: no deposit
                 int b = -1;
                 for (int bg = 0; bg < Bg; ++bg) {
                     if (!flags[bg]) continue;
