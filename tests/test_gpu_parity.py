@@ -258,7 +258,8 @@ def test_errors_and_edge_cases(gpu):
 
 
 def test_determinism_and_energy_bound():
-    """Same seed, same flux; with periodic walls a canopy absorbs at most what enters its top."""
+    """Same seed, same flux.  With periodic walls a canopy lit by the sun alone (or the
+    sky alone) absorbs at most what enters its top."""
     rad = _canopy_model(n_leaves=4000, depth=3, periodic=True)
     rad.setSeed(99)
     f1 = rad.runBand("SW").astype(np.float64)
@@ -266,10 +267,36 @@ def test_determinism_and_energy_bound():
     f2 = rad.runBand("SW").astype(np.float64)
     np.testing.assert_allclose(f1, f2, rtol=1e-6, atol=1e-6)
     T, ty, area = rad.context.arrays()
-    absorbed = float((f1[:, 0] * area).sum())
     (x0, x1), (y0, y1), _ = rad.context.getDomainBoundingBox()
-    incident = (1000.0 * math.cos(math.radians(30)) + 100.0) * (x1 - x0) * (y1 - y0)
-    assert absorbed <= incident * 1.01
+    top = (x1 - x0) * (y1 - y0)
+    rad.setDiffuseRadiationFlux("SW", 0.0)
+    sun = float((rad.runBand("SW")[:, 0] * area).sum())
+    assert sun <= 1000.0 * math.cos(math.radians(30)) * top * 1.005
+    rad.setDiffuseRadiationFlux("SW", 100.0)
+    rad.setSourceFlux(0, "SW", 0.0)
+    sky = float((rad.runBand("SW")[:, 0] * area).sum())
+    assert sky <= 100.0 * top * 1.01
+
+
+def test_sun_plus_sky_nonadditivity_matches_reference(oracle_mod):
+    """RadiationModel::runBand with direct + diffuse + scattering and no emission gathers the
+    direct-scattered energy twice and drops the sky's first scatter (RadiationModel.cpp:4236-4298),
+    so runBand(sun+sky) != runBand(sun) + runBand(sky).  The drop-in reproduces that sequence."""
+    def total(sun, sky, engine):
+        rad = _canopy_model(n_leaves=1500, depth=3, periodic=True)
+        rad.setSourceFlux(0, "SW", sun)
+        rad.setDiffuseRadiationFlux("SW", sky)
+        rad.setSeed(31)
+        if engine == "gpu":
+            f = rad.runBand("SW")
+        else:
+            f, _ = run_oracle(rad, ["SW"], oracle_mod, seed=31)
+        return float((np.asarray(f)[:, 0] * rad.context.arrays()[2]).sum())
+    g = [total(1000, 0, "gpu"), total(0, 100, "gpu"), total(1000, 100, "gpu")]
+    o = [total(1000, 0, "cpu"), total(0, 100, "cpu"), total(1000, 100, "cpu")]
+    np.testing.assert_allclose(g, o, rtol=1e-6)
+    excess = g[2] - g[0] - g[1]
+    assert excess > 0.01 * g[2]
 
 
 def test_traversal_counts_match_oracle(gpu, oracle_mod):
