@@ -1,0 +1,211 @@
+/** GB300Backend.cpp -- helios::RayTracingBackend over the libhrt C ABI.
+ *
+ * Semantics follow the reference backend each virtual replaces
+ * (plugins/radiation/src/backends/OptiX8Backend.cpp):
+ *   updateGeometry            :327-517   -> hrt_update_geometry
+ *   buildAccelerationStructure:519-532   -> hrt_build_accel
+ *   launchDirectRays          :813-870   -> hrt_launch_direct
+ *   launchDiffuseRays         :872-1002  -> hrt_launch_diffuse (uploads radiation_out first)
+ *   getRadiationResults       :1119-1143 -> hrt_get_results
+ *   zero/copy/upload          :1168-1250 -> hrt_zero_* / hrt_copy_scatter_to_radiation / hrt_upload_radiation_out
+ */
+#include "GB300Backend.h"
+
+#include <algorithm>
+#include <iostream>
+#include <string>
+
+namespace helios {
+
+GB300Backend::GB300Backend(int device) : device_(device) {}
+
+GB300Backend::~GB300Backend() { shutdown(); }
+
+void GB300Backend::check(int rc, const char *where) const {
+    if (rc != HRT_OK) {
+        helios_runtime_error(std::string("ERROR (GB300Backend::") + where + "): " +
+                             (ctx_ ? hrt_last_error(ctx_) : "no device context") + " (code " + std::to_string(rc) + ")");
+    }
+}
+
+void GB300Backend::initialize() {
+    if (ctx_) return;
+    check(hrt_create(&ctx_, device_), "initialize");
+}
+
+void GB300Backend::shutdown() {
+    if (ctx_) {
+        hrt_destroy(ctx_);
+        ctx_ = nullptr;
+    }
+}
+
+void GB300Backend::updateGeometry(const RayTracingGeometry &geometry) {
+    validateGeometryBeforeUpload(geometry);
+    std::vector<int8_t> twosided(geometry.twosided_flags.begin(), geometry.twosided_flags.end());
+    std::vector<float> bbox;
+    bbox.reserve(geometry.bboxes.vertices.size() * 3);
+    for (const auto &v : geometry.bboxes.vertices) {
+        bbox.push_back(v.x);
+        bbox.push_back(v.y);
+        bbox.push_back(v.z);
+    }
+    hrt_geometry g{};
+    g.n = (int32_t)geometry.primitive_count;
+    g.transform = geometry.transform_matrices.data();
+    g.type = geometry.primitive_types.data();
+    g.twosided = twosided.data();
+    g.nbbox = (int32_t)geometry.bbox_count;
+    g.bbox_vertices = bbox.empty() ? nullptr : bbox.data();
+    g.periodic_x = geometry.periodic_flag.x;
+    g.periodic_y = geometry.periodic_flag.y;
+    check(hrt_update_geometry(ctx_, &g), "updateGeometry");
+    nprims_ = geometry.primitive_count;
+}
+
+void GB300Backend::buildAccelerationStructure() { check(hrt_build_accel(ctx_), "buildAccelerationStructure"); }
+
+void GB300Backend::updateMaterials(const RayTracingMaterial &m) {
+    check(hrt_update_materials(ctx_, (int32_t)m.num_sources, (int32_t)m.num_primitives, (int32_t)m.num_bands,
+                               m.reflectivity.data(), m.transmissivity.data()),
+          "updateMaterials");
+}
+
+void GB300Backend::updateSources(const std::vector<RayTracingSource> &sources) {
+    std::vector<hrt_source> s(sources.size());
+    for (size_t i = 0; i < sources.size(); ++i) {
+        s[i].type = sources[i].type;
+        s[i].position[0] = sources[i].position.x;
+        s[i].position[1] = sources[i].position.y;
+        s[i].position[2] = sources[i].position.z;
+        s[i].width[0] = sources[i].width.x;
+        s[i].width[1] = sources[i].width.y;
+        s[i].rotation[0] = sources[i].rotation.x;
+        s[i].rotation[1] = sources[i].rotation.y;
+        s[i].rotation[2] = sources[i].rotation.z;
+    }
+    check(hrt_update_sources(ctx_, (int32_t)s.size(), s.data()), "updateSources");
+}
+
+// Diffuse parameters travel with each launch (as in OptiX8Backend::launchDiffuseRays).
+void GB300Backend::updateDiffuseRadiation(const std::vector<float> &, const std::vector<float> &,
+                                          const std::vector<helios::vec3> &, const std::vector<float> &,
+                                          const std::vector<float> &) {}
+
+// Sky radiance for cameras: cameras are not provided by this backend.
+void GB300Backend::updateSkyModel(const std::vector<helios::vec4> &, const std::vector<float> &, const helios::vec3 &,
+                                  const std::vector<float> &, float, const std::vector<float> &,
+                                  const std::vector<uint32_t> &) {}
+
+hrt_launch GB300Backend::makeLaunch(const RayTracingLaunchParams &p, std::vector<uint8_t> &flags,
+                                    std::vector<float> &peak, std::vector<float> &sky) const {
+    flags.assign(p.band_launch_flag.begin(), p.band_launch_flag.end());
+    for (const auto &d : p.diffuse_peak_dir) {
+        peak.push_back(d.x);
+        peak.push_back(d.y);
+        peak.push_back(d.z);
+    }
+    for (const auto &v : p.sky_radiance_params) {
+        sky.push_back(v.x);
+        sky.push_back(v.y);
+        sky.push_back(v.z);
+        sky.push_back(v.w);
+    }
+    hrt_launch L{};
+    L.launch_offset = p.launch_offset;
+    L.launch_count = p.launch_count;
+    L.rays_per_primitive = p.rays_per_primitive;
+    L.random_seed = p.random_seed;
+    L.nbands_global = p.num_bands_global;
+    L.nbands_launch = p.num_bands_launch;
+    L.band_launch_flag = flags.data();
+    L.launch_face = p.launch_face;
+    L.diffuse_flux = p.diffuse_flux.empty() ? nullptr : p.diffuse_flux.data();
+    L.diffuse_extinction = p.diffuse_extinction.empty() ? nullptr : p.diffuse_extinction.data();
+    L.diffuse_peak_dir = peak.empty() ? nullptr : peak.data();
+    L.diffuse_dist_norm = p.diffuse_dist_norm.empty() ? nullptr : p.diffuse_dist_norm.data();
+    L.sky_radiance_params = sky.empty() ? nullptr : sky.data();
+    L.radiation_out_top = p.radiation_out_top.empty() ? nullptr : p.radiation_out_top.data();
+    L.radiation_out_bottom = p.radiation_out_bottom.empty() ? nullptr : p.radiation_out_bottom.data();
+    return L;
+}
+
+void GB300Backend::launchDirectRays(const RayTracingLaunchParams &p) {
+    std::vector<uint8_t> flags;
+    std::vector<float> peak, sky;
+    hrt_launch L = makeLaunch(p, flags, peak, sky);
+    L.pass_id = 0;
+    check(hrt_launch_direct(ctx_, &L), "launchDirectRays");
+}
+
+void GB300Backend::launchDiffuseRays(const RayTracingLaunchParams &p) {
+    std::vector<uint8_t> flags;
+    std::vector<float> peak, sky;
+    hrt_launch L = makeLaunch(p, flags, peak, sky);
+    L.pass_id = 1 + p.scattering_iteration;
+    check(hrt_launch_diffuse(ctx_, &L), "launchDiffuseRays");
+}
+
+void GB300Backend::launchCameraRays(const RayTracingLaunchParams &) {
+    helios_runtime_error("ERROR (GB300Backend::launchCameraRays): radiation cameras are not provided by the GB300 backend.");
+}
+
+void GB300Backend::launchPixelLabelRays(const RayTracingLaunchParams &) {
+    helios_runtime_error("ERROR (GB300Backend::launchPixelLabelRays): pixel labelling is not provided by the GB300 backend.");
+}
+
+void GB300Backend::getRadiationResults(RayTracingResults &r) {
+    const size_t m = nprims_ * launch_bands_;
+    r.num_primitives = nprims_;
+    r.num_bands = launch_bands_;
+    r.radiation_in.assign(m, 0.f);
+    r.radiation_out_top.assign(m, 0.f);
+    r.radiation_out_bottom.assign(m, 0.f);
+    r.scatter_buff_top.assign(m, 0.f);
+    r.scatter_buff_bottom.assign(m, 0.f);
+    if (m == 0) return;
+    check(hrt_get_results(ctx_, r.radiation_in.data(), r.radiation_out_top.data(), r.radiation_out_bottom.data(),
+                          r.scatter_buff_top.data(), r.scatter_buff_bottom.data()),
+          "getRadiationResults");
+}
+
+void GB300Backend::getCameraResults(std::vector<float> &, std::vector<uint> &, std::vector<float> &, uint,
+                                    const helios::int2 &) {
+    helios_runtime_error("ERROR (GB300Backend::getCameraResults): radiation cameras are not provided by the GB300 backend.");
+}
+
+void GB300Backend::zeroRadiationBuffers(size_t launch_band_count) {
+    check(hrt_zero_radiation_buffers(ctx_, launch_band_count), "zeroRadiationBuffers");
+    launch_bands_ = launch_band_count;
+}
+
+void GB300Backend::zeroScatterBuffers() { check(hrt_zero_scatter_buffers(ctx_), "zeroScatterBuffers"); }
+
+void GB300Backend::zeroCameraPixelBuffers(const helios::int2 &) {}
+
+void GB300Backend::copyScatterToRadiation() { check(hrt_copy_scatter_to_radiation(ctx_), "copyScatterToRadiation"); }
+
+void GB300Backend::uploadRadiationOut(const std::vector<float> &top, const std::vector<float> &bottom) {
+    size_t n = std::max(top.size(), bottom.size());
+    check(hrt_upload_radiation_out(ctx_, top.empty() ? nullptr : top.data(), bottom.empty() ? nullptr : bottom.data(), n),
+          "uploadRadiationOut");
+}
+
+void GB300Backend::zeroCameraScatterBuffers(size_t) {}
+
+void GB300Backend::uploadSourceFluxes(const std::vector<float> &fluxes) {
+    check(hrt_upload_source_fluxes(ctx_, fluxes.data(), fluxes.size()), "uploadSourceFluxes");
+}
+
+void GB300Backend::uploadSourceFluxesCam(const std::vector<float> &) {}
+
+void GB300Backend::queryGPUMemory() const {
+    size_t f = 0, t = 0;
+    check(hrt_query_memory(ctx_, &f, &t), "queryGPUMemory");
+    std::cout << "GPU memory: " << f / (1024.0 * 1024.0) << " MB free / " << t / (1024.0 * 1024.0) << " MB total"
+              << std::endl;
+}
+
+std::string GB300Backend::getBackendName() const { return hrt_backend_name(); }
+
+}  // namespace helios
