@@ -23,7 +23,7 @@ EXPORTS = [
     "hrt_launch_diffuse", "hrt_get_results", "hrt_zero_radiation_buffers", "hrt_zero_scatter_buffers",
     "hrt_copy_scatter_to_radiation", "hrt_upload_radiation_out", "hrt_query_memory", "hrt_backend_name",
     "hrt_run_band", "hrt_last_stats", "hrt_device_status", "hrt_trace_rays", "hrt_gen_rays", "hrt_get_bvh",
-    "hrt_source_rotation", "hrt_set_measure", "hrt_get_measure",
+    "hrt_source_rotation", "hrt_set_measure", "hrt_get_measure", "hrt_build_accel_static",
 ]
 
 
@@ -104,6 +104,7 @@ def load(path: str | None = None):
         "hrt_source_rotation": (None, [VP, VP]),
         "hrt_set_measure": (C.c_int, [VP, C.c_int]),
         "hrt_get_measure": (C.c_int, [VP, VP, C.c_int]),
+        "hrt_build_accel_static": (C.c_int, [VP, VP, C.c_int32, VP, VP, VP, VP, VP, VP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

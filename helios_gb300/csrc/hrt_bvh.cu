@@ -417,30 +417,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
 
-size_t bvh_scratch_bytes(int n) {
-    size_t nn = (size_t)(n > 1 ? n : 1);
-    size_t ni = (size_t)(n > 1 ? n - 1 : 1);
-    size_t nblk = (nn + kSortTile - 1) / kSortTile;
-    size_t nh = 256 * nblk;
-    size_t nparts = 1024;
-    size_t b = 0;
-    b += align256(nn * 4 * sizeof(float4));   // rec_tmp
-    b += align256(nn * 6 * sizeof(float));    // aabb
-    b += align256(nn * 6 * sizeof(float));    // leafbox
-    b += align256(ni * 6 * sizeof(float));    // nodebox
-    b += align256(16 * sizeof(float));        // bounds
-    b += align256(nparts * 12 * sizeof(float));
-    b += align256(nn * sizeof(uint64_t));     // keys_alt
-    b += align256(nn * sizeof(uint32_t));     // vals_alt
-    b += align256(nh * sizeof(uint32_t));     // hist
-    b += align256(nh * sizeof(uint32_t));     // hist scanned (offsets)
-    b += align256((2 * ((nh + kSortTile - 1) / kSortTile) + 64) * sizeof(uint32_t));
-    b += align256(2 * ni * sizeof(int32_t));  // child
-    b += align256(ni * sizeof(int32_t));      // parent_int
-    b += align256(nn * sizeof(int32_t));      // parent_leaf
-    b += align256(ni * sizeof(uint32_t));     // flags
-    return b;
-}
+size_t bvh_scratch_bytes(int n) { return bvh_scratch_bytes_c(n); }
 
 void bvh_carve(BvhBuffers &bb, void *scratch, int n) {
     size_t nn = (size_t)(n > 1 ? n : 1);

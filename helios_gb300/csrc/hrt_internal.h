@@ -85,6 +85,16 @@ struct BvhBuffers {
     uint32_t *flags;    // [n-1]
     uint32_t *status;   // device error word
 };
+// Scratch bytes of bvh_build for n primitives (each piece rounded up to 256 B).
+constexpr size_t align256c(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t bvh_scratch_bytes_c(int n) {
+    size_t nn = (size_t)(n > 1 ? n : 1), ni = (size_t)(n > 1 ? n - 1 : 1);
+    size_t nh = 256 * ((nn + 2047) / 2048);
+    return align256c(nn * 4 * 16) + align256c(nn * 6 * 4) + align256c(nn * 6 * 4) + align256c(ni * 6 * 4) +
+           align256c(16 * 4) + align256c(1024 * 12 * 4) + align256c(nn * 8) + align256c(nn * 4) +
+           align256c(nh * 4) + align256c(nh * 4) + align256c((2 * ((nh + 2047) / 2048) + 64) * 4) +
+           align256c(2 * ni * 4) + align256c(ni * 4) + align256c(nn * 4) + align256c(ni * 4);
+}
 size_t bvh_scratch_bytes(int n);
 void bvh_carve(BvhBuffers &b, void *scratch, int n);
 cudaError_t bvh_build(const float *T, const uint32_t *type, int n, BvhBuffers &b, cudaStream_t s);

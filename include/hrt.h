@@ -171,6 +171,24 @@ int hrt_get_bvh(hrt_context *ctx, uint64_t *codes, uint32_t *perm, uint32_t *nod
  * [3] diffuse ms, [4] node visits, [5] primitive tests. */
 int hrt_set_measure(hrt_context *ctx, int flags);
 int hrt_get_measure(hrt_context *ctx, double *out, int count);
+/* ---- BVH build that allocates nothing (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc -- code that hands out all device memory
+ * from its own arena or framework allocator, and latency-critical loops where an
+ * allocation would synchronise the device.  Builds the same LBVH as hrt_build_accel()
+ * from caller-owned DEVICE buffers into caller-owned DEVICE buffers:
+ *   d_transform [n*16] float, d_type [n] uint32 (inputs);
+ *   d_records [n*64 B], d_origins [n*64 B], d_nodes [max(n-1,1)*64 B], d_codes [n],
+ *   d_perm [n] (outputs; nodes/codes/perm in the hrt_get_bvh layout).
+ * Scratch is a static device array sized for at most HRT_STATIC_MAX_PRIMS primitives
+ * (about 5.6 MB held by every GPU that loads the library, until exit); larger n is
+ * rejected with HRT_EINVAL.  The first call on a device looks the array's address up
+ * and caches it: make it before any stream capture.  All calls share the array: calls
+ * whose GPU work overlaps (other streams or threads) race.  Work is queued on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) and the call returns after
+ * it finished: HRT_OK, HRT_EINVAL, HRT_ECUDA or HRT_EDEVICE (device error word set). */
+#define HRT_STATIC_MAX_PRIMS 32768
+int hrt_build_accel_static(const float *d_transform, const uint32_t *d_type, int32_t n, void *d_records,
+                           void *d_origins, void *d_nodes, uint64_t *d_codes, uint32_t *d_perm, void *stream);
 /* Rotation matrix (row-major 3x3) that rect/disk sources use, from Euler angles
  * (same convention as the reference's d_makeTransformMatrix, OptiX8DeviceCode.cu:191-201). */
 void hrt_source_rotation(const float rotation[3], float out[9]);
