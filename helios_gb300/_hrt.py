@@ -23,7 +23,7 @@ EXPORTS = [
     "hrt_launch_diffuse", "hrt_get_results", "hrt_zero_radiation_buffers", "hrt_zero_scatter_buffers",
     "hrt_copy_scatter_to_radiation", "hrt_upload_radiation_out", "hrt_query_memory", "hrt_backend_name",
     "hrt_run_band", "hrt_last_stats", "hrt_device_status", "hrt_trace_rays", "hrt_gen_rays", "hrt_get_bvh",
-    "hrt_source_rotation", "hrt_set_measure", "hrt_get_measure", "hrt_build_accel_static",
+    "hrt_source_rotation", "hrt_set_measure", "hrt_get_measure", "hrt_build_accel_static", "hrt_run_sweep",
 ]
 
 
@@ -61,6 +61,12 @@ class BandSolve(C.Structure):
                 ("direct_rays", C.c_void_p), ("diffuse_rays", C.c_void_p), ("scattering_depth", C.c_void_p),
                 ("emission", C.c_void_p), ("emissivity", C.c_void_p), ("temperature", C.c_void_p),
                 ("seed", C.c_uint32)]
+
+
+class Sweep(C.Structure):
+    _fields_ = [("nsun", C.c_int32), ("sun_dir", C.c_void_p), ("nbands", C.c_int32), ("direct_flux", C.c_void_p),
+                ("diffuse_flux", C.c_void_p), ("rho", C.c_void_p), ("tau", C.c_void_p), ("direct_rays", C.c_int32),
+                ("diffuse_rays", C.c_int32), ("scattering_depth", C.c_int32), ("seed", C.c_uint32)]
 
 
 _lib = None
@@ -105,6 +111,7 @@ def load(path: str | None = None):
         "hrt_set_measure": (C.c_int, [VP, C.c_int]),
         "hrt_get_measure": (C.c_int, [VP, VP, C.c_int]),
         "hrt_build_accel_static": (C.c_int, [VP, VP, C.c_int32, VP, VP, VP, VP, VP, VP]),
+        "hrt_run_sweep": (C.c_int, [VP, C.POINTER(Sweep), VP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -313,6 +320,22 @@ class Context:
         bl = int(np.count_nonzero(np.asarray(solve["band_launch"])))
         flux = np.zeros((self.n, bl), np.float32) if out else None
         self.check(self.lib.hrt_run_band(self.h, C.byref(s), ptr(flux)))
+        return flux
+
+    def run_sweep(self, sun_dir, direct_flux, diffuse_flux, rho, tau, direct_rays, diffuse_rays, depth, seed,
+                  out=True):
+        """Batched solves: returns flux [n, nsun, nbands] (channel c = sun * nbands + band)."""
+        sd = f32(sun_dir).reshape(-1, 3)
+        nsun = sd.shape[0]
+        df = f32(direct_flux).reshape(nsun, -1)
+        nb = df.shape[1]
+        sk = f32(diffuse_flux).reshape(nsun, nb)
+        rh = f32(rho).reshape(self.n, nb)
+        ta = f32(tau).reshape(self.n, nb)
+        S = Sweep(nsun, ptr(sd), nb, ptr(df), ptr(sk), ptr(rh), ptr(ta), int(direct_rays), int(diffuse_rays),
+                  int(depth), int(seed) & 0xFFFFFFFF)
+        flux = np.zeros((self.n, nsun, nb), np.float32) if out else None
+        self.check(self.lib.hrt_run_sweep(self.h, C.byref(S), ptr(flux)))
         return flux
 
     def last_stats(self):

@@ -67,7 +67,8 @@ struct hrt_context {
     std::vector<float> h_src_flux;
     // radiation buffers
     int Bl = 0;
-    DevBuf rin, stop, sbot, otop, obot, ftop, fbot, Gd, Gt, Gb, flags, sky, fin, status, counter, emis, emis_eps, emis_T;
+    DevBuf rin, stop, sbot, otop, obot, ftop, fbot, Gd, Gt, Gb, flags, sky, fin, status, counter, emis, emis_eps, emis_T,
+        fetch;
     size_t emis_eps_count = 0, emis_T_count = 0;
     DevBuf io_a, io_b, io_c;  // staging for inspection calls
     uint64_t last_rays = 0, last_kernels = 0;
@@ -80,6 +81,11 @@ struct hrt_context {
     };
     std::vector<Timed> timed;
     double meas[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // batched sweep: inputs, accumulators, recorded hits and the captured graph
+    DevBuf sw_in, sw_mat, sw_acc, sw_out, sw_hits;
+    cudaGraphExec_t sw_exec = nullptr;
+    std::string sw_key;
+    int sw_kernels = 0;
 };
 
 namespace {
@@ -302,6 +308,8 @@ int diffuse_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp
     P.sky = sky;
     P.Gt = ctx->Gt.as<double>();
     P.Gb = ctx->Gb.as<double>();
+    CU(ctx->fetch.ensure(sizeof(unsigned long long)));
+    P.fetch = ctx->fetch.as<unsigned long long>();
     CU(timed_launch(ctx, 1, [&] {
         return (ctx->measure & 1) ? launch_diffuse_stats(P, max_blocks(ctx), ctx->stream)
                                   : launch_diffuse(P, max_blocks(ctx), ctx->stream);
@@ -370,6 +378,7 @@ int hrt_destroy(hrt_context *ctx) {
     if (!ctx) return HRT_EINVAL;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->sw_exec) cudaGraphExecDestroy(ctx->sw_exec);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
     return HRT_OK;
@@ -780,6 +789,189 @@ int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
     CU(launch_final_flux(m, ctx->rin.as<double>(), ctx->stop.as<double>(), ctx->sbot.as<double>(), ctx->fin.as<float>(), st));
     ctx->last_kernels += 1;
     if (flux_out) CU(cudaMemcpyAsync(flux_out, ctx->fin.p, m * sizeof(float), cudaMemcpyDeviceToHost, st));
+    unsigned long long rays = 0;
+    CU(cudaMemcpyAsync(&rays, ctx->counter.p, sizeof(rays), cudaMemcpyDeviceToHost, st));
+    r = sync_and_status(ctx);
+    ctx->last_rays = rays;
+    return r;
+}
+
+// ------------------------------------------------------------ batched sweep --
+int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
+    if (!ctx || !s) return HRT_EINVAL;
+    int r = check_built(ctx);
+    if (r) return r;
+    CU(cudaSetDevice(ctx->device));
+    const int n = ctx->n, nsun = s->nsun, Bl = s->nbands;
+    if (nsun < 1 || Bl < 1 || !s->sun_dir || !s->direct_flux || !s->diffuse_flux || !s->rho || !s->tau)
+        return fail(ctx, HRT_EINVAL, "sweep needs suns, bands, fluxes and materials");
+    const int C = nsun * Bl;
+    if (C > 256) return fail(ctx, HRT_EUNSUPPORTED, "a sweep holds at most 256 channels");
+    if (s->direct_rays < 0 || s->diffuse_rays < 0 || s->scattering_depth < 0) return fail(ctx, HRT_EINVAL, "negative count");
+    const size_t m = (size_t)n * C;
+    cudaStream_t st = ctx->stream;
+    // per-channel pass-sequence flags of the plain runBand each channel stands for
+    const bool scattering = s->scattering_depth > 0;
+    std::vector<uint8_t> all(C, 1), rundirect(C), diffuse(C), fold(C), copy0(C), active(C);
+    bool any_direct = false, any_diffuse = false, any_copy0 = false, any_active = false;
+    for (int c = 0; c < C; ++c) {
+        rundirect[c] = s->direct_flux[c] > 0.f;
+        diffuse[c] = s->diffuse_flux[c] > 0.f;
+        fold[c] = scattering && rundirect[c];
+        copy0[c] = scattering && diffuse[c] && !rundirect[c];
+        active[c] = diffuse[c] || rundirect[c];
+        any_direct = any_direct || rundirect[c];
+        any_diffuse = any_diffuse || diffuse[c];
+        any_copy0 = any_copy0 || copy0[c];
+        any_active = any_active || active[c];
+    }
+    int dimx, dimy;
+    strata((uint32_t)s->direct_rays, &dimx, &dimy);
+    uint32_t rpp_d;
+    {
+        double c = std::ceil(std::sqrt((double)s->diffuse_rays));
+        rpp_d = (uint32_t)(c * c);
+    }
+    int ddx, ddy;
+    strata(rpp_d, &ddx, &ddy);
+    const int Rd = ddx * ddy;
+    // device inputs: [sun 3*nsun][flux C][sky C][zero C] floats, masks 6*C bytes, materials
+    CU(ctx->sw_in.ensure((3 * (size_t)nsun + 3 * (size_t)C) * sizeof(float) + 6 * (size_t)C + 256));
+    float *d_sun = ctx->sw_in.as<float>(), *d_flux = d_sun + 3 * nsun, *d_sky = d_flux + C, *d_zero = d_sky + C;
+    uint8_t *d_masks = (uint8_t *)(d_zero + C);
+    {
+        std::vector<float> h(3 * (size_t)nsun + 3 * (size_t)C, 0.f);
+        std::copy(s->sun_dir, s->sun_dir + 3 * nsun, h.begin());
+        std::copy(s->direct_flux, s->direct_flux + C, h.begin() + 3 * nsun);
+        std::copy(s->diffuse_flux, s->diffuse_flux + C, h.begin() + 3 * nsun + C);
+        std::vector<uint8_t> mk8;
+        for (auto *v : {&all, &fold, &diffuse, &copy0, &active, &rundirect}) mk8.insert(mk8.end(), v->begin(), v->end());
+        CU(cudaMemcpyAsync(d_sun, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+        CU(cudaMemcpyAsync(d_masks, mk8.data(), mk8.size(), cudaMemcpyHostToDevice, st));
+    }
+    uint8_t *m_all = d_masks, *m_fold = d_masks + C, *m_diff = d_masks + 2 * C, *m_copy0 = d_masks + 3 * C,
+            *m_active = d_masks + 4 * C;
+    CU(ctx->sw_mat.ensure(2 * (size_t)n * Bl * sizeof(float)));
+    float *d_rho = ctx->sw_mat.as<float>(), *d_tau = d_rho + (size_t)n * Bl;
+    CU(cudaMemcpyAsync(d_rho, s->rho, (size_t)n * Bl * sizeof(float), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_tau, s->tau, (size_t)n * Bl * sizeof(float), cudaMemcpyHostToDevice, st));
+    // buffers
+    CU(ctx->sw_acc.ensure(5 * m * sizeof(double)));
+    double *rin = ctx->sw_acc.as<double>(), *stp = rin + m, *sbt = stp + m, *Gt = sbt + m, *Gb = Gt + m;
+    CU(ctx->sw_out.ensure(3 * m * sizeof(float)));
+    float *otop = ctx->sw_out.as<float>(), *obot = otop + m, *fin = obot + m;
+    const size_t nhits = 2 * (size_t)n * (size_t)std::max(Rd, 1);
+    CU(ctx->sw_hits.ensure(nhits * sizeof(uint32_t)));
+    CU(ctx->Gd.ensure(std::max<size_t>((size_t)n * nsun * 2, 1) * sizeof(double)));
+    CU(ctx->fetch.ensure(sizeof(unsigned long long)));
+    // capture the pass sequence once per shape
+    char key[256];
+    std::snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%u/%d%d%d%d/%p/%p", n, nsun, Bl, s->direct_rays, s->diffuse_rays,
+                  s->scattering_depth, s->seed, (int)any_direct, (int)any_diffuse, (int)any_copy0, (int)any_active,
+                  ctx->sw_acc.p, ctx->sw_hits.p);
+    {
+        char more[128];
+        std::snprintf(more, sizeof more, "/%p/%p/%p/%p/%p", ctx->sw_in.p, ctx->sw_mat.p, ctx->sw_out.p, ctx->Gd.p,
+                      (void *)ctx->stream);
+        std::strncat(key, more, sizeof key - std::strlen(key) - 1);
+    }
+    if (!ctx->sw_exec || ctx->sw_key != key) {
+        if (ctx->sw_exec) {
+            cudaGraphExecDestroy(ctx->sw_exec);
+            ctx->sw_exec = nullptr;
+        }
+        CU(cudaStreamSynchronize(st));
+        CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int nk = 0;
+        auto enqueue = [&]() -> cudaError_t {
+            cudaError_t e;
+            TraceScene sc = scene_of(ctx);
+            sc.visits = nullptr;
+            if ((e = cudaMemsetAsync(rin, 0, 3 * m * sizeof(double), st)) != cudaSuccess) return e;
+            if ((e = cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), st)) != cudaSuccess) return e;
+            ChannelEpilogue E{};
+            E.n = n;
+            E.C = C;
+            E.Bl = Bl;
+            E.rho = d_rho;
+            E.tau = d_tau;
+            E.rin = rin;
+            E.stop = stp;
+            E.sbot = sbt;
+            if (any_direct && dimx * dimy > 0) {
+                if ((e = cudaMemsetAsync(ctx->Gd.p, 0, (size_t)n * nsun * 2 * sizeof(double), st)) != cudaSuccess) return e;
+                SweepDirectParams D{sc, d_sun, nsun, dimx, dimy, s->seed, ctx->Gd.as<double>()};
+                if ((e = launch_direct_sweep(D, max_blocks(ctx), st)) != cudaSuccess) return e;
+                E.flux = d_flux;
+                E.mask = m_all;
+                E.Gd = ctx->Gd.as<double>();
+                if ((e = launch_epilogue_direct_channels(E, st)) != cudaSuccess) return e;
+                nk += 2;
+            }
+            if ((e = launch_fold_channels(n, C, m_fold, sc.twosided, stp, sbt, otop, obot, st)) != cudaSuccess) return e;
+            ++nk;
+            DiffuseParams P{};
+            P.sc = sc;
+            P.dimx = ddx;
+            P.dimy = ddy;
+            P.seed = s->seed;
+            P.offset = 0;
+            P.count = (uint32_t)n;
+            P.faces = 3;
+            P.fetch = ctx->fetch.as<unsigned long long>();
+            GatherParams Gp{n, C, Rd, 3, sc.twosided, ctx->sw_hits.as<uint32_t>(), otop, obot, d_sky, Gt, Gb};
+            E.Gt = Gt;
+            E.Gb = Gb;
+            E.strength = 1.0 / (double)std::max(Rd, 1);
+            auto pass = [&](uint32_t pass_id, const float *sky, const uint8_t *mask) -> cudaError_t {
+                cudaError_t e2;
+                P.pass = pass_id;
+                if ((e2 = launch_diffuse_record(P, ctx->sw_hits.as<uint32_t>(), st)) != cudaSuccess) return e2;
+                Gp.sky = sky;
+                if ((e2 = launch_gather(Gp, st)) != cudaSuccess) return e2;
+                E.mask = mask;
+                if ((e2 = launch_epilogue_diffuse_channels(E, st)) != cudaSuccess) return e2;
+                nk += 3;
+                return cudaSuccess;
+            };
+            if (any_diffuse && Rd > 0) {
+                if ((e = pass(1u, d_sky, m_diff)) != cudaSuccess) return e;
+            }
+            if (any_copy0) {
+                if ((e = launch_copy_channels(n, C, m_copy0, stp, sbt, otop, obot, 1, st)) != cudaSuccess) return e;
+                ++nk;
+            }
+            if (scattering && any_active && Rd > 0) {
+                for (int it = 0; it < s->scattering_depth; ++it) {
+                    if (it > 0) {
+                        if ((e = launch_copy_channels(n, C, m_all, stp, sbt, otop, obot, 0, st)) != cudaSuccess) return e;
+                        ++nk;
+                    }
+                    if ((e = cudaMemsetAsync(stp, 0, 2 * m * sizeof(double), st)) != cudaSuccess) return e;
+                    if ((e = pass(2u + (uint32_t)it, d_zero, m_active)) != cudaSuccess) return e;
+                }
+            }
+            if ((e = launch_final_flux(m, rin, stp, sbt, fin, st)) != cudaSuccess) return e;
+            ++nk;
+            return cudaSuccess;
+        };
+        cudaError_t ee = enqueue();
+        cudaGraph_t g = nullptr;
+        cudaError_t ec = cudaStreamEndCapture(st, &g);
+        if (ee != cudaSuccess || ec != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return fail(ctx, HRT_ECUDA, std::string("sweep capture failed: ") +
+                                            cudaGetErrorString(ee != cudaSuccess ? ee : ec));
+        }
+        cudaError_t ei = cudaGraphInstantiate(&ctx->sw_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) return fail(ctx, HRT_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+        ctx->sw_key = key;
+        ctx->sw_kernels = nk;
+    }
+    CU(cudaGraphLaunch(ctx->sw_exec, st));
+    ctx->last_kernels = ctx->sw_kernels;
+    if (flux_out) CU(cudaMemcpyAsync(flux_out, fin, m * sizeof(float), cudaMemcpyDeviceToHost, st));
     unsigned long long rays = 0;
     CU(cudaMemcpyAsync(&rays, ctx->counter.p, sizeof(rays), cudaMemcpyDeviceToHost, st));
     r = sync_and_status(ctx);

@@ -305,6 +305,19 @@ __device__ __forceinline__ bool slab(f3 o, f3 inv, f3 lo, f3 hi, float tmin, flo
     return tn <= tf;
 }
 
+// Slab test for BVH node boxes with the ray's origin pre-multiplied (ooi = o * inv):
+// t = lo * inv - ooi in one fused multiply-add per plane.  Node boxes are padded, so
+// the rounding of ooi never culls a box that holds an accepted hit.
+__device__ __forceinline__ bool slab_node(f3 ooi, f3 inv, f3 lo, f3 hi, float tmin, float tmax, float *tnear) {
+    float t0x = __fmaf_rn(lo.x, inv.x, -ooi.x), t1x = __fmaf_rn(hi.x, inv.x, -ooi.x);
+    float t0y = __fmaf_rn(lo.y, inv.y, -ooi.y), t1y = __fmaf_rn(hi.y, inv.y, -ooi.y);
+    float t0z = __fmaf_rn(lo.z, inv.z, -ooi.z), t1z = __fmaf_rn(hi.z, inv.z, -ooi.z);
+    float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+    float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax));
+    *tnear = tn;
+    return tn <= tf;
+}
+
 // Disk: plane hit inside the radius (reference OptiX 6 primitiveIntersection.cu:236-300).
 __device__ __forceinline__ bool disk_hit(f3 o, f3 d, float tmin, f3 c, f3 n, float rad, float tmax, float *t_out,
                                          int *face_out) {

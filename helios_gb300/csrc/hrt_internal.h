@@ -58,6 +58,8 @@ struct DiffuseParams {
     const float *otop, *obot; // radiation_out [n*Bl]
     SkyParams sky;
     double *Gt, *Gb;          // [n*Bl] sums of incoming values per origin face
+    unsigned long long *fetch; // ray-id counter of the persistent kernel (zeroed by the launcher)
+    uint32_t *hits;            // record mode: hit code per ray id, else unused
 };
 
 // ---------------------------------------------------------------- BVH build
@@ -110,6 +112,49 @@ cudaError_t launch_trace_rays(const TraceScene &sc, int64_t nrays, const float *
                               float tmax, int anyhit, int32_t *hit, float *t, int32_t *face, cudaStream_t s);
 cudaError_t launch_gen_rays(const TraceScene &sc, int kind, uint32_t seed, uint32_t pass, int dimx, int dimy,
                             int face, float dx, float dy, float dz, float *o, float *d, cudaStream_t s);
+
+// ---------------------------------------------------------------- batched sweep
+// C = nsun * Bl channels share one scene; channel c = sun * Bl + band.
+struct SweepDirectParams {
+    TraceScene sc;
+    const float *sun_dir;     // [nsun*3] unit directions toward the suns (device)
+    int nsun;
+    int dimx, dimy;
+    uint32_t seed;
+    double *G;                // [n*nsun*2] strength sums of unoccluded rays, [p][sun][face]
+};
+struct GatherParams {
+    int n, C, R;              // primitives, channels, rays per primitive and face
+    int faces;                // bit 0 top, bit 1 bottom
+    const int8_t *twosided;
+    const uint32_t *hits;     // [face][n][R] hit codes (prim<<1|face, kMissCode, kLostCode)
+    const float *otop, *obot; // [n*C]
+    const float *sky;         // [C] isotropic sky flux per channel (0 in scattering passes)
+    double *Gt, *Gb;          // [n*C]
+};
+constexpr uint32_t kMissCode = 0xFFFFFFFFu, kLostCode = 0xFFFFFFFEu;
+cudaError_t launch_direct_sweep(const SweepDirectParams &p, int max_blocks, cudaStream_t s);
+// Persistent diffuse trace that stores every ray's hit code instead of accumulating.
+cudaError_t launch_diffuse_record(const DiffuseParams &p, uint32_t *hits, cudaStream_t s);
+cudaError_t launch_gather(const GatherParams &p, cudaStream_t s);
+struct ChannelEpilogue {
+    int n, C, Bl;
+    const float *rho, *tau;   // [n*Bl]
+    const float *flux;        // direct: [C] source flux per channel
+    const uint8_t *mask;      // [C] 1 = apply this pass to the channel
+    double *rin, *stop, *sbot;
+    const double *Gt, *Gb;    // diffuse [n*C]
+    const double *Gd;         // direct [n*nsun*2]
+    double strength;          // diffuse 1/R
+};
+cudaError_t launch_epilogue_direct_channels(const ChannelEpilogue &p, cudaStream_t s);
+cudaError_t launch_epilogue_diffuse_channels(const ChannelEpilogue &p, cudaStream_t s);
+// out = (float)src for channels with mask[c]; optionally src = 0 afterwards (zero != 0)
+cudaError_t launch_copy_channels(int n, int C, const uint8_t *mask, double *src_top, double *src_bot, float *otop,
+                                 float *obot, int zero, cudaStream_t s);
+// one-sided fold of the direct scatter for masked channels, then scatter = 0 for them
+cudaError_t launch_fold_channels(int n, int C, const uint8_t *mask, const int8_t *twosided, double *stop,
+                                 double *sbot, float *otop, float *obot, cudaStream_t s);
 
 // Epilogues: fold per-face sums into radiation_in / scatter buffers.
 struct EpilogueParams {

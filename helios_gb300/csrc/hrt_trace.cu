@@ -13,6 +13,8 @@
 // before one atomic per (primitive, band) segment.  Material factors
 // (1-rho-tau, rho, tau) are applied afterwards per primitive (epilogues), which
 // equals the reference's per-ray products in exact arithmetic.
+#include <cstdlib>
+
 #include "hrt_device.cuh"
 #include "hrt_internal.h"
 
@@ -43,6 +45,7 @@ __device__ Hit trace_bvh(const TraceScene &sc, f3 o, f3 d, float tmin, float tma
     if (sc.n == 0) return h;
     WT w = wt_setup(d);
     f3 inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+    f3 ooi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
     int32_t stack[kStack];
     int sp = 0;
     int32_t cur = 0;
@@ -60,8 +63,8 @@ __device__ Hit trace_bvh(const TraceScene &sc, f3 o, f3 d, float tmin, float tma
         int32_t c[2] = {__float_as_int(n3.x), __float_as_int(n3.y)};
         float tn0, tn1;
         bool hb[2];
-        hb[0] = slab(o, inv, mk(n0.x, n0.y, n0.z), mk(n0.w, n1.x, n1.y), tmin, best, &tn0);
-        hb[1] = slab(o, inv, mk(n1.z, n1.w, n2.x), mk(n2.y, n2.z, n2.w), tmin, best, &tn1);
+        hb[0] = slab_node(ooi, inv, mk(n0.x, n0.y, n0.z), mk(n0.w, n1.x, n1.y), tmin, best, &tn0);
+        hb[1] = slab_node(ooi, inv, mk(n1.z, n1.w, n2.x), mk(n2.y, n2.z, n2.w), tmin, best, &tn1);
         int32_t next[2];
         int nn = 0;
 #pragma unroll
@@ -433,6 +436,244 @@ __global__ void __launch_bounds__(kBlock) k_diffuse(const DiffuseParams P) {
     }
 }
 
+// ------------------------------------------------------- persistent diffuse --
+// Persistent threads with dynamic ray fetch and speculative while-while traversal
+// (after Aila & Laine, "Understanding the Efficiency of Ray Traversal on GPUs",
+// HPG 2009): a lane whose ray has ended takes the next ray id from a global
+// counter at the top of the next round, so lanes do not idle until the longest
+// ray of the warp ends; leaves are postponed until every active lane has one, so
+// node visits and primitive tests run in separate, convergent loops.  Hit results
+// equal those of trace_bvh (same tests, same tie rule; only the order differs).
+// Each lane keeps a running FP64 sum for its current origin (primitive, face) and
+// adds it to G only when the origin changes.
+constexpr int32_t kSentinel = 0x7FFFFFF0;
+
+#ifndef HRT_PS_MIN_BLOCKS
+#define HRT_PS_MIN_BLOCKS 3
+#endif
+template <int NB, bool RECORD>
+__global__ void __launch_bounds__(kBlock, HRT_PS_MIN_BLOCKS) k_diffuse_ps(const DiffuseParams P) {
+    unsigned long long *fetch = P.fetch;
+    const int lane = threadIdx.x & 31;
+    const uint32_t R = (uint32_t)(P.dimx * P.dimy);
+    const uint32_t per_face = P.count * R;
+    const int nf = ((P.faces & 1) ? 1 : 0) + ((P.faces & 2) ? 1 : 0);
+    const unsigned long long total = (unsigned long long)per_face * (unsigned long long)nf;
+    const uint32_t ni = (uint32_t)(P.sc.n > 1 ? P.sc.n - 1 : 1);
+    const TraceScene &sc = P.sc;
+
+    bool live = false, exhausted = false;
+    f3 o = mk(0.f, 0.f, 0.f), d = o, inv = o, ooi = o;
+    WT w = wt_setup(mk(0.f, 0.f, 1.f));
+    float best = 1e38f;
+    uint32_t bprim = 0xFFFFFFFFu;
+    int bface = 0;
+    int32_t cur = kSentinel, leaf = 0;
+    int sp = 0;
+    int32_t stack[kStack];
+    uint32_t budget = 0;
+    int wraps = 0;
+    uint32_t p = 0;
+    int face = 1;
+    unsigned long long rid = 0;
+    uint32_t akey = 0xFFFFFFFFu;
+    double acc[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) acc[j] = 0.0;
+    unsigned long long nrays = 0;
+
+    for (;;) {
+        // ---- refill lanes without a ray
+        const bool need = !live && !exhausted;
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(fetch, (unsigned long long)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                const unsigned long long id = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
+                if (id >= total) {
+                    exhausted = true;
+                } else {
+                    rid = id;
+                    const uint32_t fi = (uint32_t)(id / per_face);
+                    const uint32_t rem = (uint32_t)(id - (unsigned long long)fi * per_face);
+                    face = (nf == 2) ? (fi == 0 ? 1 : 0) : ((P.faces & 1) ? 1 : 0);
+                    p = P.offset + rem / R;
+                    const uint32_t r = rem % R;
+                    const int ts = sc.twosided[p];
+                    const bool skip = (face == 1 && ts == 3) || (face == 0 && ts != 1);
+                    if (!skip) {
+                        float4 g[4];
+                        load_rgen(sc, p, g);
+                        const uint32_t type = __float_as_uint(g[0].w);
+                        const u4 u = philox(r, p, (uint32_t)face, 0u, P.seed, P.pass);
+                        const int ti = (int)(r % (uint32_t)P.dimx), pi = (int)(r / (uint32_t)P.dimx);
+                        d = diffuse_dir(xyz(g[3]), ti, pi, P.dimx, P.dimy, u01(u.a), u01(u.b));
+                        if (face == 0) d = mk(-d.x, -d.y, -d.z);
+                        o = sample_point(g, type, u01(u.c), u01(u.d));
+                        w = wt_setup(d);
+                        inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+                        ooi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+                        best = 1e38f;
+                        bprim = 0xFFFFFFFFu;
+                        bface = 0;
+                        cur = (sc.n > 0) ? 0 : kSentinel;
+                        leaf = 0;
+                        sp = 0;
+                        budget = 2u * (uint32_t)sc.n + 64u;
+                        wraps = 0;
+                        live = true;
+                        ++nrays;
+                    }
+                }
+            }
+        }
+        // A lane may be idle because its id was skipped by the face rule; only when every
+        // lane has run past the end of the id range is the warp done.
+        if (__all_sync(0xffffffffu, exhausted && !live)) break;
+        if (!live) continue;
+
+        // ---- internal nodes; leaves are postponed
+        while (cur >= 0 && cur != kSentinel) {
+            if ((uint32_t)cur >= ni || budget-- == 0u) {
+                raise(sc.status, ERR_BOUNDS);
+                cur = kSentinel;
+                leaf = 0;
+                break;
+            }
+            const float4 *nd = sc.nodes + 4 * (size_t)cur;
+            const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
+            int32_t c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+            float tn0, tn1;
+            const bool h0 = c0 != kEmptyChild &&
+                            slab_node(ooi, inv, mk(n0.x, n0.y, n0.z), mk(n0.w, n1.x, n1.y), 1e-4f, best, &tn0);
+            const bool h1 = c1 != kEmptyChild &&
+                            slab_node(ooi, inv, mk(n1.z, n1.w, n2.x), mk(n2.y, n2.z, n2.w), 1e-4f, best, &tn1);
+            if (!h0 && !h1) {
+                cur = sp > 0 ? stack[--sp] : kSentinel;
+            } else {
+                cur = h0 ? c0 : c1;
+                if (h0 && h1) {
+                    int32_t farc = c1;
+                    if (tn1 < tn0) {
+                        cur = c1;
+                        farc = c0;
+                    }
+                    if (sp >= kStack) {
+                        raise(sc.status, ERR_STACK);
+                        cur = kSentinel;
+                        leaf = 0;
+                        break;
+                    }
+                    stack[sp++] = farc;
+                }
+            }
+            if (cur < 0 && leaf == 0) {
+                leaf = cur;
+                cur = sp > 0 ? stack[--sp] : kSentinel;
+            }
+            if (__all_sync(__activemask(), leaf != 0)) break;
+        }
+        // ---- primitive tests
+        while (leaf != 0) {
+            const uint32_t slot = (uint32_t)(~leaf);
+            if (slot < (uint32_t)sc.n) {
+                float t;
+                int fc;
+                uint32_t orig;
+                if (rec_hit(sc.rec, slot, w, o, d, inv, 1e-4f, best, &t, &fc, &orig)) {
+                    if (bprim == 0xFFFFFFFFu || t < best || (t == best && orig < bprim)) {
+                        best = t;
+                        bprim = orig;
+                        bface = fc;
+                    }
+                }
+            } else {
+                raise(sc.status, ERR_BOUNDS);
+            }
+            leaf = 0;
+            if (cur < 0) {
+                leaf = cur;
+                cur = sp > 0 ? stack[--sp] : kSentinel;
+            }
+        }
+        if (cur != kSentinel || leaf != 0) continue;  // traversal of this ray goes on next round
+
+        // ---- periodic walls: wrap and restart, or finish the ray
+        bool lost = false;
+        if (sc.nbbox > 0) {
+            float tb;
+            int which = -1;
+            if (wall_closest(sc, o, d, 1e-4f, (bprim != 0xFFFFFFFFu) ? best : 1e38f, &tb, &which) &&
+                (bprim == 0xFFFFFFFFu || tb < best)) {
+                if (wraps >= 9) {
+                    lost = true;
+                } else {
+                    f3 hp = add(o, scl(d, tb));
+                    if ((sc.periodic_x == 1.f) && which < 2) {
+                        float width = sc.bbox[4].x - sc.bbox[0].x;
+                        hp.x = hp.x + ((which == 0) ? width : -width);
+                    } else {
+                        int yb = (sc.periodic_x == 1.f) ? 2 : 0;
+                        float width = sc.bbox[4 * (yb + 1)].y - sc.bbox[4 * yb].y;
+                        hp.y = hp.y + ((which == yb) ? width : -width);
+                    }
+                    o = hp;
+                    ooi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+                    best = 1e38f;
+                    bprim = 0xFFFFFFFFu;
+                    cur = 0;
+                    sp = 0;
+                    budget = 2u * (uint32_t)sc.n + 64u;
+                    ++wraps;
+                    continue;
+                }
+            }
+        }
+        // ---- value of the finished ray, added to the lane's running sum
+        live = false;
+        if (RECORD) {
+            P.hits[rid] = lost ? kLostCode : ((bprim == 0xFFFFFFFFu) ? kMissCode : ((bprim << 1) | (uint32_t)bface));
+            continue;
+        }
+        if (lost) continue;
+        const uint32_t key = 2u * p + (uint32_t)face;
+        if (key != akey) {
+            if (akey != 0xFFFFFFFFu) {
+                double *dst = ((akey & 1u) ? P.Gt : P.Gb) + (size_t)(akey >> 1) * P.Bl;
+#pragma unroll
+                for (int j = 0; j < NB; ++j)
+                    if (j < P.Bc && acc[j] != 0.0) atomicAdd(dst + j, acc[j]);
+            }
+            akey = key;
+#pragma unroll
+            for (int j = 0; j < NB; ++j) acc[j] = 0.0;
+        }
+        if (bprim != 0xFFFFFFFFu) {
+            const float *src = (bface ? P.otop : P.obot) + (size_t)bprim * P.Bl;
+#pragma unroll
+            for (int j = 0; j < NB; ++j)
+                if (j < P.Bc) acc[j] += (double)__ldg(src + j);
+        } else {
+#pragma unroll
+            for (int j = 0; j < NB; ++j)
+                if (j < P.Bc) {
+                    float fl = P.sky.flux[j];
+                    if (fl > 0.f) acc[j] += sky_fd(d, P.sky, j) * (double)fl;
+                }
+        }
+    }
+    if (akey != 0xFFFFFFFFu) {
+        double *dst = ((akey & 1u) ? P.Gt : P.Gb) + (size_t)(akey >> 1) * P.Bl;
+#pragma unroll
+        for (int j = 0; j < NB; ++j)
+            if (j < P.Bc && acc[j] != 0.0) atomicAdd(dst + j, acc[j]);
+    }
+    if (sc.rays && nrays) atomicAdd(sc.rays, nrays);
+}
+
 // ------------------------------------------------------------------ testing --
 __global__ void k_trace_rays(const TraceScene sc, int64_t nrays, const float *__restrict__ o,
                              const float *__restrict__ d, float tmin, float tmax, int anyhit, int32_t *hit, float *t,
@@ -576,6 +817,175 @@ __global__ void k_final(size_t nb, const double *__restrict__ rin, const double 
     if (i < nb) out[i] = (float)((rin[i] + stop[i]) + sbot[i]);
 }
 
+
+// ---------------------------------------------------------------- batched sweep --
+// Shadow rays of many suns in one launch.  Ray ids are sun-major, so a warp holds
+// 32 strata of one primitive toward ONE sun (coherent rays).  Origins and strengths
+// are exactly those of a plain direct pass with the same seed (source slot 0).
+__global__ void __launch_bounds__(kBlock) k_direct_sweep(const SweepDirectParams P) {
+    const uint32_t R = (uint32_t)(P.dimx * P.dimy);
+    const unsigned long long per_sun = (unsigned long long)P.sc.n * R;
+    const unsigned long long total = per_sun * (unsigned long long)P.nsun;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const double inv_nr = 1.0 / (double)R;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
+         base += stride) {
+        const unsigned long long id = base + (threadIdx.x & 31);
+        const bool active = id < total;
+        uint32_t sun = 0, p = 0, r = 0;
+        if (active) {
+            sun = (uint32_t)(id / per_sun);
+            const unsigned long long rem = id - (unsigned long long)sun * per_sun;
+            p = (uint32_t)(rem / R);
+            r = (uint32_t)(rem % R);
+        }
+        double v[2] = {0.0, 0.0};
+        bool live = false;
+        if (active) {
+            float4 g[4];
+            load_rgen(P.sc, p, g);
+            const int ts = P.sc.twosided[p];
+            const uint32_t type = __float_as_uint(g[0].w);
+            const u4 u = philox(r, p, 0u, 0u, P.seed, 0u);
+            float uu = u01(u.a), vv = u01(u.b);
+            if (type != PT_TRI) {
+                const int xi = (int)(r % (uint32_t)P.dimx), yi = (int)(r / (uint32_t)P.dimx);
+                uu = ((float)xi + uu) / (float)P.dimx;
+                vv = ((float)yi + vv) / (float)P.dimy;
+            }
+            const f3 org = sample_point(g, type, uu, vv);
+            const f3 nrm = xyz(g[3]);
+            const f3 dd = normalize(mk(P.sun_dir[3 * sun], P.sun_dir[3 * sun + 1], P.sun_dir[3 * sun + 2]));
+            const double strength = inv_nr * (double)fabsf(dot(nrm, dd));
+            const bool face = dot(dd, nrm) > 0.f;
+            if (!((!face && ts == 0) || ts == 3)) {
+                live = true;
+                uint32_t nv = 0, np = 0;
+                const Hit h = trace_full<false>(P.sc, org, dd, 1e-4f, 1e38f, true, &nv, &np);
+                if (h.prim == 0xFFFFFFFFu) v[face ? 1 : 0] = strength;
+            }
+        }
+        count_rays(P.sc, live);
+        const uint32_t key = active ? (p * (uint32_t)P.nsun + sun) : 0xFFFFFFFFu;
+        warp_segment_add<2>(key, v, 2, P.G, 2);
+    }
+}
+
+// One warp per (face, primitive): lanes run over channels, the R recorded hits of the
+// primitive are read in order, so every sum is deterministic.  A hit reads the row
+// radiation_out[hit][0..C) (coalesced); a miss adds the channel's sky flux.
+template <int CPL>
+__global__ void __launch_bounds__(256) k_gather(const GatherParams P) {
+    const int lane = threadIdx.x & 31;
+    const int nf = ((P.faces & 1) ? 1 : 0) + ((P.faces & 2) ? 1 : 0);
+    const long long items = (long long)nf * P.n;
+    const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long item = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < items; item += warps) {
+        const int fi = (int)(item / P.n);
+        const int p = (int)(item % P.n);
+        const int face = (nf == 2) ? (fi == 0 ? 1 : 0) : ((P.faces & 1) ? 1 : 0);
+        const int ts = P.twosided[p];
+        if ((face == 1 && ts == 3) || (face == 0 && ts != 1)) {  // face not launched: its sums are zero
+            double *G = (face ? P.Gt : P.Gb) + (size_t)p * P.C;
+            for (int c = lane; c < P.C; c += 32) G[c] = 0.0;
+            continue;
+        }
+        double acc[CPL];
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) acc[k] = 0.0;
+        const uint32_t *row = P.hits + ((size_t)fi * P.n + p) * P.R;
+        for (int r = 0; r < P.R; ++r) {
+            const uint32_t h = __ldg(row + r);
+            if (h == kLostCode) continue;
+            if (h == kMissCode) {
+#pragma unroll
+                for (int k = 0; k < CPL; ++k) {
+                    const int c = lane + 32 * k;
+                    if (c < P.C) acc[k] += (double)__ldg(P.sky + c);
+                }
+            } else {
+                const float *src = ((h & 1u) ? P.otop : P.obot) + (size_t)(h >> 1) * P.C;
+#pragma unroll
+                for (int k = 0; k < CPL; ++k) {
+                    const int c = lane + 32 * k;
+                    if (c < P.C) acc[k] += (double)__ldg(src + c);
+                }
+            }
+        }
+        double *G = (face ? P.Gt : P.Gb) + (size_t)p * P.C;
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) {
+            const int c = lane + 32 * k;
+            if (c < P.C) G[c] = acc[k];
+        }
+    }
+}
+
+__global__ void k_epilogue_diffuse_channels(const ChannelEpilogue P) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)P.n * P.C) return;
+    const int p = (int)(i / P.C), c = (int)(i % P.C), b = c % P.Bl;
+    if (!P.mask[c]) return;
+    const double gt = P.Gt[i] * P.strength, gb = P.Gb[i] * P.strength;
+    const double rho = P.rho[(size_t)p * P.Bl + b], tau = P.tau[(size_t)p * P.Bl + b];
+    P.rin[i] += (gt + gb) * (1.0 - rho - tau);
+    if (rho > 0.0 || tau > 0.0) {
+        P.stop[i] += gt * rho + gb * tau;
+        P.sbot[i] += gt * tau + gb * rho;
+    }
+}
+
+__global__ void k_epilogue_direct_channels(const ChannelEpilogue P, int nsun) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)P.n * P.C) return;
+    const int p = (int)(i / P.C), c = (int)(i % P.C), b = c % P.Bl, sun = c / P.Bl;
+    if (!P.mask[c]) return;
+    const double flux = (double)P.flux[c];
+    const double g0 = P.Gd[((size_t)p * nsun + sun) * 2] * flux, g1 = P.Gd[((size_t)p * nsun + sun) * 2 + 1] * flux;
+    const double rho = P.rho[(size_t)p * P.Bl + b], tau = P.tau[(size_t)p * P.Bl + b];
+    P.rin[i] += (g0 + g1) * (1.0 - rho - tau);
+    if (rho > 0.0 || tau > 0.0) {
+        P.stop[i] += g1 * rho + g0 * tau;
+        P.sbot[i] += g1 * tau + g0 * rho;
+    }
+}
+
+__global__ void k_copy_channels(int n, int C, const uint8_t *__restrict__ mask, double *st, double *sb, float *ot,
+                                float *ob, int zero) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)n * C) return;
+    if (!mask[i % C]) return;
+    ot[i] = (float)st[i];
+    ob[i] = (float)sb[i];
+    if (zero) {
+        st[i] = 0.0;
+        sb[i] = 0.0;
+    }
+}
+
+__global__ void k_fold_channels(int n, int C, const uint8_t *__restrict__ mask, const int8_t *__restrict__ ts,
+                                double *st, double *sb, float *ot, float *ob) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)n * C) return;
+    const int p = (int)(i / C);
+    if (!mask[i % C]) {
+        ot[i] = 0.f;
+        ob[i] = 0.f;
+        return;
+    }
+    const double a = st[i], b = sb[i];
+    if (ts[p] == 0) {
+        const double t = a + b;
+        ot[i] = (float)t;
+        ob[i] = (float)t;
+    } else {
+        ot[i] = (float)a;
+        ob[i] = (float)b;
+    }
+    st[i] = 0.0;
+    sb[i] = 0.0;
+}
+
 inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 }  // namespace
@@ -590,10 +1000,43 @@ static cudaError_t direct_impl(const DirectParams &p, int max_blocks, cudaStream
     return cudaGetLastError();
 }
 
+template <int NB>
+static cudaError_t diffuse_ps_launch(const DiffuseParams &p, cudaStream_t s) {
+    static int blocks_per_sm = 0, sms = 0;
+    if (blocks_per_sm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<NB, false>, kBlock, 0);
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    cudaError_t e = cudaMemsetAsync(p.fetch, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    k_diffuse_ps<NB, false><<<sms * blocks_per_sm, kBlock, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+static bool use_persistent() {
+    static int v = -1;
+    if (v < 0) {
+        const char *e = getenv("HRT_TRAVERSAL");
+        v = (e && e[0] == 's') ? 0 : 1;  // "simple" selects the one-ray-per-thread kernel
+    }
+    return v == 1;
+}
+
 template <bool STATS>
 static cudaError_t diffuse_impl(const DiffuseParams &p, int max_blocks, cudaStream_t s) {
     int64_t total = (int64_t)p.count * p.dimx * p.dimy;
     if (total <= 0 || p.Bc <= 0) return cudaSuccess;
+    if (!STATS && p.fetch && use_persistent()) {
+        if (p.Bc <= 1) return diffuse_ps_launch<1>(p, s);
+        if (p.Bc <= 2) return diffuse_ps_launch<2>(p, s);
+        if (p.Bc <= 4) return diffuse_ps_launch<4>(p, s);
+        if (p.Bc <= 8) return diffuse_ps_launch<8>(p, s);
+        if (p.Bc <= 16) return diffuse_ps_launch<16>(p, s);
+        return cudaErrorInvalidValue;
+    }
     unsigned nb = blocks_for(total, kBlock);
     if ((int)nb > max_blocks) nb = (unsigned)max_blocks;
     dim3 grid(nb, 2);
@@ -675,6 +1118,79 @@ cudaError_t launch_final_flux(size_t nb, const double *rin, const double *stop, 
                               cudaStream_t s) {
     if (nb == 0) return cudaSuccess;
     k_final<<<blocks_for((int64_t)nb, 256), 256, 0, s>>>(nb, rin, stop, sbot, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_direct_sweep(const SweepDirectParams &p, int max_blocks, cudaStream_t s) {
+    const long long total = (long long)p.sc.n * p.dimx * p.dimy * p.nsun;
+    if (total <= 0) return cudaSuccess;
+    unsigned nb = blocks_for(total, kBlock);
+    if ((int)nb > max_blocks) nb = (unsigned)max_blocks;
+    k_direct_sweep<<<nb, kBlock, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_diffuse_record(const DiffuseParams &p, uint32_t *hits, cudaStream_t s) {
+    if ((long long)p.count * p.dimx * p.dimy <= 0) return cudaSuccess;
+    static int blocks_per_sm = 0, sms = 0;
+    if (blocks_per_sm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<1, true>, kBlock, 0);
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    DiffuseParams q = p;
+    q.hits = hits;
+    q.Bc = 1;
+    cudaError_t e = cudaMemsetAsync(q.fetch, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    k_diffuse_ps<1, true><<<sms * blocks_per_sm, kBlock, 0, s>>>(q);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const GatherParams &p, cudaStream_t s) {
+    const int nf = ((p.faces & 1) ? 1 : 0) + ((p.faces & 2) ? 1 : 0);
+    const long long warps = (long long)nf * p.n;
+    if (warps <= 0) return cudaSuccess;
+    long long blocks = (warps * 32 + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    const int cpl = (p.C + 31) / 32;
+    if (cpl <= 1) k_gather<1><<<(unsigned)blocks, 256, 0, s>>>(p);
+    else if (cpl <= 2) k_gather<2><<<(unsigned)blocks, 256, 0, s>>>(p);
+    else if (cpl <= 4) k_gather<4><<<(unsigned)blocks, 256, 0, s>>>(p);
+    else if (cpl <= 8) k_gather<8><<<(unsigned)blocks, 256, 0, s>>>(p);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_epilogue_direct_channels(const ChannelEpilogue &p, cudaStream_t s) {
+    const long long m = (long long)p.n * p.C;
+    if (m <= 0) return cudaSuccess;
+    k_epilogue_direct_channels<<<blocks_for(m, 256), 256, 0, s>>>(p, p.C / p.Bl);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_epilogue_diffuse_channels(const ChannelEpilogue &p, cudaStream_t s) {
+    const long long m = (long long)p.n * p.C;
+    if (m <= 0) return cudaSuccess;
+    k_epilogue_diffuse_channels<<<blocks_for(m, 256), 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_copy_channels(int n, int C, const uint8_t *mask, double *src_top, double *src_bot, float *otop,
+                                 float *obot, int zero, cudaStream_t s) {
+    const long long m = (long long)n * C;
+    if (m <= 0) return cudaSuccess;
+    k_copy_channels<<<blocks_for(m, 256), 256, 0, s>>>(n, C, mask, src_top, src_bot, otop, obot, zero);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fold_channels(int n, int C, const uint8_t *mask, const int8_t *twosided, double *stop,
+                                 double *sbot, float *otop, float *obot, cudaStream_t s) {
+    const long long m = (long long)n * C;
+    if (m <= 0) return cudaSuccess;
+    k_fold_channels<<<blocks_for(m, 256), 256, 0, s>>>(n, C, mask, twosided, stop, sbot, otop, obot);
     return cudaGetLastError();
 }
 

@@ -230,3 +230,37 @@ def sun_direction(zenith_deg: float, azimuth_deg: float) -> np.ndarray:
     el = math.radians(90.0 - zenith_deg)
     az = math.radians(azimuth_deg)
     return np.array([math.cos(el) * math.sin(az), math.cos(el) * math.cos(az), math.sin(el)], np.float32)
+
+
+def day_sweep(latitude_deg=38.5, day_of_year=180, n=96, bands=("PAR", "NIR")):
+    """Sun positions every 24h/n of local solar time (Cooper's declination, hour angle) and a
+    simple clear-sky split per band: direct normal flux S*k^(1/sin(elev)-1) and isotropic
+    sky flux f*S*sin(elev), both zero with the sun below the horizon.
+    Returns (sun_dir [n,3] toward the sun, direct [n,B], diffuse [n,B], elevation [n] rad)."""
+    params = {"PAR": (500.0, 0.75, 0.15), "NIR": (450.0, 0.80, 0.10)}
+    lat = math.radians(latitude_deg)
+    dec = math.radians(23.45) * math.sin(2.0 * math.pi * (284 + day_of_year) / 365.0)
+    dirs, direct, diffuse, elev = [], [], [], []
+    for k in range(n):
+        hour = 24.0 * k / n
+        w = math.radians(15.0 * (hour - 12.0))
+        se = math.sin(lat) * math.sin(dec) + math.cos(lat) * math.cos(dec) * math.cos(w)
+        el = math.asin(max(-1.0, min(1.0, se)))
+        # azimuth from north toward east
+        az = math.atan2(-math.sin(w) * math.cos(dec),
+                        math.cos(lat) * math.sin(dec) - math.sin(lat) * math.cos(dec) * math.cos(w))
+        dirs.append([math.cos(el) * math.sin(az), math.cos(el) * math.cos(az), math.sin(el)])
+        row_d, row_s = [], []
+        for b in bands:
+            S, kk, f = params[b]
+            if se > 1e-3:
+                row_d.append(S * kk ** (1.0 / se - 1.0))
+                row_s.append(f * S * se)
+            else:
+                row_d.append(0.0)
+                row_s.append(0.0)
+        direct.append(row_d)
+        diffuse.append(row_s)
+        elev.append(el)
+    return (np.asarray(dirs, np.float32), np.asarray(direct, np.float32), np.asarray(diffuse, np.float32),
+            np.asarray(elev))

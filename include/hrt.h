@@ -151,6 +151,27 @@ const char *hrt_backend_name(void);
  * flux_out: host [n*Bl] = radiation_in + scatter_top + scatter_bottom
  * (RadiationModel.cpp:4652), or NULL to leave the result on the device. */
 int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out);
+/* ---- many solves of one scene in one launch graph (no counterpart in the reference;
+ * it replaces nsun*nbands separate runBand calls).  Channel c = sun*nbands + band is the
+ * solve RadiationModel::runBand(band) would give with one collimated source toward
+ * sun_dir[sun], source flux direct_flux[c], isotropic sky flux diffuse_flux[c], the same
+ * ray counts, depth and seed; no emission.  Direct rays are traced per sun; every diffuse
+ * and scattering pass is traced ONCE for all channels (the rays do not depend on the sun)
+ * and each ray's hit is gathered for every channel.  The whole sweep is captured into a
+ * CUDA graph on the first call of a given shape and replayed afterwards. */
+typedef struct {
+    int32_t nsun;
+    const float *sun_dir;        /* [nsun*3] direction toward each sun */
+    int32_t nbands;
+    const float *direct_flux;    /* [nsun*nbands] (0 with the sun below the horizon) */
+    const float *diffuse_flux;   /* [nsun*nbands] isotropic sky flux */
+    const float *rho, *tau;      /* [n*nbands] */
+    int32_t direct_rays, diffuse_rays, scattering_depth;
+    uint32_t seed;
+} hrt_sweep;
+/* flux_out: host [n*nsun*nbands] (channel fastest), or NULL. */
+int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out);
+
 /* Statistics of the last hrt_run_band: [0] rays traced, [1] kernels launched. */
 int hrt_last_stats(const hrt_context *ctx, uint64_t *stats, int count);
 /* Device status word (HRT error bits) accumulated since the last reset. */

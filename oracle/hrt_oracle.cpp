@@ -319,6 +319,18 @@ inline bool slab(const V3 &o, const V3 &inv, V3 lo, V3 hi, float tmin, float tma
     *tnear = tn;
     return tn <= tf;
 }
+// BVH node boxes: t = lo * inv - o * inv with one fused multiply-add per plane.
+inline bool slab_node(const V3 &ooi, const V3 &inv, V3 lo, V3 hi, float tmin, float tmax, float *tnear) {
+    float t0x = std::fma(lo.x, inv.x, -ooi.x), t1x = std::fma(hi.x, inv.x, -ooi.x);
+    float t0y = std::fma(lo.y, inv.y, -ooi.y), t1y = std::fma(hi.y, inv.y, -ooi.y);
+    float t0z = std::fma(lo.z, inv.z, -ooi.z), t1z = std::fma(hi.z, inv.z, -ooi.z);
+    float tn = std::fmax(std::fmax(std::fmin(t0x, t1x), std::fmin(t0y, t1y)),
+                         std::fmax(std::fmin(t0z, t1z), tmin));
+    float tf = std::fmin(std::fmin(std::fmax(t0x, t1x), std::fmax(t0y, t1y)),
+                         std::fmin(std::fmax(t0z, t1z), tmax));
+    *tnear = tn;
+    return tn <= tf;
+}
 inline float safe_inv(float d) {
     if (std::fabs(d) < 1e-30f) d = std::copysign(1e-30f, d);
     return 1.0f / d;
@@ -623,6 +635,7 @@ Hit trace_bvh(const Scene &s, const Ray &ray, bool anyhit, TraceStats *st) {
     if (s.n == 0) return h;
     WT w = wt_setup(ray.d);
     V3 inv = v3(safe_inv(ray.d.x), safe_inv(ray.d.y), safe_inv(ray.d.z));
+    V3 ooi = v3(ray.o.x * inv.x, ray.o.y * inv.y, ray.o.z * inv.z);
     int32_t stack[128];
     int sp = 0;
     int32_t cur = 0;
@@ -631,10 +644,10 @@ Hit trace_bvh(const Scene &s, const Ray &ray, bool anyhit, TraceStats *st) {
         const Node &nd = s.nodes[cur];
         if (st) st->nodes++;
         float tn0, tn1;
-        bool h0 = slab(ray.o, inv, v3(nd.b[0], nd.b[1], nd.b[2]), v3(nd.b[3], nd.b[4], nd.b[5]),
-                       ray.tmin, best, &tn0);
-        bool h1 = slab(ray.o, inv, v3(nd.b[6], nd.b[7], nd.b[8]), v3(nd.b[9], nd.b[10], nd.b[11]),
-                       ray.tmin, best, &tn1);
+        bool h0 = slab_node(ooi, inv, v3(nd.b[0], nd.b[1], nd.b[2]), v3(nd.b[3], nd.b[4], nd.b[5]),
+                            ray.tmin, best, &tn0);
+        bool h1 = slab_node(ooi, inv, v3(nd.b[6], nd.b[7], nd.b[8]), v3(nd.b[9], nd.b[10], nd.b[11]),
+                            ray.tmin, best, &tn1);
         int32_t c0 = nd.c[0], c1 = nd.c[1];
         // leaves are tested immediately, internal children are traversed near-first
         int32_t next[2];

@@ -88,8 +88,9 @@ def test_hit_ids_exact(gpu, oracle_mod, anyhit):
     assert gpu.device_status() == 0
 
 
-def _canopy_model(n_leaves=2000, depth=3, periodic=False, mode="device"):
-    sc = scenes.homogeneous_canopy(n_leaves=n_leaves, leaf=0.1, domain=math.sqrt(n_leaves * 0.01 / 2.0), seed=0)
+def _canopy_model(n_leaves=2000, depth=3, periodic=False, mode="device", ground_div=1):
+    sc = scenes.homogeneous_canopy(n_leaves=n_leaves, leaf=0.1, domain=math.sqrt(n_leaves * 0.01 / 2.0), seed=0,
+                                   ground_div=ground_div)
     ctx = Context()
     ctx.addScene(sc)
     ctx.setPrimitiveData(sc.groups["leaves"], "reflectivity_SW", np.full(n_leaves, 0.10))
@@ -114,6 +115,18 @@ def test_canopy_flux_vs_oracle(oracle_mod, periodic):
     rad.setSeed(77)
     got = rad.runBand("SW")
     ref, st = run_oracle(rad, ["SW"], oracle_mod, seed=77)
+    worst, _ = _flux_close(got, ref)
+    assert worst <= FLUX_RTOL, worst
+    assert rad.last_stats["rays"] == st["rays"]
+
+
+def test_many_onesided_before_twosided(oracle_mod):
+    """A 40 x 40 one-sided ground tile comes first, so the bottom-face ray range starts with
+    1600 x 324 rays that the face rule skips; every later two-sided primitive must still be traced."""
+    rad = _canopy_model(n_leaves=1500, depth=1, periodic=True, ground_div=40)
+    rad.setSeed(17)
+    got = rad.runBand("SW")
+    ref, st = run_oracle(rad, ["SW"], oracle_mod, seed=17)
     worst, _ = _flux_close(got, ref)
     assert worst <= FLUX_RTOL, worst
     assert rad.last_stats["rays"] == st["rays"]

@@ -1,0 +1,59 @@
+"""Batched day sweep (hrt_run_sweep): every channel equals the plain runBand it stands for."""
+import numpy as np
+import pytest
+
+from helios_gb300 import scenes
+from helios_gb300.radiation import Context, RadiationModel
+
+pytestmark = pytest.mark.gpu
+
+
+def _orchard(mode="device"):
+    sc = scenes.orchard(nx=2, ny=2, leaves_per_tree=800, side=0.06, seed=3, ground=True)
+    ctx = Context()
+    ctx.addScene(sc)
+    lv = sc.groups["leaves"]
+    ctx.setPrimitiveData(lv, "reflectivity_PAR", np.full(lv.size, 0.08))
+    ctx.setPrimitiveData(lv, "transmissivity_PAR", np.full(lv.size, 0.05))
+    ctx.setPrimitiveData(lv, "reflectivity_NIR", np.full(lv.size, 0.45))
+    ctx.setPrimitiveData(lv, "transmissivity_NIR", np.full(lv.size, 0.40))
+    rad = RadiationModel(ctx, mode=mode)
+    for b in ("PAR", "NIR"):
+        rad.addRadiationBand(b)
+        rad.disableEmission(b)
+        rad.setDirectRayCount(b, 49)
+        rad.setDiffuseRayCount(b, 64)
+        rad.setScatteringDepth(b, 3)
+    return rad, sc
+
+
+def test_sweep_channels_equal_plain_solves():
+    rad, sc = _orchard()
+    dirs, direct, diffuse, _ = scenes.day_sweep(n=8)
+    # force one twilight channel (sky only) to exercise the sequence without a direct pass
+    direct[2, :] = 0.0
+    diffuse[2, :] = [20.0, 15.0]
+    rad.updateGeometry()
+    desc = rad.solve_description(["PAR", "NIR"])
+    n = sc.n
+    rho = desc["rho"][0]  # [n, Bg] (bands in std::map order: NIR, PAR)
+    tau = desc["tau"][0]
+    order = ["NIR", "PAR"]
+    sweep = rad.ctx.run_sweep(dirs, direct[:, ::-1], diffuse[:, ::-1], rho, tau, 49, 64, 3, seed=123)
+    assert sweep.shape == (n, 8, 2)
+    sun = 0  # the collimated source solve_description() created (Philox source slot 0)
+    assert len(rad.sources) == 1
+    for s in range(8):
+        for bi, band in enumerate(order):
+            rad.sources[sun]["position"] = tuple(float(x) for x in dirs[s])
+            rad.setSourceFlux(sun, band, float(direct[s, 1 - bi]))
+            rad.setDiffuseRadiationFlux(band, float(diffuse[s, 1 - bi]))
+            rad.setSeed(123)
+            plain = rad.runBand(band)[:, 0].astype(np.float64)
+            got = sweep[:, s, bi].astype(np.float64)
+            floor = 1e-3 * max(float(np.abs(plain).mean()), 1e-30)
+            err = np.abs(got - plain) / np.maximum(np.abs(plain), floor)
+            assert err.max() <= 1e-5, (s, band, err.max())
+    # a replay of the captured graph gives the same numbers
+    again = rad.ctx.run_sweep(dirs, direct[:, ::-1], diffuse[:, ::-1], rho, tau, 49, 64, 3, seed=123)
+    np.testing.assert_allclose(again, sweep, rtol=1e-6, atol=1e-6)
