@@ -178,6 +178,50 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_batched(rad, ctx, desc, stream, args):
+    """Day sweep: 96 sun positions x (PAR, NIR) = 192 solves of the same orchard in one
+    graph-captured launch, against plain single-band runBand solves on the same GPU."""
+    import torch
+
+    from helios_gb300 import scenes
+
+    dirs, direct, diffuse, _ = scenes.day_sweep(latitude_deg=38.5, day_of_year=180, n=96, bands=("NIR", "PAR"))
+    bands_sorted = sorted(["LW", "NIR", "PAR"])
+    cols = [bands_sorted.index("NIR"), bands_sorted.index("PAR")]
+    rho = desc["rho"][0][:, cols]
+    tau = desc["tau"][0][:, cols]
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.run_sweep(dirs, direct, diffuse, rho, tau, 100, 200, 5, seed=7, out=False)  # capture + warm-up
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    reps = max(1, min(args.steps, 2))
+    for _ in range(reps):
+        ctx.run_sweep(dirs, direct, diffuse, rho, tau, 100, 200, 5, seed=7, out=False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_sweep = ev0.elapsed_time(ev1) / 1e3 / reps
+    sweep_rays = ctx.last_stats()["rays"]
+    # plain: one runBand per (sun, band); timed on single-band solves at the bench's sun
+    plain = rad.solve_description(["PAR"])
+    ctx.run_band(plain, out=False)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(2):
+        ctx.run_band(plain, out=False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_plain = ev0.elapsed_time(ev1) / 1e3 / 2
+    plain_rays = ctx.last_stats()["rays"]
+    nsol = dirs.shape[0] * 2
+    return {"workload": "day sweep: 96 sun positions (15 min, 38.5N, day 180) x PAR, NIR = 192 solves, depth 5",
+            "s_per_sweep": t_sweep, "solves_per_s": nsol / t_sweep, "rays_per_sweep": sweep_rays,
+            "rays_per_s": sweep_rays / t_sweep, "plain_s_per_solve": t_plain, "plain_solves_per_s": 1.0 / t_plain,
+            "plain_rays_per_solve": plain_rays, "speedup_solves_per_s": (nsol / t_sweep) * t_plain,
+            "graph_kernels": ctx.last_stats()["kernels"],
+            "plain_note": "plain = one single-band runBand (direct + primary diffuse + 5 scattering passes) timed "
+                          "twice; 192 plain solves take 192x that"}
+
+
 def run_gpu(args):
     import torch
 
@@ -246,6 +290,9 @@ def run_gpu(args):
         flux = ctx.run_band(full, out=True)
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(rad, ctx, desc, stream, args)
     if rank != 0:
         return
     hbm, peak_kind = peaks()
@@ -283,6 +330,7 @@ def run_gpu(args):
                 "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s},
         "gpu_launches": None,
         "cpu_baseline": cpu,
+        "batched": batched,
     }
     line["gpu_launches"] = int(ctx.last_stats()["kernels"]) * args.steps
     print(json.dumps(line))
@@ -295,6 +343,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="hrt", choices=["hrt", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the day-sweep measurement")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--trees", type=int, nargs=2, default=(20, 10), help="orchard grid (default 20 x 10 = 1M leaves)")
     args = ap.parse_args()
