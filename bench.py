@@ -222,6 +222,73 @@ def run_batched(rad, ctx, desc, stream, args):
                           "twice; 192 plain solves take 192x that"}
 
 
+def run_served(args, device=0):
+    """Served stream: Poisson arrivals at 50/s of homogeneous-canopy scenes with sizes
+    log-uniform in [2k, 2M] (patch:triangle 1:1), 1-4 bands, sun zenith U[0,75], 50-400
+    diffuse rays, 100 direct rays, scattering depth 1, through the continuous-batching
+    server; against the plain per-solve path (geometry upload + BVH build + solve per
+    request, one at a time) on the same requests."""
+    from helios_gb300 import _hrt, scenes
+
+    sizes, lais, reqs = scenes.served_stream(n_requests=args.serve_requests, rate=50.0, n_scenes=args.serve_scenes,
+                                             seed=0)
+    built = {}
+    used = sorted({r["scene"] for r in reqs})
+    for k in used:
+        built[k] = scenes.mixed_canopy(int(sizes[k]), float(lais[k]), seed=k)
+
+    def mats(sc):
+        rho = np.tile(scenes.SERVED_RHO, (sc.n, 1))
+        tau = np.tile(scenes.SERVED_TAU, (sc.n, 1))
+        rho[0] = 0.0
+        tau[0] = 0.0
+        return rho, tau
+
+    depth = 1
+    srv = _hrt.Server(device=device, workers=8, hbm_budget=64 << 30)
+    for k in used:
+        rho, tau = mats(built[k])
+        srv.add_scene(k, built[k].T, built[k].ptype, built[k].twosided, rho, tau)
+    for r in reqs:
+        srv.submit(r["id"], r["scene"], r["arrival"], r["bands"], r["sun"], r["direct"], r["diffuse"], 100,
+                   r["diffuse_rays"], depth, r["seed"])
+    t0 = time.perf_counter()
+    srv.start()
+    srv.wait()
+    wall = time.perf_counter() - t0
+    res = [srv.result(r["id"]) for r in reqs]
+    lat = np.array([x["done"] - x["arrival"] for x in res])
+    rays = sum(x["rays"] for x in res)
+    span = max(x["done"] for x in res) - min(x["arrival"] for x in res)
+    st = srv.stats()
+    srv.close()
+    # plain per-solve path on a prefix of the same requests
+    nplain = min(len(reqs), args.serve_plain)
+    ctx = _hrt.Context(device)
+    t0 = time.perf_counter()
+    for r in reqs[:nplain]:
+        sc = built[r["scene"]]
+        rho, tau = mats(sc)
+        bl = int(r["bands"].sum())
+        ctx.update_geometry(sc.T, sc.ptype, sc.twosided)
+        ctx.build_accel()
+        ctx.run_band({"band_launch": r["bands"], "sources": [{"type": 0, "position": tuple(r["sun"])}],
+                      "source_flux": r["direct"], "rho": rho, "tau": tau, "diffuse_flux": r["diffuse"],
+                      "direct_rays": np.full(bl, 100), "diffuse_rays": np.full(bl, r["diffuse_rays"]),
+                      "depth": np.full(bl, depth), "emission": np.zeros(bl, np.uint8), "seed": r["seed"]})
+    t_plain = time.perf_counter() - t0
+    served_sps = len(reqs) / span
+    plain_sps = nplain / t_plain
+    return {"workload": f"{len(reqs)} requests, Poisson 50/s, {len(used)} canopy scenes log-uniform 2k-2M "
+                        f"(patch:triangle 1:1), LAI U[0.5,5], 1-4 bands, zenith U[0,75], 50-400 diffuse rays, "
+                        f"100 direct, depth {depth}",
+            "offered_rate_per_s": 50.0, "solves_per_s": served_sps, "rays_per_s": rays / span,
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "wall_s": wall, "bvh_builds": st["builds"], "evictions": st["evictions"],
+            "plain_solves_per_s": plain_sps, "plain_requests_timed": nplain,
+            "speedup_solves_per_s": served_sps / plain_sps}
+
+
 def run_gpu(args):
     import torch
 
@@ -293,6 +360,9 @@ def run_gpu(args):
     batched = None
     if not args.no_batched:
         batched = run_batched(rad, ctx, desc, stream, args)
+    served = None
+    if args.serve_requests > 0:
+        served = run_served(args, device=local)
     if rank != 0:
         return
     hbm, peak_kind = peaks()
@@ -331,6 +401,7 @@ def run_gpu(args):
         "gpu_launches": None,
         "cpu_baseline": cpu,
         "batched": batched,
+        "served": served,
     }
     line["gpu_launches"] = int(ctx.last_stats()["kernels"]) * args.steps
     print(json.dumps(line))
@@ -344,6 +415,9 @@ def main():
     ap.add_argument("--impl", default="hrt", choices=["hrt", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the day-sweep measurement")
+    ap.add_argument("--serve-requests", type=int, default=100, help="served-stream requests (0 = skip)")
+    ap.add_argument("--serve-scenes", type=int, default=16, help="distinct scenes in the served stream")
+    ap.add_argument("--serve-plain", type=int, default=30, help="requests timed on the plain per-solve path")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--trees", type=int, nargs=2, default=(20, 10), help="orchard grid (default 20 x 10 = 1M leaves)")
     args = ap.parse_args()

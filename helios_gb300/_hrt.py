@@ -24,6 +24,8 @@ EXPORTS = [
     "hrt_copy_scatter_to_radiation", "hrt_upload_radiation_out", "hrt_query_memory", "hrt_backend_name",
     "hrt_run_band", "hrt_last_stats", "hrt_device_status", "hrt_trace_rays", "hrt_gen_rays", "hrt_get_bvh",
     "hrt_source_rotation", "hrt_set_measure", "hrt_get_measure", "hrt_build_accel_static", "hrt_run_sweep",
+    "hrt_server_create", "hrt_server_add_scene", "hrt_server_submit", "hrt_server_start", "hrt_server_wait",
+    "hrt_server_result", "hrt_server_stats", "hrt_server_destroy",
 ]
 
 
@@ -69,6 +71,13 @@ class Sweep(C.Structure):
                 ("diffuse_rays", C.c_int32), ("scattering_depth", C.c_int32), ("seed", C.c_uint32)]
 
 
+class ServeRequest(C.Structure):
+    _fields_ = [("request_id", C.c_uint64), ("scene_id", C.c_uint32), ("arrival_s", C.c_double),
+                ("band_launch", C.c_void_p), ("sun_dir", C.c_float * 3), ("source_flux", C.c_void_p),
+                ("diffuse_flux", C.c_void_p), ("direct_rays", C.c_int32), ("diffuse_rays", C.c_int32),
+                ("scattering_depth", C.c_int32), ("seed", C.c_uint32), ("keep_result", C.c_int32)]
+
+
 _lib = None
 VP = C.c_void_p
 
@@ -112,6 +121,14 @@ def load(path: str | None = None):
         "hrt_get_measure": (C.c_int, [VP, VP, C.c_int]),
         "hrt_build_accel_static": (C.c_int, [VP, VP, C.c_int32, VP, VP, VP, VP, VP, VP]),
         "hrt_run_sweep": (C.c_int, [VP, C.POINTER(Sweep), VP]),
+        "hrt_server_create": (C.c_int, [C.POINTER(VP), C.c_int, C.c_int, C.c_size_t]),
+        "hrt_server_add_scene": (C.c_int, [VP, C.c_uint32, C.POINTER(Geometry), C.c_int32, VP, VP]),
+        "hrt_server_submit": (C.c_int, [VP, C.POINTER(ServeRequest)]),
+        "hrt_server_start": (C.c_int, [VP]),
+        "hrt_server_wait": (C.c_int, [VP]),
+        "hrt_server_result": (C.c_int, [VP, C.c_uint64, VP, C.c_size_t, VP, VP, VP]),
+        "hrt_server_stats": (C.c_int, [VP, VP, C.c_int]),
+        "hrt_server_destroy": (C.c_int, [VP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -384,3 +401,72 @@ class Context:
         st = C.c_uint32()
         self.check(self.lib.hrt_device_status(self.h, C.byref(st), int(reset)))
         return st.value
+
+
+class Server:
+    """Continuous-batching server over libhrt (hrt_server_*)."""
+
+    def __init__(self, device=0, workers=8, hbm_budget=32 << 30):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.hrt_server_create(C.byref(h), device, workers, int(hbm_budget))
+        if rc != HRT_OK:
+            raise HrtError(rc, "hrt_server_create failed")
+        self.h = h
+        self.scenes = {}
+
+    def check(self, rc, what):
+        if rc != HRT_OK:
+            raise HrtError(rc, what)
+
+    def add_scene(self, scene_id, T, ptype, twosided, rho, tau):
+        T = f32(T).reshape(-1, 16)
+        ty = np.ascontiguousarray(ptype, np.uint32)
+        ts = np.ascontiguousarray(twosided, np.int8)
+        rho = f32(rho).reshape(T.shape[0], -1)
+        tau = f32(tau).reshape(T.shape[0], -1)
+        g = Geometry(T.shape[0], ptr(T), ptr(ty), ptr(ts), 0, None, 0.0, 0.0)
+        self.check(self.lib.hrt_server_add_scene(self.h, scene_id, C.byref(g), rho.shape[1], ptr(rho), ptr(tau)),
+                   "add_scene")
+        self.scenes[scene_id] = (T.shape[0], rho.shape[1])
+
+    def submit(self, request_id, scene_id, arrival_s, band_launch, sun_dir, source_flux, diffuse_flux,
+               direct_rays, diffuse_rays, depth, seed, keep=False):
+        bl = np.ascontiguousarray(band_launch, np.uint8)
+        sf, df = f32(source_flux).ravel(), f32(diffuse_flux).ravel()
+        q = ServeRequest(int(request_id), int(scene_id), float(arrival_s), ptr(bl), (C.c_float * 3)(*sun_dir),
+                         ptr(sf), ptr(df), int(direct_rays), int(diffuse_rays), int(depth), int(seed) & 0xFFFFFFFF,
+                         int(bool(keep)))
+        self.check(self.lib.hrt_server_submit(self.h, C.byref(q)), "submit")
+
+    def start(self):
+        self.check(self.lib.hrt_server_start(self.h), "start")
+
+    def wait(self):
+        self.check(self.lib.hrt_server_wait(self.h), "wait")
+
+    def result(self, request_id, count=0):
+        timing = np.zeros(3, np.float64)
+        cs = C.c_double()
+        rays = C.c_uint64()
+        flux = np.zeros(count, np.float32) if count else None
+        self.check(self.lib.hrt_server_result(self.h, int(request_id), ptr(flux), count, ptr(timing), C.byref(cs),
+                                              C.byref(rays)), "result")
+        return {"arrival": timing[0], "admit": timing[1], "done": timing[2], "checksum": cs.value,
+                "rays": rays.value, "flux": flux}
+
+    def stats(self):
+        out = np.zeros(4, np.float64)
+        self.check(self.lib.hrt_server_stats(self.h, ptr(out), 4), "stats")
+        return {"builds": int(out[0]), "evictions": int(out[1]), "resident_bytes": out[2], "budget": out[3]}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.hrt_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

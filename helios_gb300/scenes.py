@@ -264,3 +264,60 @@ def day_sweep(latitude_deg=38.5, day_of_year=180, n=96, bands=("PAR", "NIR")):
         elev.append(el)
     return (np.asarray(dirs, np.float32), np.asarray(direct, np.float32), np.asarray(diffuse, np.float32),
             np.asarray(elev))
+
+
+def mixed_canopy(n, lai, seed=0, height=3.0, leaf_area=0.0025):
+    """Homogeneous canopy of n leaves, half square patches and half equilateral triangles
+    (patch:triangle 1:1) of equal area, spherical leaf angles, over a one-sided ground
+    patch; the domain side follows from the leaf area index: sqrt(n * leaf_area / LAI)."""
+    rng = np.random.default_rng(seed)
+    n_patch = n // 2
+    n_tri = n - n_patch
+    dom = math.sqrt(max(n, 1) * leaf_area / lai)
+    side_p = math.sqrt(leaf_area)
+    side_t = math.sqrt(4.0 * leaf_area / math.sqrt(3.0))
+    c = np.stack([rng.uniform(0, dom, n), rng.uniform(0, dom, n), rng.uniform(0.05, height, n)], -1)
+    nrm = uniform_sphere(rng, n)
+    spin = rng.uniform(0, 2 * math.pi, n)
+    Tp = frame_T(c[:n_patch], np.full(n_patch, side_p), np.full(n_patch, side_p), nrm[:n_patch], spin[:n_patch])
+    ct, nt, st = c[n_patch:], nrm[n_patch:], spin[n_patch:]
+    helper = np.where(np.abs(nt[:, 2:3]) < 0.9, np.array([0.0, 0.0, 1.0]), np.array([1.0, 0.0, 0.0]))
+    ex = np.cross(helper, nt)
+    ex /= np.linalg.norm(ex, axis=-1, keepdims=True)
+    ey = np.cross(nt, ex)
+    R = side_t / math.sqrt(3.0)
+    vs = [ct + R * (np.cos(st + 2 * math.pi * k / 3)[:, None] * ex + np.sin(st + 2 * math.pi * k / 3)[:, None] * ey)
+          for k in range(3)]
+    Tt = triangle_T(vs[0], vs[1], vs[2])
+    ground = helios_patch_T((0.5 * dom, 0.5 * dom, 0.0), (dom, dom))[None, :]
+    T, ty, ts, area = _concat([(ground, PATCH, 0, np.array([dom * dom])), (Tp, PATCH, 1, np.full(n_patch, leaf_area)),
+                               (Tt, TRIANGLE, 1, np.full(n_tri, leaf_area))])
+    return Scene(T, ty, ts, area, {"ground": np.array([0]), "leaves": np.arange(1, n + 1)})
+
+
+def served_stream(n_requests=2000, rate=50.0, n_scenes=32, n_min=2000, n_max=2000000, seed=0):
+    """Request stream of the served configuration: Poisson arrivals, scene sizes
+    log-uniform in [n_min, n_max] (patch:triangle 1:1), LAI U[0.5, 5], 1-4 of 4 bands,
+    sun zenith U[0, 75] deg, 50-400 diffuse rays.  Requests draw from a pool of
+    n_scenes scenes so that resident BVHs are reused."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(math.log(n_min), math.log(n_max), n_scenes)).astype(int)
+    lais = rng.uniform(0.5, 5.0, n_scenes)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    reqs = []
+    for i in range(n_requests):
+        nb = int(rng.integers(1, 5))
+        flags = np.zeros(4, np.uint8)
+        flags[rng.choice(4, nb, replace=False)] = 1
+        zen = rng.uniform(0.0, 75.0)
+        az = rng.uniform(0.0, 360.0)
+        reqs.append({"id": i, "scene": int(rng.integers(n_scenes)), "arrival": float(arrivals[i]), "bands": flags,
+                     "sun": sun_direction(zen, az), "direct": rng.uniform(100.0, 600.0, nb).astype(np.float32),
+                     "diffuse": rng.uniform(20.0, 150.0, nb).astype(np.float32),
+                     "diffuse_rays": int(rng.integers(50, 401)), "seed": int(rng.integers(1 << 31))})
+    return sizes, lais, reqs
+
+
+# leaf optical properties of the four served bands (PAR, NIR, red, green)
+SERVED_RHO = np.array([0.08, 0.45, 0.06, 0.12], np.float32)
+SERVED_TAU = np.array([0.05, 0.40, 0.04, 0.10], np.float32)

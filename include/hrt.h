@@ -172,6 +172,41 @@ typedef struct {
 /* flux_out: host [n*nsun*nbands] (channel fastest), or NULL. */
 int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out);
 
+/* ---- continuous-batching server (no counterpart in the reference; a serving front end
+ * for many radiation solves of uneven size).  Scenes are registered once (geometry and
+ * one-source rho/tau for nbands_global bands).  Requests carry an arrival time (seconds
+ * after hrt_server_start) and one runBand's parameters; a dispatcher thread admits them
+ * in arrival order when the scene's device context is idle and its footprint fits in
+ * hbm_budget_bytes (least-recently-used idle scenes are evicted; resident scenes keep
+ * their BVH and buffers).  Worker threads run the solves on per-scene CUDA streams, so
+ * solves of different scenes overlap on the GPU.  A result depends only on the request,
+ * not on what else is in flight. */
+typedef struct hrt_server hrt_server;
+typedef struct {
+    uint64_t request_id;
+    uint32_t scene_id;
+    double arrival_s;
+    const uint8_t *band_launch;   /* [nbands_global of the scene] */
+    float sun_dir[3];             /* collimated source direction */
+    const float *source_flux;     /* [Bl] */
+    const float *diffuse_flux;    /* [Bl] isotropic sky */
+    int32_t direct_rays, diffuse_rays, scattering_depth;
+    uint32_t seed;
+    int32_t keep_result;          /* keep the [n*Bl] flux for hrt_server_result */
+} hrt_serve_request;
+int hrt_server_create(hrt_server **out, int device, int workers, size_t hbm_budget_bytes);
+int hrt_server_add_scene(hrt_server *s, uint32_t scene_id, const hrt_geometry *g, int32_t nbands_global,
+                         const float *rho, const float *tau);
+int hrt_server_submit(hrt_server *s, const hrt_serve_request *req);
+int hrt_server_start(hrt_server *s);
+int hrt_server_wait(hrt_server *s);
+/* timing: [arrival, admit, done] seconds; checksum = sum of the request's flux values. */
+int hrt_server_result(hrt_server *s, uint64_t request_id, float *flux_out, size_t count, double *timing,
+                      double *checksum, uint64_t *rays);
+/* out: [0] BVH builds, [1] evictions, [2] bytes accounted resident, [3] budget. */
+int hrt_server_stats(hrt_server *s, double *out, int count);
+int hrt_server_destroy(hrt_server *s);
+
 /* Statistics of the last hrt_run_band: [0] rays traced, [1] kernels launched. */
 int hrt_last_stats(const hrt_context *ctx, uint64_t *stats, int count);
 /* Device status word (HRT error bits) accumulated since the last reset. */
