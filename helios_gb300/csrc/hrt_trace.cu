@@ -448,11 +448,10 @@ __global__ void __launch_bounds__(kBlock) k_diffuse(const DiffuseParams P) {
 // adds it to G only when the origin changes.
 constexpr int32_t kSentinel = 0x7FFFFFF0;
 
-#ifndef HRT_PS_MIN_BLOCKS
-#define HRT_PS_MIN_BLOCKS 3
-#endif
-template <int NB, bool RECORD>
-__global__ void __launch_bounds__(kBlock, HRT_PS_MIN_BLOCKS) k_diffuse_ps(const DiffuseParams P) {
+// MINB: resident blocks per SM the register allocation must allow (4, the default: 64
+// registers; 3: more registers, fewer warps).
+template <int NB, bool RECORD, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams P) {
     unsigned long long *fetch = P.fetch;
     const int lane = threadIdx.x & 31;
     const uint32_t R = (uint32_t)(P.dimx * P.dimy);
@@ -477,9 +476,13 @@ __global__ void __launch_bounds__(kBlock, HRT_PS_MIN_BLOCKS) k_diffuse_ps(const 
     int face = 1;
     unsigned long long rid = 0;
     uint32_t akey = 0xFFFFFFFFu;
-    double acc[NB];
+    // running sums live in shared memory (one slot row per thread) to keep registers
+    // for the traversal state
+    __shared__ double s_sum[NB][kBlock];
+    double *sum_j = &s_sum[0][threadIdx.x];
+#define ACC(j) sum_j[(j) * kBlock]
 #pragma unroll
-    for (int j = 0; j < NB; ++j) acc[j] = 0.0;
+    for (int j = 0; j < NB; ++j) ACC(j) = 0.0;
     unsigned long long nrays = 0;
 
     for (;;) {
@@ -645,23 +648,23 @@ __global__ void __launch_bounds__(kBlock, HRT_PS_MIN_BLOCKS) k_diffuse_ps(const 
                 double *dst = ((akey & 1u) ? P.Gt : P.Gb) + (size_t)(akey >> 1) * P.Bl;
 #pragma unroll
                 for (int j = 0; j < NB; ++j)
-                    if (j < P.Bc && acc[j] != 0.0) atomicAdd(dst + j, acc[j]);
+                    if (j < P.Bc && ACC(j) != 0.0) atomicAdd(dst + j, ACC(j));
             }
             akey = key;
 #pragma unroll
-            for (int j = 0; j < NB; ++j) acc[j] = 0.0;
+            for (int j = 0; j < NB; ++j) ACC(j) = 0.0;
         }
         if (bprim != 0xFFFFFFFFu) {
             const float *src = (bface ? P.otop : P.obot) + (size_t)bprim * P.Bl;
 #pragma unroll
             for (int j = 0; j < NB; ++j)
-                if (j < P.Bc) acc[j] += (double)__ldg(src + j);
+                if (j < P.Bc) ACC(j) += (double)__ldg(src + j);
         } else {
 #pragma unroll
             for (int j = 0; j < NB; ++j)
                 if (j < P.Bc) {
                     float fl = P.sky.flux[j];
-                    if (fl > 0.f) acc[j] += sky_fd(d, P.sky, j) * (double)fl;
+                    if (fl > 0.f) ACC(j) += sky_fd(d, P.sky, j) * (double)fl;
                 }
         }
     }
@@ -669,9 +672,10 @@ __global__ void __launch_bounds__(kBlock, HRT_PS_MIN_BLOCKS) k_diffuse_ps(const 
         double *dst = ((akey & 1u) ? P.Gt : P.Gb) + (size_t)(akey >> 1) * P.Bl;
 #pragma unroll
         for (int j = 0; j < NB; ++j)
-            if (j < P.Bc && acc[j] != 0.0) atomicAdd(dst + j, acc[j]);
+            if (j < P.Bc && ACC(j) != 0.0) atomicAdd(dst + j, ACC(j));
     }
     if (sc.rays && nrays) atomicAdd(sc.rays, nrays);
+#undef ACC
 }
 
 // ------------------------------------------------------------------ testing --
@@ -986,6 +990,7 @@ __global__ void k_fold_channels(int n, int C, const uint8_t *__restrict__ mask, 
     sb[i] = 0.0;
 }
 
+
 inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 }  // namespace
@@ -1000,20 +1005,34 @@ static cudaError_t direct_impl(const DirectParams &p, int max_blocks, cudaStream
     return cudaGetLastError();
 }
 
-template <int NB>
-static cudaError_t diffuse_ps_launch(const DiffuseParams &p, cudaStream_t s) {
+static int ps_min_blocks() {
+    static int v = -1;
+    if (v < 0) {
+        const char *e = getenv("HRT_PS_MINB");
+        v = (e && e[0] == '3') ? 3 : 4;
+    }
+    return v;
+}
+
+template <int NB, int MINB>
+static cudaError_t diffuse_ps_launch_b(const DiffuseParams &p, cudaStream_t s) {
     static int blocks_per_sm = 0, sms = 0;
     if (blocks_per_sm == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<NB, false>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<NB, false, MINB>, kBlock, 0);
         if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
     cudaError_t e = cudaMemsetAsync(p.fetch, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
-    k_diffuse_ps<NB, false><<<sms * blocks_per_sm, kBlock, 0, s>>>(p);
+    k_diffuse_ps<NB, false, MINB><<<sms * blocks_per_sm, kBlock, 0, s>>>(p);
     return cudaGetLastError();
+}
+
+template <int NB>
+static cudaError_t diffuse_ps_launch(const DiffuseParams &p, cudaStream_t s) {
+    return ps_min_blocks() == 4 ? diffuse_ps_launch_b<NB, 4>(p, s) : diffuse_ps_launch_b<NB, 3>(p, s);
 }
 
 static bool use_persistent() {
@@ -1137,7 +1156,7 @@ cudaError_t launch_diffuse_record(const DiffuseParams &p, uint32_t *hits, cudaSt
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<1, true>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<1, true, 3>, kBlock, 0);
         if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
     DiffuseParams q = p;
@@ -1145,7 +1164,7 @@ cudaError_t launch_diffuse_record(const DiffuseParams &p, uint32_t *hits, cudaSt
     q.Bc = 1;
     cudaError_t e = cudaMemsetAsync(q.fetch, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
-    k_diffuse_ps<1, true><<<sms * blocks_per_sm, kBlock, 0, s>>>(q);
+    k_diffuse_ps<1, true, 3><<<sms * blocks_per_sm, kBlock, 0, s>>>(q);
     return cudaGetLastError();
 }
 
