@@ -38,7 +38,7 @@ class HrtError(RuntimeError):
 class Geometry(C.Structure):
     _fields_ = [("n", C.c_int32), ("transform", C.c_void_p), ("type", C.c_void_p), ("twosided", C.c_void_p),
                 ("nbbox", C.c_int32), ("bbox_vertices", C.c_void_p), ("periodic_x", C.c_float),
-                ("periodic_y", C.c_float)]
+                ("periodic_y", C.c_float), ("voxel_lad", C.c_void_p)]
 
 
 class Source(C.Structure):
@@ -62,7 +62,7 @@ class BandSolve(C.Structure):
                 ("diffuse_dist_norm", C.c_void_p), ("sky_radiance_params", C.c_void_p),
                 ("direct_rays", C.c_void_p), ("diffuse_rays", C.c_void_p), ("scattering_depth", C.c_void_p),
                 ("emission", C.c_void_p), ("emissivity", C.c_void_p), ("temperature", C.c_void_p),
-                ("seed", C.c_uint32)]
+                ("seed", C.c_uint32), ("scatter_tolerance", C.c_double)]
 
 
 class Sweep(C.Structure):
@@ -189,13 +189,15 @@ class Context:
         self.check(self.lib.hrt_set_stream(self.h, stream_handle))
 
     # -------------------------------------------------------------- geometry
-    def update_geometry(self, T, ptype, twosided, bbox_verts=None, periodic=(0.0, 0.0)):
+    def update_geometry(self, T, ptype, twosided, bbox_verts=None, periodic=(0.0, 0.0), voxel_lad=None):
+        """voxel_lad: [n] leaf area density, read for voxel primitives (required when there are any)."""
         T = f32(T).reshape(-1, 16)
         ty = np.ascontiguousarray(ptype, np.uint32)
         ts = np.ascontiguousarray(twosided, np.int8)
         bb = None if bbox_verts is None else f32(bbox_verts).reshape(-1, 4, 3)
+        lad = None if voxel_lad is None else f32(voxel_lad)
         g = Geometry(T.shape[0], ptr(T), ptr(ty), ptr(ts), 0 if bb is None else bb.shape[0], ptr(bb),
-                     float(periodic[0]), float(periodic[1]))
+                     float(periodic[0]), float(periodic[1]), ptr(lad))
         self.check(self.lib.hrt_update_geometry(self.h, C.byref(g)))
         self.n = T.shape[0]
 
@@ -330,6 +332,7 @@ class Context:
         s.emissivity = a("eps", np.float32)
         s.temperature = a("temperature", np.float32)
         s.seed = int(solve.get("seed", 0)) & 0xFFFFFFFF
+        s.scatter_tolerance = float(solve.get("scatter_tolerance", 0.0))
         return s, keep
 
     def run_band(self, solve: dict, out: bool = True):
@@ -356,9 +359,9 @@ class Context:
         return flux
 
     def last_stats(self):
-        st = np.zeros(2, np.uint64)
-        self.check(self.lib.hrt_last_stats(self.h, ptr(st), 2))
-        return {"rays": int(st[0]), "kernels": int(st[1])}
+        st = np.zeros(3, np.uint64)
+        self.check(self.lib.hrt_last_stats(self.h, ptr(st), 3))
+        return {"rays": int(st[0]), "kernels": int(st[1]), "iterations": int(st[2])}
 
     # -------------------------------------------------------------- inspection
     def trace_rays(self, o, d, tmin=1e-4, tmax=1e38, anyhit=False):

@@ -21,7 +21,8 @@ SOURCES = ["hrt_bvh.cu", "hrt_trace.cu", "hrt_api.cu", "hrt_static.cu", "hrt_ser
 HEADERS = ["hrt_device.cuh", "hrt_internal.h", os.path.join("..", "..", "include", "hrt.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
-           "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "--expt-relaxed-constexpr"]
+           "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "-Xcompiler", "-ffp-contract=off",
+           "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:

@@ -47,6 +47,23 @@ struct DevBuf {
     ~DevBuf() { release(); }
 };
 
+// Surface area of a primitive in FP64 from its FP32 transform (a voxel's: its leaf area,
+// LAD x volume).  Triangles span half the parallelogram of their two edges, disks are
+// the unit disk scaled by the transform.
+double prim_area(const float *T, uint32_t type, float lad) {
+    double ax = T[0], ay = T[4], az = T[8], bx = T[1], by = T[5], bz = T[9];
+    if (type == PT_VOXEL) {
+        double cx = T[2], cy = T[6], cz = T[10];
+        double det = ax * (by * cz - bz * cy) - bx * (ay * cz - az * cy) + cx * (ay * bz - az * by);
+        return (double)lad * std::fabs(det);
+    }
+    double x = ay * bz - az * by, y = az * bx - ax * bz, z = ax * by - ay * bx;
+    double a = std::sqrt(x * x + y * y + z * z);
+    if (type == PT_TRI) return 0.5 * a;
+    if (type == PT_DISK) return M_PI * a;
+    return a;
+}
+
 }  // namespace
 
 struct hrt_context {
@@ -59,7 +76,8 @@ struct hrt_context {
     float px = 0.f, py = 0.f;
     bool have_geometry = false, built = false;
     std::vector<int8_t> h_twosided;
-    DevBuf T, type, twosided, bbox, rec, rgen, nodes, codes, perm, bvh_scratch;
+    std::vector<uint32_t> h_voxels;  // original indices of voxel primitives
+    DevBuf T, type, twosided, bbox, rec, rgen, nodes, codes, perm, bvh_scratch, lad, area;
     // materials and sources
     int mS = 0, mN = 0, mB = 0;
     DevBuf rho, tau, src, src_flux;
@@ -72,7 +90,8 @@ struct hrt_context {
         fetch;
     size_t emis_eps_count = 0, emis_T_count = 0;
     DevBuf io_a, io_b, io_c;  // staging for inspection calls
-    uint64_t last_rays = 0, last_kernels = 0;
+    uint64_t last_rays = 0, last_kernels = 0, last_iters = 0;
+    DevBuf resid;  // scattering residual: block partials and the per-band result
     // measurement: bit 0 counts traversal work, bit 1 times trace launches
     int measure = 0;
     DevBuf visits;
@@ -111,6 +130,7 @@ TraceScene scene_of(hrt_context *ctx) {
     sc.bbox = ctx->nbbox ? ctx->bbox.as<float4>() : nullptr;
     sc.n = ctx->n;
     sc.nbbox = ctx->nbbox;
+    sc.voxels = ctx->h_voxels.empty() ? 0 : 1;
     sc.periodic_x = ctx->px;
     sc.periodic_y = ctx->py;
     sc.twosided = ctx->twosided.as<int8_t>();
@@ -400,19 +420,40 @@ int hrt_update_geometry(hrt_context *ctx, const hrt_geometry *g) {
         return fail(ctx, HRT_EINVAL, "null geometry array");
     if (!(g->nbbox == 0 || g->nbbox == 2 || g->nbbox == 4) || (g->nbbox > 0 && !g->bbox_vertices))
         return fail(ctx, HRT_EINVAL, "periodic walls must be 0, 2 or 4 quads");
-    for (int i = 0; i < g->n; ++i)
+    std::vector<uint32_t> voxels;
+    for (int i = 0; i < g->n; ++i) {
         if (g->type[i] > 4) return fail(ctx, HRT_EUNSUPPORTED, "unsupported primitive type " + std::to_string(g->type[i]));
+        if (g->type[i] == PT_VOXEL) voxels.push_back((uint32_t)i);
+    }
+    if (!voxels.empty()) {
+        if (!g->voxel_lad) return fail(ctx, HRT_EINVAL, "voxels need voxel_lad (leaf area density)");
+        for (uint32_t i : voxels)
+            if (!(g->voxel_lad[i] >= 0.f) || std::isinf(g->voxel_lad[i]))
+                return fail(ctx, HRT_EINVAL, "voxel leaf area density must be finite and >= 0");
+    }
     CU(cudaSetDevice(ctx->device));
     size_t n = (size_t)g->n;
     CU(ctx->T.ensure(std::max<size_t>(n, 1) * 16 * sizeof(float)));
     CU(ctx->type.ensure(std::max<size_t>(n, 1) * sizeof(uint32_t)));
     CU(ctx->twosided.ensure(std::max<size_t>(n, 1)));
+    CU(ctx->area.ensure(std::max<size_t>(n, 1) * sizeof(double)));
+    ctx->h_twosided.assign(g->twosided, g->twosided + n);
+    for (uint32_t i : voxels) ctx->h_twosided[i] = 1;  // a voxel launches both directions of each sample
+    // primitive areas (voxels: leaf area) weight the scattering residual
+    std::vector<double> area(n);
+    for (size_t i = 0; i < n; ++i)
+        area[i] = prim_area(g->transform + 16 * i, g->type[i], g->type[i] == PT_VOXEL ? g->voxel_lad[i] : 0.f);
     if (n) {
         CU(cudaMemcpyAsync(ctx->T.p, g->transform, n * 16 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
         CU(cudaMemcpyAsync(ctx->type.p, g->type, n * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
-        CU(cudaMemcpyAsync(ctx->twosided.p, g->twosided, n, cudaMemcpyHostToDevice, ctx->stream));
+        CU(cudaMemcpyAsync(ctx->twosided.p, ctx->h_twosided.data(), n, cudaMemcpyHostToDevice, ctx->stream));
+        CU(cudaMemcpyAsync(ctx->area.p, area.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     }
-    ctx->h_twosided.assign(g->twosided, g->twosided + n);
+    if (!voxels.empty()) {
+        CU(ctx->lad.ensure(n * sizeof(float)));
+        CU(cudaMemcpyAsync(ctx->lad.p, g->voxel_lad, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    ctx->h_voxels.swap(voxels);
     ctx->nbbox = g->nbbox;
     ctx->px = g->periodic_x;
     ctx->py = g->periodic_y;
@@ -454,7 +495,8 @@ int hrt_build_accel(hrt_context *ctx) {
     b.codes = ctx->codes.as<uint64_t>();
     b.perm = ctx->perm.as<uint32_t>();
     b.status = ctx->status.as<uint32_t>();
-    CU(bvh_build(ctx->T.as<float>(), ctx->type.as<uint32_t>(), n, b, ctx->stream));
+    CU(bvh_build(ctx->T.as<float>(), ctx->type.as<uint32_t>(), ctx->h_voxels.empty() ? nullptr : ctx->lad.as<float>(), n,
+                 b, ctx->stream));
     int r = sync_and_status(ctx);
     if (r) return r;
     ctx->built = true;
@@ -469,6 +511,23 @@ int hrt_update_materials(hrt_context *ctx, int32_t nsources, int32_t nprims, int
     CU(cudaSetDevice(ctx->device));
     CU(ctx->rho.ensure(std::max<size_t>(m, 1) * sizeof(float)));
     CU(ctx->tau.ensure(std::max<size_t>(m, 1) * sizeof(float)));
+    std::vector<float> vr, vt;
+    if (m && !ctx->h_voxels.empty() && nprims == ctx->n) {
+        // A voxel's leaves scatter rho + tau into one isotropic field: half of it is routed
+        // to each face, so both faces emit the same radiance.
+        vr.assign(rho, rho + m);
+        vt.assign(tau, tau + m);
+        for (int32_t src = 0; src < nsources; ++src)
+            for (uint32_t p : ctx->h_voxels)
+                for (int32_t b = 0; b < nbands_global; ++b) {
+                    size_t i = ((size_t)src * nprims + p) * nbands_global + b;
+                    float h = 0.5f * (vr[i] + vt[i]);
+                    vr[i] = h;
+                    vt[i] = h;
+                }
+        rho = vr.data();
+        tau = vt.data();
+    }
     if (m) {
         CU(cudaMemcpyAsync(ctx->rho.p, rho, m * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
         CU(cudaMemcpyAsync(ctx->tau.p, tau, m * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
@@ -654,6 +713,8 @@ int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
     if (!s->direct_rays || !s->diffuse_rays || !s->scattering_depth || !s->emission || !s->diffuse_flux)
         return fail(ctx, HRT_EINVAL, "null per-band array");
     ctx->last_kernels = 0;
+    int iters = 0;
+    if (!(s->scatter_tolerance >= 0.0)) return fail(ctx, HRT_EINVAL, "scatter_tolerance must be >= 0");
     // materials / sources: NULL keeps what is resident on the device
     if (s->rho || s->tau) {
         if (!s->rho || !s->tau) return fail(ctx, HRT_EINVAL, "rho and tau must be given together");
@@ -767,13 +828,15 @@ int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
             CU(cudaMemsetAsync((void *)sky.flux, 0, (size_t)Bl * sizeof(float), st));
             sky0 = sky;
         }
-        std::vector<uint8_t> sflags = flags;
+        std::vector<uint8_t> sflags = flags, conv(Bg, 0);
+        const bool residual = s->scatter_tolerance > 0.0;
+        if (residual) CU(ctx->resid.ensure((64 + (size_t)kResidualBlocks * Bl * 2) * sizeof(double)));
         for (int it = 0; it < depth; ++it) {
             int b = -1;
             for (int bg = 0; bg < Bg; ++bg) {
                 if (!sflags[bg]) continue;
                 ++b;
-                if (it + 1 > s->scattering_depth[b]) sflags[bg] = 0;
+                if (it + 1 > s->scattering_depth[b] || conv[bg]) sflags[bg] = 0;
             }
             if ((r = upload_flags(ctx, Bg, sflags.data()))) return r;
             if (it > 0 || (emission && rundirect)) {
@@ -785,6 +848,27 @@ int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
             CU(cudaMemsetAsync(ctx->sbot.p, 0, m * sizeof(double), st));
             int Bc = count_flags(Bg, sflags.data());
             if ((r = diffuse_pass(ctx, 0, (uint32_t)n, rpp_d, s->seed, 2u + (uint32_t)it, 3, Bg, Bc, Bl, sky0))) return r;
+            iters = it + 1;
+            if (residual) {
+                // FP64 convergence check: a band stops once the power its last iteration
+                // scattered (not yet propagated) is at most scatter_tolerance of its total.
+                double h[32];
+                CU(launch_residual(n, Bl, ctx->area.as<double>(), ctx->rin.as<double>(), ctx->stop.as<double>(),
+                                   ctx->sbot.as<double>(), ctx->resid.as<double>(), st));
+                CU(cudaMemcpyAsync(h, ctx->resid.p, 2 * (size_t)Bl * sizeof(double), cudaMemcpyDeviceToHost, st));
+                CU(cudaStreamSynchronize(st));
+                ctx->last_kernels += 2;
+                bool all = true;
+                int c = -1;
+                for (int bg = 0; bg < Bg; ++bg) {
+                    if (!flags[bg]) continue;
+                    ++c;
+                    if (!sflags[bg]) continue;
+                    if (h[2 * c] <= s->scatter_tolerance * h[2 * c + 1]) conv[bg] = 1;
+                    else all = false;
+                }
+                if (all) break;
+            }
         }
     }
     CU(launch_final_flux(m, ctx->rin.as<double>(), ctx->stop.as<double>(), ctx->sbot.as<double>(), ctx->fin.as<float>(), st));
@@ -794,6 +878,7 @@ int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
     CU(cudaMemcpyAsync(&rays, ctx->counter.p, sizeof(rays), cudaMemcpyDeviceToHost, st));
     r = sync_and_status(ctx);
     ctx->last_rays = rays;
+    ctx->last_iters = (uint64_t)iters;
     return r;
 }
 
@@ -803,6 +888,7 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
     int r = check_built(ctx);
     if (r) return r;
     CU(cudaSetDevice(ctx->device));
+    if (!ctx->h_voxels.empty()) return fail(ctx, HRT_EUNSUPPORTED, "the batched sweep does not trace voxels");
     const int n = ctx->n, nsun = s->nsun, Bl = s->nbands;
     if (nsun < 1 || Bl < 1 || !s->sun_dir || !s->direct_flux || !s->diffuse_flux || !s->rho || !s->tau)
         return fail(ctx, HRT_EINVAL, "sweep needs suns, bands, fluxes and materials");
@@ -977,6 +1063,7 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
     CU(cudaMemcpyAsync(&rays, ctx->counter.p, sizeof(rays), cudaMemcpyDeviceToHost, st));
     r = sync_and_status(ctx);
     ctx->last_rays = rays;
+    ctx->last_iters = (uint64_t)s->scattering_depth;
     return r;
 }
 
@@ -984,6 +1071,7 @@ int hrt_last_stats(const hrt_context *ctx, uint64_t *stats, int count) {
     if (!ctx || !stats) return HRT_EINVAL;
     if (count > 0) stats[0] = ctx->last_rays;
     if (count > 1) stats[1] = ctx->last_kernels;
+    if (count > 2) stats[2] = ctx->last_iters;
     return HRT_OK;
 }
 

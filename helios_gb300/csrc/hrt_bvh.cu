@@ -24,7 +24,8 @@ constexpr int kThreads = 256;
 constexpr int kItems = kSortTile / kThreads;  // 8
 
 __global__ void k_records(int n, const float *__restrict__ T, const uint32_t *__restrict__ type,
-                          float4 *__restrict__ rec_tmp, float4 *__restrict__ rgen, float *__restrict__ aabb) {
+                          const float *__restrict__ lad, float4 *__restrict__ rec_tmp, float4 *__restrict__ rgen,
+                          float *__restrict__ aabb) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float t[16];
@@ -32,7 +33,7 @@ __global__ void k_records(int n, const float *__restrict__ T, const uint32_t *__
     for (int k = 0; k < 16; ++k) t[k] = T[16 * (size_t)i + k];
     float4 rec[4], g[4];
     f3 lo, hi;
-    make_records(t, type[i], rec, g, &lo, &hi);
+    make_records(t, type[i], lad ? lad[i] : 0.f, rec, g, &lo, &hi);
     rec[1].w = __uint_as_float((uint32_t)i);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -447,11 +448,11 @@ void bvh_carve(BvhBuffers &bb, void *scratch, int n) {
     bb.flags = (uint32_t *)take(ni * sizeof(uint32_t));
 }
 
-cudaError_t bvh_build(const float *T, const uint32_t *type, int n, BvhBuffers &b, cudaStream_t s) {
+cudaError_t bvh_build(const float *T, const uint32_t *type, const float *lad, int n, BvhBuffers &b, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     if (n > 33000000) return cudaErrorInvalidValue;  // radix-sort offset scan covers 2048^2 bins
     const int grid = (n + kThreads - 1) / kThreads;
-    k_records<<<grid, kThreads, 0, s>>>(n, T, type, b.rec_tmp, b.rgen, b.aabb);
+    k_records<<<grid, kThreads, 0, s>>>(n, T, type, lad, b.rec_tmp, b.rgen, b.aabb);
     int nparts = grid < 1024 ? grid : 1024;
     k_bounds_partial<<<nparts, kThreads, 0, s>>>(n, b.aabb, b.partial);
     k_bounds_final<<<1, 32, 0, s>>>(nparts, b.partial, b.bounds);

@@ -107,6 +107,53 @@ __device__ __forceinline__ void sincos2pi(float u, float *c_out, float *s_out) {
     }
 }
 
+// Natural logarithm of x in (0, 1] for the voxel free-path draw: x = m * 2^e with m in
+// [sqrt(1/2), sqrt(2)), ln m = 2 atanh(z), z = (m - 1) / (m + 1), Taylor series to z^9
+// (|z| <= 0.172; truncation below 1e-9).  Plain single-precision steps, so the host
+// restatement gives the same bits.
+__device__ __forceinline__ float ln_unit(float x) {
+    uint32_t b = __float_as_uint(x);
+    int e = (int)((b >> 23) & 0xFFu) - 127;
+    float m = __uint_as_float((b & 0x7FFFFFu) | 0x3F800000u);
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e = e + 1;
+    }
+    float z = (m - 1.0f) / (m + 1.0f);
+    float z2 = z * z;
+    float s = 1.0f + z2 * (0.333333333f + z2 * (0.2f + z2 * (0.142857143f + z2 * 0.111111111f)));
+    return (float)e * 0.693147181f + 2.0f * z * s;
+}
+
+// Concentric square-to-disk map (Shirley & Chiu, JGT 1997) of (u, v) in [0,1)^2.
+__device__ __forceinline__ void concentric(float u, float v, float *x, float *y) {
+    float sx = -1.0f + 2.0f * u, sy = -1.0f + 2.0f * v;
+    float r, ph;  // ph in units of pi/4
+    if (sx > -sy) {
+        if (sx > sy) {
+            r = sx;
+            ph = sy / sx;
+        } else {
+            r = sy;
+            ph = 2.0f - sx / sy;
+        }
+    } else {
+        if (sx < sy) {
+            r = -sx;
+            ph = 4.0f + sy / sx;
+        } else {
+            r = -sy;
+            ph = (sy != 0.f) ? 6.0f - sx / sy : 0.f;
+        }
+    }
+    float frac = ph * 0.125f;
+    if (frac < 0.f) frac = frac + 1.0f;
+    float c, s;
+    sincos2pi(frac, &c, &s);
+    *x = r * c;
+    *y = r * s;
+}
+
 // Orthonormal basis about unit n (Duff et al., JCGT 6(1), 2017).
 __device__ __forceinline__ void onb(f3 n, f3 *t1, f3 *t2) {
     float sign = copysignf(1.0f, n.z);
@@ -131,17 +178,41 @@ __device__ __forceinline__ f3 diffuse_dir(f3 n, int ti, int pi, int dimx, int di
               (t1.z * lx + t2.z * ly) + n.z * ct);
 }
 
+// Voxel leaves scatter isotropically: stratified uniform direction on the upper
+// hemisphere (cos theta = 1 - Rt, as OptiX 6 rayGeneration.cu:401-415 samples voxels);
+// the bottom-face ray of the same sample flips it, so each pair covers the sphere.
+__device__ __forceinline__ f3 voxel_dir(int ti, int pi, int dimx, int dimy, float j0, float j1) {
+    float Rt = ((float)ti + j0) / (float)dimx;
+    float Rp = ((float)pi + j1) / (float)dimy;
+    float ct = 1.0f - Rt;
+    float st = sqrtf(fmaxf(0.f, 1.0f - ct * ct));
+    float cp, sp;
+    sincos2pi(Rp, &cp, &sp);
+    return mk(st * cp, st * sp, ct);
+}
+
+// Projection coefficient of a voxel's leaves (spherical leaf-angle distribution).
+constexpr float kVoxelG = 0.5f;
+
+// Counter words and key of a ray's voxel free-path draws: the draw for voxel v is
+// philox(c0, c1, c2 | wrap << 16, v + 1; k0, k1).  It depends on the ray's identity
+// and wrap count only, never on traversal order or on how launches are batched.
+struct VoxKey {
+    uint32_t c0, c1, c2, k0, k1;
+};
+
 // ------------------------------------------------------------------ records ---
 // Intersection record (64 B, BVH leaf order):
 //   r0 = (p0.xyz, type bits)  r1 = (p1.xyz, original index bits)
-//   r2 = (p2.xyz, 0)          r3 = (p3.xyz, 0)
+//   r2 = (p2.xyz, k)          r3 = (p3.xyz, 0)
 // patch/bbox: 4 corners; triangle: v0,v1,v2 (r3 = v2); disk: centre, unit normal, (radius,0,0);
-// voxel: lo, hi.
+// voxel: lo, hi, with k = G * LAD its extinction coefficient (0 for other types).
 // Ray-origin record (64 B, original order):
 //   g0 = (P.xyz, type bits) g1 = (A.xyz, twosided bits) g2 = (B.xyz, 0) g3 = (N.xyz, 0)
-// with sample point P + u*A + v*B and unit normal N.
+// with sample point P + u*A + v*B and unit normal N (disk: P = centre, unit disk over A, B;
+// voxel: P = lower corner, g3 = third edge C, point P + u*A + v*B + w*C).
 
-__device__ __forceinline__ void make_records(const float *T, uint32_t type, float4 rec[4], float4 g[4],
+__device__ __forceinline__ void make_records(const float *T, uint32_t type, float lad, float4 rec[4], float4 g[4],
                                              f3 *lo, f3 *hi) {
     f3 p0, p1, p2, p3;
     uint32_t rt = type;
@@ -172,7 +243,7 @@ __device__ __forceinline__ void make_records(const float *T, uint32_t type, floa
     }
     rec[0] = make_float4(p0.x, p0.y, p0.z, __uint_as_float(rt));
     rec[1] = make_float4(p1.x, p1.y, p1.z, 0.f);
-    rec[2] = make_float4(p2.x, p2.y, p2.z, 0.f);
+    rec[2] = make_float4(p2.x, p2.y, p2.z, (rt == PT_VOXEL) ? kVoxelG * lad : 0.f);
     rec[3] = make_float4(p3.x, p3.y, p3.z, 0.f);
     // bounds
     if (rt == PT_DISK) {
@@ -199,6 +270,14 @@ __device__ __forceinline__ void make_records(const float *T, uint32_t type, floa
     if (type == PT_TRI) {
         P = mk(T[3], T[7], T[11]);
         N = normalize(cross(B, A));
+    } else if (type == PT_DISK) {
+        P = mk(T[3], T[7], T[11]);
+        N = normalize(cross(A, B));
+    } else if (type == PT_VOXEL) {
+        N = mk(T[2], T[6], T[10]);
+        P = mk(((T[0] * -0.5f + T[1] * -0.5f) + T[2] * -0.5f) + T[3],
+               ((T[4] * -0.5f + T[5] * -0.5f) + T[6] * -0.5f) + T[7],
+               ((T[8] * -0.5f + T[9] * -0.5f) + T[10] * -0.5f) + T[11]);
     } else {
         P = xform(T, -0.5f, -0.5f);
         N = normalize(cross(A, B));
@@ -209,11 +288,23 @@ __device__ __forceinline__ void make_records(const float *T, uint32_t type, floa
     g[3] = make_float4(N.x, N.y, N.z, 0.f);
 }
 
-__device__ __forceinline__ f3 sample_point(const float4 g[4], uint32_t type, float u, float v) {
+// Ray origin from uniform numbers u, v (w: voxels only).  Disks use the concentric map
+// (OptiX 6 rayGeneration.cu:346-390), voxels the whole box (rayGeneration.cu:392-397).
+__device__ __forceinline__ f3 sample_point(const float4 g[4], uint32_t type, float u, float v, float w) {
     f3 P = xyz(g[0]), A = xyz(g[1]), B = xyz(g[2]);
     if (type == PT_TRI) {
         float a = u < v ? u : v, b = u < v ? v : u;
         return mk((P.x + a * A.x) + b * B.x, (P.y + a * A.y) + b * B.y, (P.z + a * A.z) + b * B.z);
+    }
+    if (type == PT_DISK) {
+        float x, y;
+        concentric(u, v, &x, &y);
+        return mk((P.x + x * A.x) + y * B.x, (P.y + x * A.y) + y * B.y, (P.z + x * A.z) + y * B.z);
+    }
+    if (type == PT_VOXEL) {
+        f3 C = xyz(g[3]);
+        return mk(((P.x + u * A.x) + v * B.x) + w * C.x, ((P.y + u * A.y) + v * B.y) + w * C.y,
+                  ((P.z + u * A.z) + v * B.z) + w * C.z);
     }
     return mk((P.x + u * A.x) + v * B.x, (P.y + u * A.y) + v * B.y, (P.z + u * A.z) + v * B.z);
 }
@@ -332,21 +423,34 @@ __device__ __forceinline__ bool disk_hit(f3 o, f3 d, float tmin, f3 c, f3 n, flo
     return true;
 }
 
-// Voxel: no hit when the origin is inside (reference OptiX 6 primitiveIntersection.cu:330-374).
-__device__ __forceinline__ bool voxel_hit(f3 o, f3 inv, float tmin, f3 lo, f3 hi, float tmax, float *t_out,
-                                          int *face_out) {
-    if (o.x >= lo.x && o.x <= hi.x && o.y >= lo.y && o.y <= hi.y && o.z >= lo.z && o.z <= hi.z) return false;
-    float tn;
-    if (!slab(o, inv, lo, hi, tmin, tmax, &tn)) return false;
-    if (!(tn > 1e-5f)) return false;
-    *t_out = tn;
+// Voxel: a turbid medium with extinction k = G * LAD.  The reference defines no voxel
+// physics (its OptiX 6 absorption is commented out, rayHit.cu:278-290), so this engine
+// does: the ray's path through the box, from max(entry, tmin) to the exit, is
+// intercepted at the free path s = -ln(xi) / k with xi in (0, 1] drawn per (ray, voxel,
+// wrap).  A ray starting inside the box crosses the rest of it.  The hit face is the top.
+__device__ __forceinline__ bool voxel_hit(f3 o, f3 inv, float tmin, f3 lo, f3 hi, float k, float tmax,
+                                          const VoxKey &vk, uint32_t vid, float *t_out, int *face_out) {
+    if (!(k > 0.f)) return false;
+    float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
+    float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
+    float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
+    float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+    float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+    if (!(tn < tf)) return false;
+    u4 u = philox(vk.c0, vk.c1, vk.c2, vid + 1u, vk.k0, vk.k1);
+    float t = tn + -ln_unit(1.0f - u01(u.a)) / k;
+    if (!(t < tf) || !(t <= tmax)) return false;
+    *t_out = t;
     *face_out = 1;
     return true;
 }
 
 // Test record `slot`; on success returns t, face and the original primitive index.
+// VOX = false leaves voxels out (for scenes known to hold none).
+template <bool VOX = true>
 __device__ __forceinline__ bool rec_hit(const float4 *__restrict__ rec, uint32_t slot, const WT &w, f3 o, f3 d,
-                                        f3 inv, float tmin, float tmax, float *t, int *face, uint32_t *orig) {
+                                        f3 inv, float tmin, float tmax, const VoxKey &vk, float *t, int *face,
+                                        uint32_t *orig) {
     const float4 *r = rec + 4 * (size_t)slot;
     float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2);
     uint32_t type = __float_as_uint(r0.w);
@@ -361,8 +465,8 @@ __device__ __forceinline__ bool rec_hit(const float4 *__restrict__ rec, uint32_t
         ok = poly_hit<4>(w, o, tmin, v, tmax, t, face);
     } else if (type == PT_DISK) {
         ok = disk_hit(o, d, tmin, xyz(r0), xyz(r1), r2.x, tmax, t, face);
-    } else if (type == PT_VOXEL) {
-        ok = voxel_hit(o, inv, tmin, xyz(r0), xyz(r1), tmax, t, face);
+    } else if (VOX && type == PT_VOXEL) {
+        ok = voxel_hit(o, inv, tmin, xyz(r0), xyz(r1), r2.w, tmax, vk, *orig, t, face);
     } else {
         ok = false;
     }

@@ -14,6 +14,7 @@ struct TraceScene {
     const float4 *bbox;   // [nbbox*4] periodic wall corners (xyz, w unused)
     int n;
     int nbbox;
+    int voxels;           // the scene holds voxel primitives
     float periodic_x, periodic_y;
     const int8_t *twosided; // [n] two-sided flags
     uint32_t *status;     // device error word (ERR_* bits)
@@ -99,7 +100,8 @@ constexpr size_t bvh_scratch_bytes_c(int n) {
 }
 size_t bvh_scratch_bytes(int n);
 void bvh_carve(BvhBuffers &b, void *scratch, int n);
-cudaError_t bvh_build(const float *T, const uint32_t *type, int n, BvhBuffers &b, cudaStream_t s);
+// lad: [n] leaf area density of voxels (original order), or null (voxels then hold no leaves).
+cudaError_t bvh_build(const float *T, const uint32_t *type, const float *lad, int n, BvhBuffers &b, cudaStream_t s);
 constexpr int kSortTile = 2048;
 
 // ---------------------------------------------------------------- passes
@@ -179,5 +181,10 @@ cudaError_t launch_emission(int n, int Bl, const uint8_t *emission, const int32_
                             cudaStream_t s);
 cudaError_t launch_final_flux(size_t nb, const double *rin, const double *stop, const double *sbot, float *out,
                               cudaStream_t s);
+// Per-band scattering residual sums into scratch[0 .. 2*Bl): (num, den) pairs, see
+// k_residual.  scratch holds 64 + kResidualBlocks * Bl * 2 doubles.
+constexpr int kResidualBlocks = 304;
+cudaError_t launch_residual(int n, int Bl, const double *area, const double *rin, const double *stop,
+                            const double *sbot, double *scratch, cudaStream_t s);
 
 }  // namespace hrt

@@ -74,7 +74,7 @@ extern "C" int hrt_build_accel_static(const float *d_transform, const uint32_t *
     b.codes = d_codes;
     b.perm = d_perm;
     b.status = status;
-    if (bvh_build(d_transform, d_type, n, b, s) != cudaSuccess) return HRT_ECUDA;
+    if (bvh_build(d_transform, d_type, nullptr, n, b, s) != cudaSuccess) return HRT_ECUDA;
     uint32_t st = 0;
     if (cudaMemcpyAsync(&st, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess) return HRT_ECUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return HRT_ECUDA;

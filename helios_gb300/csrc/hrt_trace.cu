@@ -39,8 +39,8 @@ __device__ __forceinline__ void raise(uint32_t *status, uint32_t bit) {
 // tested against the current best distance; leaf children are intersected at
 // once; of two internal children the nearer is entered and the farther pushed.
 template <bool STATS>
-__device__ Hit trace_bvh(const TraceScene &sc, f3 o, f3 d, float tmin, float tmax, bool anyhit, uint32_t *nv,
-                         uint32_t *np) {
+__device__ Hit trace_bvh(const TraceScene &sc, f3 o, f3 d, float tmin, float tmax, bool anyhit, const VoxKey &vk,
+                         uint32_t *nv, uint32_t *np) {
     Hit h{tmax, 0xFFFFFFFFu, 0};
     if (sc.n == 0) return h;
     WT w = wt_setup(d);
@@ -81,7 +81,7 @@ __device__ Hit trace_bvh(const TraceScene &sc, f3 o, f3 d, float tmin, float tma
                 int face;
                 uint32_t orig;
                 if (STATS) ++*np;
-                if (rec_hit(sc.rec, (uint32_t)(~ck), w, o, d, inv, tmin, best, &t, &face, &orig)) {
+                if (rec_hit(sc.rec, (uint32_t)(~ck), w, o, d, inv, tmin, best, vk, &t, &face, &orig)) {
                     if (h.prim == 0xFFFFFFFFu || t < h.t || (t == h.t && orig < h.prim)) {
                         h.t = t;
                         h.prim = orig;
@@ -138,10 +138,12 @@ __device__ __forceinline__ bool wall_closest(const TraceScene &sc, f3 o, f3 d, f
 
 // Trace with periodic wrapping (<= 10 wraps; OptiX8DeviceCode.cu:763-789, 1440-1459).
 template <bool STATS>
-__device__ Hit trace_full(const TraceScene &sc, f3 o, f3 d, float tmin, float tmax, bool anyhit, uint32_t *nv,
-                          uint32_t *np) {
+__device__ Hit trace_full(const TraceScene &sc, f3 o, f3 d, float tmin, float tmax, bool anyhit, VoxKey vk,
+                          uint32_t *nv, uint32_t *np) {
+    const uint32_t c2 = vk.c2;
     for (int wrap = 0; wrap < 10; ++wrap) {
-        Hit h = trace_bvh<STATS>(sc, o, d, tmin, tmax, anyhit && sc.nbbox == 0, nv, np);
+        vk.c2 = c2 | ((uint32_t)wrap << 16);
+        Hit h = trace_bvh<STATS>(sc, o, d, tmin, tmax, anyhit && sc.nbbox == 0, vk, nv, np);
         if (sc.nbbox == 0) return h;
         float tb;
         int which = -1;
@@ -213,14 +215,57 @@ __device__ __forceinline__ void warp_segment_add(uint32_t key, double (&v)[NV], 
     }
 }
 
+// ------------------------------------------------------------------ origins --
+// Leaf-projection factor of a direct ray's strength: |n . d| on a surface, G on a voxel.
+__device__ __forceinline__ double proj(f3 nrm, f3 d, bool vox) {
+    return vox ? (double)kVoxelG : (double)fabsf(dot(nrm, d));
+}
+
+// Origin of direct ray r of primitive p; u = philox(r, p, c2, 0; seed, pass), c2 =
+// source << 1.  Non-triangles are stratified over dimx x dimy cells
+// (OptiX8DeviceCode.cu:1270-1290); a voxel's third coordinate uses counter c2 | 1.
+__device__ __forceinline__ f3 direct_origin(const float4 g[4], uint32_t type, uint32_t r, uint32_t p, uint32_t c2,
+                                            int dimx, int dimy, uint32_t seed, uint32_t pass, const u4 &u) {
+    float uu = u01(u.a), vv = u01(u.b), ww = 0.f;
+    if (type != PT_TRI) {
+        const int xi = (int)(r % (uint32_t)dimx), yi = (int)(r / (uint32_t)dimx);
+        uu = ((float)xi + uu) / (float)dimx;
+        vv = ((float)yi + vv) / (float)dimy;
+    }
+    if (type == PT_VOXEL) ww = u01(philox(r, p, c2 | 1u, 0u, seed, pass).a);
+    return sample_point(g, type, uu, vv, ww);
+}
+
+// Origin and direction of diffuse ray r of primitive p from face `face` (1 top, 0
+// bottom).  Surfaces: cosine-weighted about the normal, counter (r, p, face, 0).  Voxels
+// (VOX builds only): both faces share the sample of counter (r, p, 1, 0), the third
+// coordinate comes from (r, p, 2, 0), and the bottom face flips the direction.
+template <bool VOX>
+__device__ __forceinline__ void diffuse_ray(const float4 g[4], uint32_t type, uint32_t r, uint32_t p, int face,
+                                            int dimx, int dimy, uint32_t seed, uint32_t pass, f3 *org, f3 *dir) {
+    const int ti = (int)(r % (uint32_t)dimx), pi = (int)(r / (uint32_t)dimx);
+    f3 dd;
+    if (VOX && type == PT_VOXEL) {
+        const u4 u = philox(r, p, 1u, 0u, seed, pass);
+        const float w = u01(philox(r, p, 2u, 0u, seed, pass).a);
+        dd = voxel_dir(ti, pi, dimx, dimy, u01(u.a), u01(u.b));
+        *org = sample_point(g, type, u01(u.c), u01(u.d), w);
+    } else {
+        const u4 u = philox(r, p, (uint32_t)face, 0u, seed, pass);
+        dd = diffuse_dir(xyz(g[3]), ti, pi, dimx, dimy, u01(u.a), u01(u.b));
+        *org = sample_point(g, type, u01(u.c), u01(u.d), 0.f);
+    }
+    *dir = (face == 0) ? mk(-dd.x, -dd.y, -dd.z) : dd;
+}
+
 // ------------------------------------------------------------------ direct --
-__device__ __forceinline__ bool direct_ray(const SourceDev &src, f3 org, f3 nrm, uint32_t rx, uint32_t ry,
+__device__ __forceinline__ bool direct_ray(const SourceDev &src, f3 org, f3 nrm, bool vox, uint32_t rx, uint32_t ry,
                                            double inv_nr, f3 *dir, float *tmax, double *strength) {
     if (src.type == 0) {
         f3 dd = normalize(mk(src.pos[0], src.pos[1], src.pos[2]));
         *dir = dd;
         *tmax = 1e38f;
-        *strength = inv_nr * (double)fabsf(dot(nrm, dd));
+        *strength = inv_nr * proj(nrm, dd, vox);
         return true;
     }
     f3 spos = mk(src.pos[0], src.pos[1], src.pos[2]);
@@ -244,7 +289,7 @@ __device__ __forceinline__ bool direct_ray(const SourceDev &src, f3 org, f3 nrm,
                 float sti = sqrtf(fmaxf(0.f, 1.0f - cti * cti));
                 f3 l = mk(sti * cpj, sti * spj, cti);
                 if (dot(l, dd) < 0.f) {
-                    acc += inv_nr * (double)fabsf(dot(nrm, dd)) * (double)fabsf(dot(l, dd)) /
+                    acc += inv_nr * proj(nrm, dd, vox) * (double)fabsf(dot(l, dd)) /
                            ((double)dist * (double)dist) / (double)(N * N) * (double)src.w0 * (double)src.w0;
                 }
             }
@@ -294,7 +339,7 @@ __device__ __forceinline__ bool direct_ray(const SourceDev &src, f3 org, f3 nrm,
         dd = normalize(dd);
         double area = (src.type == 3) ? (double)src.w0 * (double)src.w1 / 3.14159265358979323846
                                       : (double)src.w0 * (double)src.w0;
-        *strength = inv_nr * (double)fabsf(dot(nrm, dd)) * (double)fabsf(dot(ldir, dd)) /
+        *strength = inv_nr * proj(nrm, dd, vox) * (double)fabsf(dot(ldir, dd)) /
                     ((double)dist * (double)dist) * area;
         *dir = dd;
         *tmax = dist;
@@ -327,25 +372,22 @@ __global__ void __launch_bounds__(kBlock) k_direct(const DirectParams P) {
             double v[2] = {0.0, 0.0};  // [face0, face1]
             bool live = active;
             if (live) {
-                u4 u = philox(r, p, (uint32_t)(k << 1), 0u, P.seed, P.pass);
-                float uu = u01(u.a), vv = u01(u.b);
-                if (type != PT_TRI) {
-                    int xi = (int)(r % (uint32_t)P.dimx), yi = (int)(r / (uint32_t)P.dimx);
-                    uu = ((float)xi + uu) / (float)P.dimx;
-                    vv = ((float)yi + vv) / (float)P.dimy;
-                }
-                f3 org = sample_point(g, type, uu, vv);
+                const uint32_t c2 = (uint32_t)(k << 1);
+                u4 u = philox(r, p, c2, 0u, P.seed, P.pass);
+                const bool vox = type == PT_VOXEL;
+                f3 org = direct_origin(g, type, r, p, c2, P.dimx, P.dimy, P.seed, P.pass, u);
                 f3 nrm = xyz(g[3]);
                 f3 dir;
                 float tmax;
                 double strength;
-                live = direct_ray(P.src[k], org, nrm, u.c, u.d, inv_nr, &dir, &tmax, &strength);
+                live = direct_ray(P.src[k], org, nrm, vox, u.c, u.d, inv_nr, &dir, &tmax, &strength);
                 if (live) {
-                    bool face = dot(dir, nrm) > 0.f;
+                    bool face = vox || dot(dir, nrm) > 0.f;
                     if ((!face && ts == 0) || ts == 3) {
                         live = false;
                     } else {
-                        Hit h = trace_full<STATS>(P.sc, org, dir, 1e-4f, tmax, true, &nv, &np);
+                        Hit h = trace_full<STATS>(P.sc, org, dir, 1e-4f, tmax, true, VoxKey{r, p, c2, P.seed, P.pass},
+                                                  &nv, &np);
                         if (h.prim == 0xFFFFFFFFu) v[face ? 1 : 0] = strength;
                     }
                 }
@@ -407,12 +449,10 @@ __global__ void __launch_bounds__(kBlock) k_diffuse(const DiffuseParams P) {
             float4 g[4];
             load_rgen(P.sc, p, g);
             uint32_t type = __float_as_uint(g[0].w);
-            u4 u = philox(r, p, (uint32_t)face, 0u, P.seed, P.pass);
-            int ti = (int)(r % (uint32_t)P.dimx), pi = (int)(r / (uint32_t)P.dimx);
-            f3 dir = diffuse_dir(xyz(g[3]), ti, pi, P.dimx, P.dimy, u01(u.a), u01(u.b));
-            if (face == 0) dir = mk(-dir.x, -dir.y, -dir.z);
-            f3 org = sample_point(g, type, u01(u.c), u01(u.d));
-            Hit h = trace_full<STATS>(P.sc, org, dir, 1e-4f, 1e38f, false, &nv, &np);
+            f3 org, dir;
+            diffuse_ray<true>(g, type, r, p, face, P.dimx, P.dimy, P.seed, P.pass, &org, &dir);
+            Hit h = trace_full<STATS>(P.sc, org, dir, 1e-4f, 1e38f, false, VoxKey{r, p, (uint32_t)face, P.seed, P.pass},
+                                      &nv, &np);
             if (h.prim == kLost) {
                 // dropped ray: no deposit
             } else if (h.prim != 0xFFFFFFFFu) {
@@ -449,8 +489,9 @@ __global__ void __launch_bounds__(kBlock) k_diffuse(const DiffuseParams P) {
 constexpr int32_t kSentinel = 0x7FFFFFF0;
 
 // MINB: resident blocks per SM the register allocation must allow (4, the default: 64
-// registers; 3: more registers, fewer warps).
-template <int NB, bool RECORD, int MINB>
+// registers; 3: more registers, fewer warps).  VOX: the scene holds voxels (turbid media
+// with their own ray sampling); without it the voxel code is left out.
+template <int NB, bool RECORD, int MINB, bool VOX>
 __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams P) {
     unsigned long long *fetch = P.fetch;
     const int lane = threadIdx.x & 31;
@@ -472,7 +513,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
     int32_t stack[kStack];
     uint32_t budget = 0;
     int wraps = 0;
-    uint32_t p = 0;
+    uint32_t p = 0, rr = 0;
     int face = 1;
     unsigned long long rid = 0;
     uint32_t akey = 0xFFFFFFFFu;
@@ -511,11 +552,8 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
                         float4 g[4];
                         load_rgen(sc, p, g);
                         const uint32_t type = __float_as_uint(g[0].w);
-                        const u4 u = philox(r, p, (uint32_t)face, 0u, P.seed, P.pass);
-                        const int ti = (int)(r % (uint32_t)P.dimx), pi = (int)(r / (uint32_t)P.dimx);
-                        d = diffuse_dir(xyz(g[3]), ti, pi, P.dimx, P.dimy, u01(u.a), u01(u.b));
-                        if (face == 0) d = mk(-d.x, -d.y, -d.z);
-                        o = sample_point(g, type, u01(u.c), u01(u.d));
+                        diffuse_ray<VOX>(g, type, r, p, face, P.dimx, P.dimy, P.seed, P.pass, &o, &d);
+                        if (VOX) rr = r;
                         w = wt_setup(d);
                         inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
                         ooi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
@@ -586,7 +624,8 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
                 float t;
                 int fc;
                 uint32_t orig;
-                if (rec_hit(sc.rec, slot, w, o, d, inv, 1e-4f, best, &t, &fc, &orig)) {
+                const VoxKey vk{rr, p, (uint32_t)face | ((uint32_t)wraps << 16), P.seed, P.pass};
+                if (rec_hit<VOX>(sc.rec, slot, w, o, d, inv, 1e-4f, best, vk, &t, &fc, &orig)) {
                     if (bprim == 0xFFFFFFFFu || t < best || (t == best && orig < bprim)) {
                         best = t;
                         bprim = orig;
@@ -687,7 +726,9 @@ __global__ void k_trace_rays(const TraceScene sc, int64_t nrays, const float *__
     f3 oo = mk(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
     f3 dd = mk(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
     uint32_t nv = 0, np = 0;
-    Hit h = trace_bvh<false>(sc, oo, dd, tmin, tmax, anyhit != 0, &nv, &np);
+    // voxel draws of explicit ray i: counter (i, i >> 32, 2^31), key (0, ~0)
+    const VoxKey vk{(uint32_t)i, (uint32_t)((uint64_t)i >> 32), 0x80000000u, 0u, 0xFFFFFFFFu};
+    Hit h = trace_bvh<false>(sc, oo, dd, tmin, tmax, anyhit != 0, vk, &nv, &np);
     hit[i] = (h.prim == 0xFFFFFFFFu) ? -1 : (int32_t)h.prim;
     t[i] = h.t;
     face[i] = h.face;
@@ -703,22 +744,13 @@ __global__ void k_gen_rays(const TraceScene sc, int kind, uint32_t seed, uint32_
     float4 g[4];
     load_rgen(sc, p, g);
     uint32_t type = __float_as_uint(g[0].w);
-    u4 u = philox(r, p, (uint32_t)face, 0u, seed, pass);
     f3 org, dir;
     if (kind == 0) {
-        float uu = u01(u.a), vv = u01(u.b);
-        if (type != PT_TRI) {
-            int xi = (int)(r % (uint32_t)dimx), yi = (int)(r / (uint32_t)dimx);
-            uu = ((float)xi + uu) / (float)dimx;
-            vv = ((float)yi + vv) / (float)dimy;
-        }
-        org = sample_point(g, type, uu, vv);
+        const u4 u = philox(r, p, (uint32_t)face, 0u, seed, pass);
+        org = direct_origin(g, type, r, p, (uint32_t)face, dimx, dimy, seed, pass, u);
         dir = normalize(mk(dx, dy, dz));
     } else {
-        int ti = (int)(r % (uint32_t)dimx), pi = (int)(r / (uint32_t)dimx);
-        dir = diffuse_dir(xyz(g[3]), ti, pi, dimx, dimy, u01(u.a), u01(u.b));
-        if (face == 0) dir = mk(-dir.x, -dir.y, -dir.z);
-        org = sample_point(g, type, u01(u.c), u01(u.d));
+        diffuse_ray<true>(g, type, r, p, face, dimx, dimy, seed, pass, &org, &dir);
     }
     o[3 * i] = org.x;
     o[3 * i + 1] = org.y;
@@ -851,13 +883,7 @@ __global__ void __launch_bounds__(kBlock) k_direct_sweep(const SweepDirectParams
             const int ts = P.sc.twosided[p];
             const uint32_t type = __float_as_uint(g[0].w);
             const u4 u = philox(r, p, 0u, 0u, P.seed, 0u);
-            float uu = u01(u.a), vv = u01(u.b);
-            if (type != PT_TRI) {
-                const int xi = (int)(r % (uint32_t)P.dimx), yi = (int)(r / (uint32_t)P.dimx);
-                uu = ((float)xi + uu) / (float)P.dimx;
-                vv = ((float)yi + vv) / (float)P.dimy;
-            }
-            const f3 org = sample_point(g, type, uu, vv);
+            const f3 org = direct_origin(g, type, r, p, 0u, P.dimx, P.dimy, P.seed, 0u, u);
             const f3 nrm = xyz(g[3]);
             const f3 dd = normalize(mk(P.sun_dir[3 * sun], P.sun_dir[3 * sun + 1], P.sun_dir[3 * sun + 2]));
             const double strength = inv_nr * (double)fabsf(dot(nrm, dd));
@@ -865,7 +891,7 @@ __global__ void __launch_bounds__(kBlock) k_direct_sweep(const SweepDirectParams
             if (!((!face && ts == 0) || ts == 3)) {
                 live = true;
                 uint32_t nv = 0, np = 0;
-                const Hit h = trace_full<false>(P.sc, org, dd, 1e-4f, 1e38f, true, &nv, &np);
+                const Hit h = trace_full<false>(P.sc, org, dd, 1e-4f, 1e38f, true, VoxKey{r, p, 0u, P.seed, 0u}, &nv, &np);
                 if (h.prim == 0xFFFFFFFFu) v[face ? 1 : 0] = strength;
             }
         }
@@ -1014,25 +1040,26 @@ static int ps_min_blocks() {
     return v;
 }
 
-template <int NB, int MINB>
+template <int NB, int MINB, bool VOX>
 static cudaError_t diffuse_ps_launch_b(const DiffuseParams &p, cudaStream_t s) {
     static int blocks_per_sm = 0, sms = 0;
     if (blocks_per_sm == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<NB, false, MINB>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<NB, false, MINB, VOX>, kBlock, 0);
         if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
     cudaError_t e = cudaMemsetAsync(p.fetch, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
-    k_diffuse_ps<NB, false, MINB><<<sms * blocks_per_sm, kBlock, 0, s>>>(p);
+    k_diffuse_ps<NB, false, MINB, VOX><<<sms * blocks_per_sm, kBlock, 0, s>>>(p);
     return cudaGetLastError();
 }
 
 template <int NB>
 static cudaError_t diffuse_ps_launch(const DiffuseParams &p, cudaStream_t s) {
-    return ps_min_blocks() == 4 ? diffuse_ps_launch_b<NB, 4>(p, s) : diffuse_ps_launch_b<NB, 3>(p, s);
+    if (p.sc.voxels) return diffuse_ps_launch_b<NB, 4, true>(p, s);
+    return ps_min_blocks() == 4 ? diffuse_ps_launch_b<NB, 4, false>(p, s) : diffuse_ps_launch_b<NB, 3, false>(p, s);
 }
 
 static bool use_persistent() {
@@ -1140,6 +1167,61 @@ cudaError_t launch_final_flux(size_t nb, const double *rin, const double *stop, 
     return cudaGetLastError();
 }
 
+// Scattering residual per band: num = sum_p area_p (stop + sbot), den = sum_p area_p
+// (rin + stop + sbot), in FP64 by a fixed two-stage reduction (grid-stride partial sums
+// in a fixed order, a shared-memory tree per block, block partials added in block
+// order), so the result does not depend on scheduling.
+__global__ void __launch_bounds__(256) k_residual(int n, int Bl, const double *__restrict__ area,
+                                                  const double *__restrict__ rin, const double *__restrict__ stop,
+                                                  const double *__restrict__ sbot, double *__restrict__ partial) {
+    __shared__ double sh[2][256];
+    const int tid = threadIdx.x;
+    for (int b = 0; b < Bl; ++b) {
+        double num = 0.0, den = 0.0;
+        for (int p = blockIdx.x * blockDim.x + tid; p < n; p += gridDim.x * blockDim.x) {
+            const size_t i = (size_t)p * Bl + b;
+            const double sc = stop[i] + sbot[i];
+            num += area[p] * sc;
+            den += area[p] * (rin[i] + sc);
+        }
+        sh[0][tid] = num;
+        sh[1][tid] = den;
+        __syncthreads();
+        for (int off = 128; off > 0; off >>= 1) {
+            if (tid < off) {
+                sh[0][tid] += sh[0][tid + off];
+                sh[1][tid] += sh[1][tid + off];
+            }
+            __syncthreads();
+        }
+        if (tid == 0) {
+            partial[((size_t)blockIdx.x * Bl + b) * 2] = sh[0][0];
+            partial[((size_t)blockIdx.x * Bl + b) * 2 + 1] = sh[1][0];
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_residual_final(int nblocks, int Bl, const double *__restrict__ partial, double *__restrict__ out) {
+    const int b = threadIdx.x;
+    if (b >= Bl) return;
+    double num = 0.0, den = 0.0;
+    for (int k = 0; k < nblocks; ++k) {
+        num += partial[((size_t)k * Bl + b) * 2];
+        den += partial[((size_t)k * Bl + b) * 2 + 1];
+    }
+    out[2 * b] = num;
+    out[2 * b + 1] = den;
+}
+
+cudaError_t launch_residual(int n, int Bl, const double *area, const double *rin, const double *stop,
+                            const double *sbot, double *scratch, cudaStream_t s) {
+    if (n <= 0 || Bl <= 0 || Bl > 32) return cudaErrorInvalidValue;
+    k_residual<<<kResidualBlocks, 256, 0, s>>>(n, Bl, area, rin, stop, sbot, scratch + 64);
+    k_residual_final<<<1, 32, 0, s>>>(kResidualBlocks, Bl, scratch + 64, scratch);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_direct_sweep(const SweepDirectParams &p, int max_blocks, cudaStream_t s) {
     const long long total = (long long)p.sc.n * p.dimx * p.dimy * p.nsun;
     if (total <= 0) return cudaSuccess;
@@ -1156,7 +1238,7 @@ cudaError_t launch_diffuse_record(const DiffuseParams &p, uint32_t *hits, cudaSt
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<1, true, 3>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<1, true, 3, false>, kBlock, 0);
         if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
     DiffuseParams q = p;
@@ -1164,7 +1246,7 @@ cudaError_t launch_diffuse_record(const DiffuseParams &p, uint32_t *hits, cudaSt
     q.Bc = 1;
     cudaError_t e = cudaMemsetAsync(q.fetch, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
-    k_diffuse_ps<1, true, 3><<<sms * blocks_per_sm, kBlock, 0, s>>>(q);
+    k_diffuse_ps<1, true, 3, false><<<sms * blocks_per_sm, kBlock, 0, s>>>(q);
     return cudaGetLastError();
 }
 

@@ -78,6 +78,8 @@ class Context:
         return self._add(T, scenes.DISK, math.pi * radius * radius)
 
     def addVoxel(self, center, size):
+        """Voxel primitive; its leaves come from primitive data ``leaf_area_density``
+        (m^2/m^3).  Its radiation fluxes are per unit leaf area."""
         T = scenes.voxel_T(np.asarray(center, np.float64)[None], size)[0]
         return self._add(T, scenes.VOXEL, 2 * (size[0] * size[1] + size[1] * size[2] + size[0] * size[2]))
 
@@ -91,7 +93,10 @@ class Context:
         return uuids
 
     def addScene(self, sc: "scenes.Scene"):
-        return self.addPrimitives(sc.T, sc.ptype, sc.area, sc.twosided)
+        uuids = self.addPrimitives(sc.T, sc.ptype, sc.area, sc.twosided)
+        if sc.lad is not None:
+            self.setPrimitiveData(uuids, "leaf_area_density", np.asarray(sc.lad, np.float64))
+        return uuids
 
     def getPrimitiveCount(self):
         return self._n
@@ -232,6 +237,7 @@ class RadiationModel:
         self._geom_n = -1
         self.rho_default, self.tau_default, self.eps_default = 0.0, 0.0, 1.0
         self.temperature_default = 300.0
+        self.scatter_tolerance = 0.0
         self.last_stats = {}
 
     @property
@@ -381,9 +387,27 @@ class RadiationModel:
             faces.append([(x0, y1, z0), (x1, y1, z0), (x1, y1, z1), (x0, y1, z1)])
         return np.asarray(faces, np.float32)
 
+    def setScatteringResidualTolerance(self, tol: float):
+        """Stop a band's scattering iterations once the FP64 residual (power scattered by
+        the last iteration over the band's total) is at most ``tol``; 0 (the default) runs
+        every iteration up to the scattering depth, as the reference does.  No counterpart
+        in the reference."""
+        if not tol >= 0.0:
+            raise HeliosRuntimeError("ERROR (RadiationModel::setScatteringResidualTolerance): tolerance must be >= 0.")
+        self.scatter_tolerance = float(tol)
+
+    def voxel_lad(self):
+        """Leaf area density of every primitive (read for voxels, primitive data
+        ``leaf_area_density``), or None when the context holds no voxels."""
+        _, ty, _ = self.context.arrays()
+        if not (ty == scenes.VOXEL).any():
+            return None
+        return self.context.primitive_array("leaf_area_density", 0.0).astype(np.float32)
+
     def geometry_arrays(self):
         T, ty, area = self.context.arrays()
         ts = self.context.primitive_array("twosided_flag", 1).astype(np.int8)
+        ts[ty == scenes.VOXEL] = 1  # a voxel launches both directions of each sample
         keep = (area > 0) | (ty == scenes.TILE)  # zero-area primitives are skipped (RadiationModel.cpp:5813-5824)
         if not keep.all():
             raise HeliosRuntimeError("zero-area primitives are not supported by this mirror")
@@ -392,7 +416,7 @@ class RadiationModel:
     def updateGeometry(self):
         T, ty, ts = self.geometry_arrays()
         self._ts = ts
-        self.ctx.update_geometry(T, ty, ts, self._bbox_faces(), self.periodic)
+        self.ctx.update_geometry(T, ty, ts, self._bbox_faces(), self.periodic, self.voxel_lad())
         self.ctx.build_accel()
         self._geom_n = T.shape[0]
 
@@ -469,6 +493,7 @@ class RadiationModel:
             "emission": np.array([1 if x.emissionFlag else 0 for x in B], np.uint8),
             "eps": eps, "temperature": temp,
             "seed": self.seed if seed is None else seed,
+            "scatter_tolerance": self.scatter_tolerance,
             "n": n,
         }
         return desc

@@ -34,6 +34,7 @@ class Scene:
     groups: dict = field(default_factory=dict)   # name -> index array
     bbox_verts: np.ndarray | None = None         # periodic walls [nb, 4, 3]
     periodic: tuple = (0.0, 0.0)
+    lad: np.ndarray | None = None                # [n] leaf area density of voxels (0 elsewhere)
 
     @property
     def n(self) -> int:
@@ -222,6 +223,88 @@ def voxel_T(centers, size) -> np.ndarray:
     T[:, :3, 3] = centers
     T[:, 3, 3] = 1.0
     return T.reshape(n, 16).astype(np.float32)
+
+
+def voxel_grid(lo, hi, div, lad) -> Scene:
+    """div[0] x div[1] x div[2] axis-aligned voxels filling the box [lo, hi]; lad is a
+    scalar or an array of div[0]*div[1]*div[2] leaf area densities (x fastest)."""
+    lo, hi = np.asarray(lo, np.float64), np.asarray(hi, np.float64)
+    nx, ny, nz = div
+    size = (hi - lo) / np.array([nx, ny, nz], np.float64)
+    ix, iy, iz = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    idx = np.stack([ix.ravel(order="F"), iy.ravel(order="F"), iz.ravel(order="F")], -1)
+    centers = lo + (idx + 0.5) * size
+    n = centers.shape[0]
+    T = voxel_T(centers, size)
+    lad = np.broadcast_to(np.asarray(lad, np.float64), (n,)).astype(np.float32)
+    vol = float(np.prod(size))
+    return Scene(T, np.full(n, VOXEL, np.uint32), np.ones(n, np.int8), lad.astype(np.float64) * vol,
+                 {"voxels": np.arange(n)}, lad=lad)
+
+
+def disk_leaves(centers, normals, radius) -> np.ndarray:
+    """Disk leaves of one radius centred at `centers` with the given normals."""
+    return disks(np.asarray(centers, np.float64), radius, normals)
+
+
+def concat_scenes(*parts: Scene) -> Scene:
+    """Primitives of several scenes in order; groups are renamed <i>:<name> and shifted."""
+    T = np.concatenate([p.T for p in parts]).astype(np.float32)
+    ty = np.concatenate([p.ptype for p in parts]).astype(np.uint32)
+    ts = np.concatenate([p.twosided for p in parts]).astype(np.int8)
+    area = np.concatenate([p.area for p in parts])
+    lad = np.concatenate([p.lad if p.lad is not None else np.zeros(p.n, np.float32) for p in parts])
+    groups, off = {}, 0
+    for i, p in enumerate(parts):
+        for k, v in p.groups.items():
+            groups[f"{i}:{k}"] = np.asarray(v) + off
+        off += p.n
+    return Scene(T, ty, ts, area, groups, lad=lad if (ty == VOXEL).any() else None)
+
+
+def deep_scatter(n_tri=3_000_000, n_patch=500_000, n_disk=500_000, vox_div=64, domain=24.0, height=4.0,
+                 tri_side=0.03, patch_side=0.04, disk_radius=0.02, lad_max=2.0, seed=0) -> Scene:
+    """Deep-scattering stress scene: a one-sided ground patch under two-sided leaves --
+    n_tri equilateral triangles, n_patch square patches and n_disk disks (spherical leaf
+    angles, centres uniform in [0, domain]^2 x [0.05, height]) -- and a vox_div^3 voxel
+    grid over the same box with leaf area density uniform in [0, lad_max]."""
+    rng = np.random.default_rng(seed)
+
+    def centres(k):
+        return np.stack([rng.uniform(0, domain, k), rng.uniform(0, domain, k), rng.uniform(0.05, height, k)], -1)
+
+    c = centres(n_tri)
+    nrm = uniform_sphere(rng, n_tri)
+    spin = rng.uniform(0, 2 * math.pi, n_tri)
+    helper = np.where(np.abs(nrm[:, 2:3]) < 0.9, np.array([0.0, 0.0, 1.0]), np.array([1.0, 0.0, 0.0]))
+    ex = np.cross(helper, nrm)
+    ex /= np.linalg.norm(ex, axis=-1, keepdims=True)
+    ey = np.cross(nrm, ex)
+    R = tri_side / math.sqrt(3.0)
+    vs = [c + R * (np.cos(spin + 2 * math.pi * k / 3)[:, None] * ex + np.sin(spin + 2 * math.pi * k / 3)[:, None] * ey)
+          for k in range(3)]
+    tris = Scene(triangle_T(vs[0], vs[1], vs[2]), np.full(n_tri, TRIANGLE, np.uint32), np.ones(n_tri, np.int8),
+                 np.full(n_tri, math.sqrt(3.0) / 4.0 * tri_side * tri_side), {"triangles": np.arange(n_tri)})
+    c = centres(n_patch)
+    Tp = frame_T(c, np.full(n_patch, patch_side), np.full(n_patch, patch_side), uniform_sphere(rng, n_patch),
+                 rng.uniform(0, 2 * math.pi, n_patch))
+    patches = Scene(Tp, np.full(n_patch, PATCH, np.uint32), np.ones(n_patch, np.int8),
+                    np.full(n_patch, patch_side * patch_side), {"patches": np.arange(n_patch)})
+    c = centres(n_disk)
+    Td = disk_leaves(c, uniform_sphere(rng, n_disk), disk_radius)
+    dsk = Scene(Td, np.full(n_disk, DISK, np.uint32), np.ones(n_disk, np.int8),
+                np.full(n_disk, math.pi * disk_radius * disk_radius), {"disks": np.arange(n_disk)})
+    nv = vox_div ** 3
+    vox = voxel_grid((0.0, 0.0, 0.0), (domain, domain, height), (vox_div, vox_div, vox_div),
+                     rng.uniform(0.0, lad_max, nv))
+    ground = Scene(helios_patch_T((0.5 * domain, 0.5 * domain, 0.0), (domain, domain))[None, :],
+                   np.array([PATCH], np.uint32), np.zeros(1, np.int8), np.array([domain * domain]),
+                   {"ground": np.array([0])})
+    sc = concat_scenes(ground, tris, patches, dsk, vox)
+    sc.groups = {"ground": np.array([0]), "triangles": 1 + np.arange(n_tri),
+                 "patches": 1 + n_tri + np.arange(n_patch), "disks": 1 + n_tri + n_patch + np.arange(n_disk),
+                 "voxels": 1 + n_tri + n_patch + n_disk + np.arange(nv)}
+    return sc
 
 
 def sun_direction(zenith_deg: float, azimuth_deg: float) -> np.ndarray:

@@ -44,15 +44,25 @@ typedef struct hrt_context hrt_context;
 /* Geometry, the subset of helios::RayTracingGeometry (RayTracingTypes.h:40-155)
  * that the radiation solve reads.  Primitive types: 0 patch, 1 triangle, 2 disk,
  * 3 tile (traced as a patch), 4 voxel.  Periodic walls are the reference's
- * "bbox" primitives (type 5), passed separately as world-space quads. */
+ * "bbox" primitives (type 5), passed separately as world-space quads.
+ *
+ * Disks are native unit disks scaled by their transform (the OptiX 6 semantics of
+ * primitiveIntersection.cu:236-300; the reference's OptiX 8 backend has none).
+ * Voxels are axis-aligned boxes filled with a turbid medium of leaves with a spherical
+ * angle distribution: extinction G * LAD with G = 0.5, free-path interception drawn per
+ * (ray, voxel), isotropic launch (pairs of opposite directions), leaves scattering
+ * rho + tau isotropically.  Their fluxes are per unit LEAF area (LAD x volume).  The
+ * reference has no voxel radiation physics (OptiX 6 rayHit.cu:278-290 is commented
+ * out), so these are this library's definitions. */
 typedef struct {
     int32_t n;                    /* primitive_count */
     const float *transform;       /* [n*16] row-major 4x4 (transform_matrices) */
     const uint32_t *type;         /* [n] primitive_types */
-    const int8_t *twosided;       /* [n] twosided_flags: 0 one-sided, 1 two-sided, 2, 3 (skip) */
+    const int8_t *twosided;       /* [n] twosided_flags: 0 one-sided, 1 two-sided, 2, 3 (skip); voxels are two-sided */
     int32_t nbbox;                /* bbox_count: 0, 2 or 4 periodic walls */
     const float *bbox_vertices;   /* [nbbox*4*3] wall corners (bboxes.vertices) */
     float periodic_x, periodic_y; /* periodic_flag */
+    const float *voxel_lad;       /* [n] leaf area density (m^2/m^3) read for voxels; may be NULL without voxels */
 } hrt_geometry;
 
 /* helios::RayTracingSource (RayTracingTypes.h:189-196) without the flux vectors,
@@ -106,6 +116,12 @@ typedef struct {
     const float *emissivity;            /* [n*Bl], or NULL to reuse the array of an earlier call */
     const float *temperature;           /* [n] kelvin, or NULL to reuse the array of an earlier call */
     uint32_t seed;
+    /* > 0: FP64 convergence check after every scattering iteration (no counterpart in the
+     * reference, which always runs scattering_depth iterations).  A band stops once the
+     * area-weighted power its last iteration scattered, not yet propagated, is at most
+     * scatter_tolerance times its total (absorbed + that); that power stays in the flux
+     * as at the depth limit.  0 runs the reference's fixed iteration count. */
+    double scatter_tolerance;
 } hrt_band_solve;
 
 /* ---- lifecycle: RayTracingBackend::initialize / shutdown (RayTracingBackend.h:54,61) */
@@ -207,7 +223,8 @@ int hrt_server_result(hrt_server *s, uint64_t request_id, float *flux_out, size_
 int hrt_server_stats(hrt_server *s, double *out, int count);
 int hrt_server_destroy(hrt_server *s);
 
-/* Statistics of the last hrt_run_band: [0] rays traced, [1] kernels launched. */
+/* Statistics of the last hrt_run_band: [0] rays traced, [1] kernels launched,
+ * [2] scattering iterations run. */
 int hrt_last_stats(const hrt_context *ctx, uint64_t *stats, int count);
 /* Device status word (HRT error bits) accumulated since the last reset. */
 int hrt_device_status(hrt_context *ctx, uint32_t *status, int reset);
@@ -235,6 +252,7 @@ int hrt_get_measure(hrt_context *ctx, double *out, int count);
  *   d_transform [n*16] float, d_type [n] uint32 (inputs);
  *   d_records [n*64 B], d_origins [n*64 B], d_nodes [max(n-1,1)*64 B], d_codes [n],
  *   d_perm [n] (outputs; nodes/codes/perm in the hrt_get_bvh layout).
+ * It takes no leaf area densities: voxels are built as empty boxes that no ray hits.
  * Scratch is a static device array sized for at most HRT_STATIC_MAX_PRIMS primitives
  * (about 5.6 MB held by every GPU that loads the library, until exit); larger n is
  * rejected with HRT_EINVAL.  The first call on a device looks the array's address up

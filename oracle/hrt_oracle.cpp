@@ -125,6 +125,48 @@ inline void sincos2pi(float u, float *c_out, float *s_out) {
     }
 }
 
+// Natural logarithm of x in (0, 1] (the free-path draw of the voxel medium), in plain
+// IEEE single-precision steps so host and device agree bit for bit: x = m * 2^e with
+// m in [sqrt(1/2), sqrt(2)), then ln m = 2 atanh(z), z = (m - 1) / (m + 1), by its
+// Taylor series to z^9 (|z| <= 0.172, truncation below 1e-9).
+inline float ln_unit(float x) {
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    int e = (int)((b >> 23) & 0xFFu) - 127;
+    uint32_t mb = (b & 0x7FFFFFu) | 0x3F800000u;
+    float m;
+    std::memcpy(&m, &mb, 4);
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e = e + 1;
+    }
+    float z = (m - 1.0f) / (m + 1.0f);
+    float z2 = z * z;
+    float s = 1.0f + z2 * (0.333333333f + z2 * (0.2f + z2 * (0.142857143f + z2 * 0.111111111f)));
+    return (float)e * 0.693147181f + 2.0f * z * s;
+}
+
+// Concentric square-to-disk map (Shirley & Chiu, "A Low Distortion Map Between Disk and
+// Square", JGT 1997) of (u, v) in [0,1)^2 to the unit disk; the angle is evaluated as a
+// fraction of a turn by sincos2pi.
+inline void concentric(float u, float v, float *x, float *y) {
+    float sx = -1.0f + 2.0f * u, sy = -1.0f + 2.0f * v;
+    float r, ph;  // ph in units of pi/4
+    if (sx > -sy) {
+        if (sx > sy) { r = sx; ph = sy / sx; }
+        else { r = sy; ph = 2.0f - sx / sy; }
+    } else {
+        if (sx < sy) { r = -sx; ph = 4.0f + sy / sx; }
+        else { r = -sy; ph = (sy != 0.f) ? 6.0f - sx / sy : 0.f; }
+    }
+    float frac = ph * 0.125f;
+    if (frac < 0.f) frac = frac + 1.0f;
+    float c, s;
+    sincos2pi(frac, &c, &s);
+    *x = r * c;
+    *y = r * s;
+}
+
 // Orthonormal basis around unit n (Duff, Burgess, Christensen, Hery, Kensler,
 // Liani, Villemin: "Building an Orthonormal Basis, Revisited", JCGT 6(1), 2017).
 inline void onb(V3 n, V3 *t1, V3 *t2) {
@@ -142,12 +184,16 @@ enum { PT_PATCH = 0, PT_TRI = 1, PT_DISK = 2, PT_TILE = 3, PT_VOXEL = 4, PT_BBOX
 struct Rec {        // intersection record, one per primitive
     V3 p[4];        // patch/bbox: 4 corners; triangle: v0,v1,v2; disk: centre, normal(unit), (r,0,0)
     int type;       // voxel: p[0]=lo, p[1]=hi
+    float k;        // voxel: extinction coefficient G * LAD (1/m), G = 0.5
 };
 struct RGen {       // ray-origin sampling record
-    V3 P, A, B, N;  // point = P + u*A + v*B ; N = unit normal
+    V3 P, A, B, N;  // point = P + u*A + v*B ; N = unit normal (voxel: N = third box edge C)
 };
 
-Rec make_rec(const float *T, int type) {
+// Projection coefficient of the voxel medium's leaves: G = 0.5 (spherical leaf angles).
+constexpr float kVoxelG = 0.5f;
+
+Rec make_rec(const float *T, int type, float lad) {
     Rec r{};
     r.type = type;
     if (type == PT_TRI) {
@@ -171,6 +217,7 @@ Rec make_rec(const float *T, int type) {
         r.p[1] = vadd(c, h);
         r.p[2] = r.p[0];
         r.p[3] = r.p[1];
+        r.k = kVoxelG * lad;
     } else {  // patch, tile
         r.type = PT_PATCH;
         r.p[0] = xform(T, -0.5f, -0.5f);
@@ -188,11 +235,35 @@ RGen make_rgen(const float *T, int type) {
     if (type == PT_TRI) {
         g.P = v3(T[3], T[7], T[11]);
         g.N = vnormalize(vcross(g.B, g.A));  // = normalize(cross(v1-v0, v2-v0))
+    } else if (type == PT_DISK) {
+        g.P = v3(T[3], T[7], T[11]);         // centre; the unit disk spans A and B
+        g.N = vnormalize(vcross(g.A, g.B));
+    } else if (type == PT_VOXEL) {
+        g.N = v3(T[2], T[6], T[10]);         // third edge of the box
+        g.P = v3(((T[0] * -0.5f + T[1] * -0.5f) + T[2] * -0.5f) + T[3],
+                 ((T[4] * -0.5f + T[5] * -0.5f) + T[6] * -0.5f) + T[7],
+                 ((T[8] * -0.5f + T[9] * -0.5f) + T[10] * -0.5f) + T[11]);
     } else {
         g.P = xform(T, -0.5f, -0.5f);
         g.N = vnormalize(vcross(g.A, g.B));
     }
     return g;
+}
+
+// Surface area of a primitive (leaf area for a voxel: LAD x volume), in FP64 from the
+// FP32 transform; it weights the scattering residual.
+double prim_area(const float *T, int type, float lad) {
+    double ax = T[0], ay = T[4], az = T[8], bx = T[1], by = T[5], bz = T[9];
+    if (type == PT_VOXEL) {
+        double cx = T[2], cy = T[6], cz = T[10];
+        double det = ax * (by * cz - bz * cy) - bx * (ay * cz - az * cy) + cx * (ay * bz - az * by);
+        return (double)lad * std::fabs(det);
+    }
+    double x = ay * bz - az * by, y = az * bx - ax * bz, z = ax * by - ay * bx;
+    double a = std::sqrt(x * x + y * y + z * z);
+    if (type == PT_TRI) return 0.5 * a;
+    if (type == PT_DISK) return M_PI * a;
+    return a;
 }
 
 void rec_bounds(const Rec &r, V3 *lo, V3 *hi) {
@@ -218,9 +289,16 @@ void rec_bounds(const Rec &r, V3 *lo, V3 *hi) {
 }
 
 // ---------------------------------------------------------------- rays -----
+// Philox counter words c0..c2 and key of a ray's voxel free-path draws; the draw for
+// voxel v is philox(c0, c1, c2 | wrap << 16, v + 1; k0, k1), so it depends on the ray's
+// identity and the periodic wrap only, never on traversal order or launch batching.
+struct VoxKey {
+    uint32_t c0, c1, c2, k0, k1;
+};
 struct Ray {
     V3 o, d;
     float tmin, tmax;
+    VoxKey key;
 };
 struct Hit {
     float t;
@@ -336,23 +414,34 @@ inline float safe_inv(float d) {
     return 1.0f / d;
 }
 
-// Voxel: a ray whose origin lies inside the box does not hit it (OptiX 6
-// primitiveIntersection.cu:330-374); otherwise the entry distance is the hit.
-inline bool voxel_hit(const Ray &ray, const V3 &inv, const Rec &r, float tmax, float *t_out,
+// Voxel: a turbid medium of leaf area density LAD with extinction k = G * LAD.  The
+// reference has no voxel physics (its OptiX 6 voxel absorption is commented out,
+// rayHit.cu:278-290), so this one is defined here: the ray's path through the box from
+// max(entry, tmin) to the exit is intercepted at the free path s = -ln(xi) / k, xi
+// uniform in (0, 1] drawn per (ray, voxel, wrap).  A ray starting inside the box crosses
+// the rest of it (the reference's "inside origin: no hit" rule, primitiveIntersection.cu:
+// 330-374, would let a voxel's own leaves see through it).  The hit is always the top face.
+inline bool voxel_hit(const Ray &ray, const V3 &inv, const Rec &r, uint32_t vid, float tmax, float *t_out,
                       int *face_out) {
-    V3 lo = r.p[0], hi = r.p[1];
-    V3 o = ray.o;
-    if (o.x >= lo.x && o.x <= hi.x && o.y >= lo.y && o.y <= hi.y && o.z >= lo.z && o.z <= hi.z)
-        return false;
-    float tn;
-    if (!slab(o, inv, lo, hi, ray.tmin, tmax, &tn)) return false;
-    if (!(tn > 1e-5f)) return false;
-    *t_out = tn;
+    if (!(r.k > 0.f)) return false;
+    V3 lo = r.p[0], hi = r.p[1], o = ray.o;
+    float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
+    float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
+    float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
+    float tn = std::fmax(std::fmax(std::fmin(t0x, t1x), std::fmin(t0y, t1y)),
+                         std::fmax(std::fmin(t0z, t1z), ray.tmin));
+    float tf = std::fmin(std::fmin(std::fmax(t0x, t1x), std::fmax(t0y, t1y)), std::fmax(t0z, t1z));
+    if (!(tn < tf)) return false;
+    U4 u = philox(ray.key.c0, ray.key.c1, ray.key.c2, vid + 1u, ray.key.k0, ray.key.k1);
+    float s = -ln_unit(1.0f - u01(u.v[0])) / r.k;
+    float t = tn + s;
+    if (!(t < tf) || !(t <= tmax)) return false;
+    *t_out = t;
     *face_out = 1;
     return true;
 }
 
-inline bool prim_hit(const WT &w, const Ray &ray, const V3 &inv, const Rec &r, float tmax,
+inline bool prim_hit(const WT &w, const Ray &ray, const V3 &inv, const Rec &r, uint32_t id, float tmax,
                      float *t, int *face) {
     switch (r.type) {
         case PT_TRI:
@@ -363,7 +452,7 @@ inline bool prim_hit(const WT &w, const Ray &ray, const V3 &inv, const Rec &r, f
         case PT_DISK:
             return disk_hit(ray, r, tmax, t, face);
         case PT_VOXEL:
-            return voxel_hit(ray, inv, r, tmax, t, face);
+            return voxel_hit(ray, inv, r, id, tmax, t, face);
     }
     return false;
 }
@@ -451,6 +540,7 @@ struct Scene {
     std::vector<int8_t> twosided;
     std::vector<Rec> rec;       // original order
     std::vector<RGen> rgen;     // original order
+    std::vector<double> area;   // original order (voxels: leaf area)
     // BVH
     std::vector<uint64_t> codes;    // sorted Morton codes
     std::vector<uint32_t> perm;     // sorted slot -> original primitive
@@ -663,7 +753,7 @@ Hit trace_bvh(const Scene &s, const Ray &ray, bool anyhit, TraceStats *st) {
                 if (st) st->prims++;
                 float t;
                 int face;
-                if (prim_hit(w, ray, inv, s.rec[p], best, &t, &face)) {
+                if (prim_hit(w, ray, inv, s.rec[p], (uint32_t)p, best, &t, &face)) {
                     if (h.prim < 0 || better(t, p, h.t, h.prim)) {
                         h.t = t;
                         h.prim = p;
@@ -701,7 +791,7 @@ Hit trace_brute(const Scene &s, const Ray &ray, bool reference_formula) {
         int face;
         bool ok = reference_formula
                       ? prim_hit_reference(ray, &s.T[16 * (size_t)p], (int)s.type[p], ray.tmax, &t, &face)
-                      : prim_hit(w, ray, inv, s.rec[p], ray.tmax, &t, &face);
+                      : prim_hit(w, ray, inv, s.rec[p], (uint32_t)p, ray.tmax, &t, &face);
         if (ok && (h.prim < 0 || better(t, p, h.t, h.prim))) {
             h.t = t;
             h.prim = p;
@@ -734,7 +824,9 @@ inline bool bbox_closest(const Scene &s, const Ray &ray, float tmax, float *t_ou
 
 // Full trace with periodic wrapping (<= 10 wraps, OptiX8DeviceCode.cu:1440-1459, 763-789).
 Hit trace_full(const Scene &s, Ray ray, bool anyhit, TraceStats *st) {
+    const uint32_t c2 = ray.key.c2;
     for (int wrap = 0; wrap < 10; ++wrap) {
+        ray.key.c2 = c2 | ((uint32_t)wrap << 16);
         Hit h = trace_bvh(s, ray, anyhit && s.nbbox == 0, st);
         if (s.nbbox == 0) return h;
         float tb;
@@ -767,26 +859,53 @@ struct Source {
     float R[9];      // rotation matrix (row-major) for rect / disk sources
 };
 
-// Sample origin on primitive p: (u, v) are the two uniform numbers.
-inline V3 sample_point(const RGen &g, int type, float u, float v) {
+// Sample origin on primitive p from uniform numbers u, v (and w, voxels only).
+// Disks: concentric map onto the unit disk (OptiX 6 rayGeneration.cu:346-389 uses the
+// same map); voxels: uniform in the box (rayGeneration.cu:391-396).
+inline V3 sample_point(const RGen &g, int type, float u, float v, float w) {
     if (type == PT_TRI) {
         float a = u < v ? u : v, b = u < v ? v : u;  // sorted (OptiX8DeviceCode.cu:1288-1289)
         return v3((g.P.x + a * g.A.x) + b * g.B.x, (g.P.y + a * g.A.y) + b * g.B.y,
                   (g.P.z + a * g.A.z) + b * g.B.z);
     }
+    if (type == PT_DISK) {
+        float x, y;
+        concentric(u, v, &x, &y);
+        return v3((g.P.x + x * g.A.x) + y * g.B.x, (g.P.y + x * g.A.y) + y * g.B.y,
+                  (g.P.z + x * g.A.z) + y * g.B.z);
+    }
+    if (type == PT_VOXEL)
+        return v3(((g.P.x + u * g.A.x) + v * g.B.x) + w * g.N.x, ((g.P.y + u * g.A.y) + v * g.B.y) + w * g.N.y,
+                  ((g.P.z + u * g.A.z) + v * g.B.z) + w * g.N.z);
     return v3((g.P.x + u * g.A.x) + v * g.B.x, (g.P.y + u * g.A.y) + v * g.B.y,
               (g.P.z + u * g.A.z) + v * g.B.z);
 }
 
+// Isotropic directions of a voxel's leaves: stratified uniform on the upper hemisphere
+// (cos theta = 1 - Rt, OptiX 6 rayGeneration.cu:401-415); the bottom-face ray of the same
+// sample takes the opposite direction, so each pair samples the sphere antithetically.
+inline V3 voxel_dir(int ti, int pi, int dimx, int dimy, float j0, float j1) {
+    float Rt = ((float)ti + j0) / (float)dimx;
+    float Rp = ((float)pi + j1) / (float)dimy;
+    float ct = 1.0f - Rt;
+    float st = std::sqrt(std::fmax(0.f, 1.0f - ct * ct));
+    float cp, sp;
+    sincos2pi(Rp, &cp, &sp);
+    return v3(st * cp, st * sp, ct);
+}
+
+// Leaf-projection factor of a direct ray's strength: |n . d| on a surface, G on a voxel.
+inline double proj(V3 nrm, V3 d, bool vox) { return vox ? (double)kVoxelG : (double)std::fabs(vdot(nrm, d)); }
+
 // Direction (and tmax, FP64 strength) of a direct ray towards source `src`
 // (OptiX8DeviceCode.cu:1329-1415).  Returns false if the source emits away.
-inline bool direct_dir(const Source &src, V3 org, V3 nrm, uint32_t rx, uint32_t ry, double inv_nr,
+inline bool direct_dir(const Source &src, V3 org, V3 nrm, bool vox, uint32_t rx, uint32_t ry, double inv_nr,
                        V3 *dir, float *tmax, double *strength) {
     if (src.type == 0) {
         V3 d = vnormalize(src.pos);
         *dir = d;
         *tmax = 1e38f;
-        *strength = inv_nr * (double)std::fabs(vdot(nrm, d));
+        *strength = inv_nr * proj(nrm, d, vox);
         return true;
     }
     if (src.type == 1 || src.type == 2) {
@@ -809,7 +928,7 @@ inline bool direct_dir(const Source &src, V3 org, V3 nrm, uint32_t rx, uint32_t 
                 float sti = std::sqrt(std::fmax(0.f, 1.0f - cti * cti));
                 V3 l = v3(sti * cpj, sti * spj, cti);
                 if (vdot(l, d) < 0.f) {
-                    acc += inv_nr * (double)std::fabs(vdot(nrm, d)) * (double)std::fabs(vdot(l, d)) /
+                    acc += inv_nr * proj(nrm, d, vox) * (double)std::fabs(vdot(l, d)) /
                            ((double)dist * (double)dist) / (double)(N * N) * (double)src.w0 *
                            (double)src.w0;
                 }
@@ -851,7 +970,7 @@ inline bool direct_dir(const Source &src, V3 org, V3 nrm, uint32_t rx, uint32_t 
         d = vnormalize(d);
         double area = (src.type == 3) ? (double)src.w0 * (double)src.w1 / M_PI
                                       : (double)src.w0 * (double)src.w0;
-        *strength = inv_nr * (double)std::fabs(vdot(nrm, d)) * (double)std::fabs(vdot(ldir, d)) /
+        *strength = inv_nr * proj(nrm, d, vox) * (double)std::fabs(vdot(ldir, d)) /
                     ((double)dist * (double)dist) * area;
         *dir = d;
         *tmax = dist;
@@ -873,6 +992,52 @@ inline V3 diffuse_dir(V3 n, int ti, int pi, int dimx, int dimy, float j0, float 
     onb(n, &t1, &t2);
     return v3((t1.x * lx + t2.x * ly) + n.x * ct, (t1.y * lx + t2.y * ly) + n.y * ct,
               (t1.z * lx + t2.z * ly) + n.z * ct);
+}
+
+// Origin of direct ray r of primitive p; u = philox(r, p, c2, 0; seed, pass) with c2 =
+// source << 1.  Patches, disks and voxels are stratified in (u, v) over dimx x dimy cells
+// (OptiX8DeviceCode.cu:1270-1290); a voxel's third coordinate comes from counter c2 | 1.
+inline V3 direct_origin(const RGen &g, int type, uint32_t r, uint32_t p, uint32_t c2, int dimx, int dimy,
+                        uint32_t seed, uint32_t pass, const U4 &u) {
+    float uu = u01(u.v[0]), vv = u01(u.v[1]), ww = 0.f;
+    if (type != PT_TRI) {
+        int xi = (int)(r % (uint32_t)dimx), yi = (int)(r / (uint32_t)dimx);
+        uu = ((float)xi + uu) / (float)dimx;
+        vv = ((float)yi + vv) / (float)dimy;
+    }
+    if (type == PT_VOXEL) ww = u01(philox(r, p, c2 | 1u, 0u, seed, pass).v[0]);
+    return sample_point(g, type, uu, vv, ww);
+}
+
+// Origin and direction of diffuse ray r of primitive p leaving face `face` (1 top, 0
+// bottom): cosine-weighted about the normal from counter (r, p, face, 0) on surfaces;
+// on voxels both faces share the sample of counter (r, p, 1, 0) (third coordinate from
+// (r, p, 2, 0)) and the bottom face flips the direction.
+inline void diffuse_ray(const RGen &g, int type, uint32_t r, uint32_t p, int face, int dimx, int dimy,
+                        uint32_t seed, uint32_t pass, V3 *org, V3 *dir) {
+    int ti = (int)(r % (uint32_t)dimx), pi = (int)(r / (uint32_t)dimx);
+    V3 dd;
+    if (type == PT_VOXEL) {
+        U4 u = philox(r, p, 1u, 0u, seed, pass);
+        U4 uw = philox(r, p, 2u, 0u, seed, pass);
+        dd = voxel_dir(ti, pi, dimx, dimy, u01(u.v[0]), u01(u.v[1]));
+        *org = sample_point(g, type, u01(u.v[2]), u01(u.v[3]), u01(uw.v[0]));
+    } else {
+        U4 u = philox(r, p, (uint32_t)face, 0u, seed, pass);
+        dd = diffuse_dir(g.N, ti, pi, dimx, dimy, u01(u.v[0]), u01(u.v[1]));
+        *org = sample_point(g, type, u01(u.v[2]), u01(u.v[3]), 0.f);
+    }
+    *dir = (face == 0) ? v3(-dd.x, -dd.y, -dd.z) : dd;
+}
+
+// Material of primitive p as the deposits use it: a voxel's leaves scatter rho + tau,
+// half of it routed to each face (both faces emit into the same isotropic field).
+inline void eff_material(int type, float *rho, float *tau) {
+    if (type == PT_VOXEL) {
+        float h = 0.5f * (*rho + *tau);
+        *rho = h;
+        *tau = h;
+    }
 }
 
 // Sky angular distribution (OptiX8DeviceCode.cu:148-164).
@@ -905,6 +1070,7 @@ typedef struct {
     int32_t nbbox;            // periodic walls (0, 2 or 4)
     const float *bbox_verts;  // nbbox*4*3 world-space corners
     float periodic_x, periodic_y;
+    const float *voxel_lad;   // n leaf area density (m^2/m^3), read for voxels; may be null without voxels
 } orc_geometry;
 
 typedef struct {
@@ -932,6 +1098,7 @@ typedef struct {
     uint32_t seed;
     int32_t threads;              // OpenMP threads (<=0: all)
     int32_t prim_limit;           // >0: launch rays only from the first prim_limit primitives (timing samples)
+    double scatter_tol;           // >0: a band stops scattering once its residual falls to this value
 } orc_solve;
 
 void *orc_scene_create(const orc_geometry *g) {
@@ -942,9 +1109,20 @@ void *orc_scene_create(const orc_geometry *g) {
     s->twosided.assign(g->twosided, g->twosided + g->n);
     s->rec.resize(g->n);
     s->rgen.resize(g->n);
+    s->area.resize(g->n);
     for (int i = 0; i < g->n; ++i) {
-        s->rec[i] = make_rec(&s->T[16 * (size_t)i], (int)s->type[i]);
+        float lad = 0.f;
+        if (s->type[i] == PT_VOXEL) {
+            if (!g->voxel_lad) {
+                delete s;
+                return nullptr;
+            }
+            lad = g->voxel_lad[i];
+            s->twosided[i] = 1;  // a voxel launches both ray directions of each sample
+        }
+        s->rec[i] = make_rec(&s->T[16 * (size_t)i], (int)s->type[i], lad);
         s->rgen[i] = make_rgen(&s->T[16 * (size_t)i], (int)s->type[i]);
+        s->area[i] = prim_area(&s->T[16 * (size_t)i], (int)s->type[i], lad);
     }
     s->nbbox = g->nbbox;
     s->periodic[0] = g->periodic_x;
@@ -972,6 +1150,11 @@ void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
 // sincos2pi for a batch (tests of the polynomial against libm).
 void orc_sincos2pi(int64_t n, const float *u, float *c, float *s) {
     for (int64_t i = 0; i < n; ++i) sincos2pi(u[i], &c[i], &s[i]);
+}
+
+// ln_unit for a batch (accuracy tests against libm).
+void orc_ln_unit(int64_t n, const float *x, float *out) {
+    for (int64_t i = 0; i < n; ++i) out[i] = ln_unit(x[i]);
 }
 
 // Export the host-built BVH for bit-exact comparison with the device build.
@@ -1003,7 +1186,9 @@ int orc_trace(void *h, int64_t nrays, const float *o, const float *d, float tmin
 #endif
 #pragma omp parallel for schedule(dynamic, 1024) reduction(+ : cn, cp)
     for (int64_t i = 0; i < nrays; ++i) {
-        Ray r{v3(o[3 * i], o[3 * i + 1], o[3 * i + 2]), v3(d[3 * i], d[3 * i + 1], d[3 * i + 2]), tmin, tmax};
+        // voxel draws of explicit ray i: counter (i, i >> 32, 2^31), key (0, ~0)
+        Ray r{v3(o[3 * i], o[3 * i + 1], o[3 * i + 2]), v3(d[3 * i], d[3 * i + 1], d[3 * i + 2]), tmin, tmax,
+              VoxKey{(uint32_t)i, (uint32_t)((uint64_t)i >> 32), 0x80000000u, 0u, 0xFFFFFFFFu}};
         Hit hh;
         TraceStats st;
         if (mode == 0 || mode == 3) hh = trace_bvh(*s, r, mode == 3, &st);
@@ -1034,22 +1219,14 @@ int orc_gen_rays(void *h, int kind, uint32_t seed, uint32_t pass, int32_t rpp, i
     for (int p = 0; p < s->n; ++p) {
         const RGen &g = s->rgen[p];
         for (int r = 0; r < nr; ++r) {
-            U4 u = philox((uint32_t)r, (uint32_t)p, (uint32_t)face, 0u, seed, pass);
             V3 org, dir;
             if (kind == 0) {
-                int xi = r % dimx, yi = r / dimx;
-                float uu = u01(u.v[0]), vv = u01(u.v[1]);
-                if (s->type[p] != PT_TRI) {
-                    uu = ((float)xi + uu) / (float)dimx;
-                    vv = ((float)yi + vv) / (float)dimy;
-                }
-                org = sample_point(g, (int)s->type[p], uu, vv);
+                U4 u = philox((uint32_t)r, (uint32_t)p, (uint32_t)face, 0u, seed, pass);
+                org = direct_origin(g, (int)s->type[p], (uint32_t)r, (uint32_t)p, (uint32_t)face, dimx, dimy, seed,
+                                    pass, u);
                 dir = vnormalize(v3(dir3[0], dir3[1], dir3[2]));
             } else {
-                int ti = r % dimx, pi = r / dimx;
-                dir = diffuse_dir(g.N, ti, pi, dimx, dimy, u01(u.v[0]), u01(u.v[1]));
-                if (face == 0) dir = v3(-dir.x, -dir.y, -dir.z);
-                org = sample_point(g, (int)s->type[p], u01(u.v[2]), u01(u.v[3]));
+                diffuse_ray(g, (int)s->type[p], (uint32_t)r, (uint32_t)p, face, dimx, dimy, seed, pass, &org, &dir);
             }
             size_t k = (size_t)p * nr + r;
             o[3 * k] = org.x;
@@ -1067,7 +1244,8 @@ int orc_gen_rays(void *h, int kind, uint32_t seed, uint32_t pass, int32_t rpp, i
 // Restatement of RadiationModel::runBand (RadiationModel.cpp:3470-4663) driving the
 // OptiX8 device-program semantics, with FP64 buffers.  flux_out: [n*Bl] =
 // radiation_in + scatter_top + scatter_bottom (RadiationModel.cpp:4652).
-// stats (may be null): [0] rays traced, [1] BVH node visits, [2] primitive tests, [3] hits.
+// stats (may be null): [0] rays traced, [1] BVH node visits, [2] primitive tests, [3] hits,
+// [4] scattering iterations run.
 int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats) {
     Scene *s = (Scene *)h;
     const int n = s->n;
@@ -1103,6 +1281,7 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
         depth = std::max(depth, q->depth[b]);
     }
     uint64_t n_rays = 0, n_nodes = 0, n_prims = 0, n_hits = 0;
+    int iters = 0;
     const int nl = (q->prim_limit > 0 && q->prim_limit < n) ? q->prim_limit : n;
     auto matidx = [&](int srcid, int p, int bg) { return ((size_t)srcid * n + p) * Bg + bg; };
 
@@ -1116,25 +1295,23 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
             const RGen &g = s->rgen[p];
             int ts = s->twosided[p];
             std::vector<double> d_in(Bl, 0.0), d_top(Bl, 0.0), d_bot(Bl, 0.0);
+            const int type = (int)s->type[p];
+            const bool vox = type == PT_VOXEL;
             for (int r = 0; r < dimx * dimy; ++r) {
-                int xi = r % dimx, yi = r / dimx;
                 for (int k = 0; k < S; ++k) {
-                    U4 u = philox((uint32_t)r, (uint32_t)p, (uint32_t)(k << 1), 0u, q->seed, 0u);
-                    float uu = u01(u.v[0]), vv = u01(u.v[1]);
-                    if (s->type[p] != PT_TRI) {
-                        uu = ((float)xi + uu) / (float)dimx;
-                        vv = ((float)yi + vv) / (float)dimy;
-                    }
-                    V3 org = sample_point(g, (int)s->type[p], uu, vv);
+                    const uint32_t c2 = (uint32_t)(k << 1);
+                    U4 u = philox((uint32_t)r, (uint32_t)p, c2, 0u, q->seed, 0u);
+                    V3 org = direct_origin(g, type, (uint32_t)r, (uint32_t)p, c2, dimx, dimy, q->seed, 0u, u);
                     V3 dir;
                     float tmax;
                     double strength;
-                    if (!direct_dir(src[k], org, g.N, u.v[2], u.v[3], inv_nr, &dir, &tmax, &strength)) continue;
-                    bool face = vdot(dir, g.N) > 0.f;
+                    if (!direct_dir(src[k], org, g.N, vox, u.v[2], u.v[3], inv_nr, &dir, &tmax, &strength)) continue;
+                    bool face = vox || vdot(dir, g.N) > 0.f;
                     if (!face && ts == 0) continue;
                     if (ts == 3) continue;
                     TraceStats st;
-                    Hit hh = trace_full(*s, Ray{org, dir, 1e-4f, tmax}, true, &st);
+                    Hit hh = trace_full(*s, Ray{org, dir, 1e-4f, tmax, VoxKey{(uint32_t)r, (uint32_t)p, c2, q->seed, 0u}},
+                                        true, &st);
                     n_rays++;
                     n_nodes += st.nodes;
                     n_prims += st.prims;
@@ -1145,6 +1322,7 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
                         if (!q->band_launch[bg]) continue;
                         ++b;
                         float rho = q->rho[matidx(k, p, bg)], tau = q->tau[matidx(k, p, bg)];
+                        eff_material(type, &rho, &tau);
                         double str = strength * (double)q->source_flux[k * Bl + b];
                         d_in[b] += str * (1.0 - rho - tau);
                         if (rho > 0.f || tau > 0.f) {
@@ -1184,15 +1362,17 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
             if (face == 1 && ts == 3) continue;
             if (face == 0 && ts != 1) continue;
             const RGen &g = s->rgen[p];
+            const int type = (int)s->type[p];
+            // a voxel's two ray directions both deposit on its top face
+            const int dface = (type == PT_VOXEL) ? 1 : face;
             std::vector<double> d_in(Bl, 0.0), d_top(Bl, 0.0), d_bot(Bl, 0.0);
             for (int r = 0; r < dimx * dimy; ++r) {
-                int ti = r % dimx, pi = r / dimx;
-                U4 u = philox((uint32_t)r, (uint32_t)p, (uint32_t)face, 0u, q->seed, pass);
-                V3 dir = diffuse_dir(g.N, ti, pi, dimx, dimy, u01(u.v[0]), u01(u.v[1]));
-                if (face == 0) dir = v3(-dir.x, -dir.y, -dir.z);
-                V3 org = sample_point(g, (int)s->type[p], u01(u.v[2]), u01(u.v[3]));
+                V3 org, dir;
+                diffuse_ray(g, type, (uint32_t)r, (uint32_t)p, face, dimx, dimy, q->seed, pass, &org, &dir);
                 TraceStats st;
-                Hit hh = trace_full(*s, Ray{org, dir, 1e-4f, 1e38f}, false, &st);
+                Hit hh = trace_full(
+                    *s, Ray{org, dir, 1e-4f, 1e38f, VoxKey{(uint32_t)r, (uint32_t)p, (uint32_t)face, q->seed, pass}},
+                    false, &st);
                 n_rays++;
                 n_nodes += st.nodes;
                 n_prims += st.prims;
@@ -1218,9 +1398,10 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
                         val = sky_fd(dir, pk, K, kn, pr) * (double)dflux[b] * strength;
                     }
                     float rho = q->rho[matidx(0, p, bg)], tau = q->tau[matidx(0, p, bg)];
+                    eff_material(type, &rho, &tau);
                     d_in[b] += val * (1.0 - rho - tau);
                     if (rho > 0.f || tau > 0.f) {
-                        if (face) {
+                        if (dface) {
                             d_top[b] += val * rho;
                             d_bot[b] += val * tau;
                         } else {
@@ -1288,12 +1469,13 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
     if (scattering && (emission || diffuse || rundirect)) {
         std::fill(dflux.begin(), dflux.end(), 0.f);
         std::vector<uint8_t> sflags = flags;
+        std::vector<uint8_t> conv(Bg, 0);
         for (int it = 0; it < depth; ++it) {
             int b = -1;
             for (int bg = 0; bg < Bg; ++bg) {
                 if (!sflags[bg]) continue;
                 ++b;
-                if (it + 1 > q->depth[b]) sflags[bg] = 0;
+                if (it + 1 > q->depth[b] || conv[bg]) sflags[bg] = 0;
             }
             if (it > 0 || (emission && rundirect)) {
                 otop = stop;
@@ -1303,6 +1485,29 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
             std::fill(sbot.begin(), sbot.end(), 0.0);
             diffuse_pass(1, 2u + (uint32_t)it, sflags, dflux);
             diffuse_pass(0, 2u + (uint32_t)it, sflags, dflux);
+            iters = it + 1;
+            if (q->scatter_tol > 0.0) {
+                // Residual of band column c: area-weighted power scattered by this
+                // iteration and not yet propagated, over the band's total so far.  It
+                // bounds the relative change of the summed flux if the band stops here.
+                bool all = true;
+                int c = -1;
+                for (int bg = 0; bg < Bg; ++bg) {
+                    if (!q->band_launch[bg]) continue;
+                    ++c;
+                    if (!sflags[bg]) continue;
+                    double num = 0.0, den = 0.0;
+                    for (int p = 0; p < n; ++p) {
+                        size_t i = (size_t)p * Bl + c;
+                        double sc = stop[i] + sbot[i];
+                        num += s->area[p] * sc;
+                        den += s->area[p] * (rin[i] + sc);
+                    }
+                    if (num <= q->scatter_tol * den) conv[bg] = 1;
+                    else all = false;
+                }
+                if (all) break;
+            }
         }
     }
     for (size_t i = 0; i < (size_t)n * Bl; ++i) flux_out[i] = rin[i] + stop[i] + sbot[i];
@@ -1311,6 +1516,7 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
         stats[1] = n_nodes;
         stats[2] = n_prims;
         stats[3] = n_hits;
+        stats[4] = (uint64_t)iters;
     }
     return 0;
 }

@@ -40,6 +40,7 @@ class _Geometry(C.Structure):
         ("bbox_verts", C.c_void_p),
         ("periodic_x", C.c_float),
         ("periodic_y", C.c_float),
+        ("voxel_lad", C.c_void_p),
     ]
 
 
@@ -69,6 +70,7 @@ class _Solve(C.Structure):
         ("seed", C.c_uint32),
         ("threads", C.c_int32),
         ("prim_limit", C.c_int32),
+        ("scatter_tol", C.c_double),
     ]
 
 
@@ -87,6 +89,7 @@ def _load():
         _lib.orc_run_band.argtypes = [C.c_void_p, C.POINTER(_Solve), C.c_void_p, C.c_void_p]
         _lib.orc_philox.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_sincos2pi.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_ln_unit.argtypes = [C.c_int64, C.c_void_p, C.c_void_p]
     return _lib
 
 
@@ -97,17 +100,20 @@ def _ptr(a):
 class OracleScene:
     """Host scene: primitive records, the host LBVH twin and the FP64 solver."""
 
-    def __init__(self, T, ptype, twosided, bbox_verts=None, periodic=(0.0, 0.0)):
+    def __init__(self, T, ptype, twosided, bbox_verts=None, periodic=(0.0, 0.0), voxel_lad=None):
         lib = _load()
         self.T = np.ascontiguousarray(T, dtype=np.float32).reshape(-1, 16)
         self.n = self.T.shape[0]
         self.type = np.ascontiguousarray(ptype, dtype=np.uint32)
         self.twosided = np.ascontiguousarray(twosided, dtype=np.int8)
         self.bbox = None if bbox_verts is None else np.ascontiguousarray(bbox_verts, dtype=np.float32)
+        self.lad = None if voxel_lad is None else np.ascontiguousarray(voxel_lad, dtype=np.float32)
         g = _Geometry(self.n, _ptr(self.T), _ptr(self.type), _ptr(self.twosided),
                       0 if self.bbox is None else self.bbox.shape[0], _ptr(self.bbox),
-                      float(periodic[0]), float(periodic[1]))
+                      float(periodic[0]), float(periodic[1]), _ptr(self.lad))
         self._h = lib.orc_scene_create(C.byref(g))
+        if not self._h:
+            raise ValueError("oracle scene rejected (voxels need voxel_lad)")
 
     def close(self):
         if self._h:
@@ -190,11 +196,12 @@ class OracleScene:
         s.seed = int(solve.get("seed", 0)) & 0xFFFFFFFF
         s.threads = int(threads)
         s.prim_limit = int(prim_limit)
+        s.scatter_tol = float(solve.get("scatter_tolerance", 0.0))
         flux = np.zeros((self.n, bl), np.float64)
-        stats = np.zeros(4, np.uint64)
+        stats = np.zeros(5, np.uint64)
         _load().orc_run_band(self._h, C.byref(s), _ptr(flux), _ptr(stats))
         return flux, {"rays": int(stats[0]), "nodes": int(stats[1]), "prims": int(stats[2]),
-                      "hits": int(stats[3])}
+                      "hits": int(stats[3]), "iterations": int(stats[4])}
 
 
 def philox(ctr, key):
@@ -211,3 +218,10 @@ def sincos2pi(u):
     s = np.zeros_like(u)
     _load().orc_sincos2pi(u.size, _ptr(u), _ptr(c), _ptr(s))
     return c, s
+
+
+def ln_unit(x):
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros_like(x)
+    _load().orc_ln_unit(x.size, _ptr(x), _ptr(out))
+    return out

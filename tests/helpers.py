@@ -22,6 +22,7 @@ def oracle_solve(desc: dict, rotation=rotation_np) -> dict:
     d = {k: desc[k] for k in ("band_launch", "source_flux", "rho", "tau", "diffuse_flux", "diffuse_ext",
                               "diffuse_norm", "diffuse_peak", "prague", "direct_rays", "diffuse_rays", "depth",
                               "emission", "eps", "temperature", "seed")}
+    d["scatter_tolerance"] = desc.get("scatter_tolerance", 0.0)
     d["source_type"] = np.array([s["type"] for s in srcs], np.int32)
     d["source_pos"] = np.array([s["position"] for s in srcs], np.float32)
     d["source_width"] = np.array([s["width"] for s in srcs], np.float32)
@@ -32,7 +33,7 @@ def oracle_solve(desc: dict, rotation=rotation_np) -> dict:
 def oracle_scene_for(rad, oracle_mod):
     T, ty, ts = rad.geometry_arrays()
     bb = rad._bbox_faces()
-    return oracle_mod.OracleScene(T, ty, ts, bb, rad.periodic)
+    return oracle_mod.OracleScene(T, ty, ts, bb, rad.periodic, rad.voxel_lad())
 
 
 def run_oracle(rad, labels, oracle_mod, scene=None, seed=None, threads=0):

@@ -225,10 +225,122 @@ def launch_batching(run):
     return [("batch_min", float(f.min()), 1000.0, 0.02), ("batch_max", float(f.max()), 1000.0, 0.02)]
 
 
+def _voxel_slab(lad, domain=2.0, zlo=0.5, zhi=1.5, div=(4, 4, 2), ground_div=4, ceiling=False):
+    """Periodic layer of voxels (leaf area density lad) over a one-sided ground tile at
+    z = 0 (and, with ceiling, under a downward-facing one-sided tile at z = zhi)."""
+    ctx = Context()
+    g = ctx.addScene(scenes.tile_grid((0.5 * domain, 0.5 * domain, 0.0), (domain, domain),
+                                      (ground_div, ground_div)))
+    c = None
+    if ceiling:
+        top = scenes.tile_grid((0.5 * domain, 0.5 * domain, zhi), (domain, domain), (ground_div, ground_div))
+        flip = np.diag([1.0, -1.0, -1.0, 1.0])  # rotate pi about x: the face looks down
+        top.T = np.stack([(t.reshape(4, 4) @ flip).reshape(16) for t in top.T.astype(np.float64)]).astype(np.float32)
+        c = ctx.addScene(top)
+    v = ctx.addScene(scenes.voxel_grid((0.0, 0.0, zlo), (domain, domain, zhi), div, lad))
+    rad = RadiationModel(ctx)
+    rad.enforcePeriodicBoundary("xy")
+    return ctx, rad, np.asarray(g), (None if c is None else np.asarray(c)), np.asarray(v)
+
+
+def voxel_beer(run, lad=1.0, zenith=30.0, ndir=2500, ndiff=2500):
+    """Turbid-medium voxels against Beer's law (G = 0.5): a periodic voxel layer of leaf
+    area index L = lad * thickness over a black ground transmits exp(-G L / cos(zenith))
+    of the direct beam and 1 - beer_diffuse(L) of an isotropic sky; the voxels intercept
+    the rest (their fluxes are per unit leaf area)."""
+    zlo, zhi, domain = 0.5, 1.5, 2.0
+    ctx, rad, g, _, v = _voxel_slab(lad, domain, zlo, zhi)
+    L = lad * (zhi - zlo)
+    th = math.radians(zenith)
+    rad.addRadiationBand("direct")
+    rad.disableEmission("direct")
+    rad.setDirectRayCount("direct", ndir)
+    rad.setScatteringDepth("direct", 0)
+    sun = rad.addCollimatedRadiationSource(scenes.sun_direction(zenith, 30.0))
+    rad.setSourceFlux(sun, "direct", 1.0 / math.cos(th))
+    rad.addRadiationBand("diffuse")
+    rad.disableEmission("diffuse")
+    rad.setDiffuseRayCount("diffuse", ndiff)
+    rad.setDiffuseRadiationFlux("diffuse", 1.0)
+    rad.setScatteringDepth("diffuse", 0)
+    fd = run(rad, ["direct"], 31)[:, 0]
+    fdf = run(rad, ["diffuse"], 32)[:, 0]
+    _, _, area = ctx.arrays()  # voxels: leaf area
+    ag = float(area[g].sum())
+    la = area[v]
+    t_dir = math.exp(-0.5 * L / math.cos(th))
+    t_dif = 1.0 - beer_diffuse(L)
+    return [("voxel_beer_ground_direct", float((fd[g] * area[g]).sum() / ag), t_dir, 0.01),
+            ("voxel_beer_leaf_direct", float((fd[v] * la).sum() / ag), 1.0 - t_dir, 0.01),
+            ("voxel_beer_ground_diffuse", float((fdf[g] * area[g]).sum() / ag), t_dif, 0.01),
+            ("voxel_beer_leaf_diffuse", float((fdf[v] * la).sum() / ag), 1.0 - t_dif, 0.01)]
+
+
+def voxel_isothermal(run, eps=1.0, lad=2.0, rays=400, depth=20, tol=1e-7):
+    """Second law in a closed isothermal cavity of voxels: a periodic voxel layer between a
+    black floor and a black ceiling, everything at 300 K.  Every ray sees radiance
+    sigma T^4 / pi, so each wall absorbs sigma T^4 and each voxel 2 eps sigma T^4 per unit
+    leaf area (both leaf faces).  With eps = 1 this holds ray by ray (exact up to
+    rounding); with eps < 1 it is reached by the scattering iterations, stopped by the FP64
+    residual."""
+    T0 = 300.0
+    ctx, rad, g, c, v = _voxel_slab(lad, 2.0, 0.0, 1.0, ceiling=True)
+    n = ctx.getPrimitiveCount()
+    uu = np.arange(n)
+    ctx.setPrimitiveData(uu, "temperature", np.full(n, T0))
+    ctx.setPrimitiveData(np.concatenate([g, c]), "twosided_flag", np.zeros(g.size + c.size))
+    ctx.setPrimitiveData(v, "emissivity_LW", np.full(v.size, eps))
+    rad.addRadiationBand("LW")
+    rad.setDirectRayCount("LW", rays)
+    rad.setDiffuseRayCount("LW", rays)
+    rad.setDiffuseRadiationFlux("LW", 0.0)
+    rad.setScatteringDepth("LW", 0 if eps == 1.0 else depth)
+    rad.setScatteringResidualTolerance(tol)
+    f = run(rad, ["LW"], 41)[:, 0]
+    s4 = SIGMA * T0 ** 4
+    wall = np.concatenate([g, c])
+    ew = np.abs(f[wall] - s4) / s4
+    ev = np.abs(f[v] - 2.0 * eps * s4) / (2.0 * eps * s4)
+    if eps == 1.0:
+        # Exact ray by ray (up to the FP32 rounding of the emitted value), except for the
+        # rare ray that slips through the 1e-5 padding between the periodic walls and the
+        # floor/ceiling edge (the reference pads its walls the same way,
+        # RadiationModel.cpp:6046-6063) and gathers nothing.
+        exact = float(np.mean(np.concatenate([ew, ev]) < 1e-6))
+        worst = float(max(ew.max() * rays, ev.max() * 2 * rays))  # in rays lost
+        return [("voxel_isothermal_exact_fraction", exact, 1.0, 0.05),
+                ("voxel_isothermal_worst_rays_lost", worst, 0.0, 1.001)]
+    mw = float(np.mean(f[wall])) / s4 - 1.0
+    mv = float(np.mean(f[v])) / (2.0 * eps * s4) - 1.0
+    return [(f"voxel_isothermal_wall_eps{eps}", mw, 0.0, 3e-3), (f"voxel_isothermal_voxel_eps{eps}", mv, 0.0, 3e-3)]
+
+
+def disk_view_factor(run, ensemble=4, rays=50000, r=0.5, h=0.5):
+    """Native disks: two coaxial one-sided black disks of radius r facing each other at
+    distance h under a unit isotropic sky; each absorbs 1 - F12 with the coaxial-disk view
+    factor F12 = (S - sqrt(S^2 - 4)) / 2, S = 1 + (1 + R^2) / R^2, R = r / h."""
+    R = r / h
+    S = 1.0 + (1.0 + R * R) / (R * R)
+    F12 = 0.5 * (S - math.sqrt(S * S - 4.0))
+    ctx = Context()
+    d0 = ctx.addDisk((0.0, 0.0, 0.0), r, (0.0, 0.0, 1.0))
+    d1 = ctx.addDisk((0.0, 0.0, h), r, (0.0, 0.0, -1.0))
+    ctx.setPrimitiveData(d0, "twosided_flag", 0)
+    ctx.setPrimitiveData(d1, "twosided_flag", 0)
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("SW")
+    rad.disableEmission("SW")
+    rad.setDiffuseRayCount("SW", rays)
+    rad.setDiffuseRadiationFlux("SW", 1.0)
+    rad.setScatteringDepth("SW", 0)
+    f = _ensemble(run, rad, ["SW"], ensemble)
+    return [("disk_view_0", f[0, 0], 1 - F12, 0.005), ("disk_view_1", f[1, 0], 1 - F12, 0.005)]
+
+
 def check(results, abs_tol_names=()):
     bad = []
     for name, val, exp, tol in results:
-        if name.startswith("canopy") or name in abs_tol_names or exp == 0.0:
+        if name.startswith("canopy") or name.startswith("voxel") or name in abs_tol_names or exp == 0.0:
             err = abs(val - exp)
         else:
             err = abs(val - exp) / abs(exp)

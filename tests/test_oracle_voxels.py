@@ -1,0 +1,124 @@
+"""The oracle's native disks, turbid-medium voxels and FP64 scattering residual.
+
+The reference has disk and voxel intersection only in its OptiX 6 programs
+(plugins/radiation/src/primitiveIntersection.cu:236-374) and no voxel radiation
+physics at all (rayHit.cu:278-290 is commented out), so these checks are
+analytic: a coaxial-disk view factor, Beer's law through a voxel layer
+(G = 0.5), and the second law in a closed isothermal voxel cavity."""
+import math
+
+import numpy as np
+import pytest
+
+import scenarios
+from helpers import oracle_scene_for, oracle_solve, run_oracle
+from helios_gb300 import scenes
+from helios_gb300.radiation import Context, RadiationModel
+
+
+@pytest.fixture(scope="module")
+def run(oracle_mod):
+    def _run(rad, labels, seed):
+        return run_oracle(rad, labels, oracle_mod, seed=seed)[0]
+    return _run
+
+
+@pytest.mark.parametrize("name", ["disk_view_factor", "voxel_beer", "voxel_isothermal"])
+def test_known_answer(run, name):
+    res = getattr(scenarios, name)(run)
+    assert not scenarios.check(res), scenarios.check(res)
+
+
+def test_gray_voxel_cavity_second_law(run):
+    """Scattering voxels (eps 0.6, rho 0.4) reach 2 eps sigma T^4 per unit leaf area."""
+    res = scenarios.voxel_isothermal(run, eps=0.6)
+    assert not scenarios.check(res), scenarios.check(res)
+
+
+def test_ln_unit_accuracy(oracle_mod):
+    """The free-path logarithm (own series, not libm) against numpy on every 97th
+    24-bit value of (0, 1]: within 2e-7 relative, exact at 1."""
+    x = (np.arange(1, 1 << 24, 97, dtype=np.float64) / 2 ** 24).astype(np.float32)
+    x = np.concatenate([x, np.float32([1.0, 0.5, 2.0 ** -24])])
+    y = oracle_mod.ln_unit(x).astype(np.float64)
+    ref = np.log(x.astype(np.float64))
+    assert y[-3] == 0.0
+    big = np.abs(ref) > 1e-2
+    assert np.max(np.abs(y[big] - ref[big]) / np.abs(ref[big])) < 2e-7
+    assert np.max(np.abs(y - ref)) < 2e-6
+
+
+def test_voxel_scene_requires_lad(oracle_mod):
+    v = scenes.voxel_grid((0, 0, 0), (1, 1, 1), (2, 1, 1), 1.0)
+    with pytest.raises(ValueError):
+        oracle_mod.OracleScene(v.T, v.ptype, v.twosided)
+
+
+def test_voxel_medium_hits_are_order_independent(oracle_mod):
+    """Free-path draws depend on (ray, voxel) only: the BVH and the brute-force
+    traversal (different test orders) return identical hits through a voxel stack."""
+    v = scenes.voxel_grid((0, 0, 0), (2, 2, 2), (4, 4, 4), np.linspace(0.2, 3.0, 64))
+    sc = oracle_mod.OracleScene(v.T, v.ptype, v.twosided, voxel_lad=v.lad)
+    rng = np.random.default_rng(3)
+    o = np.concatenate([rng.uniform(-0.5, 2.5, (4000, 2)), rng.uniform(-1.0, 3.0, (4000, 1))], 1)
+    d = scenes.uniform_sphere(rng, 4000)
+    h0, t0, f0, _ = sc.trace(o, d, mode=0)
+    h1, t1, f1, _ = sc.trace(o, d, mode=1)
+    assert (h0 >= 0).mean() > 0.1
+    assert np.array_equal(h0, h1)
+    assert np.array_equal(t0[h0 >= 0], t1[h1 >= 0])
+
+
+def test_voxel_free_path_distribution(oracle_mod):
+    """Rays crossing one voxel of extinction k = G LAD are intercepted with probability
+    1 - exp(-k l), l the chord, and the hit distance follows the truncated exponential."""
+    lad = 1.5
+    v = scenes.voxel_grid((0, 0, 0), (1, 1, 1), (1, 1, 1), lad)
+    sc = oracle_mod.OracleScene(v.T, v.ptype, v.twosided, voxel_lad=v.lad)
+    n = 200000
+    rng = np.random.default_rng(5)
+    o = np.stack([rng.uniform(0.05, 0.95, n), rng.uniform(0.05, 0.95, n), np.full(n, -1.0)], 1)
+    d = np.tile([0.0, 0.0, 1.0], (n, 1))
+    hit, t, face, _ = sc.trace(o, d)
+    k = 0.5 * lad
+    p = (hit == 0).mean()
+    assert abs(p - (1 - math.exp(-k))) < 4 * math.sqrt(p * (1 - p) / n)
+    depth = t[hit == 0] - 1.0
+    # mean depth of the exponential truncated at the chord length 1
+    mean = 1.0 / k - math.exp(-k) / (1 - math.exp(-k))
+    assert abs(depth.mean() - mean) < 0.01
+    assert np.all(face[hit == 0] == 1)
+
+
+def test_residual_stop(oracle_mod):
+    """The FP64 residual ends the scattering loop early, the flux changes by at most
+    about the tolerance, and tolerance 0 runs the full depth."""
+    sc = scenes.deep_scatter(n_tri=3000, n_patch=500, n_disk=500, vox_div=4, domain=3.0, height=1.5, seed=1)
+    ctx = Context()
+    ctx.addScene(sc)
+    rad = RadiationModel(ctx)
+    rad.enforcePeriodicBoundary("xy")
+    rad.addRadiationBand("NIR")
+    rad.disableEmission("NIR")
+    n = ctx.getPrimitiveCount()
+    uu = np.arange(1, n)
+    ctx.setPrimitiveData(uu, "reflectivity_NIR", np.full(n - 1, 0.45))
+    ctx.setPrimitiveData(uu, "transmissivity_NIR", np.full(n - 1, 0.40))
+    rad.setDirectRayCount("NIR", 16)
+    rad.setDiffuseRayCount("NIR", 16)
+    rad.setDiffuseRadiationFlux("NIR", 100.0)
+    rad.setScatteringDepth("NIR", 20)
+    src = rad.addCollimatedRadiationSource(scenes.sun_direction(30.0, 0.0))
+    rad.setSourceFlux(src, "NIR", 400.0)
+    scene = oracle_scene_for(rad, oracle_mod)
+    out = {}
+    for tol in (0.0, 1e-3, 1e-6):
+        rad.setScatteringResidualTolerance(tol)
+        f, st = scene.run_band(oracle_solve(rad.solve_description(["NIR"], seed=7)))
+        out[tol] = (f[:, 0], st["iterations"])
+    assert out[0.0][1] == 20
+    assert out[1e-3][1] < out[1e-6][1] <= 20
+    area = sc.area
+    tot = {k: float((v[0] * area).sum()) for k, v in out.items()}
+    assert abs(tot[1e-3] - tot[0.0]) <= 2e-3 * tot[0.0]
+    assert abs(tot[1e-6] - tot[0.0]) <= 1e-5 * tot[0.0]
