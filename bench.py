@@ -218,6 +218,7 @@ def run_batched(rad, ctx, desc, stream, args):
             "rays_per_s": sweep_rays / t_sweep, "plain_s_per_solve": t_plain, "plain_solves_per_s": 1.0 / t_plain,
             "plain_rays_per_solve": plain_rays, "speedup_solves_per_s": (nsol / t_sweep) * t_plain,
             "graph_kernels": ctx.last_stats()["kernels"],
+            "autotune": [x for x in ctx.tuning_report().splitlines() if x.startswith("record")],
             "plain_note": "plain = one single-band runBand (direct + primary diffuse + 5 scattering passes) timed "
                           "twice; 192 plain solves take 192x that"}
 
@@ -287,6 +288,69 @@ def run_served(args, device=0):
             "wall_s": wall, "bvh_builds": st["builds"], "evictions": st["evictions"],
             "plain_solves_per_s": plain_sps, "plain_requests_timed": nplain,
             "speedup_solves_per_s": served_sps / plain_sps}
+
+
+def stress_model(scale=1.0, device=0):
+    """Deep-scattering stress workload: 3 M equilateral 3 cm triangles, 0.5 M 4 cm square
+    patches and 0.5 M disks of 2 cm radius (two-sided, spherical leaf angles, uniform in
+    a 24 x 24 x 4 m periodic box) over a one-sided ground, plus a 64^3 voxel grid over
+    the same box with leaf area density U[0, 2]; NIR (rho 0.45, tau 0.40 for leaves and
+    voxels), sun at zenith 30 deg (400 W/m^2) and 100 W/m^2 sky, 100 direct and 400
+    (20 x 20) diffuse rays, scattering depth 20 with the FP64 residual stop at 1e-6.
+    `scale` shrinks the primitive counts (and the voxel grid by its cube root)."""
+    from helios_gb300 import scenes
+    from helios_gb300.radiation import Context, RadiationModel
+
+    div = max(2, int(round(64 * scale ** (1.0 / 3.0))))
+    sc = scenes.deep_scatter(n_tri=int(3_000_000 * scale), n_patch=int(500_000 * scale),
+                             n_disk=int(500_000 * scale), vox_div=div, seed=0)
+    ctx = Context()
+    ctx.addScene(sc)
+    n = sc.n
+    leaves = np.arange(1, n)
+    ctx.setPrimitiveData(leaves, "reflectivity_NIR", np.full(n - 1, 0.45))
+    ctx.setPrimitiveData(leaves, "transmissivity_NIR", np.full(n - 1, 0.40))
+    rad = RadiationModel(ctx, device=device)
+    rad.enforcePeriodicBoundary("xy")
+    rad.addRadiationBand("NIR")
+    rad.disableEmission("NIR")
+    rad.setDirectRayCount("NIR", 100)
+    rad.setDiffuseRayCount("NIR", 400)
+    rad.setDiffuseRadiationFlux("NIR", 100.0)
+    rad.setScatteringDepth("NIR", 20)
+    rad.setScatteringResidualTolerance(1e-6)
+    sun = rad.addCollimatedRadiationSource(scenes.sun_direction(30.0, 0.0))
+    rad.setSourceFlux(sun, "NIR", 400.0)
+    return rad, sc
+
+
+def run_stress(args, stream, device=0):
+    """One timed solve of the deep-scattering stress workload (after one untimed solve)."""
+    import torch
+
+    rad, sc = stress_model(args.stress_scale, device=device)
+    rad.ctx.set_stream(stream.cuda_stream)
+    rad.setSeed(99)
+    t0 = time.perf_counter()
+    rad.updateGeometry()
+    t_build = time.perf_counter() - t0
+    desc = rad.solve_description(["NIR"])
+    ctx = rad.ctx
+    ctx.run_band(desc, out=False)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    ctx.run_band(desc, out=False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t = ev0.elapsed_time(ev1) / 1e3
+    st = ctx.last_stats()
+    counts = np.bincount(sc.ptype, minlength=5)
+    return {"workload": f"deep scatter: {int(counts[1])} triangles, {int(counts[0]) - 1} patches, "
+                        f"{int(counts[2])} disks, {int(counts[4])} voxels (LAD U[0,2]) + ground, NIR, "
+                        "100 direct / 400 diffuse rays, depth 20, FP64 residual stop 1e-6",
+            "primitives": int(sc.n), "s_per_solve": t, "rays_per_solve": st["rays"], "rays_per_s": st["rays"] / t,
+            "scattering_iterations": st["iterations"], "kernels": st["kernels"], "setup_build_s": t_build}
 
 
 def run_gpu(args):
@@ -363,6 +427,9 @@ def run_gpu(args):
     served = None
     if args.serve_requests > 0:
         served = run_served(args, device=local)
+    stress = None
+    if args.stress:
+        stress = run_stress(args, stream, device=local)
     if rank != 0:
         return
     hbm, peak_kind = peaks()
@@ -395,6 +462,7 @@ def run_gpu(args):
                      "kernel_ms": diff_ms, "kernel_share": diff_share,
                      "node_visits_per_ray": stats["node_visits"] / max(rays_per_step, 1),
                      "prim_tests_per_ray": stats["prim_tests"] / max(rays_per_step, 1)},
+        "autotune": [x for x in ctx.tuning_report().splitlines() if x.startswith("accumulate")],
         "clocks": clk.summary(),
         "e2e": {"value": rays_per_step / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s},
@@ -402,6 +470,7 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "batched": batched,
         "served": served,
+        "stress": stress,
     }
     line["gpu_launches"] = int(ctx.last_stats()["kernels"]) * args.steps
     print(json.dumps(line))
@@ -420,6 +489,8 @@ def main():
     ap.add_argument("--serve-plain", type=int, default=30, help="requests timed on the plain per-solve path")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--trees", type=int, nargs=2, default=(20, 10), help="orchard grid (default 20 x 10 = 1M leaves)")
+    ap.add_argument("--stress", action="store_true", help="also time the deep-scattering stress workload")
+    ap.add_argument("--stress-scale", type=float, default=1.0, help="primitive-count scale of the stress workload")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -25,7 +25,7 @@ EXPORTS = [
     "hrt_run_band", "hrt_last_stats", "hrt_device_status", "hrt_trace_rays", "hrt_gen_rays", "hrt_get_bvh",
     "hrt_source_rotation", "hrt_set_measure", "hrt_get_measure", "hrt_build_accel_static", "hrt_run_sweep",
     "hrt_server_create", "hrt_server_add_scene", "hrt_server_submit", "hrt_server_start", "hrt_server_wait",
-    "hrt_server_result", "hrt_server_stats", "hrt_server_destroy",
+    "hrt_server_result", "hrt_server_stats", "hrt_server_destroy", "hrt_set_tuning", "hrt_tuning_report",
 ]
 
 
@@ -112,6 +112,8 @@ def load(path: str | None = None):
         "hrt_backend_name": (C.c_char_p, []),
         "hrt_run_band": (C.c_int, [VP, C.POINTER(BandSolve), VP]),
         "hrt_last_stats": (C.c_int, [VP, VP, C.c_int]),
+        "hrt_set_tuning": (C.c_int, [VP, C.c_int]),
+        "hrt_tuning_report": (C.c_size_t, [VP, VP, C.c_size_t]),
         "hrt_device_status": (C.c_int, [VP, C.POINTER(C.c_uint32), C.c_int]),
         "hrt_trace_rays": (C.c_int, [VP, C.c_int64, VP, VP, C.c_float, C.c_float, C.c_int, VP, VP, VP]),
         "hrt_gen_rays": (C.c_int, [VP, C.c_int, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, VP, VP, VP]),
@@ -357,6 +359,16 @@ class Context:
         flux = np.zeros((self.n, nsun, nb), np.float32) if out else None
         self.check(self.lib.hrt_run_sweep(self.h, C.byref(S), ptr(flux)))
         return flux
+
+    def set_tuning(self, mode: int):
+        """1: tune kernel variants per pass shape (default); 0: fixed default; 2: retune."""
+        self.check(self.lib.hrt_set_tuning(self.h, int(mode)))
+
+    def tuning_report(self) -> str:
+        k = self.lib.hrt_tuning_report(self.h, None, 0)
+        buf = C.create_string_buffer(int(k))
+        self.lib.hrt_tuning_report(self.h, buf, k)
+        return buf.value.decode()
 
     def last_stats(self):
         st = np.zeros(3, np.uint64)

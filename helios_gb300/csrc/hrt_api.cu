@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -106,6 +107,11 @@ struct hrt_context {
     cudaGraphExec_t sw_exec = nullptr;
     std::string sw_key;
     int sw_kernels = 0;
+    // kernel-variant tuner: choice per pass shape, and a log of the trials
+    int tune = 1;
+    std::map<std::string, int> tuned;
+    std::string tune_log;
+    DevBuf tune_g;
 };
 
 namespace {
@@ -302,6 +308,81 @@ int direct_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp,
 }
 
 // Diffuse pass over one or both faces + epilogue (__raygen__diffuse, __closesthit__diffuse, __miss__diffuse).
+// ------------------------------------------------------------------ tuner --
+// The diffuse trace has interchangeable kernel variants (persistent with 4 or 3 resident
+// blocks per SM -- 64 registers with a few spills, or ~80 without -- and one ray per
+// thread).  Which is fastest depends on the scene (BVH depth, primitive mix) and on the
+// band count, so the first pass of each shape is timed on a sample: the rays of the
+// first max(count/8, 4096) primitives, written to scratch sums (or the hit buffer of a
+// recorded pass, rewritten by the real pass) and not counted.  The choice is cached
+// per (mode, n, count, rays per face, faces, bands, voxels); passes under kTuneMinRays
+// rays keep the default.  Choices differ only in the order of the FP64 atomic sums.
+constexpr long long kTuneMinRays = 20000000;
+
+int tuned_variant(hrt_context *ctx, const DiffuseParams &P0, bool record, int *variant) {
+    const int nf = ((P0.faces & 1) ? 1 : 0) + ((P0.faces & 2) ? 1 : 0);
+    const long long rays = (long long)P0.count * P0.dimx * P0.dimy * nf;
+    *variant = record ? DV_PS3 : DV_DEFAULT;
+    if (!ctx->tune || rays < kTuneMinRays || (ctx->measure & 1)) return HRT_OK;
+    char key[160];
+    std::snprintf(key, sizeof key, "%s n=%d count=%u rays_per_face=%d faces=%d bands=%d voxels=%d",
+                  record ? "record" : "accumulate", ctx->n, P0.count, P0.dimx * P0.dimy, P0.faces, P0.Bc,
+                  P0.sc.voxels);
+    auto it = ctx->tuned.find(key);
+    if (it != ctx->tuned.end()) {
+        *variant = it->second;
+        return HRT_OK;
+    }
+    std::vector<int> cand;
+    if (record) cand = {DV_PS3, DV_PS4};
+    else if (P0.sc.voxels) cand = {DV_PS4, DV_SIMPLE};
+    else cand = {DV_PS4, DV_PS3, DV_SIMPLE};
+    DiffuseParams P = P0;
+    P.count = std::min(P0.count, std::max(P0.count / 8u, 4096u));
+    P.sc.rays = nullptr;
+    P.sc.visits = nullptr;
+    if (!record) {
+        const size_t m = (size_t)ctx->n * P0.Bl;
+        CU(ctx->tune_g.ensure(2 * m * sizeof(double)));
+        P.Gt = ctx->tune_g.as<double>();
+        P.Gb = P.Gt + m;
+    }
+    cudaEvent_t a = nullptr, b = nullptr;
+    CU(cudaEventCreate(&a));
+    CU(cudaEventCreate(&b));
+    auto launch = [&](int v) {
+        return record ? launch_diffuse_record(P, P0.hits, v, ctx->stream)
+                      : launch_diffuse_variant(P, v, max_blocks(ctx), ctx->stream);
+    };
+    int best = cand[0];
+    float best_ms = 1e30f;
+    std::string line = std::string(key) + ":";
+    cudaError_t e = cudaSuccess;
+    for (int v : cand) {
+        float ms = 0.f;
+        if ((e = launch(v)) != cudaSuccess) break;  // first launch also loads the kernel
+        if ((e = cudaEventRecord(a, ctx->stream)) != cudaSuccess || (e = launch(v)) != cudaSuccess ||
+            (e = cudaEventRecord(b, ctx->stream)) != cudaSuccess || (e = cudaEventSynchronize(b)) != cudaSuccess ||
+            (e = cudaEventElapsedTime(&ms, a, b)) != cudaSuccess)
+            break;
+        char t[48];
+        std::snprintf(t, sizeof t, " %s=%.3fms", v == DV_PS4 ? "ps4" : (v == DV_PS3 ? "ps3" : "simple"), ms);
+        line += t;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = v;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    CU(e);
+    line += std::string(" -> ") + (best == DV_PS4 ? "ps4" : (best == DV_PS3 ? "ps3" : "simple")) + "\n";
+    ctx->tune_log += line;
+    ctx->tuned[key] = best;
+    *variant = best;
+    return HRT_OK;
+}
+
 int diffuse_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp, uint32_t seed, uint32_t pass, int faces,
                  int Bg, int Bc, int Bl, const SkyParams &sky) {
     int dimx, dimy;
@@ -331,9 +412,12 @@ int diffuse_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp
     P.Gb = ctx->Gb.as<double>();
     CU(ctx->fetch.ensure(sizeof(unsigned long long)));
     P.fetch = ctx->fetch.as<unsigned long long>();
+    P.hits = nullptr;
+    int variant = DV_DEFAULT, r;
+    if ((r = tuned_variant(ctx, P, false, &variant))) return r;
     CU(timed_launch(ctx, 1, [&] {
         return (ctx->measure & 1) ? launch_diffuse_stats(P, max_blocks(ctx), ctx->stream)
-                                  : launch_diffuse(P, max_blocks(ctx), ctx->stream);
+                                  : launch_diffuse_variant(P, variant, max_blocks(ctx), ctx->stream);
     }));
     EpilogueParams E{};
     E.n = ctx->n;
@@ -951,6 +1035,23 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
     CU(ctx->sw_hits.ensure(nhits * sizeof(uint32_t)));
     CU(ctx->Gd.ensure(std::max<size_t>((size_t)n * nsun * 2, 1) * sizeof(double)));
     CU(ctx->fetch.ensure(sizeof(unsigned long long)));
+    // choose the recording kernel's variant before capture (timing cannot run inside a capture)
+    int rec_variant = DV_PS3;
+    if (Rd > 0 && (any_diffuse || any_active)) {
+        DiffuseParams T0{};
+        T0.sc = scene_of(ctx);
+        T0.dimx = ddx;
+        T0.dimy = ddy;
+        T0.seed = s->seed;
+        T0.pass = 1;
+        T0.count = (uint32_t)n;
+        T0.faces = 3;
+        T0.Bc = 1;
+        T0.Bl = 1;
+        T0.fetch = ctx->fetch.as<unsigned long long>();
+        T0.hits = ctx->sw_hits.as<uint32_t>();
+        if ((r = tuned_variant(ctx, T0, true, &rec_variant))) return r;
+    }
     // capture the pass sequence once per shape
     char key[256];
     std::snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%u/%d%d%d%d/%p/%p", n, nsun, Bl, s->direct_rays, s->diffuse_rays,
@@ -958,8 +1059,8 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
                   ctx->sw_acc.p, ctx->sw_hits.p);
     {
         char more[128];
-        std::snprintf(more, sizeof more, "/%p/%p/%p/%p/%p", ctx->sw_in.p, ctx->sw_mat.p, ctx->sw_out.p, ctx->Gd.p,
-                      (void *)ctx->stream);
+        std::snprintf(more, sizeof more, "/%p/%p/%p/%p/%p/v%d", ctx->sw_in.p, ctx->sw_mat.p, ctx->sw_out.p, ctx->Gd.p,
+                      (void *)ctx->stream, rec_variant);
         std::strncat(key, more, sizeof key - std::strlen(key) - 1);
     }
     if (!ctx->sw_exec || ctx->sw_key != key) {
@@ -1013,7 +1114,8 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
             auto pass = [&](uint32_t pass_id, const float *sky, const uint8_t *mask) -> cudaError_t {
                 cudaError_t e2;
                 P.pass = pass_id;
-                if ((e2 = launch_diffuse_record(P, ctx->sw_hits.as<uint32_t>(), st)) != cudaSuccess) return e2;
+                if ((e2 = launch_diffuse_record(P, ctx->sw_hits.as<uint32_t>(), rec_variant, st)) != cudaSuccess)
+                    return e2;
                 Gp.sky = sky;
                 if ((e2 = launch_gather(Gp, st)) != cudaSuccess) return e2;
                 E.mask = mask;
@@ -1065,6 +1167,27 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
     ctx->last_rays = rays;
     ctx->last_iters = (uint64_t)s->scattering_depth;
     return r;
+}
+
+int hrt_set_tuning(hrt_context *ctx, int mode) {
+    if (!ctx || mode < 0 || mode > 2) return HRT_EINVAL;
+    if (mode == 2) {
+        ctx->tuned.clear();
+        ctx->tune_log.clear();
+        mode = 1;
+    }
+    ctx->tune = mode;
+    return HRT_OK;
+}
+
+size_t hrt_tuning_report(const hrt_context *ctx, char *buf, size_t len) {
+    if (!ctx) return 0;
+    if (buf && len) {
+        size_t k = std::min(len - 1, ctx->tune_log.size());
+        std::memcpy(buf, ctx->tune_log.data(), k);
+        buf[k] = 0;
+    }
+    return ctx->tune_log.size() + 1;
 }
 
 int hrt_last_stats(const hrt_context *ctx, uint64_t *stats, int count) {

@@ -309,6 +309,22 @@ __device__ __forceinline__ f3 sample_point(const float4 g[4], uint32_t type, flo
     return mk((P.x + u * A.x) + v * B.x, (P.y + u * A.y) + v * B.y, (P.z + u * A.z) + v * B.z);
 }
 
+// ------------------------------------------------------- compressed 4-wide BVH ---
+// Node (64 B, one 4 x float4 load):
+//   q0 = (px, py, pz, ebits)    origin p (the node box's lower corner), ebits = ex | ey << 8 |
+//                               ez << 16 with s_k = 2^(e_k - 127) the per-axis step
+//   q1 = (lox, loy, loz, hix)   quantised child boxes, byte k = child k (0 <= q <= 255)
+//   q2 = (hiy, hiz, c0, c1)     child refs c_k: >= 0 node, ~slot leaf, kEmptyChild none
+//   q3 = (c2, c3, 0, 0)
+// Child k's box per axis: [p + lo_k * s, p + hi_k * s] in FP32 (q * s is exact; one rounded
+// add).  The build picks the bytes so that these values enclose the child's FP32 box (itself
+// padded), so a slab test on the decoded box never culls an accepted hit (after Ylitie,
+// Karras, Laine, "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs",
+// HPG 2017, with 4 children per node).
+__device__ __forceinline__ float q_step(uint32_t e) { return __uint_as_float(e << 23); }
+__device__ __forceinline__ float q_decode(float p, uint32_t q, float s) { return p + (float)q * s; }
+__device__ __forceinline__ uint32_t q_byte(uint32_t w, int k) { return (w >> (8 * k)) & 0xFFu; }
+
 // Leaf-box padding: each face moves out by (|x| + extent) * 2^-20.
 __device__ __forceinline__ float pad_lo(float x, float ext) { return x - (fabsf(x) + ext) * 9.5367431640625e-07f; }
 __device__ __forceinline__ float pad_hi(float x, float ext) { return x + (fabsf(x) + ext) * 9.5367431640625e-07f; }

@@ -10,6 +10,8 @@ namespace hrt {
 struct TraceScene {
     const float4 *rec;    // [n*4] intersection records, BVH leaf order
     const float4 *nodes;  // [max(n-1,1)*4] BVH2 nodes
+    const float4 *nodes4; // [n4*4] compressed 4-wide nodes (hrt_device.cuh), root 0
+    int n4;
     const float4 *rgen;   // [n*4] ray-origin records, original order
     const float4 *bbox;   // [nbbox*4] periodic wall corners (xyz, w unused)
     int n;
@@ -100,6 +102,11 @@ constexpr size_t bvh_scratch_bytes_c(int n) {
 }
 size_t bvh_scratch_bytes(int n);
 void bvh_carve(BvhBuffers &b, void *scratch, int n);
+// Compressed 4-wide BVH collapsed from the binary nodes (hrt_bvh4.cu): nodes4 holds
+// max(n-1,1) * 4 float4, scratch bvh4_scratch_bytes(n); *count_out = nodes written.
+size_t bvh4_scratch_bytes(int n);
+cudaError_t bvh4_build(const float4 *nodes2, int n, float4 *nodes4, void *scratch, uint32_t *status, int *count_out,
+                       cudaStream_t s);
 // lad: [n] leaf area density of voxels (original order), or null (voxels then hold no leaves).
 cudaError_t bvh_build(const float *T, const uint32_t *type, const float *lad, int n, BvhBuffers &b, cudaStream_t s);
 constexpr int kSortTile = 2048;
@@ -107,6 +114,9 @@ constexpr int kSortTile = 2048;
 // ---------------------------------------------------------------- passes
 cudaError_t launch_direct(const DirectParams &p, int max_blocks, cudaStream_t s);
 cudaError_t launch_diffuse(const DiffuseParams &p, int max_blocks, cudaStream_t s);
+// Diffuse kernel variants the tuner chooses between.
+enum DiffuseVariant { DV_DEFAULT = 0, DV_PS4 = 1, DV_PS3 = 2, DV_SIMPLE = 3 };
+cudaError_t launch_diffuse_variant(const DiffuseParams &p, int variant, int max_blocks, cudaStream_t s);
 // Same launches with per-ray node-visit / primitive-test counting into sc.visits.
 cudaError_t launch_direct_stats(const DirectParams &p, int max_blocks, cudaStream_t s);
 cudaError_t launch_diffuse_stats(const DiffuseParams &p, int max_blocks, cudaStream_t s);
@@ -137,7 +147,7 @@ struct GatherParams {
 constexpr uint32_t kMissCode = 0xFFFFFFFFu, kLostCode = 0xFFFFFFFEu;
 cudaError_t launch_direct_sweep(const SweepDirectParams &p, int max_blocks, cudaStream_t s);
 // Persistent diffuse trace that stores every ray's hit code instead of accumulating.
-cudaError_t launch_diffuse_record(const DiffuseParams &p, uint32_t *hits, cudaStream_t s);
+cudaError_t launch_diffuse_record(const DiffuseParams &p, uint32_t *hits, int variant, cudaStream_t s);
 cudaError_t launch_gather(const GatherParams &p, cudaStream_t s);
 struct ChannelEpilogue {
     int n, C, Bl;

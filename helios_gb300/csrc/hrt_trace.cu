@@ -1056,10 +1056,12 @@ static cudaError_t diffuse_ps_launch_b(const DiffuseParams &p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// minb: 4 or 3 (resident blocks per SM the register budget allows); 0 = the default.
 template <int NB>
-static cudaError_t diffuse_ps_launch(const DiffuseParams &p, cudaStream_t s) {
+static cudaError_t diffuse_ps_launch(const DiffuseParams &p, int minb, cudaStream_t s) {
     if (p.sc.voxels) return diffuse_ps_launch_b<NB, 4, true>(p, s);
-    return ps_min_blocks() == 4 ? diffuse_ps_launch_b<NB, 4, false>(p, s) : diffuse_ps_launch_b<NB, 3, false>(p, s);
+    if (minb == 0) minb = ps_min_blocks();
+    return minb == 4 ? diffuse_ps_launch_b<NB, 4, false>(p, s) : diffuse_ps_launch_b<NB, 3, false>(p, s);
 }
 
 static bool use_persistent() {
@@ -1071,16 +1073,20 @@ static bool use_persistent() {
     return v == 1;
 }
 
+// variant: DV_DEFAULT (persistent unless HRT_TRAVERSAL=simple), DV_PS4 / DV_PS3 (persistent,
+// 4 or 3 resident blocks per SM), DV_SIMPLE (one ray per thread).
 template <bool STATS>
-static cudaError_t diffuse_impl(const DiffuseParams &p, int max_blocks, cudaStream_t s) {
+static cudaError_t diffuse_impl(const DiffuseParams &p, int variant, int max_blocks, cudaStream_t s) {
     int64_t total = (int64_t)p.count * p.dimx * p.dimy;
     if (total <= 0 || p.Bc <= 0) return cudaSuccess;
-    if (!STATS && p.fetch && use_persistent()) {
-        if (p.Bc <= 1) return diffuse_ps_launch<1>(p, s);
-        if (p.Bc <= 2) return diffuse_ps_launch<2>(p, s);
-        if (p.Bc <= 4) return diffuse_ps_launch<4>(p, s);
-        if (p.Bc <= 8) return diffuse_ps_launch<8>(p, s);
-        if (p.Bc <= 16) return diffuse_ps_launch<16>(p, s);
+    const bool persistent = variant == DV_DEFAULT ? use_persistent() : variant != DV_SIMPLE;
+    if (!STATS && p.fetch && persistent) {
+        const int minb = variant == DV_PS4 ? 4 : (variant == DV_PS3 ? 3 : 0);
+        if (p.Bc <= 1) return diffuse_ps_launch<1>(p, minb, s);
+        if (p.Bc <= 2) return diffuse_ps_launch<2>(p, minb, s);
+        if (p.Bc <= 4) return diffuse_ps_launch<4>(p, minb, s);
+        if (p.Bc <= 8) return diffuse_ps_launch<8>(p, minb, s);
+        if (p.Bc <= 16) return diffuse_ps_launch<16>(p, minb, s);
         return cudaErrorInvalidValue;
     }
     unsigned nb = blocks_for(total, kBlock);
@@ -1099,13 +1105,16 @@ cudaError_t launch_direct(const DirectParams &p, int max_blocks, cudaStream_t s)
     return direct_impl<false>(p, max_blocks, s);
 }
 cudaError_t launch_diffuse(const DiffuseParams &p, int max_blocks, cudaStream_t s) {
-    return diffuse_impl<false>(p, max_blocks, s);
+    return diffuse_impl<false>(p, DV_DEFAULT, max_blocks, s);
+}
+cudaError_t launch_diffuse_variant(const DiffuseParams &p, int variant, int max_blocks, cudaStream_t s) {
+    return diffuse_impl<false>(p, variant, max_blocks, s);
 }
 cudaError_t launch_direct_stats(const DirectParams &p, int max_blocks, cudaStream_t s) {
     return direct_impl<true>(p, max_blocks, s);
 }
 cudaError_t launch_diffuse_stats(const DiffuseParams &p, int max_blocks, cudaStream_t s) {
-    return diffuse_impl<true>(p, max_blocks, s);
+    return diffuse_impl<true>(p, DV_DEFAULT, max_blocks, s);
 }
 
 cudaError_t launch_trace_rays(const TraceScene &sc, int64_t nrays, const float *o, const float *d, float tmin,
@@ -1231,23 +1240,29 @@ cudaError_t launch_direct_sweep(const SweepDirectParams &p, int max_blocks, cuda
     return cudaGetLastError();
 }
 
-cudaError_t launch_diffuse_record(const DiffuseParams &p, uint32_t *hits, cudaStream_t s) {
-    if ((long long)p.count * p.dimx * p.dimy <= 0) return cudaSuccess;
+template <int MINB>
+static cudaError_t diffuse_record_b(const DiffuseParams &q, cudaStream_t s) {
     static int blocks_per_sm = 0, sms = 0;
     if (blocks_per_sm == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<1, true, 3, false>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<1, true, MINB, false>, kBlock, 0);
         if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
+    cudaError_t e = cudaMemsetAsync(q.fetch, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    k_diffuse_ps<1, true, MINB, false><<<sms * blocks_per_sm, kBlock, 0, s>>>(q);
+    return cudaGetLastError();
+}
+
+// variant: DV_PS4 for 4 resident blocks per SM, anything else 3 (the default).
+cudaError_t launch_diffuse_record(const DiffuseParams &p, uint32_t *hits, int variant, cudaStream_t s) {
+    if ((long long)p.count * p.dimx * p.dimy <= 0) return cudaSuccess;
     DiffuseParams q = p;
     q.hits = hits;
     q.Bc = 1;
-    cudaError_t e = cudaMemsetAsync(q.fetch, 0, sizeof(unsigned long long), s);
-    if (e != cudaSuccess) return e;
-    k_diffuse_ps<1, true, 3, false><<<sms * blocks_per_sm, kBlock, 0, s>>>(q);
-    return cudaGetLastError();
+    return variant == DV_PS4 ? diffuse_record_b<4>(q, s) : diffuse_record_b<3>(q, s);
 }
 
 cudaError_t launch_gather(const GatherParams &p, cudaStream_t s) {

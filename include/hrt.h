@@ -223,6 +223,17 @@ int hrt_server_result(hrt_server *s, uint64_t request_id, float *flux_out, size_
 int hrt_server_stats(hrt_server *s, double *out, int count);
 int hrt_server_destroy(hrt_server *s);
 
+/* Kernel-variant tuner (no counterpart in the reference).  The diffuse trace has
+ * interchangeable variants (persistent threads with 4 or 3 resident blocks per SM, one
+ * ray per thread); the first pass of each shape (rays per face, faces, bands, scene
+ * size) of at least 2e7 rays times them on a sample of its rays and keeps the fastest
+ * for later passes, solves and sweep graphs of that shape.  mode 1 (default) tunes,
+ * 0 uses the fixed default, 2 forgets earlier choices and tunes again.  Variants give
+ * the same results up to the order of FP64 sums. */
+int hrt_set_tuning(hrt_context *ctx, int mode);
+/* Text log of the tuner's trials and choices, one line per shape; returns the bytes
+ * needed (including the terminating zero); buf may be NULL. */
+size_t hrt_tuning_report(const hrt_context *ctx, char *buf, size_t len);
 /* Statistics of the last hrt_run_band: [0] rays traced, [1] kernels launched,
  * [2] scattering iterations run. */
 int hrt_last_stats(const hrt_context *ctx, uint64_t *stats, int count);
