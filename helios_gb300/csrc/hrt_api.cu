@@ -78,7 +78,8 @@ struct hrt_context {
     bool have_geometry = false, built = false;
     std::vector<int8_t> h_twosided;
     std::vector<uint32_t> h_voxels;  // original indices of voxel primitives
-    DevBuf T, type, twosided, bbox, rec, rgen, nodes, codes, perm, bvh_scratch, lad, area;
+    DevBuf T, type, twosided, bbox, rec, rgen, nodes, codes, perm, bvh_scratch, lad, area, nodes4;
+    int n4 = 0;  // compressed 4-wide nodes built
     // materials and sources
     int mS = 0, mN = 0, mB = 0;
     DevBuf rho, tau, src, src_flux;
@@ -132,6 +133,8 @@ TraceScene scene_of(hrt_context *ctx) {
     TraceScene sc;
     sc.rec = ctx->rec.as<float4>();
     sc.nodes = ctx->nodes.as<float4>();
+    sc.nodes4 = ctx->n4 > 0 ? ctx->nodes4.as<float4>() : nullptr;
+    sc.n4 = ctx->n4;
     sc.rgen = ctx->rgen.as<float4>();
     sc.bbox = ctx->nbbox ? ctx->bbox.as<float4>() : nullptr;
     sc.n = ctx->n;
@@ -319,10 +322,26 @@ int direct_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp,
 // rays keep the default.  Choices differ only in the order of the FP64 atomic sums.
 constexpr long long kTuneMinRays = 20000000;
 
+const char *variant_name(int v) {
+    switch (v) {
+        case DV_W4: return "wide4";
+        case DV_W43: return "wide4-3";
+        case DV_PS4: return "binary4";
+        case DV_PS3: return "binary3";
+        case DV_SIMPLE: return "simple";
+        default: return "default";
+    }
+}
+
 int tuned_variant(hrt_context *ctx, const DiffuseParams &P0, bool record, int *variant) {
     const int nf = ((P0.faces & 1) ? 1 : 0) + ((P0.faces & 2) ? 1 : 0);
     const long long rays = (long long)P0.count * P0.dimx * P0.dimy * nf;
-    *variant = record ? DV_PS3 : DV_DEFAULT;
+    *variant = record ? (P0.sc.nodes4 ? DV_W4 : DV_PS3) : DV_DEFAULT;
+    if (ctx->tune >= 16) {  // forced variant (tests, experiments)
+        const int v = ctx->tune - 16;
+        if (!(record && v == DV_SIMPLE)) *variant = v;
+        return HRT_OK;
+    }
     if (!ctx->tune || rays < kTuneMinRays || (ctx->measure & 1)) return HRT_OK;
     char key[160];
     std::snprintf(key, sizeof key, "%s n=%d count=%u rays_per_face=%d faces=%d bands=%d voxels=%d",
@@ -334,9 +353,11 @@ int tuned_variant(hrt_context *ctx, const DiffuseParams &P0, bool record, int *v
         return HRT_OK;
     }
     std::vector<int> cand;
-    if (record) cand = {DV_PS3, DV_PS4};
-    else if (P0.sc.voxels) cand = {DV_PS4, DV_SIMPLE};
-    else cand = {DV_PS4, DV_PS3, DV_SIMPLE};
+    const bool w4 = P0.sc.nodes4 != nullptr;
+    if (record) cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_PS3, DV_PS4} : std::vector<int>{DV_PS3, DV_PS4};
+    else if (P0.sc.voxels) cand = w4 ? std::vector<int>{DV_W4, DV_PS4, DV_SIMPLE} : std::vector<int>{DV_PS4, DV_SIMPLE};
+    else cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_PS4, DV_PS3, DV_SIMPLE}
+                   : std::vector<int>{DV_PS4, DV_PS3, DV_SIMPLE};
     DiffuseParams P = P0;
     P.count = std::min(P0.count, std::max(P0.count / 8u, 4096u));
     P.sc.rays = nullptr;
@@ -366,7 +387,7 @@ int tuned_variant(hrt_context *ctx, const DiffuseParams &P0, bool record, int *v
             (e = cudaEventElapsedTime(&ms, a, b)) != cudaSuccess)
             break;
         char t[48];
-        std::snprintf(t, sizeof t, " %s=%.3fms", v == DV_PS4 ? "ps4" : (v == DV_PS3 ? "ps3" : "simple"), ms);
+        std::snprintf(t, sizeof t, " %s=%.3fms", variant_name(v), ms);
         line += t;
         if (ms < best_ms) {
             best_ms = ms;
@@ -376,7 +397,7 @@ int tuned_variant(hrt_context *ctx, const DiffuseParams &P0, bool record, int *v
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     CU(e);
-    line += std::string(" -> ") + (best == DV_PS4 ? "ps4" : (best == DV_PS3 ? "ps3" : "simple")) + "\n";
+    line += std::string(" -> ") + variant_name(best) + "\n";
     ctx->tune_log += line;
     ctx->tuned[key] = best;
     *variant = best;
@@ -416,7 +437,8 @@ int diffuse_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp
     int variant = DV_DEFAULT, r;
     if ((r = tuned_variant(ctx, P, false, &variant))) return r;
     CU(timed_launch(ctx, 1, [&] {
-        return (ctx->measure & 1) ? launch_diffuse_stats(P, max_blocks(ctx), ctx->stream)
+        return (ctx->measure & 1)
+                   ? launch_diffuse_stats(P, (ctx->measure & 4) ? DV_SIMPLE : DV_DEFAULT, max_blocks(ctx), ctx->stream)
                                   : launch_diffuse_variant(P, variant, max_blocks(ctx), ctx->stream);
     }));
     EpilogueParams E{};
@@ -583,6 +605,15 @@ int hrt_build_accel(hrt_context *ctx) {
                  b, ctx->stream));
     int r = sync_and_status(ctx);
     if (r) return r;
+    // compressed 4-wide nodes for the persistent diffuse trace (scratch reuses the build's)
+    ctx->n4 = 0;
+    CU(ctx->nodes4.ensure(ni * 4 * sizeof(float4)));
+    if (bvh4_scratch_bytes(n) > ctx->bvh_scratch.cap) CU(ctx->bvh_scratch.ensure(bvh4_scratch_bytes(n)));
+    int n4 = 0;
+    CU(bvh4_build(ctx->nodes.as<float4>(), n, ctx->nodes4.as<float4>(), ctx->bvh_scratch.p, ctx->status.as<uint32_t>(),
+                  &n4, ctx->stream));
+    if ((r = sync_and_status(ctx))) return r;
+    ctx->n4 = n4;
     ctx->built = true;
     return HRT_OK;
 }
@@ -1036,7 +1067,7 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
     CU(ctx->Gd.ensure(std::max<size_t>((size_t)n * nsun * 2, 1) * sizeof(double)));
     CU(ctx->fetch.ensure(sizeof(unsigned long long)));
     // choose the recording kernel's variant before capture (timing cannot run inside a capture)
-    int rec_variant = DV_PS3;
+    int rec_variant = ctx->n4 > 0 ? DV_W4 : DV_PS3;
     if (Rd > 0 && (any_diffuse || any_active)) {
         DiffuseParams T0{};
         T0.sc = scene_of(ctx);
@@ -1170,7 +1201,7 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
 }
 
 int hrt_set_tuning(hrt_context *ctx, int mode) {
-    if (!ctx || mode < 0 || mode > 2) return HRT_EINVAL;
+    if (!ctx || mode < 0 || (mode > 2 && !(mode >= 16 + DV_PS4 && mode <= 16 + DV_W43))) return HRT_EINVAL;
     if (mode == 2) {
         ctx->tuned.clear();
         ctx->tune_log.clear();

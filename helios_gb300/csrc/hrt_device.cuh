@@ -324,6 +324,22 @@ __device__ __forceinline__ f3 sample_point(const float4 g[4], uint32_t type, flo
 __device__ __forceinline__ float q_step(uint32_t e) { return __uint_as_float(e << 23); }
 __device__ __forceinline__ float q_decode(float p, uint32_t q, float s) { return p + (float)q * s; }
 __device__ __forceinline__ uint32_t q_byte(uint32_t w, int k) { return (w >> (8 * k)) & 0xFFu; }
+// Three-input minimum / maximum (PTX min.f32 / max.f32 with three sources; a NaN input
+// is ignored, as by fminf / fmaxf).
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+// Byte k of w as an exact float: one byte permute builds 0x4B0000qq = 2^23 + q.
+__device__ __forceinline__ float q_float(uint32_t w, int k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, (uint32_t)k | 0x7540u)) - 8388608.0f;
+}
 
 // Leaf-box padding: each face moves out by (|x| + extent) * 2^-20.
 __device__ __forceinline__ float pad_lo(float x, float ext) { return x - (fabsf(x) + ext) * 9.5367431640625e-07f; }

@@ -114,12 +114,20 @@ constexpr int kSortTile = 2048;
 // ---------------------------------------------------------------- passes
 cudaError_t launch_direct(const DirectParams &p, int max_blocks, cudaStream_t s);
 cudaError_t launch_diffuse(const DiffuseParams &p, int max_blocks, cudaStream_t s);
-// Diffuse kernel variants the tuner chooses between.
-enum DiffuseVariant { DV_DEFAULT = 0, DV_PS4 = 1, DV_PS3 = 2, DV_SIMPLE = 3 };
+// Diffuse kernel variants the tuner chooses between: persistent threads over binary nodes
+// (PS4 / PS3: 4 or 3 resident blocks per SM), over compressed 4-wide nodes (W4 / W43), or
+// one ray per thread over binary nodes (SIMPLE).
+enum DiffuseVariant { DV_DEFAULT = 0, DV_PS4 = 1, DV_PS3 = 2, DV_SIMPLE = 3, DV_W4 = 4, DV_W43 = 5 };
 cudaError_t launch_diffuse_variant(const DiffuseParams &p, int variant, int max_blocks, cudaStream_t s);
+// persistent-kernel launchers (hrt_ps_accumulate.cu, hrt_ps_special.cu)
+cudaError_t launch_ps_accumulate(const DiffuseParams &p, int variant, cudaStream_t s);
+cudaError_t launch_ps_voxels(const DiffuseParams &p, int variant, cudaStream_t s);
+cudaError_t launch_ps_stats(const DiffuseParams &p, cudaStream_t s);
 // Same launches with per-ray node-visit / primitive-test counting into sc.visits.
 cudaError_t launch_direct_stats(const DirectParams &p, int max_blocks, cudaStream_t s);
-cudaError_t launch_diffuse_stats(const DiffuseParams &p, int max_blocks, cudaStream_t s);
+// variant DV_SIMPLE counts on the binary tree (the structure the host oracle traverses),
+// DV_DEFAULT on the tree the default kernel traverses.
+cudaError_t launch_diffuse_stats(const DiffuseParams &p, int variant, int max_blocks, cudaStream_t s);
 cudaError_t launch_trace_rays(const TraceScene &sc, int64_t nrays, const float *o, const float *d, float tmin,
                               float tmax, int anyhit, int32_t *hit, float *t, int32_t *face, cudaStream_t s);
 cudaError_t launch_gen_rays(const TraceScene &sc, int kind, uint32_t seed, uint32_t pass, int dimx, int dimy,

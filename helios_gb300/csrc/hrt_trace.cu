@@ -13,250 +13,11 @@
 // before one atomic per (primitive, band) segment.  Material factors
 // (1-rho-tau, rho, tau) are applied afterwards per primitive (epilogues), which
 // equals the reference's per-ray products in exact arithmetic.
-#include <cstdlib>
-
-#include "hrt_device.cuh"
-#include "hrt_internal.h"
+#include "hrt_trace.cuh"
 
 namespace hrt {
 
 namespace {
-
-constexpr int kBlock = 256;
-
-struct Hit {
-    float t;
-    uint32_t prim;  // original index, 0xFFFFFFFF = miss, kLost = dropped after the wrap limit
-    int face;
-};
-constexpr uint32_t kLost = 0xFFFFFFFEu;
-
-__device__ __forceinline__ void raise(uint32_t *status, uint32_t bit) {
-    if (status) atomicOr(status, bit);
-}
-
-// Closest (or any) hit over the BVH.  Visiting order: both child boxes are
-// tested against the current best distance; leaf children are intersected at
-// once; of two internal children the nearer is entered and the farther pushed.
-template <bool STATS>
-__device__ Hit trace_bvh(const TraceScene &sc, f3 o, f3 d, float tmin, float tmax, bool anyhit, const VoxKey &vk,
-                         uint32_t *nv, uint32_t *np) {
-    Hit h{tmax, 0xFFFFFFFFu, 0};
-    if (sc.n == 0) return h;
-    WT w = wt_setup(d);
-    f3 inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
-    f3 ooi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
-    int32_t stack[kStack];
-    int sp = 0;
-    int32_t cur = 0;
-    float best = tmax;
-    const uint32_t ni = (uint32_t)(sc.n > 1 ? sc.n - 1 : 1);
-    uint32_t budget = 2u * (uint32_t)sc.n + 64u;  // a ray visits each node at most once
-    for (;;) {
-        if ((uint32_t)cur >= ni || budget-- == 0u) {
-            raise(sc.status, ERR_BOUNDS);
-            return h;
-        }
-        if (STATS) ++*nv;
-        const float4 *nd = sc.nodes + 4 * (size_t)cur;
-        float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
-        int32_t c[2] = {__float_as_int(n3.x), __float_as_int(n3.y)};
-        float tn0, tn1;
-        bool hb[2];
-        hb[0] = slab_node(ooi, inv, mk(n0.x, n0.y, n0.z), mk(n0.w, n1.x, n1.y), tmin, best, &tn0);
-        hb[1] = slab_node(ooi, inv, mk(n1.z, n1.w, n2.x), mk(n2.y, n2.z, n2.w), tmin, best, &tn1);
-        int32_t next[2];
-        int nn = 0;
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            if (!hb[k]) continue;
-            int32_t ck = c[k];
-            if (ck < 0) {
-                if (ck == kEmptyChild) continue;
-                if ((uint32_t)(~ck) >= (uint32_t)sc.n) {
-                    raise(sc.status, ERR_BOUNDS);
-                    continue;
-                }
-                float t;
-                int face;
-                uint32_t orig;
-                if (STATS) ++*np;
-                if (rec_hit(sc.rec, (uint32_t)(~ck), w, o, d, inv, tmin, best, vk, &t, &face, &orig)) {
-                    if (h.prim == 0xFFFFFFFFu || t < h.t || (t == h.t && orig < h.prim)) {
-                        h.t = t;
-                        h.prim = orig;
-                        h.face = face;
-                        best = t;
-                    }
-                    if (anyhit) return h;
-                }
-            } else {
-                next[nn++] = ck;
-            }
-        }
-        if (nn == 2) {
-            bool sw = tn1 < tn0;
-            int32_t nearc = sw ? next[1] : next[0];
-            int32_t farc = sw ? next[0] : next[1];
-            if (sp >= kStack) {
-                raise(sc.status, ERR_STACK);
-                return h;
-            }
-            stack[sp++] = farc;
-            cur = nearc;
-        } else if (nn == 1) {
-            cur = next[0];
-        } else {
-            if (sp == 0) break;
-            cur = stack[--sp];
-        }
-    }
-    return h;
-}
-
-// Periodic walls: closest wall before `lim`.
-__device__ __forceinline__ bool wall_closest(const TraceScene &sc, f3 o, f3 d, float tmin, float lim, float *tb,
-                                             int *which) {
-    WT w = wt_setup(d);
-    bool any = false;
-    float best = lim;
-    for (int b = 0; b < sc.nbbox; ++b) {
-        f3 v[4] = {xyz(sc.bbox[4 * b]), xyz(sc.bbox[4 * b + 1]), xyz(sc.bbox[4 * b + 2]), xyz(sc.bbox[4 * b + 3])};
-        float t;
-        int face;
-        if (poly_hit<4>(w, o, tmin, v, best, &t, &face)) {
-            if (!any || t < best) {
-                best = t;
-                *which = b;
-                any = true;
-            }
-        }
-    }
-    *tb = best;
-    return any;
-}
-
-// Trace with periodic wrapping (<= 10 wraps; OptiX8DeviceCode.cu:763-789, 1440-1459).
-template <bool STATS>
-__device__ Hit trace_full(const TraceScene &sc, f3 o, f3 d, float tmin, float tmax, bool anyhit, VoxKey vk,
-                          uint32_t *nv, uint32_t *np) {
-    const uint32_t c2 = vk.c2;
-    for (int wrap = 0; wrap < 10; ++wrap) {
-        vk.c2 = c2 | ((uint32_t)wrap << 16);
-        Hit h = trace_bvh<STATS>(sc, o, d, tmin, tmax, anyhit && sc.nbbox == 0, vk, nv, np);
-        if (sc.nbbox == 0) return h;
-        float tb;
-        int which = -1;
-        float lim = (h.prim != 0xFFFFFFFFu) ? h.t : tmax;
-        if (!wall_closest(sc, o, d, tmin, lim, &tb, &which) || (h.prim != 0xFFFFFFFFu && !(tb < h.t))) return h;
-        f3 hp = add(o, scl(d, tb));
-        bool xwall = (sc.periodic_x == 1.f) && which < 2;
-        if (xwall) {
-            float width = sc.bbox[4].x - sc.bbox[0].x;
-            hp.x = hp.x + ((which == 0) ? width : -width);
-        } else {
-            int yb = (sc.periodic_x == 1.f) ? 2 : 0;
-            float width = sc.bbox[4 * (yb + 1)].y - sc.bbox[4 * yb].y;
-            hp.y = hp.y + ((which == yb) ? width : -width);
-        }
-        o = hp;
-    }
-    // The tenth trace ended on a wall again: the reference's loop stops there and no
-    // miss or closest-hit program deposits anything for this ray.
-    return Hit{tmax, kLost, 0};
-}
-
-__device__ __forceinline__ void load_rgen(const TraceScene &sc, uint32_t p, float4 g[4]) {
-    const float4 *s = sc.rgen + 4 * (size_t)p;
-    g[0] = __ldg(s);
-    g[1] = __ldg(s + 1);
-    g[2] = __ldg(s + 2);
-    g[3] = __ldg(s + 3);
-}
-
-__device__ __forceinline__ void count_visits(const TraceScene &sc, uint32_t nv, uint32_t np) {
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        nv += __shfl_down_sync(0xffffffffu, nv, d);
-        np += __shfl_down_sync(0xffffffffu, np, d);
-    }
-    if ((threadIdx.x & 31) == 0 && sc.visits) {
-        atomicAdd(sc.visits, (unsigned long long)nv);
-        atomicAdd(sc.visits + 1, (unsigned long long)np);
-    }
-}
-
-__device__ __forceinline__ void count_rays(const TraceScene &sc, bool traced) {
-    unsigned m = __ballot_sync(0xffffffffu, traced);
-    if ((threadIdx.x & 31) == 0 && m && sc.rays) atomicAdd(sc.rays, (unsigned long long)__popc(m));
-}
-
-// Segmented warp sum over consecutive lanes with equal key; the last lane of
-// each segment adds the segment total to dst[key*stride + j].  All 32 lanes
-// must call this (inactive lanes pass key = 0xFFFFFFFF).
-template <int NV>
-__device__ __forceinline__ void warp_segment_add(uint32_t key, double (&v)[NV], int nv, double *dst, int stride) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int dlt = 1; dlt < 32; dlt <<= 1) {
-        uint32_t ok = __shfl_up_sync(0xffffffffu, key, dlt);
-        bool same = lane >= dlt && ok == key;
-#pragma unroll
-        for (int j = 0; j < NV; ++j) {
-            double y = __shfl_up_sync(0xffffffffu, v[j], dlt);
-            if (same) v[j] += y;
-        }
-    }
-    uint32_t nk = __shfl_down_sync(0xffffffffu, key, 1);
-    bool tail = (lane == 31) || nk != key;
-    if (tail && key != 0xFFFFFFFFu) {
-        for (int j = 0; j < nv && j < NV; ++j)
-            if (v[j] != 0.0) atomicAdd(dst + (size_t)key * stride + j, v[j]);
-    }
-}
-
-// ------------------------------------------------------------------ origins --
-// Leaf-projection factor of a direct ray's strength: |n . d| on a surface, G on a voxel.
-__device__ __forceinline__ double proj(f3 nrm, f3 d, bool vox) {
-    return vox ? (double)kVoxelG : (double)fabsf(dot(nrm, d));
-}
-
-// Origin of direct ray r of primitive p; u = philox(r, p, c2, 0; seed, pass), c2 =
-// source << 1.  Non-triangles are stratified over dimx x dimy cells
-// (OptiX8DeviceCode.cu:1270-1290); a voxel's third coordinate uses counter c2 | 1.
-__device__ __forceinline__ f3 direct_origin(const float4 g[4], uint32_t type, uint32_t r, uint32_t p, uint32_t c2,
-                                            int dimx, int dimy, uint32_t seed, uint32_t pass, const u4 &u) {
-    float uu = u01(u.a), vv = u01(u.b), ww = 0.f;
-    if (type != PT_TRI) {
-        const int xi = (int)(r % (uint32_t)dimx), yi = (int)(r / (uint32_t)dimx);
-        uu = ((float)xi + uu) / (float)dimx;
-        vv = ((float)yi + vv) / (float)dimy;
-    }
-    if (type == PT_VOXEL) ww = u01(philox(r, p, c2 | 1u, 0u, seed, pass).a);
-    return sample_point(g, type, uu, vv, ww);
-}
-
-// Origin and direction of diffuse ray r of primitive p from face `face` (1 top, 0
-// bottom).  Surfaces: cosine-weighted about the normal, counter (r, p, face, 0).  Voxels
-// (VOX builds only): both faces share the sample of counter (r, p, 1, 0), the third
-// coordinate comes from (r, p, 2, 0), and the bottom face flips the direction.
-template <bool VOX>
-__device__ __forceinline__ void diffuse_ray(const float4 g[4], uint32_t type, uint32_t r, uint32_t p, int face,
-                                            int dimx, int dimy, uint32_t seed, uint32_t pass, f3 *org, f3 *dir) {
-    const int ti = (int)(r % (uint32_t)dimx), pi = (int)(r / (uint32_t)dimx);
-    f3 dd;
-    if (VOX && type == PT_VOXEL) {
-        const u4 u = philox(r, p, 1u, 0u, seed, pass);
-        const float w = u01(philox(r, p, 2u, 0u, seed, pass).a);
-        dd = voxel_dir(ti, pi, dimx, dimy, u01(u.a), u01(u.b));
-        *org = sample_point(g, type, u01(u.c), u01(u.d), w);
-    } else {
-        const u4 u = philox(r, p, (uint32_t)face, 0u, seed, pass);
-        dd = diffuse_dir(xyz(g[3]), ti, pi, dimx, dimy, u01(u.a), u01(u.b));
-        *org = sample_point(g, type, u01(u.c), u01(u.d), 0.f);
-    }
-    *dir = (face == 0) ? mk(-dd.x, -dd.y, -dd.z) : dd;
-}
 
 // ------------------------------------------------------------------ direct --
 __device__ __forceinline__ bool direct_ray(const SourceDev &src, f3 org, f3 nrm, bool vox, uint32_t rx, uint32_t ry,
@@ -401,27 +162,6 @@ __global__ void __launch_bounds__(kBlock) k_direct(const DirectParams P) {
     }
 }
 
-// ------------------------------------------------------------------ diffuse --
-__device__ __forceinline__ double sky_fd(f3 dir, const SkyParams &sky, int b) {
-    float K = sky.K ? sky.K[b] : 0.f;
-    if (K > 0.f) {
-        f3 pk = mk(sky.peak[3 * b], sky.peak[3 * b + 1], sky.peak[3 * b + 2]);
-        double c = fmax(-1.0, fmin(1.0, (double)dot(pk, dir)));
-        double psi = fmax(acos(c), 3.14159265358979323846 / 180.0);
-        return pow(psi, -(double)K) * (double)(sky.knorm ? sky.knorm[b] : 1.f);
-    }
-    if (sky.prague && sky.prague[4 * b + 3] > 0.f) {
-        f3 pk = sky.peak ? mk(sky.peak[3 * b], sky.peak[3 * b + 1], sky.peak[3 * b + 2]) : mk(0.f, 0.f, 1.f);
-        const float *pr = sky.prague + 4 * b;
-        double c = fmax(-1.0, fmin(1.0, (double)dot(dir, pk)));
-        double gamma = acos(c) * 180.0 / 3.14159265358979323846;
-        double cth = fmax((double)dir.z, 0.0);
-        double pat = (1.0 + pr[0] * exp(-gamma / pr[1])) * (1.0 + (pr[2] - 1.0) * (1.0 - cth));
-        return pat * pr[3] * 3.14159265358979323846;
-    }
-    return 1.0;
-}
-
 template <int NB, bool STATS>
 __global__ void __launch_bounds__(kBlock) k_diffuse(const DiffuseParams P) {
     const uint32_t R = (uint32_t)(P.dimx * P.dimy);
@@ -474,247 +214,6 @@ __global__ void __launch_bounds__(kBlock) k_diffuse(const DiffuseParams P) {
         uint32_t key = active ? p : 0xFFFFFFFFu;
         warp_segment_add<NB>(key, v, P.Bc, G, P.Bl);
     }
-}
-
-// ------------------------------------------------------- persistent diffuse --
-// Persistent threads with dynamic ray fetch and speculative while-while traversal
-// (after Aila & Laine, "Understanding the Efficiency of Ray Traversal on GPUs",
-// HPG 2009): a lane whose ray has ended takes the next ray id from a global
-// counter at the top of the next round, so lanes do not idle until the longest
-// ray of the warp ends; leaves are postponed until every active lane has one, so
-// node visits and primitive tests run in separate, convergent loops.  Hit results
-// equal those of trace_bvh (same tests, same tie rule; only the order differs).
-// Each lane keeps a running FP64 sum for its current origin (primitive, face) and
-// adds it to G only when the origin changes.
-constexpr int32_t kSentinel = 0x7FFFFFF0;
-
-// MINB: resident blocks per SM the register allocation must allow (4, the default: 64
-// registers; 3: more registers, fewer warps).  VOX: the scene holds voxels (turbid media
-// with their own ray sampling); without it the voxel code is left out.
-template <int NB, bool RECORD, int MINB, bool VOX>
-__global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams P) {
-    unsigned long long *fetch = P.fetch;
-    const int lane = threadIdx.x & 31;
-    const uint32_t R = (uint32_t)(P.dimx * P.dimy);
-    const uint32_t per_face = P.count * R;
-    const int nf = ((P.faces & 1) ? 1 : 0) + ((P.faces & 2) ? 1 : 0);
-    const unsigned long long total = (unsigned long long)per_face * (unsigned long long)nf;
-    const uint32_t ni = (uint32_t)(P.sc.n > 1 ? P.sc.n - 1 : 1);
-    const TraceScene &sc = P.sc;
-
-    bool live = false, exhausted = false;
-    f3 o = mk(0.f, 0.f, 0.f), d = o, inv = o, ooi = o;
-    WT w = wt_setup(mk(0.f, 0.f, 1.f));
-    float best = 1e38f;
-    uint32_t bprim = 0xFFFFFFFFu;
-    int bface = 0;
-    int32_t cur = kSentinel, leaf = 0;
-    int sp = 0;
-    int32_t stack[kStack];
-    uint32_t budget = 0;
-    int wraps = 0;
-    uint32_t p = 0, rr = 0;
-    int face = 1;
-    unsigned long long rid = 0;
-    uint32_t akey = 0xFFFFFFFFu;
-    // running sums live in shared memory (one slot row per thread) to keep registers
-    // for the traversal state
-    __shared__ double s_sum[NB][kBlock];
-    double *sum_j = &s_sum[0][threadIdx.x];
-#define ACC(j) sum_j[(j) * kBlock]
-#pragma unroll
-    for (int j = 0; j < NB; ++j) ACC(j) = 0.0;
-    unsigned long long nrays = 0;
-
-    for (;;) {
-        // ---- refill lanes without a ray
-        const bool need = !live && !exhausted;
-        const unsigned m = __ballot_sync(0xffffffffu, need);
-        if (m) {
-            const int leader = __ffs(m) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(fetch, (unsigned long long)__popc(m));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (need) {
-                const unsigned long long id = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
-                if (id >= total) {
-                    exhausted = true;
-                } else {
-                    rid = id;
-                    const uint32_t fi = (uint32_t)(id / per_face);
-                    const uint32_t rem = (uint32_t)(id - (unsigned long long)fi * per_face);
-                    face = (nf == 2) ? (fi == 0 ? 1 : 0) : ((P.faces & 1) ? 1 : 0);
-                    p = P.offset + rem / R;
-                    const uint32_t r = rem % R;
-                    const int ts = sc.twosided[p];
-                    const bool skip = (face == 1 && ts == 3) || (face == 0 && ts != 1);
-                    if (!skip) {
-                        float4 g[4];
-                        load_rgen(sc, p, g);
-                        const uint32_t type = __float_as_uint(g[0].w);
-                        diffuse_ray<VOX>(g, type, r, p, face, P.dimx, P.dimy, P.seed, P.pass, &o, &d);
-                        if (VOX) rr = r;
-                        w = wt_setup(d);
-                        inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
-                        ooi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
-                        best = 1e38f;
-                        bprim = 0xFFFFFFFFu;
-                        bface = 0;
-                        cur = (sc.n > 0) ? 0 : kSentinel;
-                        leaf = 0;
-                        sp = 0;
-                        budget = 2u * (uint32_t)sc.n + 64u;
-                        wraps = 0;
-                        live = true;
-                        ++nrays;
-                    }
-                }
-            }
-        }
-        // A lane may be idle because its id was skipped by the face rule; only when every
-        // lane has run past the end of the id range is the warp done.
-        if (__all_sync(0xffffffffu, exhausted && !live)) break;
-        if (!live) continue;
-
-        // ---- internal nodes; leaves are postponed
-        while (cur >= 0 && cur != kSentinel) {
-            if ((uint32_t)cur >= ni || budget-- == 0u) {
-                raise(sc.status, ERR_BOUNDS);
-                cur = kSentinel;
-                leaf = 0;
-                break;
-            }
-            const float4 *nd = sc.nodes + 4 * (size_t)cur;
-            const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
-            int32_t c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
-            float tn0, tn1;
-            const bool h0 = c0 != kEmptyChild &&
-                            slab_node(ooi, inv, mk(n0.x, n0.y, n0.z), mk(n0.w, n1.x, n1.y), 1e-4f, best, &tn0);
-            const bool h1 = c1 != kEmptyChild &&
-                            slab_node(ooi, inv, mk(n1.z, n1.w, n2.x), mk(n2.y, n2.z, n2.w), 1e-4f, best, &tn1);
-            if (!h0 && !h1) {
-                cur = sp > 0 ? stack[--sp] : kSentinel;
-            } else {
-                cur = h0 ? c0 : c1;
-                if (h0 && h1) {
-                    int32_t farc = c1;
-                    if (tn1 < tn0) {
-                        cur = c1;
-                        farc = c0;
-                    }
-                    if (sp >= kStack) {
-                        raise(sc.status, ERR_STACK);
-                        cur = kSentinel;
-                        leaf = 0;
-                        break;
-                    }
-                    stack[sp++] = farc;
-                }
-            }
-            if (cur < 0 && leaf == 0) {
-                leaf = cur;
-                cur = sp > 0 ? stack[--sp] : kSentinel;
-            }
-            if (__all_sync(__activemask(), leaf != 0)) break;
-        }
-        // ---- primitive tests
-        while (leaf != 0) {
-            const uint32_t slot = (uint32_t)(~leaf);
-            if (slot < (uint32_t)sc.n) {
-                float t;
-                int fc;
-                uint32_t orig;
-                const VoxKey vk{rr, p, (uint32_t)face | ((uint32_t)wraps << 16), P.seed, P.pass};
-                if (rec_hit<VOX>(sc.rec, slot, w, o, d, inv, 1e-4f, best, vk, &t, &fc, &orig)) {
-                    if (bprim == 0xFFFFFFFFu || t < best || (t == best && orig < bprim)) {
-                        best = t;
-                        bprim = orig;
-                        bface = fc;
-                    }
-                }
-            } else {
-                raise(sc.status, ERR_BOUNDS);
-            }
-            leaf = 0;
-            if (cur < 0) {
-                leaf = cur;
-                cur = sp > 0 ? stack[--sp] : kSentinel;
-            }
-        }
-        if (cur != kSentinel || leaf != 0) continue;  // traversal of this ray goes on next round
-
-        // ---- periodic walls: wrap and restart, or finish the ray
-        bool lost = false;
-        if (sc.nbbox > 0) {
-            float tb;
-            int which = -1;
-            if (wall_closest(sc, o, d, 1e-4f, (bprim != 0xFFFFFFFFu) ? best : 1e38f, &tb, &which) &&
-                (bprim == 0xFFFFFFFFu || tb < best)) {
-                if (wraps >= 9) {
-                    lost = true;
-                } else {
-                    f3 hp = add(o, scl(d, tb));
-                    if ((sc.periodic_x == 1.f) && which < 2) {
-                        float width = sc.bbox[4].x - sc.bbox[0].x;
-                        hp.x = hp.x + ((which == 0) ? width : -width);
-                    } else {
-                        int yb = (sc.periodic_x == 1.f) ? 2 : 0;
-                        float width = sc.bbox[4 * (yb + 1)].y - sc.bbox[4 * yb].y;
-                        hp.y = hp.y + ((which == yb) ? width : -width);
-                    }
-                    o = hp;
-                    ooi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
-                    best = 1e38f;
-                    bprim = 0xFFFFFFFFu;
-                    cur = 0;
-                    sp = 0;
-                    budget = 2u * (uint32_t)sc.n + 64u;
-                    ++wraps;
-                    continue;
-                }
-            }
-        }
-        // ---- value of the finished ray, added to the lane's running sum
-        live = false;
-        if (RECORD) {
-            P.hits[rid] = lost ? kLostCode : ((bprim == 0xFFFFFFFFu) ? kMissCode : ((bprim << 1) | (uint32_t)bface));
-            continue;
-        }
-        if (lost) continue;
-        const uint32_t key = 2u * p + (uint32_t)face;
-        if (key != akey) {
-            if (akey != 0xFFFFFFFFu) {
-                double *dst = ((akey & 1u) ? P.Gt : P.Gb) + (size_t)(akey >> 1) * P.Bl;
-#pragma unroll
-                for (int j = 0; j < NB; ++j)
-                    if (j < P.Bc && ACC(j) != 0.0) atomicAdd(dst + j, ACC(j));
-            }
-            akey = key;
-#pragma unroll
-            for (int j = 0; j < NB; ++j) ACC(j) = 0.0;
-        }
-        if (bprim != 0xFFFFFFFFu) {
-            const float *src = (bface ? P.otop : P.obot) + (size_t)bprim * P.Bl;
-#pragma unroll
-            for (int j = 0; j < NB; ++j)
-                if (j < P.Bc) ACC(j) += (double)__ldg(src + j);
-        } else {
-#pragma unroll
-            for (int j = 0; j < NB; ++j)
-                if (j < P.Bc) {
-                    float fl = P.sky.flux[j];
-                    if (fl > 0.f) ACC(j) += sky_fd(d, P.sky, j) * (double)fl;
-                }
-        }
-    }
-    if (akey != 0xFFFFFFFFu) {
-        double *dst = ((akey & 1u) ? P.Gt : P.Gb) + (size_t)(akey >> 1) * P.Bl;
-#pragma unroll
-        for (int j = 0; j < NB; ++j)
-            if (j < P.Bc && ACC(j) != 0.0) atomicAdd(dst + j, ACC(j));
-    }
-    if (sc.rays && nrays) atomicAdd(sc.rays, nrays);
-#undef ACC
 }
 
 // ------------------------------------------------------------------ testing --
@@ -1031,63 +530,32 @@ static cudaError_t direct_impl(const DirectParams &p, int max_blocks, cudaStream
     return cudaGetLastError();
 }
 
-static int ps_min_blocks() {
+// Default diffuse variant: the persistent 4-wide traversal; HRT_TRAVERSAL=simple selects
+// the one-ray-per-thread kernel and HRT_TRAVERSAL=bvh2 the persistent binary traversal.
+static int default_variant() {
     static int v = -1;
     if (v < 0) {
-        const char *e = getenv("HRT_PS_MINB");
-        v = (e && e[0] == '3') ? 3 : 4;
+        const char *e = getenv("HRT_TRAVERSAL");
+        v = (e && e[0] == 's') ? DV_SIMPLE : ((e && e[0] == 'b') ? DV_PS4 : DV_W4);
     }
     return v;
 }
 
-template <int NB, int MINB, bool VOX>
-static cudaError_t diffuse_ps_launch_b(const DiffuseParams &p, cudaStream_t s) {
-    static int blocks_per_sm = 0, sms = 0;
-    if (blocks_per_sm == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<NB, false, MINB, VOX>, kBlock, 0);
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
-    }
-    cudaError_t e = cudaMemsetAsync(p.fetch, 0, sizeof(unsigned long long), s);
-    if (e != cudaSuccess) return e;
-    k_diffuse_ps<NB, false, MINB, VOX><<<sms * blocks_per_sm, kBlock, 0, s>>>(p);
-    return cudaGetLastError();
-}
-
-// minb: 4 or 3 (resident blocks per SM the register budget allows); 0 = the default.
-template <int NB>
-static cudaError_t diffuse_ps_launch(const DiffuseParams &p, int minb, cudaStream_t s) {
-    if (p.sc.voxels) return diffuse_ps_launch_b<NB, 4, true>(p, s);
-    if (minb == 0) minb = ps_min_blocks();
-    return minb == 4 ? diffuse_ps_launch_b<NB, 4, false>(p, s) : diffuse_ps_launch_b<NB, 3, false>(p, s);
-}
-
-static bool use_persistent() {
-    static int v = -1;
-    if (v < 0) {
-        const char *e = getenv("HRT_TRAVERSAL");
-        v = (e && e[0] == 's') ? 0 : 1;  // "simple" selects the one-ray-per-thread kernel
-    }
-    return v == 1;
-}
-
-// variant: DV_DEFAULT (persistent unless HRT_TRAVERSAL=simple), DV_PS4 / DV_PS3 (persistent,
-// 4 or 3 resident blocks per SM), DV_SIMPLE (one ray per thread).
+// variant: one of DiffuseVariant (hrt_internal.h); DV_DEFAULT resolves to default_variant().
 template <bool STATS>
 static cudaError_t diffuse_impl(const DiffuseParams &p, int variant, int max_blocks, cudaStream_t s) {
     int64_t total = (int64_t)p.count * p.dimx * p.dimy;
     if (total <= 0 || p.Bc <= 0) return cudaSuccess;
-    const bool persistent = variant == DV_DEFAULT ? use_persistent() : variant != DV_SIMPLE;
-    if (!STATS && p.fetch && persistent) {
-        const int minb = variant == DV_PS4 ? 4 : (variant == DV_PS3 ? 3 : 0);
-        if (p.Bc <= 1) return diffuse_ps_launch<1>(p, minb, s);
-        if (p.Bc <= 2) return diffuse_ps_launch<2>(p, minb, s);
-        if (p.Bc <= 4) return diffuse_ps_launch<4>(p, minb, s);
-        if (p.Bc <= 8) return diffuse_ps_launch<8>(p, minb, s);
-        if (p.Bc <= 16) return diffuse_ps_launch<16>(p, minb, s);
-        return cudaErrorInvalidValue;
+    if (variant == DV_DEFAULT) variant = default_variant();
+    if ((variant == DV_W4 || variant == DV_W43) && !p.sc.nodes4) variant = DV_PS4;
+    if (p.fetch && variant != DV_SIMPLE) {
+        if (STATS) {
+            if (p.Bc <= 4 && variant == DV_W4) return launch_ps_stats(p, s);
+        } else if (p.sc.voxels) {
+            return launch_ps_voxels(p, variant, s);
+        } else {
+            return launch_ps_accumulate(p, variant, s);
+        }
     }
     unsigned nb = blocks_for(total, kBlock);
     if ((int)nb > max_blocks) nb = (unsigned)max_blocks;
@@ -1113,8 +581,8 @@ cudaError_t launch_diffuse_variant(const DiffuseParams &p, int variant, int max_
 cudaError_t launch_direct_stats(const DirectParams &p, int max_blocks, cudaStream_t s) {
     return direct_impl<true>(p, max_blocks, s);
 }
-cudaError_t launch_diffuse_stats(const DiffuseParams &p, int max_blocks, cudaStream_t s) {
-    return diffuse_impl<true>(p, DV_DEFAULT, max_blocks, s);
+cudaError_t launch_diffuse_stats(const DiffuseParams &p, int variant, int max_blocks, cudaStream_t s) {
+    return diffuse_impl<true>(p, variant, max_blocks, s);
 }
 
 cudaError_t launch_trace_rays(const TraceScene &sc, int64_t nrays, const float *o, const float *d, float tmin,
@@ -1238,31 +706,6 @@ cudaError_t launch_direct_sweep(const SweepDirectParams &p, int max_blocks, cuda
     if ((int)nb > max_blocks) nb = (unsigned)max_blocks;
     k_direct_sweep<<<nb, kBlock, 0, s>>>(p);
     return cudaGetLastError();
-}
-
-template <int MINB>
-static cudaError_t diffuse_record_b(const DiffuseParams &q, cudaStream_t s) {
-    static int blocks_per_sm = 0, sms = 0;
-    if (blocks_per_sm == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<1, true, MINB, false>, kBlock, 0);
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
-    }
-    cudaError_t e = cudaMemsetAsync(q.fetch, 0, sizeof(unsigned long long), s);
-    if (e != cudaSuccess) return e;
-    k_diffuse_ps<1, true, MINB, false><<<sms * blocks_per_sm, kBlock, 0, s>>>(q);
-    return cudaGetLastError();
-}
-
-// variant: DV_PS4 for 4 resident blocks per SM, anything else 3 (the default).
-cudaError_t launch_diffuse_record(const DiffuseParams &p, uint32_t *hits, int variant, cudaStream_t s) {
-    if ((long long)p.count * p.dimx * p.dimy <= 0) return cudaSuccess;
-    DiffuseParams q = p;
-    q.hits = hits;
-    q.Bc = 1;
-    return variant == DV_PS4 ? diffuse_record_b<4>(q, s) : diffuse_record_b<3>(q, s);
 }
 
 cudaError_t launch_gather(const GatherParams &p, cudaStream_t s) {

@@ -228,8 +228,10 @@ int hrt_server_destroy(hrt_server *s);
  * ray per thread); the first pass of each shape (rays per face, faces, bands, scene
  * size) of at least 2e7 rays times them on a sample of its rays and keeps the fastest
  * for later passes, solves and sweep graphs of that shape.  mode 1 (default) tunes,
- * 0 uses the fixed default, 2 forgets earlier choices and tunes again.  Variants give
- * the same results up to the order of FP64 sums. */
+ * 0 uses the fixed default, 2 forgets earlier choices and tunes again, 16 + v forces
+ * variant v (1 binary nodes / 4 blocks per SM, 2 binary / 3, 3 one ray per thread,
+ * 4 compressed 4-wide / 4, 5 compressed 4-wide / 3).  Variants give the same results up
+ * to the order of FP64 sums. */
 int hrt_set_tuning(hrt_context *ctx, int mode);
 /* Text log of the tuner's trials and choices, one line per shape; returns the bytes
  * needed (including the terminating zero); buf may be NULL. */
@@ -249,7 +251,8 @@ int hrt_gen_rays(hrt_context *ctx, int kind, uint32_t seed, uint32_t pass, int32
 int hrt_get_bvh(hrt_context *ctx, uint64_t *codes, uint32_t *perm, uint32_t *nodes);
 /* Measurement controls (no counterpart in the reference; used by the benchmark).
  * flags bit 0: run the statistics variants of the trace kernels, which count BVH
- * node visits and primitive tests; bit 1: time every trace-kernel launch with CUDA
+ * node visits and primitive tests (of the tree the default kernels traverse; with bit 2
+ * also set, of the binary tree); bit 1: time every trace-kernel launch with CUDA
  * events on the context's stream.  Setting flags also resets the accumulators.
  * hrt_get_measure: [0] direct launches, [1] direct ms, [2] diffuse launches,
  * [3] diffuse ms, [4] node visits, [5] primitive tests. */
