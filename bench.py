@@ -336,7 +336,7 @@ def run_stress(args, stream, device=0):
     t_build = time.perf_counter() - t0
     desc = rad.solve_description(["NIR"])
     ctx = rad.ctx
-    ctx.run_band(desc, out=False)
+    ctx.run_band(desc, out=False)  # untimed: tuning, first touch
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
@@ -345,12 +345,23 @@ def run_stress(args, stream, device=0):
     torch.cuda.synchronize()
     t = ev0.elapsed_time(ev1) / 1e3
     st = ctx.last_stats()
+    tuning = [x for x in ctx.tuning_report().splitlines() if x.startswith("accumulate")]
+    # traversal counts (untimed) on the same workload scaled to 5 % of the primitives
+    small, _ = stress_model(0.05 * args.stress_scale, device=device)
+    small.setSeed(99)
+    small.updateGeometry()
+    small.ctx.set_measure(1)
+    small.ctx.run_band(small.solve_description(["NIR"]), out=False)
+    meas = small.ctx.get_measure()
+    small_rays = max(small.ctx.last_stats()["rays"], 1)
     counts = np.bincount(sc.ptype, minlength=5)
     return {"workload": f"deep scatter: {int(counts[1])} triangles, {int(counts[0]) - 1} patches, "
                         f"{int(counts[2])} disks, {int(counts[4])} voxels (LAD U[0,2]) + ground, NIR, "
                         "100 direct / 400 diffuse rays, depth 20, FP64 residual stop 1e-6",
             "primitives": int(sc.n), "s_per_solve": t, "rays_per_solve": st["rays"], "rays_per_s": st["rays"] / t,
-            "scattering_iterations": st["iterations"], "kernels": st["kernels"], "setup_build_s": t_build}
+            "scattering_iterations": st["iterations"], "kernels": st["kernels"], "setup_build_s": t_build,
+            "node_visits_per_ray_5pct": meas["node_visits"] / small_rays,
+            "prim_tests_per_ray_5pct": meas["prim_tests"] / small_rays, "autotune": tuning}
 
 
 def run_gpu(args):
