@@ -224,11 +224,12 @@ def run_batched(rad, ctx, desc, stream, args):
 
 
 def run_served(args, device=0):
-    """Served stream: Poisson arrivals at 50/s of homogeneous-canopy scenes with sizes
-    log-uniform in [2k, 2M] (patch:triangle 1:1), 1-4 bands, sun zenith U[0,75], 50-400
-    diffuse rays, 100 direct rays, scattering depth 1, through the continuous-batching
-    server; against the plain per-solve path (geometry upload + BVH build + solve per
-    request, one at a time) on the same requests."""
+    """Served stream: Poisson arrivals at 50/s of requests on homogeneous-canopy scenes
+    with sizes log-uniform in [2k, 2M] (patch:triangle 1:1), LAI U[0.5, 5], per scene 1-4
+    bands, 50-400 diffuse rays and a seed; per request a sun at zenith U[0,75]; 100 direct
+    rays, scattering depth 1; through the continuous-batching server, against the plain
+    per-solve path (geometry upload + BVH build + solve per request, one at a time) on the
+    same requests."""
     from helios_gb300 import _hrt, scenes
 
     sizes, lais, reqs = scenes.served_stream(n_requests=args.serve_requests, rate=50.0, n_scenes=args.serve_scenes,
@@ -246,7 +247,7 @@ def run_served(args, device=0):
         return rho, tau
 
     depth = 1
-    srv = _hrt.Server(device=device, workers=8, hbm_budget=64 << 30)
+    srv = _hrt.Server(device=device, workers=32, hbm_budget=64 << 30)
     for k in used:
         rho, tau = mats(built[k])
         srv.add_scene(k, built[k].T, built[k].ptype, built[k].twosided, rho, tau)
@@ -263,16 +264,19 @@ def run_served(args, device=0):
     span = max(x["done"] for x in res) - min(x["arrival"] for x in res)
     st = srv.stats()
     srv.close()
-    # plain per-solve path on a prefix of the same requests
-    nplain = min(len(reqs), args.serve_plain)
+    # plain per-solve path on the same requests (a prefix when --serve-plain is smaller)
+    nplain = min(len(reqs), args.serve_plain) if args.serve_plain > 0 else len(reqs)
     ctx = _hrt.Context(device)
     t0 = time.perf_counter()
+    cur = None
     for r in reqs[:nplain]:
         sc = built[r["scene"]]
         rho, tau = mats(sc)
         bl = int(r["bands"].sum())
-        ctx.update_geometry(sc.T, sc.ptype, sc.twosided)
-        ctx.build_accel()
+        if r["scene"] != cur:  # the plain path rebuilds only when the scene changes
+            ctx.update_geometry(sc.T, sc.ptype, sc.twosided)
+            ctx.build_accel()
+            cur = r["scene"]
         ctx.run_band({"band_launch": r["bands"], "sources": [{"type": 0, "position": tuple(r["sun"])}],
                       "source_flux": r["direct"], "rho": rho, "tau": tau, "diffuse_flux": r["diffuse"],
                       "direct_rays": np.full(bl, 100), "diffuse_rays": np.full(bl, r["diffuse_rays"]),
@@ -286,6 +290,7 @@ def run_served(args, device=0):
             "offered_rate_per_s": 50.0, "solves_per_s": served_sps, "rays_per_s": rays / span,
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
             "wall_s": wall, "bvh_builds": st["builds"], "evictions": st["evictions"],
+            "batches": st["batches"], "requests_per_batch": st["batched_requests"] / max(st["batches"], 1),
             "plain_solves_per_s": plain_sps, "plain_requests_timed": nplain,
             "speedup_solves_per_s": served_sps / plain_sps}
 
@@ -497,7 +502,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the day-sweep measurement")
     ap.add_argument("--serve-requests", type=int, default=100, help="served-stream requests (0 = skip)")
     ap.add_argument("--serve-scenes", type=int, default=16, help="distinct scenes in the served stream")
-    ap.add_argument("--serve-plain", type=int, default=30, help="requests timed on the plain per-solve path")
+    ap.add_argument("--serve-plain", type=int, default=0,
+                    help="requests timed on the plain per-solve path (0 = all of them)")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--trees", type=int, nargs=2, default=(20, 10), help="orchard grid (default 20 x 10 = 1M leaves)")
     ap.add_argument("--stress", action="store_true", help="also time the deep-scattering stress workload")

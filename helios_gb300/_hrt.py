@@ -26,6 +26,7 @@ EXPORTS = [
     "hrt_source_rotation", "hrt_set_measure", "hrt_get_measure", "hrt_build_accel_static", "hrt_run_sweep",
     "hrt_server_create", "hrt_server_add_scene", "hrt_server_submit", "hrt_server_start", "hrt_server_wait",
     "hrt_server_result", "hrt_server_stats", "hrt_server_destroy", "hrt_set_tuning", "hrt_tuning_report",
+    "hrt_set_ray_budget",
 ]
 
 
@@ -113,6 +114,7 @@ def load(path: str | None = None):
         "hrt_run_band": (C.c_int, [VP, C.POINTER(BandSolve), VP]),
         "hrt_last_stats": (C.c_int, [VP, VP, C.c_int]),
         "hrt_set_tuning": (C.c_int, [VP, C.c_int]),
+        "hrt_set_ray_budget": (C.c_int, [VP, C.c_uint32]),
         "hrt_tuning_report": (C.c_size_t, [VP, VP, C.c_size_t]),
         "hrt_device_status": (C.c_int, [VP, C.POINTER(C.c_uint32), C.c_int]),
         "hrt_trace_rays": (C.c_int, [VP, C.c_int64, VP, VP, C.c_float, C.c_float, C.c_int, VP, VP, VP]),
@@ -364,6 +366,10 @@ class Context:
         """1: tune kernel variants per pass shape (default); 0: fixed default; 2: retune."""
         self.check(self.lib.hrt_set_tuning(self.h, int(mode)))
 
+    def set_ray_budget(self, rays_per_thread: int):
+        """Rays a thread of the persistent trace takes before its block retires (0: no limit)."""
+        self.check(self.lib.hrt_set_ray_budget(self.h, int(rays_per_thread)))
+
     def tuning_report(self) -> str:
         k = self.lib.hrt_tuning_report(self.h, None, 0)
         buf = C.create_string_buffer(int(k))
@@ -471,9 +477,10 @@ class Server:
                 "rays": rays.value, "flux": flux}
 
     def stats(self):
-        out = np.zeros(4, np.float64)
-        self.check(self.lib.hrt_server_stats(self.h, ptr(out), 4), "stats")
-        return {"builds": int(out[0]), "evictions": int(out[1]), "resident_bytes": out[2], "budget": out[3]}
+        out = np.zeros(6, np.float64)
+        self.check(self.lib.hrt_server_stats(self.h, ptr(out), 6), "stats")
+        return {"builds": int(out[0]), "evictions": int(out[1]), "resident_bytes": out[2], "budget": out[3],
+                "batches": int(out[4]), "batched_requests": int(out[5])}
 
     def close(self):
         if getattr(self, "h", None):

@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -23,16 +24,24 @@ using namespace hrt;
 
 namespace {
 
+// Stream on which buffers being destroyed are released (set by hrt_destroy); without it
+// they are released with cudaFree.
+thread_local cudaStream_t g_release_stream = nullptr;
+
+// Device buffer of a context.  Allocation is stream-ordered (cudaMallocAsync /
+// cudaFreeAsync on the context's stream): cudaMalloc / cudaFree can wait for the whole
+// device, which would stall a context behind long kernels of other contexts sharing the
+// GPU (the served stream runs many).
 struct DevBuf {
     void *p = nullptr;
     size_t cap = 0;
-    cudaError_t ensure(size_t bytes) {
+    cudaError_t ensure(cudaStream_t s, size_t bytes) {
         if (bytes <= cap && p) return cudaSuccess;
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, s);
         p = nullptr;
         cap = 0;
         size_t want = bytes ? bytes : 16;
-        cudaError_t e = cudaMalloc(&p, want);
+        cudaError_t e = cudaMallocAsync(&p, want, s);
         if (e == cudaSuccess) cap = want;
         return e;
     }
@@ -41,12 +50,30 @@ struct DevBuf {
         return (T *)p;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (g_release_stream) cudaFreeAsync(p, g_release_stream);
+            else cudaFree(p);
+        }
         p = nullptr;
         cap = 0;
     }
     ~DevBuf() { release(); }
 };
+
+// Keep up to 16 GB of freed stream-ordered memory in the device's default pool, so that
+// growing a buffer does not unmap and map memory at every synchronisation.
+void keep_pool(int device) {
+    static std::mutex mu;
+    static std::vector<int> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (std::find(done.begin(), done.end(), device) != done.end()) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = 16ull << 30;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    done.push_back(device);
+}
 
 // Surface area of a primitive in FP64 from its FP32 transform (a voxel's: its leaf area,
 // LAD x volume).  Triangles span half the parallelogram of their two edges, disks are
@@ -108,6 +135,8 @@ struct hrt_context {
     cudaGraphExec_t sw_exec = nullptr;
     std::string sw_key;
     int sw_kernels = 0;
+    // rays a lane of the persistent trace takes before its block retires (0: no limit)
+    uint32_t lane_budget = 0;
     // kernel-variant tuner: choice per pass shape, and a log of the trials
     int tune = 1;
     std::map<std::string, int> tuned;
@@ -199,9 +228,9 @@ int check_built(hrt_context *ctx) {
 }
 
 int sync_and_status(hrt_context *ctx) {
-    CU(cudaStreamSynchronize(ctx->stream));
     uint32_t st = 0;
-    CU(cudaMemcpy(&st, ctx->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpyAsync(&st, ctx->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
     if (st) {
         CU(cudaMemsetAsync(ctx->status.p, 0, sizeof(uint32_t), ctx->stream));
         char buf[160];
@@ -215,16 +244,16 @@ int sync_and_status(hrt_context *ctx) {
 // Radiation buffers for n x Bl values.
 int ensure_buffers(hrt_context *ctx, int Bl) {
     size_t m = (size_t)std::max(ctx->n, 1) * (size_t)std::max(Bl, 1);
-    CU(ctx->rin.ensure(m * sizeof(double)));
-    CU(ctx->stop.ensure(m * sizeof(double)));
-    CU(ctx->sbot.ensure(m * sizeof(double)));
-    CU(ctx->otop.ensure(m * sizeof(float)));
-    CU(ctx->obot.ensure(m * sizeof(float)));
-    CU(ctx->ftop.ensure(m * sizeof(double)));
-    CU(ctx->fbot.ensure(m * sizeof(double)));
-    CU(ctx->Gt.ensure(m * sizeof(double)));
-    CU(ctx->Gb.ensure(m * sizeof(double)));
-    CU(ctx->fin.ensure(m * sizeof(float)));
+    CU(ctx->rin.ensure(ctx->stream, m * sizeof(double)));
+    CU(ctx->stop.ensure(ctx->stream, m * sizeof(double)));
+    CU(ctx->sbot.ensure(ctx->stream, m * sizeof(double)));
+    CU(ctx->otop.ensure(ctx->stream, m * sizeof(float)));
+    CU(ctx->obot.ensure(ctx->stream, m * sizeof(float)));
+    CU(ctx->ftop.ensure(ctx->stream, m * sizeof(double)));
+    CU(ctx->fbot.ensure(ctx->stream, m * sizeof(double)));
+    CU(ctx->Gt.ensure(ctx->stream, m * sizeof(double)));
+    CU(ctx->Gb.ensure(ctx->stream, m * sizeof(double)));
+    CU(ctx->fin.ensure(ctx->stream, m * sizeof(float)));
     return HRT_OK;
 }
 
@@ -240,7 +269,7 @@ int upload_sky(hrt_context *ctx, int Bl, const float *flux, const float *K, cons
         for (int k = 0; k < 3; ++k) h[3 * Bn + 3 * b + k] = peak ? peak[3 * b + k] : (k == 2 ? 1.f : 0.f);
         for (int k = 0; k < 4; ++k) h[6 * Bn + 4 * b + k] = prague ? prague[4 * b + k] : 0.f;
     }
-    CU(ctx->sky.ensure(h.size() * sizeof(float)));
+    CU(ctx->sky.ensure(ctx->stream, h.size() * sizeof(float)));
     CU(cudaMemcpyAsync(ctx->sky.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
     float *d = ctx->sky.as<float>();
     sp->flux = d;
@@ -252,7 +281,7 @@ int upload_sky(hrt_context *ctx, int Bl, const float *flux, const float *K, cons
 }
 
 int upload_flags(hrt_context *ctx, int Bg, const uint8_t *flags) {
-    CU(ctx->flags.ensure((size_t)std::max(Bg, 1)));
+    CU(ctx->flags.ensure(ctx->stream, (size_t)std::max(Bg, 1)));
     CU(cudaMemcpyAsync(ctx->flags.p, flags, (size_t)Bg, cudaMemcpyHostToDevice, ctx->stream));
     return HRT_OK;
 }
@@ -274,7 +303,7 @@ int direct_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp,
     if (ctx->src_flux_count < (size_t)ctx->S * Bl)
         return fail(ctx, HRT_EINVAL, "source fluxes not uploaded for every source and launched band");
     size_t ng = (size_t)ctx->n * ctx->S * 2;
-    CU(ctx->Gd.ensure(ng * sizeof(double)));
+    CU(ctx->Gd.ensure(ctx->stream, ng * sizeof(double)));
     CU(cudaMemsetAsync(ctx->Gd.p, 0, ng * sizeof(double), ctx->stream));
     DirectParams P;
     P.sc = scene_of(ctx);
@@ -316,7 +345,7 @@ int direct_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp,
 // blocks per SM -- 64 registers with a few spills, or ~80 without -- and one ray per
 // thread).  Which is fastest depends on the scene (BVH depth, primitive mix) and on the
 // band count, so the first pass of each shape is timed on a sample: the rays of the
-// first max(count/8, 4096) primitives, written to scratch sums (or the hit buffer of a
+// first max(count/32, 4096) primitives, written to scratch sums (or the hit buffer of a
 // recorded pass, rewritten by the real pass) and not counted.  The choice is cached
 // per (mode, n, count, rays per face, faces, bands, voxels); passes under kTuneMinRays
 // rays keep the default.  Choices differ only in the order of the FP64 atomic sums.
@@ -359,29 +388,32 @@ int tuned_variant(hrt_context *ctx, const DiffuseParams &P0, bool record, int *v
     else cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_PS4, DV_PS3, DV_SIMPLE}
                    : std::vector<int>{DV_PS4, DV_PS3, DV_SIMPLE};
     DiffuseParams P = P0;
-    P.count = std::min(P0.count, std::max(P0.count / 8u, 4096u));
+    P.count = std::min(P0.count, std::max(P0.count / 32u, 4096u));
     P.sc.rays = nullptr;
     P.sc.visits = nullptr;
     if (!record) {
         const size_t m = (size_t)ctx->n * P0.Bl;
-        CU(ctx->tune_g.ensure(2 * m * sizeof(double)));
+        CU(ctx->tune_g.ensure(ctx->stream, 2 * m * sizeof(double)));
         P.Gt = ctx->tune_g.as<double>();
         P.Gb = P.Gt + m;
     }
+    DiffuseParams W = P;  // warm-up launch (loads the kernel) on a smaller sample, same scratch outputs
+    W.count = std::min(P.count, std::max(P.count / 8u, 1024u));
     cudaEvent_t a = nullptr, b = nullptr;
     CU(cudaEventCreate(&a));
     CU(cudaEventCreate(&b));
-    auto launch = [&](int v) {
-        return record ? launch_diffuse_record(P, P0.hits, v, ctx->stream)
-                      : launch_diffuse_variant(P, v, max_blocks(ctx), ctx->stream);
+    auto launch_on = [&](const DiffuseParams &Q, int v) {
+        return record ? launch_diffuse_record(Q, P0.hits, v, ctx->stream)
+                      : launch_diffuse_variant(Q, v, max_blocks(ctx), ctx->stream);
     };
+    auto launch = [&](int v) { return launch_on(P, v); };
     int best = cand[0];
     float best_ms = 1e30f;
     std::string line = std::string(key) + ":";
     cudaError_t e = cudaSuccess;
     for (int v : cand) {
         float ms = 0.f;
-        if ((e = launch(v)) != cudaSuccess) break;  // first launch also loads the kernel
+        if ((e = launch_on(W, v)) != cudaSuccess) break;  // loads the kernel
         if ((e = cudaEventRecord(a, ctx->stream)) != cudaSuccess || (e = launch(v)) != cudaSuccess ||
             (e = cudaEventRecord(b, ctx->stream)) != cudaSuccess || (e = cudaEventSynchronize(b)) != cudaSuccess ||
             (e = cudaEventElapsedTime(&ms, a, b)) != cudaSuccess)
@@ -431,8 +463,9 @@ int diffuse_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp
     P.sky = sky;
     P.Gt = ctx->Gt.as<double>();
     P.Gb = ctx->Gb.as<double>();
-    CU(ctx->fetch.ensure(sizeof(unsigned long long)));
+    CU(ctx->fetch.ensure(ctx->stream, sizeof(unsigned long long)));
     P.fetch = ctx->fetch.as<unsigned long long>();
+    P.lane_budget = ctx->lane_budget;
     P.hits = nullptr;
     int variant = DV_DEFAULT, r;
     if ((r = tuned_variant(ctx, P, false, &variant))) return r;
@@ -490,13 +523,19 @@ int hrt_create(hrt_context **out, int device) {
         return HRT_ECUDA;
     }
     ctx->stream = ctx->own;
-    if (ctx->status.ensure(sizeof(uint32_t)) != cudaSuccess || ctx->counter.ensure(sizeof(unsigned long long)) != cudaSuccess) {
+    keep_pool(device);
+    if (ctx->status.ensure(ctx->stream, sizeof(uint32_t)) != cudaSuccess || ctx->counter.ensure(ctx->stream, sizeof(unsigned long long)) != cudaSuccess) {
         cudaStreamDestroy(ctx->own);
         delete ctx;
         return HRT_ENOMEM;
     }
-    cudaMemset(ctx->status.p, 0, sizeof(uint32_t));
-    cudaMemset(ctx->counter.p, 0, sizeof(unsigned long long));
+    cudaMemsetAsync(ctx->status.p, 0, sizeof(uint32_t), ctx->stream);
+    cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), ctx->stream);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        cudaStreamDestroy(ctx->own);
+        delete ctx;
+        return HRT_ECUDA;
+    }
     *out = ctx;
     return HRT_OK;
 }
@@ -504,10 +543,15 @@ int hrt_create(hrt_context **out, int device) {
 int hrt_destroy(hrt_context *ctx) {
     if (!ctx) return HRT_EINVAL;
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
+    cudaStream_t s = ctx->stream, own = ctx->own;
+    cudaStreamSynchronize(s);
     if (ctx->sw_exec) cudaGraphExecDestroy(ctx->sw_exec);
-    if (ctx->own) cudaStreamDestroy(ctx->own);
+    collect_timings(ctx);
+    g_release_stream = s;  // buffers are released on the context's stream
     delete ctx;
+    g_release_stream = nullptr;
+    cudaStreamSynchronize(s);
+    if (own) cudaStreamDestroy(own);
     return HRT_OK;
 }
 
@@ -515,6 +559,8 @@ const char *hrt_last_error(const hrt_context *ctx) { return ctx ? ctx->err.c_str
 
 int hrt_set_stream(hrt_context *ctx, void *stream) {
     if (!ctx) return HRT_EINVAL;
+    CU(cudaSetDevice(ctx->device));
+    CU(cudaStreamSynchronize(ctx->stream));  // buffers allocated on the old stream are ready
     ctx->stream = stream ? (cudaStream_t)stream : ctx->own;
     return HRT_OK;
 }
@@ -539,10 +585,10 @@ int hrt_update_geometry(hrt_context *ctx, const hrt_geometry *g) {
     }
     CU(cudaSetDevice(ctx->device));
     size_t n = (size_t)g->n;
-    CU(ctx->T.ensure(std::max<size_t>(n, 1) * 16 * sizeof(float)));
-    CU(ctx->type.ensure(std::max<size_t>(n, 1) * sizeof(uint32_t)));
-    CU(ctx->twosided.ensure(std::max<size_t>(n, 1)));
-    CU(ctx->area.ensure(std::max<size_t>(n, 1) * sizeof(double)));
+    CU(ctx->T.ensure(ctx->stream, std::max<size_t>(n, 1) * 16 * sizeof(float)));
+    CU(ctx->type.ensure(ctx->stream, std::max<size_t>(n, 1) * sizeof(uint32_t)));
+    CU(ctx->twosided.ensure(ctx->stream, std::max<size_t>(n, 1)));
+    CU(ctx->area.ensure(ctx->stream, std::max<size_t>(n, 1) * sizeof(double)));
     ctx->h_twosided.assign(g->twosided, g->twosided + n);
     for (uint32_t i : voxels) ctx->h_twosided[i] = 1;  // a voxel launches both directions of each sample
     // primitive areas (voxels: leaf area) weight the scattering residual
@@ -556,7 +602,7 @@ int hrt_update_geometry(hrt_context *ctx, const hrt_geometry *g) {
         CU(cudaMemcpyAsync(ctx->area.p, area.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     }
     if (!voxels.empty()) {
-        CU(ctx->lad.ensure(n * sizeof(float)));
+        CU(ctx->lad.ensure(ctx->stream, n * sizeof(float)));
         CU(cudaMemcpyAsync(ctx->lad.p, g->voxel_lad, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
     }
     ctx->h_voxels.swap(voxels);
@@ -567,7 +613,7 @@ int hrt_update_geometry(hrt_context *ctx, const hrt_geometry *g) {
         std::vector<float4> q((size_t)g->nbbox * 4);
         for (int i = 0; i < g->nbbox * 4; ++i)
             q[i] = make_float4(g->bbox_vertices[3 * i], g->bbox_vertices[3 * i + 1], g->bbox_vertices[3 * i + 2], 0.f);
-        CU(ctx->bbox.ensure(q.size() * sizeof(float4)));
+        CU(ctx->bbox.ensure(ctx->stream, q.size() * sizeof(float4)));
         CU(cudaMemcpyAsync(ctx->bbox.p, q.data(), q.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
     }
     ctx->n = g->n;
@@ -587,12 +633,12 @@ int hrt_build_accel(hrt_context *ctx) {
         return HRT_OK;
     }
     size_t nn = (size_t)n, ni = (size_t)std::max(n - 1, 1);
-    CU(ctx->rec.ensure(nn * 4 * sizeof(float4)));
-    CU(ctx->rgen.ensure(nn * 4 * sizeof(float4)));
-    CU(ctx->nodes.ensure(ni * 4 * sizeof(float4)));
-    CU(ctx->codes.ensure(nn * sizeof(uint64_t)));
-    CU(ctx->perm.ensure(nn * sizeof(uint32_t)));
-    CU(ctx->bvh_scratch.ensure(bvh_scratch_bytes(n)));
+    CU(ctx->rec.ensure(ctx->stream, nn * 4 * sizeof(float4)));
+    CU(ctx->rgen.ensure(ctx->stream, nn * 4 * sizeof(float4)));
+    CU(ctx->nodes.ensure(ctx->stream, ni * 4 * sizeof(float4)));
+    CU(ctx->codes.ensure(ctx->stream, nn * sizeof(uint64_t)));
+    CU(ctx->perm.ensure(ctx->stream, nn * sizeof(uint32_t)));
+    CU(ctx->bvh_scratch.ensure(ctx->stream, bvh_scratch_bytes(n)));
     BvhBuffers b;
     bvh_carve(b, ctx->bvh_scratch.p, n);
     b.rec = ctx->rec.as<float4>();
@@ -607,8 +653,8 @@ int hrt_build_accel(hrt_context *ctx) {
     if (r) return r;
     // compressed 4-wide nodes for the persistent diffuse trace (scratch reuses the build's)
     ctx->n4 = 0;
-    CU(ctx->nodes4.ensure(ni * 4 * sizeof(float4)));
-    if (bvh4_scratch_bytes(n) > ctx->bvh_scratch.cap) CU(ctx->bvh_scratch.ensure(bvh4_scratch_bytes(n)));
+    CU(ctx->nodes4.ensure(ctx->stream, ni * 4 * sizeof(float4)));
+    if (bvh4_scratch_bytes(n) > ctx->bvh_scratch.cap) CU(ctx->bvh_scratch.ensure(ctx->stream, bvh4_scratch_bytes(n)));
     int n4 = 0;
     CU(bvh4_build(ctx->nodes.as<float4>(), n, ctx->nodes4.as<float4>(), ctx->bvh_scratch.p, ctx->status.as<uint32_t>(),
                   &n4, ctx->stream));
@@ -624,8 +670,8 @@ int hrt_update_materials(hrt_context *ctx, int32_t nsources, int32_t nprims, int
     size_t m = (size_t)nsources * nprims * nbands_global;
     if (m && (!rho || !tau)) return fail(ctx, HRT_EINVAL, "null material array");
     CU(cudaSetDevice(ctx->device));
-    CU(ctx->rho.ensure(std::max<size_t>(m, 1) * sizeof(float)));
-    CU(ctx->tau.ensure(std::max<size_t>(m, 1) * sizeof(float)));
+    CU(ctx->rho.ensure(ctx->stream, std::max<size_t>(m, 1) * sizeof(float)));
+    CU(ctx->tau.ensure(ctx->stream, std::max<size_t>(m, 1) * sizeof(float)));
     std::vector<float> vr, vt;
     if (m && !ctx->h_voxels.empty() && nprims == ctx->n) {
         // A voxel's leaves scatter rho + tau into one isotropic field: half of it is routed
@@ -668,7 +714,7 @@ int hrt_update_sources(hrt_context *ctx, int32_t nsources, const hrt_source *sou
         s.w1 = sources[k].width[1];
         rotation3(sources[k].rotation, s.R);
     }
-    CU(ctx->src.ensure(h.size() * sizeof(SourceDev)));
+    CU(ctx->src.ensure(ctx->stream, h.size() * sizeof(SourceDev)));
     CU(cudaMemcpyAsync(ctx->src.p, h.data(), h.size() * sizeof(SourceDev), cudaMemcpyHostToDevice, ctx->stream));
     ctx->S = nsources;
     CU(cudaStreamSynchronize(ctx->stream));
@@ -678,7 +724,7 @@ int hrt_update_sources(hrt_context *ctx, int32_t nsources, const hrt_source *sou
 int hrt_upload_source_fluxes(hrt_context *ctx, const float *fluxes, size_t count) {
     if (!ctx || (count && !fluxes)) return HRT_EINVAL;
     CU(cudaSetDevice(ctx->device));
-    CU(ctx->src_flux.ensure(std::max<size_t>(count, 1) * sizeof(float)));
+    CU(ctx->src_flux.ensure(ctx->stream, std::max<size_t>(count, 1) * sizeof(float)));
     if (count) CU(cudaMemcpyAsync(ctx->src_flux.p, fluxes, count * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
     ctx->src_flux_count = count;
     ctx->h_src_flux.assign(fluxes, fluxes + count);
@@ -875,16 +921,16 @@ int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
         // per-band flags and depths (small, every call); emissivity and temperature when given,
         // else the arrays resident from an earlier call are used
         if (Bl > 15) return fail(ctx, HRT_EUNSUPPORTED, "emission supports at most 15 launched bands");
-        CU(ctx->emis.ensure(128));
+        CU(ctx->emis.ensure(ctx->stream, 128));
         CU(cudaMemcpyAsync(ctx->emis.p, s->emission, (size_t)Bl, cudaMemcpyHostToDevice, st));
         CU(cudaMemcpyAsync(ctx->emis.as<char>() + 64, s->scattering_depth, (size_t)Bl * 4, cudaMemcpyHostToDevice, st));
         if (s->emissivity) {
-            CU(ctx->emis_eps.ensure(m * sizeof(float)));
+            CU(ctx->emis_eps.ensure(ctx->stream, m * sizeof(float)));
             CU(cudaMemcpyAsync(ctx->emis_eps.p, s->emissivity, m * sizeof(float), cudaMemcpyHostToDevice, st));
             ctx->emis_eps_count = m;
         }
         if (s->temperature) {
-            CU(ctx->emis_T.ensure((size_t)n * sizeof(float)));
+            CU(ctx->emis_T.ensure(ctx->stream, (size_t)n * sizeof(float)));
             CU(cudaMemcpyAsync(ctx->emis_T.p, s->temperature, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, st));
             ctx->emis_T_count = (size_t)n;
         }
@@ -945,7 +991,7 @@ int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
         }
         std::vector<uint8_t> sflags = flags, conv(Bg, 0);
         const bool residual = s->scatter_tolerance > 0.0;
-        if (residual) CU(ctx->resid.ensure((64 + (size_t)kResidualBlocks * Bl * 2) * sizeof(double)));
+        if (residual) CU(ctx->resid.ensure(ctx->stream, (64 + (size_t)kResidualBlocks * Bl * 2) * sizeof(double)));
         for (int it = 0; it < depth; ++it) {
             int b = -1;
             for (int bg = 0; bg < Bg; ++bg) {
@@ -1038,7 +1084,7 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
     strata(rpp_d, &ddx, &ddy);
     const int Rd = ddx * ddy;
     // device inputs: [sun 3*nsun][flux C][sky C][zero C] floats, masks 6*C bytes, materials
-    CU(ctx->sw_in.ensure((3 * (size_t)nsun + 3 * (size_t)C) * sizeof(float) + 6 * (size_t)C + 256));
+    CU(ctx->sw_in.ensure(ctx->stream, (3 * (size_t)nsun + 3 * (size_t)C) * sizeof(float) + 6 * (size_t)C + 256));
     float *d_sun = ctx->sw_in.as<float>(), *d_flux = d_sun + 3 * nsun, *d_sky = d_flux + C, *d_zero = d_sky + C;
     uint8_t *d_masks = (uint8_t *)(d_zero + C);
     {
@@ -1053,19 +1099,19 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
     }
     uint8_t *m_all = d_masks, *m_fold = d_masks + C, *m_diff = d_masks + 2 * C, *m_copy0 = d_masks + 3 * C,
             *m_active = d_masks + 4 * C;
-    CU(ctx->sw_mat.ensure(2 * (size_t)n * Bl * sizeof(float)));
+    CU(ctx->sw_mat.ensure(ctx->stream, 2 * (size_t)n * Bl * sizeof(float)));
     float *d_rho = ctx->sw_mat.as<float>(), *d_tau = d_rho + (size_t)n * Bl;
     CU(cudaMemcpyAsync(d_rho, s->rho, (size_t)n * Bl * sizeof(float), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(d_tau, s->tau, (size_t)n * Bl * sizeof(float), cudaMemcpyHostToDevice, st));
     // buffers
-    CU(ctx->sw_acc.ensure(5 * m * sizeof(double)));
+    CU(ctx->sw_acc.ensure(ctx->stream, 5 * m * sizeof(double)));
     double *rin = ctx->sw_acc.as<double>(), *stp = rin + m, *sbt = stp + m, *Gt = sbt + m, *Gb = Gt + m;
-    CU(ctx->sw_out.ensure(3 * m * sizeof(float)));
+    CU(ctx->sw_out.ensure(ctx->stream, 3 * m * sizeof(float)));
     float *otop = ctx->sw_out.as<float>(), *obot = otop + m, *fin = obot + m;
     const size_t nhits = 2 * (size_t)n * (size_t)std::max(Rd, 1);
-    CU(ctx->sw_hits.ensure(nhits * sizeof(uint32_t)));
-    CU(ctx->Gd.ensure(std::max<size_t>((size_t)n * nsun * 2, 1) * sizeof(double)));
-    CU(ctx->fetch.ensure(sizeof(unsigned long long)));
+    CU(ctx->sw_hits.ensure(ctx->stream, nhits * sizeof(uint32_t)));
+    CU(ctx->Gd.ensure(ctx->stream, std::max<size_t>((size_t)n * nsun * 2, 1) * sizeof(double)));
+    CU(ctx->fetch.ensure(ctx->stream, sizeof(unsigned long long)));
     // choose the recording kernel's variant before capture (timing cannot run inside a capture)
     int rec_variant = ctx->n4 > 0 ? DV_W4 : DV_PS3;
     if (Rd > 0 && (any_diffuse || any_active)) {
@@ -1080,6 +1126,7 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
         T0.Bc = 1;
         T0.Bl = 1;
         T0.fetch = ctx->fetch.as<unsigned long long>();
+        T0.lane_budget = ctx->lane_budget;
         T0.hits = ctx->sw_hits.as<uint32_t>();
         if ((r = tuned_variant(ctx, T0, true, &rec_variant))) return r;
     }
@@ -1138,6 +1185,7 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
             P.count = (uint32_t)n;
             P.faces = 3;
             P.fetch = ctx->fetch.as<unsigned long long>();
+            P.lane_budget = ctx->lane_budget;
             GatherParams Gp{n, C, Rd, 3, sc.twosided, ctx->sw_hits.as<uint32_t>(), otop, obot, d_sky, Gt, Gb};
             E.Gt = Gt;
             E.Gb = Gb;
@@ -1200,6 +1248,13 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
     return r;
 }
 
+int hrt_set_ray_budget(hrt_context *ctx, uint32_t rays_per_thread) {
+    if (!ctx || rays_per_thread > (1u << 20)) return HRT_EINVAL;
+    ctx->lane_budget = rays_per_thread;
+    ctx->tuned.clear();  // the budget changes the launches the tuner timed
+    return HRT_OK;
+}
+
 int hrt_set_tuning(hrt_context *ctx, int mode) {
     if (!ctx || mode < 0 || (mode > 2 && !(mode >= 16 + DV_PS4 && mode <= 16 + DV_W43))) return HRT_EINVAL;
     if (mode == 2) {
@@ -1244,8 +1299,8 @@ int hrt_trace_rays(hrt_context *ctx, int64_t nrays, const float *origins, const 
     int r = check_built(ctx);
     if (r) return r;
     size_t nr = (size_t)nrays;
-    CU(ctx->io_a.ensure(std::max<size_t>(nr, 1) * 24));
-    CU(ctx->io_b.ensure(std::max<size_t>(nr, 1) * 12));
+    CU(ctx->io_a.ensure(ctx->stream, std::max<size_t>(nr, 1) * 24));
+    CU(ctx->io_b.ensure(ctx->stream, std::max<size_t>(nr, 1) * 12));
     float *dO = ctx->io_a.as<float>(), *dD = dO + 3 * nr;
     int32_t *dH = ctx->io_b.as<int32_t>();
     float *dT = (float *)(dH + nr);
@@ -1271,7 +1326,7 @@ int hrt_gen_rays(hrt_context *ctx, int kind, uint32_t seed, uint32_t pass, int32
         dimy = rpp;
     }
     size_t nr = (size_t)ctx->n * dimx * dimy;
-    CU(ctx->io_a.ensure(std::max<size_t>(nr, 1) * 24));
+    CU(ctx->io_a.ensure(ctx->stream, std::max<size_t>(nr, 1) * 24));
     float *dO = ctx->io_a.as<float>(), *dD = dO + 3 * nr;
     float dx = direction ? direction[0] : 0.f, dy = direction ? direction[1] : 0.f, dz = direction ? direction[2] : 1.f;
     CU(launch_gen_rays(scene_of(ctx), kind, seed, pass, dimx, dimy, face, dx, dy, dz, dO, dD, ctx->stream));
@@ -1297,10 +1352,11 @@ void hrt_source_rotation(const float rotation[3], float out[9]) { rotation3(rota
 int hrt_set_measure(hrt_context *ctx, int flags) {
     if (!ctx) return HRT_EINVAL;
     CU(cudaSetDevice(ctx->device));
-    CU(ctx->visits.ensure(2 * sizeof(unsigned long long)));
+    CU(ctx->visits.ensure(ctx->stream, 2 * sizeof(unsigned long long)));
     CU(cudaStreamSynchronize(ctx->stream));
     collect_timings(ctx);
-    CU(cudaMemset(ctx->visits.p, 0, 2 * sizeof(unsigned long long)));
+    CU(cudaMemsetAsync(ctx->visits.p, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
     for (double &m : ctx->meas) m = 0.0;
     ctx->measure = flags;
     return HRT_OK;

@@ -62,6 +62,8 @@ struct DiffuseParams {
     SkyParams sky;
     double *Gt, *Gb;          // [n*Bl] sums of incoming values per origin face
     unsigned long long *fetch; // ray-id counter of the persistent kernel (zeroed by the launcher)
+    uint32_t lane_budget;      // persistent kernel: rays a lane takes before its block retires
+                               // (0 = no limit: one resident wave of blocks runs to the end)
     uint32_t *hits;            // record mode: hit code per ray id, else unused
 };
 

@@ -9,20 +9,30 @@
 // and hands them to a pool of worker threads.  Every resident scene owns an
 // hrt_context (BVH, radiation buffers, its own CUDA stream), so solves of
 // different scenes run concurrently and overlap on the GPU; a new request for an
-// already-resident scene skips the geometry upload and BVH build.  Each solve is
-// a full hrt_run_band, so a request's result depends only on its scene, band set,
-// sun, ray counts and seed -- the same alone as in the mix.
+// already-resident scene skips the geometry upload and BVH build.
+//
+// Batching: when a scene's turn comes, every arrived request for that scene with the
+// same band set, ray counts, depth and seed joins the batch (up to kMaxChannels
+// channels).  A batch of one runs hrt_run_band; a larger batch runs hrt_run_sweep, one
+// channel per (request, band): the direct pass is traced per request sun, the diffuse
+// and scattering passes once for the whole batch.  Each channel is the solve its
+// request would get alone (same Philox streams), so a result depends only on the
+// request -- the same alone as in the mix, up to the order of FP64 sums.
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <iterator>
 #include <map>
 #include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
+
+#include <cuda_runtime.h>
 
 #include "../../include/hrt.h"
 
@@ -40,10 +50,19 @@ struct Scene {
     std::vector<float> rho, tau;  // [n*nbands], one source
     // device state
     hrt_context *ctx = nullptr;
+    cudaStream_t stream = nullptr;  // priority stream of this scene's solves
     bool busy = false;
     size_t bytes = 0;
     uint64_t last_use = 0;
 };
+
+constexpr int kMaxChannels = 256;  // hrt_run_sweep's channel limit
+constexpr uint32_t kRayBudget = 32; // rays per thread before a trace block retires (GPU sharing)
+// Batches above this many traced rays run one at a time: interleaved at block granularity,
+// several large scenes evict each other's BVH nodes from L1/L2 and the GPU's ray rate
+// drops; small batches still run beside them (higher stream priority).
+constexpr double kLargeRays = 2e8;
+constexpr int kMaxBatch = 64;      // requests per batch
 
 struct Request {
     uint64_t id = 0;
@@ -79,12 +98,13 @@ struct hrt_server {
     std::condition_variable cv_dispatch, cv_work, cv_done;
     std::map<uint32_t, std::unique_ptr<Scene>> scenes;
     std::deque<Request *> arrivals;   // sorted by arrival time when started
-    std::deque<Request *> ready;      // admitted, waiting for a worker
+    std::deque<std::vector<Request *>> ready;  // admitted batches, waiting for a worker
     std::map<uint64_t, std::unique_ptr<Request>> requests;
     std::vector<std::thread> workers;
     std::thread dispatcher;
     bool started = false, stopping = false;
-    size_t outstanding = 0, evictions = 0, builds = 0;
+    size_t outstanding = 0, evictions = 0, builds = 0, batches = 0, batched_requests = 0;
+    std::mutex large;  // held by the one large batch in flight
     clock_t_::time_point t0;
     uint64_t tick = 0;
     std::string err;
@@ -108,6 +128,11 @@ bool ensure_resident(hrt_server *s, Scene *sc, int32_t Bl, std::string &err) {
         if (!victim) return false;  // wait for a busy scene to finish
         hrt_destroy(victim->ctx);
         victim->ctx = nullptr;
+        if (victim->stream) {
+            cudaSetDevice(s->device);
+            cudaStreamDestroy(victim->stream);
+            victim->stream = nullptr;
+        }
         s->used -= victim->bytes;
         victim->bytes = 0;
         ++s->evictions;
@@ -118,21 +143,127 @@ bool ensure_resident(hrt_server *s, Scene *sc, int32_t Bl, std::string &err) {
     return true;
 }
 
+bool same_batch(const Request *a, const Request *b) {
+    return a->scene == b->scene && a->band_launch == b->band_launch && a->direct_rays == b->direct_rays &&
+           a->diffuse_rays == b->diffuse_rays && a->depth == b->depth && a->seed == b->seed;
+}
+
+// One request alone: a full runBand.
+int solve_one(Scene *sc, Request *r, int Bl) {
+    hrt_source src{};
+    src.type = 0;
+    for (int k = 0; k < 3; ++k) src.position[k] = r->sun[k];
+    std::vector<int32_t> dr(Bl, r->direct_rays), fr(Bl, r->diffuse_rays), dp(Bl, r->depth);
+    std::vector<uint8_t> em(Bl, 0);
+    hrt_band_solve b{};
+    b.nbands_global = sc->nbands;
+    b.band_launch = r->band_launch.data();
+    b.nsources = 1;
+    b.sources = &src;
+    b.source_flux = r->source_flux.data();
+    b.diffuse_flux = r->diffuse_flux.data();
+    b.direct_rays = dr.data();
+    b.diffuse_rays = fr.data();
+    b.scattering_depth = dp.data();
+    b.emission = em.data();
+    b.seed = r->seed;
+    std::vector<float> flux((size_t)sc->n * Bl);
+    int rc = hrt_run_band(sc->ctx, &b, flux.data());
+    if (rc != HRT_OK) return rc;
+    uint64_t st[2] = {0, 0};
+    hrt_last_stats(sc->ctx, st, 2);
+    r->rays = st[0];
+    double sum = 0.0;
+    for (float f : flux) sum += f;
+    r->checksum = sum;
+    if (r->keep) r->flux.swap(flux);
+    return HRT_OK;
+}
+
+// A batch of compatible requests: one sweep, channel c = request * Bl + band.
+int solve_batch(Scene *sc, const std::vector<Request *> &batch, int Bl) {
+    const int nr = (int)batch.size(), C = nr * Bl;
+    const size_t n = (size_t)sc->n;
+    std::vector<int> cols;
+    for (int b = 0; b < sc->nbands; ++b)
+        if (batch[0]->band_launch[b]) cols.push_back(b);
+    std::vector<float> rho(n * Bl), tau(n * Bl), sun(3 * (size_t)nr), dflux(C), sflux(C);
+    for (size_t p = 0; p < n; ++p)
+        for (int b = 0; b < Bl; ++b) {
+            rho[p * Bl + b] = sc->rho[p * sc->nbands + cols[b]];
+            tau[p * Bl + b] = sc->tau[p * sc->nbands + cols[b]];
+        }
+    for (int i = 0; i < nr; ++i) {
+        for (int k = 0; k < 3; ++k) sun[3 * i + k] = batch[i]->sun[k];
+        for (int b = 0; b < Bl; ++b) {
+            dflux[i * Bl + b] = batch[i]->source_flux[b];
+            sflux[i * Bl + b] = batch[i]->diffuse_flux[b];
+        }
+    }
+    hrt_sweep w{};
+    w.nsun = nr;
+    w.sun_dir = sun.data();
+    w.nbands = Bl;
+    w.direct_flux = dflux.data();
+    w.diffuse_flux = sflux.data();
+    w.rho = rho.data();
+    w.tau = tau.data();
+    w.direct_rays = batch[0]->direct_rays;
+    w.diffuse_rays = batch[0]->diffuse_rays;
+    w.scattering_depth = batch[0]->depth;
+    w.seed = batch[0]->seed;
+    std::vector<float> out(n * C);
+    int rc = hrt_run_sweep(sc->ctx, &w, out.data());
+    if (rc != HRT_OK) return rc;
+    uint64_t st[2] = {0, 0};
+    hrt_last_stats(sc->ctx, st, 2);
+    for (int i = 0; i < nr; ++i) {
+        Request *r = batch[i];
+        r->rays = st[0] / (uint64_t)nr;  // the batch's rays, shared evenly
+        std::vector<float> flux(n * Bl);
+        double sum = 0.0;
+        for (size_t p = 0; p < n; ++p)
+            for (int b = 0; b < Bl; ++b) {
+                const float v = out[p * C + (size_t)i * Bl + b];
+                flux[p * Bl + b] = v;
+                sum += v;
+            }
+        r->checksum = sum;
+        if (r->keep) r->flux.swap(flux);
+    }
+    return HRT_OK;
+}
+
 void worker_loop(hrt_server *s) {
     for (;;) {
-        Request *r = nullptr;
+        std::vector<Request *> batch;
         Scene *sc = nullptr;
         {
             std::unique_lock<std::mutex> lk(s->mu);
             s->cv_work.wait(lk, [&] { return s->stopping || !s->ready.empty(); });
             if (s->stopping && s->ready.empty()) return;
-            r = s->ready.front();
+            batch.swap(s->ready.front());
             s->ready.pop_front();
-            sc = s->scenes[r->scene].get();
+            sc = s->scenes[batch[0]->scene].get();
         }
         int rc = HRT_OK;
         if (!sc->ctx) {
             rc = hrt_create(&sc->ctx, s->device);
+            if (rc == HRT_OK) {
+                // Smaller scenes get higher stream priority and every trace block retires
+                // after kRayBudget rays per thread, so a small solve's blocks start as soon as
+                // SMs free up instead of waiting for a large solve to end.
+                int least = 0, greatest = 0;
+                cudaDeviceGetStreamPriorityRange(&least, &greatest);
+                double f = (std::log10((double)std::max(sc->n, 1)) - 3.0) / 3.5;  // 1e3 .. 3e6 prims
+                f = std::min(1.0, std::max(0.0, f));
+                const int prio = greatest + (int)std::lround(f * (double)(least - greatest));
+                if (cudaStreamCreateWithPriority(&sc->stream, cudaStreamNonBlocking, prio) == cudaSuccess)
+                    rc = hrt_set_stream(sc->ctx, sc->stream);
+                if (rc == HRT_OK) rc = hrt_set_ray_budget(sc->ctx, kRayBudget);
+                // fixed default kernels: timing trials per scene would cost more than they save
+                if (rc == HRT_OK) rc = hrt_set_tuning(sc->ctx, 0);
+            }
             if (rc == HRT_OK) {
                 hrt_geometry g{};
                 g.n = sc->n;
@@ -147,45 +278,46 @@ void worker_loop(hrt_server *s) {
             }
         }
         int Bl = 0;
-        for (uint8_t f : r->band_launch) Bl += f ? 1 : 0;
+        for (uint8_t f : batch[0]->band_launch) Bl += f ? 1 : 0;
         if (rc == HRT_OK) {
-            hrt_source src{};
-            src.type = 0;
-            for (int k = 0; k < 3; ++k) src.position[k] = r->sun[k];
-            std::vector<int32_t> dr(Bl, r->direct_rays), fr(Bl, r->diffuse_rays), dp(Bl, r->depth);
-            std::vector<uint8_t> em(Bl, 0);
-            hrt_band_solve b{};
-            b.nbands_global = sc->nbands;
-            b.band_launch = r->band_launch.data();
-            b.nsources = 1;
-            b.sources = &src;
-            b.source_flux = r->source_flux.data();
-            b.diffuse_flux = r->diffuse_flux.data();
-            b.direct_rays = dr.data();
-            b.diffuse_rays = fr.data();
-            b.scattering_depth = dp.data();
-            b.emission = em.data();
-            b.seed = r->seed;
-            std::vector<float> flux((size_t)sc->n * Bl);
-            rc = hrt_run_band(sc->ctx, &b, flux.data());
-            if (rc == HRT_OK) {
-                uint64_t st[2] = {0, 0};
-                hrt_last_stats(sc->ctx, st, 2);
-                r->rays = st[0];
-                double sum = 0.0;
-                for (float f : flux) sum += f;
-                r->checksum = sum;
-                if (r->keep) r->flux.swap(flux);
+            const Request *r0 = batch[0];
+            const double side = std::ceil(std::sqrt((double)r0->diffuse_rays));
+            const double rays = (double)sc->n * ((double)r0->direct_rays * (double)batch.size() +
+                                                 2.0 * side * side * (1.0 + (double)r0->depth));
+            std::unique_lock<std::mutex> gate(s->large, std::defer_lock);
+            if (rays > kLargeRays) {
+                gate.lock();
+                // requests of this scene that arrived while the batch waited for the GPU
+                // join it (the scene is busy, so they would otherwise wait for the next batch)
+                std::lock_guard<std::mutex> lk(s->mu);
+                const double t = s->now();
+                for (auto it = s->arrivals.begin(); it != s->arrivals.end() && (int)batch.size() < kMaxBatch &&
+                                                    (int)(batch.size() + 1) * Bl <= kMaxChannels;) {
+                    Request *q = *it;
+                    if (q->arrival > t) break;
+                    if (same_batch(batch[0], q)) {
+                        q->t_admit = t;
+                        batch.push_back(q);
+                        ++s->batched_requests;
+                        it = s->arrivals.erase(it);  // erase returns a valid iterator to the next one
+                    } else {
+                        ++it;
+                    }
+                }
             }
+            rc = batch.size() == 1 ? solve_one(sc, batch[0], Bl) : solve_batch(sc, batch, Bl);
         }
         {
             std::lock_guard<std::mutex> lk(s->mu);
-            r->t_done = s->now();
-            r->status = rc;
+            const double t = s->now();
+            for (Request *r : batch) {
+                r->t_done = t;
+                r->status = rc;
+                --s->outstanding;
+            }
             if (rc != HRT_OK && sc->ctx) s->err = hrt_last_error(sc->ctx);
             sc->busy = false;
             sc->last_use = ++s->tick;
-            --s->outstanding;
         }
         s->cv_dispatch.notify_all();
         s->cv_done.notify_all();
@@ -218,9 +350,29 @@ void dispatch_loop(hrt_server *s) {
             if (!sc->busy && ensure_resident(s, sc, Bl, err)) {
                 sc->busy = true;
                 r->t_admit = t;
-                s->ready.push_back(r);
-                it = s->arrivals.erase(it);
+                std::vector<Request *> batch{r};
+                // later arrived requests of the same scene and solve settings join the batch
+                for (auto jt = std::next(it); jt != s->arrivals.end() && (int)batch.size() < kMaxBatch &&
+                                              (int)(batch.size() + 1) * Bl <= kMaxChannels;
+                     ++jt) {
+                    Request *q = *jt;
+                    if (q->arrival > t) break;
+                    if (same_batch(r, q)) {
+                        q->t_admit = t;
+                        batch.push_back(q);
+                    }
+                }
+                // erasing from a deque invalidates its iterators: remove the batch, rescan
+                s->arrivals.erase(std::remove_if(s->arrivals.begin(), s->arrivals.end(),
+                                                 [&](const Request *x) {
+                                                     return std::find(batch.begin(), batch.end(), x) != batch.end();
+                                                 }),
+                                  s->arrivals.end());
+                ++s->batches;
+                s->batched_requests += batch.size();
+                s->ready.push_back(std::move(batch));
                 admitted = true;
+                it = s->arrivals.begin();
             } else {
                 ++it;
             }
@@ -351,8 +503,9 @@ int hrt_server_result(hrt_server *s, uint64_t request_id, float *flux_out, size_
 int hrt_server_stats(hrt_server *s, double *out, int count) {
     if (!s || !out) return HRT_EINVAL;
     std::lock_guard<std::mutex> lk(s->mu);
-    double v[4] = {(double)s->builds, (double)s->evictions, (double)s->used, (double)s->budget};
-    for (int i = 0; i < count && i < 4; ++i) out[i] = v[i];
+    double v[6] = {(double)s->builds,  (double)s->evictions, (double)s->used,
+                   (double)s->budget,  (double)s->batches,   (double)s->batched_requests};
+    for (int i = 0; i < count && i < 6; ++i) out[i] = v[i];
     return HRT_OK;
 }
 
@@ -366,8 +519,13 @@ int hrt_server_destroy(hrt_server *s) {
     s->cv_work.notify_all();
     if (s->dispatcher.joinable()) s->dispatcher.join();
     for (auto &t : s->workers) t.join();
-    for (auto &kv : s->scenes)
+    for (auto &kv : s->scenes) {
         if (kv.second->ctx) hrt_destroy(kv.second->ctx);
+        if (kv.second->stream) {
+            cudaSetDevice(s->device);
+            cudaStreamDestroy(kv.second->stream);
+        }
+    }
     delete s;
     return HRT_OK;
 }

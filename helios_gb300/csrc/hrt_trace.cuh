@@ -269,6 +269,20 @@ __device__ __forceinline__ double sky_fd(f3 dir, const SkyParams &sky, int b) {
     return 1.0;
 }
 
+// Blocks of a persistent launch: one resident wave; with a lane budget, enough blocks
+// that every ray id is taken even if each lane takes exactly its budget (the hardware
+// starts the extra blocks as earlier ones retire).
+inline unsigned ps_grid(const DiffuseParams &p, int resident) {
+    if (!p.lane_budget) return (unsigned)resident;
+    const unsigned long long nf = ((p.faces & 1) ? 1 : 0) + ((p.faces & 2) ? 1 : 0);
+    const unsigned long long total = (unsigned long long)p.count * (unsigned long long)(p.dimx * p.dimy) * nf;
+    const unsigned long long per_block = (unsigned long long)kBlock * p.lane_budget;
+    unsigned long long g = (total + per_block - 1) / per_block;
+    if (g < (unsigned long long)resident) g = (unsigned long long)resident;
+    if (g > 0x7FFFFFFFull) g = 0x7FFFFFFFull;
+    return (unsigned)g;
+}
+
 // ------------------------------------------------------- persistent diffuse --
 // Persistent threads with dynamic ray fetch and speculative while-while traversal
 // (after Aila & Laine, "Understanding the Efficiency of Ray Traversal on GPUs",
@@ -323,8 +337,11 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
     for (int j = 0; j < NB; ++j) ACC(j) = 0.0;
     unsigned long long nrays = 0;
 
+    uint32_t taken = 0;
     for (;;) {
-        // ---- refill lanes without a ray
+        // ---- refill lanes without a ray; a lane that has taken its budget retires, so
+        // that the block exits and the SM can run blocks of other launches in between
+        if (!live && P.lane_budget && taken >= P.lane_budget) exhausted = true;
         const bool need = !live && !exhausted;
         const unsigned m = __ballot_sync(0xffffffffu, need);
         if (m) {
@@ -337,6 +354,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
                 if (id >= total) {
                     exhausted = true;
                 } else {
+                    ++taken;
                     rid = id;
                     const uint32_t fi = (uint32_t)(id / per_face);
                     const uint32_t rem = (uint32_t)(id - (unsigned long long)fi * per_face);

@@ -379,25 +379,34 @@ def mixed_canopy(n, lai, seed=0, height=3.0, leaf_area=0.0025):
 
 
 def served_stream(n_requests=2000, rate=50.0, n_scenes=32, n_min=2000, n_max=2000000, seed=0):
-    """Request stream of the served configuration: Poisson arrivals, scene sizes
-    log-uniform in [n_min, n_max] (patch:triangle 1:1), LAI U[0.5, 5], 1-4 of 4 bands,
-    sun zenith U[0, 75] deg, 50-400 diffuse rays.  Requests draw from a pool of
-    n_scenes scenes so that resident BVHs are reused."""
+    """Request stream of the served configuration: Poisson arrivals at `rate`; each of
+    n_scenes scenes is a homogeneous canopy of log-uniform size in [n_min, n_max]
+    (patch:triangle 1:1) with LAI U[0.5, 5], its own band set (1-4 of 4 bands), diffuse
+    ray count U[50, 400] and seed; each request picks a scene and a sun position (zenith
+    U[0, 75] deg, azimuth U[0, 360]) with its direct and diffuse fluxes.  Returns the scene
+    sizes and LAIs and the requests (each carrying its scene's bands, rays and seed)."""
     rng = np.random.default_rng(seed)
     sizes = np.exp(rng.uniform(math.log(n_min), math.log(n_max), n_scenes)).astype(int)
     lais = rng.uniform(0.5, 5.0, n_scenes)
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
-    reqs = []
-    for i in range(n_requests):
+    scene_bands, scene_rays, scene_seed = [], [], []
+    for _ in range(n_scenes):
         nb = int(rng.integers(1, 5))
         flags = np.zeros(4, np.uint8)
         flags[rng.choice(4, nb, replace=False)] = 1
+        scene_bands.append(flags)
+        scene_rays.append(int(rng.integers(50, 401)))
+        scene_seed.append(int(rng.integers(1 << 31)))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    reqs = []
+    for i in range(n_requests):
+        k = int(rng.integers(n_scenes))
+        nb = int(scene_bands[k].sum())
         zen = rng.uniform(0.0, 75.0)
         az = rng.uniform(0.0, 360.0)
-        reqs.append({"id": i, "scene": int(rng.integers(n_scenes)), "arrival": float(arrivals[i]), "bands": flags,
+        reqs.append({"id": i, "scene": k, "arrival": float(arrivals[i]), "bands": scene_bands[k],
                      "sun": sun_direction(zen, az), "direct": rng.uniform(100.0, 600.0, nb).astype(np.float32),
                      "diffuse": rng.uniform(20.0, 150.0, nb).astype(np.float32),
-                     "diffuse_rays": int(rng.integers(50, 401)), "seed": int(rng.integers(1 << 31))})
+                     "diffuse_rays": scene_rays[k], "seed": scene_seed[k]})
     return sizes, lais, reqs
 
 

@@ -194,9 +194,12 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out);
  * after hrt_server_start) and one runBand's parameters; a dispatcher thread admits them
  * in arrival order when the scene's device context is idle and its footprint fits in
  * hbm_budget_bytes (least-recently-used idle scenes are evicted; resident scenes keep
- * their BVH and buffers).  Worker threads run the solves on per-scene CUDA streams, so
- * solves of different scenes overlap on the GPU.  A result depends only on the request,
- * not on what else is in flight. */
+ * their BVH and buffers).  Arrived requests of the same scene with the same band set,
+ * ray counts, depth and seed are batched (up to 64 requests, 256 channels) into one
+ * hrt_run_sweep: direct rays per request sun, diffuse and scattering passes traced once.
+ * Worker threads run the batches on per-scene CUDA streams, so solves of different
+ * scenes overlap on the GPU.  A result depends only on the request, not on what else is
+ * in flight (up to the order of FP64 sums). */
 typedef struct hrt_server hrt_server;
 typedef struct {
     uint64_t request_id;
@@ -219,7 +222,8 @@ int hrt_server_wait(hrt_server *s);
 /* timing: [arrival, admit, done] seconds; checksum = sum of the request's flux values. */
 int hrt_server_result(hrt_server *s, uint64_t request_id, float *flux_out, size_t count, double *timing,
                       double *checksum, uint64_t *rays);
-/* out: [0] BVH builds, [1] evictions, [2] bytes accounted resident, [3] budget. */
+/* out: [0] BVH builds, [1] evictions, [2] bytes accounted resident, [3] budget,
+ * [4] batches run, [5] requests in them. */
 int hrt_server_stats(hrt_server *s, double *out, int count);
 int hrt_server_destroy(hrt_server *s);
 
@@ -233,6 +237,13 @@ int hrt_server_destroy(hrt_server *s);
  * 4 compressed 4-wide / 4, 5 compressed 4-wide / 3).  Variants give the same results up
  * to the order of FP64 sums. */
 int hrt_set_tuning(hrt_context *ctx, int mode);
+/* Share the GPU with other streams (no counterpart in the reference).  By default the
+ * persistent diffuse trace runs one resident wave of blocks until every ray is done, so
+ * kernels of other streams wait for it.  With rays_per_thread > 0 a thread takes at most
+ * that many rays before its block retires; the launch has enough blocks for all rays and
+ * the hardware interleaves them with other streams' blocks (by stream priority).
+ * Results do not change.  0 restores the default. */
+int hrt_set_ray_budget(hrt_context *ctx, uint32_t rays_per_thread);
 /* Text log of the tuner's trials and choices, one line per shape; returns the bytes
  * needed (including the terminating zero); buf may be NULL. */
 size_t hrt_tuning_report(const hrt_context *ctx, char *buf, size_t len);

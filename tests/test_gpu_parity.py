@@ -341,3 +341,21 @@ def test_traversal_variants_agree(oracle_mod, variant):
     assert worst <= FLUX_RTOL, worst
     assert rad.last_stats["rays"] == st["rays"]
     assert rad.ctx.device_status() == 0
+
+
+def test_ray_budget_keeps_results(oracle_mod):
+    """With a per-thread ray budget the persistent trace retires blocks early and launches
+    more of them; every ray is still traced once, so fluxes and ray counts stay the same."""
+    rad = _canopy_model(n_leaves=2500, depth=2, periodic=True)
+    rad.setSeed(33)
+    base = rad.runBand("SW")
+    rays = rad.last_stats["rays"]
+    for budget in (1, 7, 32):
+        rad.ctx.set_ray_budget(budget)
+        rad.setSeed(33)
+        got = rad.runBand("SW")
+        worst, _ = _flux_close(got, base, 1e-6)
+        assert worst <= 1e-6, (budget, worst)
+        assert rad.last_stats["rays"] == rays
+    rad.ctx.set_ray_budget(0)
+    assert rad.ctx.device_status() == 0
