@@ -5,7 +5,8 @@
 // Stages, all on one stream:
 //   1. k_records   : intersection + ray-origin records and AABBs from the 4x4 transforms
 //   2. k_bounds_*  : centroid and scene bounds (exact min/max reduction)
-//   3. k_morton    : 63-bit Morton codes (21 bits per axis) of the AABB centroids
+//   3. k_morton    : 63-bit Morton codes (21 bits per axis) of the AABB centroids, bit 63
+//                    set for voxels (they form their own subtree)
 //   4. radix sort  : stable LSD, 8 passes of 8 bits over (code, index) pairs
 //   5. k_karras    : binary radix tree (Karras, HPG 2012), ties broken by index
 //   6. k_leaves    : padded leaf boxes and records in leaf order
@@ -128,8 +129,10 @@ __device__ __forceinline__ uint32_t quant21(float c, float lo, float scale) {
     return (uint32_t)q;
 }
 
+// Bit 63 (above the 63 Morton bits) marks voxels: sorted after the surfaces, they form the
+// root's second subtree, so their large boxes do not widen the nodes over the leaves.
 __global__ void k_morton(int n, const float *__restrict__ aabb, const float *__restrict__ bnd,
-                         uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+                         const uint32_t *__restrict__ type, uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float *a = aabb + 6 * (size_t)i;
@@ -139,6 +142,7 @@ __global__ void k_morton(int n, const float *__restrict__ aabb, const float *__r
         float c = (a[k] + a[3 + k]) * 0.5f;
         code |= expand21(quant21(c, bnd[k], bnd[12 + k])) << (2 - k);
     }
+    if (type[i] == PT_VOXEL) code |= 1ull << 63;
     keys[i] = code;
     vals[i] = (uint32_t)i;
 }
@@ -456,7 +460,7 @@ cudaError_t bvh_build(const float *T, const uint32_t *type, const float *lad, in
     int nparts = grid < 1024 ? grid : 1024;
     k_bounds_partial<<<nparts, kThreads, 0, s>>>(n, b.aabb, b.partial);
     k_bounds_final<<<1, 32, 0, s>>>(nparts, b.partial, b.bounds);
-    k_morton<<<grid, kThreads, 0, s>>>(n, b.aabb, b.bounds, b.codes, b.perm);
+    k_morton<<<grid, kThreads, 0, s>>>(n, b.aabb, b.bounds, type, b.codes, b.perm);
     // 8 LSD passes; even pass count leaves the result in (codes, perm).
     const int nblk = (n + kSortTile - 1) / kSortTile;
     const int nh = 256 * nblk;

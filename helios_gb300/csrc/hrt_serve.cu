@@ -82,11 +82,12 @@ struct Request {
     std::vector<float> flux;
 };
 
-// Device bytes of a resident scene solved with Bl bands (records, BVH, origins,
-// transforms, radiation buffers, BVH scratch).
+// Device bytes of a resident scene solved with Bl bands (records, binary and 4-wide BVH,
+// origins, transforms, areas, radiation buffers, BVH scratch).
 size_t footprint(int32_t n, int32_t Bl) {
     size_t nn = (size_t)std::max(n, 1);
-    return nn * (64 + 64 + 64 + 64 + 1) + nn * (size_t)std::max(Bl, 1) * (7 * 8 + 3 * 4) + nn * 200 + (8u << 20);
+    return nn * (64 + 64 + 64 + 64 + 64 + 8 + 1) + nn * (size_t)std::max(Bl, 1) * (7 * 8 + 3 * 4) + nn * 200 +
+           (8u << 20);
 }
 
 }  // namespace

@@ -585,6 +585,7 @@ void build_bvh(Scene &s) {
         uint64_t code = (expand21(quant21(cen[i].x, clo[0], scale[0])) << 2) |
                         (expand21(quant21(cen[i].y, clo[1], scale[1])) << 1) |
                         expand21(quant21(cen[i].z, clo[2], scale[2]));
+        if (s.rec[i].type == PT_VOXEL) code |= 1ull << 63;  // voxels: their own subtree
         kv[i] = {code, (uint32_t)i};
     }
     std::sort(kv.begin(), kv.end());
