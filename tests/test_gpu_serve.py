@@ -1,5 +1,5 @@
 """Served stream: continuous batching with device-resident scenes; every result equals the
-same solve run alone."""
+same solve run alone, whether it ran alone or in a batch of its scene's requests."""
 import numpy as np
 import pytest
 
@@ -54,6 +54,8 @@ def test_served_results_equal_alone(hrt_lib):
         assert err.max() <= 1e-5, (r["id"], err.max())
     st = srv.stats()
     assert st["builds"] >= 5
+    # requests of a scene that were queued together ran as one batch
+    assert st["batched_requests"] == len(reqs) and st["batches"] < len(reqs)
     srv.close()
 
 
