@@ -39,7 +39,9 @@ class HrtError(RuntimeError):
 class Geometry(C.Structure):
     _fields_ = [("n", C.c_int32), ("transform", C.c_void_p), ("type", C.c_void_p), ("twosided", C.c_void_p),
                 ("nbbox", C.c_int32), ("bbox_vertices", C.c_void_p), ("periodic_x", C.c_float),
-                ("periodic_y", C.c_float), ("voxel_lad", C.c_void_p)]
+                ("periodic_y", C.c_float), ("voxel_lad", C.c_void_p), ("mask_id", C.c_void_p),
+                ("uv_id", C.c_void_p), ("uv", C.c_void_p), ("nmasks", C.c_int32), ("mask_size", C.c_void_p),
+                ("mask_data", C.c_void_p)]
 
 
 class Source(C.Structure):
@@ -193,8 +195,11 @@ class Context:
         self.check(self.lib.hrt_set_stream(self.h, stream_handle))
 
     # -------------------------------------------------------------- geometry
-    def update_geometry(self, T, ptype, twosided, bbox_verts=None, periodic=(0.0, 0.0), voxel_lad=None):
-        """voxel_lad: [n] leaf area density, read for voxel primitives (required when there are any)."""
+    def update_geometry(self, T, ptype, twosided, bbox_verts=None, periodic=(0.0, 0.0), voxel_lad=None,
+                        masks=None):
+        """voxel_lad: [n] leaf area density, read for voxel primitives (required when there are any).
+        masks: None or dict(mask_id [n], uv_id [n] or None, uv [n, 8] or None, sizes [m, 2]
+        (width, height), data: the masks' row-major uint8 texels one after another)."""
         T = f32(T).reshape(-1, 16)
         ty = np.ascontiguousarray(ptype, np.uint32)
         ts = np.ascontiguousarray(twosided, np.int8)
@@ -202,7 +207,18 @@ class Context:
         lad = None if voxel_lad is None else f32(voxel_lad)
         g = Geometry(T.shape[0], ptr(T), ptr(ty), ptr(ts), 0 if bb is None else bb.shape[0], ptr(bb),
                      float(periodic[0]), float(periodic[1]), ptr(lad))
+        keep = []
+        if masks is not None:
+            mid = np.ascontiguousarray(masks["mask_id"], np.int32)
+            sizes = np.ascontiguousarray(masks["sizes"], np.int32).reshape(-1, 2)
+            data = np.ascontiguousarray(masks["data"], np.uint8)
+            uvid = None if masks.get("uv_id") is None else np.ascontiguousarray(masks["uv_id"], np.int32)
+            uv = None if masks.get("uv") is None else f32(masks["uv"]).reshape(-1, 8)
+            keep = [mid, sizes, data, uvid, uv]
+            g.mask_id, g.uv_id, g.uv = ptr(mid), ptr(uvid), ptr(uv)
+            g.nmasks, g.mask_size, g.mask_data = sizes.shape[0], ptr(sizes), ptr(data)
         self.check(self.lib.hrt_update_geometry(self.h, C.byref(g)))
+        del keep
         self.n = T.shape[0]
 
     def build_accel(self):

@@ -59,6 +59,41 @@ void GB300Backend::updateGeometry(const RayTracingGeometry &geometry) {
     g.bbox_vertices = bbox.empty() ? nullptr : bbox.data();
     g.periodic_x = geometry.periodic_flag.x;
     g.periodic_y = geometry.periodic_flag.y;
+    if (!voxel_lad_.empty()) {
+        if (voxel_lad_.size() != geometry.primitive_count)
+            helios_runtime_error("ERROR (GB300Backend::updateGeometry): voxel leaf area density has " +
+                                 std::to_string(voxel_lad_.size()) + " entries for " +
+                                 std::to_string(geometry.primitive_count) + " primitives");
+        g.voxel_lad = voxel_lad_.data();
+    }
+    // Texture masks: bool texels to bytes, the packed uv_data (4 entries per textured primitive
+    // in primitive order, RadiationModel.cpp:6210-6222) to 4 corners per primitive.
+    std::vector<uint8_t> mask_bytes(geometry.mask_data.begin(), geometry.mask_data.end());
+    std::vector<int32_t> mask_size;
+    for (const auto &sz : geometry.mask_sizes) {
+        mask_size.push_back(sz.x);
+        mask_size.push_back(sz.y);
+    }
+    std::vector<float> uv;
+    if (!geometry.mask_sizes.empty() && geometry.mask_IDs.size() == geometry.primitive_count) {
+        g.mask_id = geometry.mask_IDs.data();
+        g.nmasks = (int32_t)geometry.mask_sizes.size();
+        g.mask_size = mask_size.data();
+        g.mask_data = mask_bytes.data();
+        if (geometry.uv_IDs.size() == geometry.primitive_count) {
+            uv.assign(geometry.primitive_count * 8, 0.f);
+            size_t r = 0;
+            for (size_t p = 0; p < geometry.primitive_count; ++p) {
+                if (geometry.uv_IDs[p] < 0) continue;
+                for (int v = 0; v < 4 && r < geometry.uv_data.size(); ++v, ++r) {
+                    uv[p * 8 + 2 * v] = geometry.uv_data[r].x;
+                    uv[p * 8 + 2 * v + 1] = geometry.uv_data[r].y;
+                }
+            }
+            g.uv_id = geometry.uv_IDs.data();
+            g.uv = uv.data();
+        }
+    }
     check(hrt_update_geometry(ctx_, &g), "updateGeometry");
     nprims_ = geometry.primitive_count;
 }

@@ -55,6 +55,10 @@ public:
     void queryGPUMemory() const override;
     std::string getBackendName() const override;
 
+    //! Leaf area density (m^2/m^3) of each primitive, read for voxels (type 4) at the next
+    //! updateGeometry.  RayTracingGeometry carries none; a model with voxels sets it first.
+    void setVoxelLeafAreaDensity(const std::vector<float> &lad) { voxel_lad_ = lad; }
+
 private:
     void check(int rc, const char *where) const;
     hrt_launch makeLaunch(const RayTracingLaunchParams &p, std::vector<uint8_t> &flags, std::vector<float> &peak,
@@ -64,6 +68,7 @@ private:
     hrt_context *ctx_ = nullptr;
     size_t nprims_ = 0;
     size_t launch_bands_ = 0;
+    std::vector<float> voxel_lad_;
 };
 
 }  // namespace helios

@@ -106,6 +106,8 @@ struct hrt_context {
     std::vector<int8_t> h_twosided;
     std::vector<uint32_t> h_voxels;  // original indices of voxel primitives
     DevBuf T, type, twosided, bbox, rec, rgen, nodes, codes, perm, bvh_scratch, lad, area, nodes4;
+    DevBuf mask_id, mask_uv_id, mask_uv, mask_size, mask_offset, mask_data;
+    bool masks = false;
     int n4 = 0;  // compressed 4-wide nodes built
     // materials and sources
     int mS = 0, mN = 0, mB = 0;
@@ -175,6 +177,16 @@ TraceScene scene_of(hrt_context *ctx) {
     sc.status = ctx->status.as<uint32_t>();
     sc.rays = ctx->counter.as<unsigned long long>();
     sc.visits = (ctx->measure & 1) ? ctx->visits.as<unsigned long long>() : nullptr;
+    sc.masks = MaskSet{};
+    if (ctx->masks) {
+        sc.masks.id = ctx->mask_id.as<int32_t>();
+        sc.masks.uv_id = ctx->mask_uv_id.as<int32_t>();
+        sc.masks.uv = ctx->mask_uv.as<float>();
+        sc.masks.size = ctx->mask_size.as<int32_t>();
+        sc.masks.offset = ctx->mask_offset.as<uint32_t>();
+        sc.masks.data = ctx->mask_data.as<uint8_t>();
+        sc.masks.T = ctx->T.as<float>();
+    }
     return sc;
 }
 
@@ -606,6 +618,42 @@ int hrt_update_geometry(hrt_context *ctx, const hrt_geometry *g) {
         CU(cudaMemcpyAsync(ctx->lad.p, g->voxel_lad, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
     }
     ctx->h_voxels.swap(voxels);
+    // texture masks
+    ctx->masks = false;
+    if (g->mask_id && g->nmasks > 0 && n) {
+        if (!g->mask_size || !g->mask_data) return fail(ctx, HRT_EINVAL, "masks need mask_size and mask_data");
+        std::vector<uint32_t> off((size_t)g->nmasks);
+        size_t total = 0;
+        for (int k = 0; k < g->nmasks; ++k) {
+            if (g->mask_size[2 * k] < 1 || g->mask_size[2 * k + 1] < 1) return fail(ctx, HRT_EINVAL, "empty mask");
+            off[k] = (uint32_t)total;
+            total += (size_t)g->mask_size[2 * k] * (size_t)g->mask_size[2 * k + 1];
+        }
+        if (total >= (1ull << 32)) return fail(ctx, HRT_EINVAL, "mask data above 4 GB");
+        for (size_t i = 0; i < n; ++i)
+            if (g->mask_id[i] >= g->nmasks || g->mask_id[i] < -1) return fail(ctx, HRT_EINVAL, "mask id out of range");
+        std::vector<int32_t> uvid(n, -1);
+        std::vector<float> uv(8 * n, 0.f);
+        if (g->uv_id && g->uv) {
+            uvid.assign(g->uv_id, g->uv_id + n);
+            uv.assign(g->uv, g->uv + 8 * n);
+        }
+        CU(ctx->mask_id.ensure(ctx->stream, n * sizeof(int32_t)));
+        CU(ctx->mask_uv_id.ensure(ctx->stream, n * sizeof(int32_t)));
+        CU(ctx->mask_uv.ensure(ctx->stream, 8 * n * sizeof(float)));
+        CU(ctx->mask_size.ensure(ctx->stream, 2 * (size_t)g->nmasks * sizeof(int32_t)));
+        CU(ctx->mask_offset.ensure(ctx->stream, (size_t)g->nmasks * sizeof(uint32_t)));
+        CU(ctx->mask_data.ensure(ctx->stream, std::max<size_t>(total, 1)));
+        CU(cudaMemcpyAsync(ctx->mask_id.p, g->mask_id, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+        CU(cudaMemcpyAsync(ctx->mask_uv_id.p, uvid.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+        CU(cudaMemcpyAsync(ctx->mask_uv.p, uv.data(), 8 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        CU(cudaMemcpyAsync(ctx->mask_size.p, g->mask_size, 2 * (size_t)g->nmasks * sizeof(int32_t),
+                           cudaMemcpyHostToDevice, ctx->stream));
+        CU(cudaMemcpyAsync(ctx->mask_offset.p, off.data(), off.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        CU(cudaMemcpyAsync(ctx->mask_data.p, g->mask_data, total, cudaMemcpyHostToDevice, ctx->stream));
+        ctx->masks = true;
+    }
     ctx->nbbox = g->nbbox;
     ctx->px = g->periodic_x;
     ctx->py = g->periodic_y;

@@ -477,12 +477,86 @@ __device__ __forceinline__ bool voxel_hit(f3 o, f3 inv, float tmin, f3 lo, f3 hi
     return true;
 }
 
+// ---------------------------------------------------------------- texture masks ---
+// A masked patch or triangle is hit only where its mask texel is opaque (reference
+// OptiX8DeviceCode.cu:173-187, 397-416, 457-476); origins avoid transparent texels.
+struct MaskSet {
+    const int32_t *id;       // [n] mask of each primitive (original order, -1 none); null: no masks
+    const int32_t *uv_id;    // [n] >= 0: uv holds the primitive's texture coordinates
+    const float *uv;         // [n*8] corner (u,v) pairs
+    const int32_t *size;     // [nmasks*2] width, height
+    const uint32_t *offset;  // [nmasks] start of each mask in data
+    const uint8_t *data;     // row-major texels, nonzero = opaque
+    const float *T;          // [n*16] transforms (original order)
+};
+
+__device__ __forceinline__ bool mask_opaque(const MaskSet &m, int id, float u, float v) {
+    const int w = m.size[2 * id], h = m.size[2 * id + 1];
+    int ix = (int)floorf((float)(w - 1) * u);
+    int iy = (int)floorf((float)(h - 1) * (1.0f - v));
+    ix = ix < 0 ? 0 : (ix > w - 1 ? w - 1 : ix);
+    iy = iy < 0 ? 0 : (iy > h - 1 ? h - 1 : iy);
+    return m.data[m.offset[id] + (uint32_t)(iy * w + ix)] != 0;
+}
+
+// texture (u, v) of patch p at local coordinates (lu, lv) in [-0.5, 0.5]^2
+__device__ __forceinline__ void patch_uv(const MaskSet &m, uint32_t p, float lu, float lv, float *uu, float *vv) {
+    if (m.uv_id[p] >= 0) {
+        const float *q = m.uv + 8 * (size_t)p;
+        *uu = q[0] + (lu + 0.5f) * (q[2] - q[0]);
+        *vv = q[1] + (lv + 0.5f) * (q[5] - q[1]);
+    } else {
+        *uu = lu + 0.5f;
+        *vv = lv + 0.5f;
+    }
+}
+
+// texture (u, v) of triangle p at barycentrics beta (vertex 1) and gamma (vertex 2)
+__device__ __forceinline__ void tri_uv(const MaskSet &m, uint32_t p, float beta, float gamma, float *uu, float *vv) {
+    if (m.uv_id[p] >= 0) {
+        const float *q = m.uv + 8 * (size_t)p;
+        *uu = (q[0] + beta * (q[2] - q[0])) + gamma * (q[4] - q[0]);
+        *vv = 1.0f - ((q[1] + beta * (q[3] - q[1])) + gamma * (q[5] - q[1]));
+    } else {
+        *uu = beta + gamma;
+        *vv = gamma;
+    }
+}
+
+// Is the geometric hit at distance t on masked primitive p on an opaque texel?  Patches
+// use the local coordinates of the hit point, triangles the Cramer barycentrics.
+static __device__ __noinline__ bool mask_hit_opaque(const MaskSet &m, uint32_t p, uint32_t type, f3 o, f3 d, float t) {
+    const float *T = m.T + 16 * (size_t)p;
+    float uu, vv;
+    if (type == PT_TRI) {
+        const f3 v0 = mk(T[3], T[7], T[11]), v1 = xform(T, 0.f, 1.f), v2 = xform(T, 1.f, 1.f);
+        const float a = v0.x - v1.x, b = v0.x - v2.x, c = d.x, dd = v0.x - o.x;
+        const float e = v0.y - v1.y, f = v0.y - v2.y, g = d.y, h = v0.y - o.y;
+        const float i = v0.z - v1.z, j = v0.z - v2.z, k = d.z, l = v0.z - o.z;
+        const float mm = f * k - g * j, nn = h * k - g * l, pp = f * l - h * j;
+        const float q = g * i - e * k, sq = e * j - f * i;
+        const float den = a * mm + b * q + c * sq;
+        if (den == 0.f) return true;
+        const float iv = 1.f / den;
+        const float beta = (dd * mm - b * nn - c * pp) * iv;
+        const float r = e * l - h * i;
+        const float gamma = (a * nn + dd * q + c * r) * iv;
+        tri_uv(m, p, beta, gamma, &uu, &vv);
+    } else {
+        const f3 hl = sub(add(o, scl(d, t)), mk(T[3], T[7], T[11]));
+        const f3 lx = mk(T[0], T[4], T[8]), ly = mk(T[1], T[5], T[9]);
+        const float lu = dot(hl, lx) / dot(lx, lx), lv = dot(hl, ly) / dot(ly, ly);
+        patch_uv(m, p, lu, lv, &uu, &vv);
+    }
+    return mask_opaque(m, m.id[p], uu, vv);
+}
+
 // Test record `slot`; on success returns t, face and the original primitive index.
 // VOX = false leaves voxels out (for scenes known to hold none).
 template <bool VOX = true>
 __device__ __forceinline__ bool rec_hit(const float4 *__restrict__ rec, uint32_t slot, const WT &w, f3 o, f3 d,
                                         f3 inv, float tmin, float tmax, const VoxKey &vk, float *t, int *face,
-                                        uint32_t *orig) {
+                                        uint32_t *orig, const MaskSet &ms) {
     const float4 *r = rec + 4 * (size_t)slot;
     float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2);
     uint32_t type = __float_as_uint(r0.w);
@@ -502,6 +576,8 @@ __device__ __forceinline__ bool rec_hit(const float4 *__restrict__ rec, uint32_t
     } else {
         ok = false;
     }
+    if (ok && ms.id && (type == PT_TRI || type == PT_PATCH) && ms.id[*orig] >= 0)
+        ok = mask_hit_opaque(ms, *orig, type, o, d, *t);
     return ok;
 }
 

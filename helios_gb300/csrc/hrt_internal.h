@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "hrt_device.cuh"
+
 namespace hrt {
 
 // Scene as the trace kernels see it.
@@ -22,6 +24,7 @@ struct TraceScene {
     uint32_t *status;     // device error word (ERR_* bits)
     unsigned long long *rays; // traced-ray counter
     unsigned long long *visits; // [2] node visits, primitive tests (statistics launches only)
+    MaskSet masks;        // texture masks (masks.id null: none)
 };
 
 // Radiation source in device form (rotation pre-expanded to a 3x3 matrix on the host).

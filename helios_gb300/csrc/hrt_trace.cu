@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kBlock) k_direct(const DirectParams P) {
                 const uint32_t c2 = (uint32_t)(k << 1);
                 u4 u = philox(r, p, c2, 0u, P.seed, P.pass);
                 const bool vox = type == PT_VOXEL;
-                f3 org = direct_origin(g, type, r, p, c2, P.dimx, P.dimy, P.seed, P.pass, u);
+                f3 org = direct_origin(g, type, r, p, c2, P.dimx, P.dimy, P.seed, P.pass, u, P.sc.masks);
                 f3 nrm = xyz(g[3]);
                 f3 dir;
                 float tmax;
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kBlock) k_diffuse(const DiffuseParams P) {
             load_rgen(P.sc, p, g);
             uint32_t type = __float_as_uint(g[0].w);
             f3 org, dir;
-            diffuse_ray<true>(g, type, r, p, face, P.dimx, P.dimy, P.seed, P.pass, &org, &dir);
+            diffuse_ray<true>(g, type, r, p, face, P.dimx, P.dimy, P.seed, P.pass, &org, &dir, P.sc.masks);
             Hit h = trace_full<STATS>(P.sc, org, dir, 1e-4f, 1e38f, false, VoxKey{r, p, (uint32_t)face, P.seed, P.pass},
                                       &nv, &np);
             if (h.prim == kLost) {
@@ -246,10 +246,10 @@ __global__ void k_gen_rays(const TraceScene sc, int kind, uint32_t seed, uint32_
     f3 org, dir;
     if (kind == 0) {
         const u4 u = philox(r, p, (uint32_t)face, 0u, seed, pass);
-        org = direct_origin(g, type, r, p, (uint32_t)face, dimx, dimy, seed, pass, u);
+        org = direct_origin(g, type, r, p, (uint32_t)face, dimx, dimy, seed, pass, u, sc.masks);
         dir = normalize(mk(dx, dy, dz));
     } else {
-        diffuse_ray<true>(g, type, r, p, face, dimx, dimy, seed, pass, &org, &dir);
+        diffuse_ray<true>(g, type, r, p, face, dimx, dimy, seed, pass, &org, &dir, sc.masks);
     }
     o[3 * i] = org.x;
     o[3 * i + 1] = org.y;
@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(kBlock) k_direct_sweep(const SweepDirectParams
             const int ts = P.sc.twosided[p];
             const uint32_t type = __float_as_uint(g[0].w);
             const u4 u = philox(r, p, 0u, 0u, P.seed, 0u);
-            const f3 org = direct_origin(g, type, r, p, 0u, P.dimx, P.dimy, P.seed, 0u, u);
+            const f3 org = direct_origin(g, type, r, p, 0u, P.dimx, P.dimy, P.seed, 0u, u, P.sc.masks);
             const f3 nrm = xyz(g[3]);
             const f3 dd = normalize(mk(P.sun_dir[3 * sun], P.sun_dir[3 * sun + 1], P.sun_dir[3 * sun + 2]));
             const double strength = inv_nr * (double)fabsf(dot(nrm, dd));

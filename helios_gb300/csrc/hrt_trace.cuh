@@ -71,7 +71,7 @@ __device__ Hit trace_bvh(const TraceScene &sc, f3 o, f3 d, float tmin, float tma
                 int face;
                 uint32_t orig;
                 if (STATS) ++*np;
-                if (rec_hit(sc.rec, (uint32_t)(~ck), w, o, d, inv, tmin, best, vk, &t, &face, &orig)) {
+                if (rec_hit(sc.rec, (uint32_t)(~ck), w, o, d, inv, tmin, best, vk, &t, &face, &orig, sc.masks)) {
                     if (h.prim == 0xFFFFFFFFu || t < h.t || (t == h.t && orig < h.prim)) {
                         h.t = t;
                         h.prim = orig;
@@ -214,14 +214,40 @@ __device__ __forceinline__ double proj(f3 nrm, f3 d, bool vox) {
 // Origin of direct ray r of primitive p; u = philox(r, p, c2, 0; seed, pass), c2 =
 // source << 1.  Non-triangles are stratified over dimx x dimy cells
 // (OptiX8DeviceCode.cu:1270-1290); a voxel's third coordinate uses counter c2 | 1.
+// Origins on masked primitives avoid transparent texels (OptiX8DeviceCode.cu:1252-1308):
+// up to ten redraws, uniform over the primitive, from Philox counters
+// (r, p, c2, 2^31 | attempt); the tenth redraw is kept unchecked, as in the reference.
+__device__ __noinline__ void mask_origin(const MaskSet &ms, uint32_t type, uint32_t r, uint32_t p, uint32_t c2,
+                                         uint32_t seed, uint32_t pass, float *uu, float *vv) {
+    for (uint32_t a = 0; a < 10; ++a) {
+        float fu, fv;
+        if (type == PT_TRI) {
+            const float lo = *uu < *vv ? *uu : *vv, hi = *uu < *vv ? *vv : *uu;
+            tri_uv(ms, p, hi - lo, lo, &fu, &fv);
+        } else {
+            patch_uv(ms, p, *uu - 0.5f, *vv - 0.5f, &fu, &fv);
+        }
+        if (mask_opaque(ms, ms.id[p], fu, fv)) return;
+        const u4 q = philox(r, p, c2, 0x80000000u | (a + 1u), seed, pass);
+        *uu = u01(q.a);
+        *vv = u01(q.b);
+    }
+}
+
+__device__ __forceinline__ bool masked_origin(const MaskSet &ms, uint32_t type, uint32_t p) {
+    return ms.id && (type == PT_PATCH || type == PT_TILE || type == PT_TRI) && ms.id[p] >= 0;
+}
+
 __device__ __forceinline__ f3 direct_origin(const float4 g[4], uint32_t type, uint32_t r, uint32_t p, uint32_t c2,
-                                            int dimx, int dimy, uint32_t seed, uint32_t pass, const u4 &u) {
+                                            int dimx, int dimy, uint32_t seed, uint32_t pass, const u4 &u,
+                                            const MaskSet &ms) {
     float uu = u01(u.a), vv = u01(u.b), ww = 0.f;
     if (type != PT_TRI) {
         const int xi = (int)(r % (uint32_t)dimx), yi = (int)(r / (uint32_t)dimx);
         uu = ((float)xi + uu) / (float)dimx;
         vv = ((float)yi + vv) / (float)dimy;
     }
+    if (masked_origin(ms, type, p)) mask_origin(ms, type, r, p, c2, seed, pass, &uu, &vv);
     if (type == PT_VOXEL) ww = u01(philox(r, p, c2 | 1u, 0u, seed, pass).a);
     return sample_point(g, type, uu, vv, ww);
 }
@@ -232,7 +258,8 @@ __device__ __forceinline__ f3 direct_origin(const float4 g[4], uint32_t type, ui
 // coordinate comes from (r, p, 2, 0), and the bottom face flips the direction.
 template <bool VOX>
 __device__ __forceinline__ void diffuse_ray(const float4 g[4], uint32_t type, uint32_t r, uint32_t p, int face,
-                                            int dimx, int dimy, uint32_t seed, uint32_t pass, f3 *org, f3 *dir) {
+                                            int dimx, int dimy, uint32_t seed, uint32_t pass, f3 *org, f3 *dir,
+                                            const MaskSet &ms) {
     const int ti = (int)(r % (uint32_t)dimx), pi = (int)(r / (uint32_t)dimx);
     f3 dd;
     if (VOX && type == PT_VOXEL) {
@@ -243,7 +270,9 @@ __device__ __forceinline__ void diffuse_ray(const float4 g[4], uint32_t type, ui
     } else {
         const u4 u = philox(r, p, (uint32_t)face, 0u, seed, pass);
         dd = diffuse_dir(xyz(g[3]), ti, pi, dimx, dimy, u01(u.a), u01(u.b));
-        *org = sample_point(g, type, u01(u.c), u01(u.d), 0.f);
+        float uu = u01(u.c), vv = u01(u.d);
+        if (masked_origin(ms, type, p)) mask_origin(ms, type, r, p, (uint32_t)face, seed, pass, &uu, &vv);
+        *org = sample_point(g, type, uu, vv, 0.f);
     }
     *dir = (face == 0) ? mk(-dd.x, -dd.y, -dd.z) : dd;
 }
@@ -367,7 +396,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
                         float4 g[4];
                         load_rgen(sc, p, g);
                         const uint32_t type = __float_as_uint(g[0].w);
-                        diffuse_ray<VOX>(g, type, r, p, face, P.dimx, P.dimy, P.seed, P.pass, &o, &d);
+                        diffuse_ray<VOX>(g, type, r, p, face, P.dimx, P.dimy, P.seed, P.pass, &o, &d, sc.masks);
                         if (VOX) rr = r;
                         w = wt_setup(d);
                         inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
@@ -523,7 +552,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
                 int fc;
                 uint32_t orig;
                 const VoxKey vk{rr, p, (uint32_t)face | ((uint32_t)wraps << 16), P.seed, P.pass};
-                if (rec_hit<VOX>(sc.rec, slot, w, o, d, inv, 1e-4f, best, vk, &t, &fc, &orig)) {
+                if (rec_hit<VOX>(sc.rec, slot, w, o, d, inv, 1e-4f, best, vk, &t, &fc, &orig, sc.masks)) {
                     if (bprim == 0xFFFFFFFFu || t < best || (t == best && orig < bprim)) {
                         best = t;
                         bprim = orig;

@@ -41,6 +41,11 @@ class Context:
         self.primitive_data: dict[str, dict[int, object]] = {}
         self.bulk_data: dict[str, np.ndarray] = {}
         self.global_data: dict[str, object] = {}
+        # texture masks: 2-D uint8 arrays (row 0 = top of the image, nonzero = opaque)
+        self.masks: list[np.ndarray] = []
+        self._mask_index: dict[int, int] = {}
+        self.mask_of: dict[int, int] = {}
+        self.uv_of: dict[int, np.ndarray] = {}
 
     # --------------------------------------------------------------- geometry
     def _add_many(self, T, ptype, area):
@@ -56,18 +61,62 @@ class Context:
     def _add(self, T, ptype, area):
         return self._add_many(T, ptype, area)
 
-    def addPatch(self, center=(0, 0, 0), size=(1, 1), rotation=(0.0, 0.0)):
-        """rotation = (elevation, azimuth) radians, as SphericalCoord(1, elevation, azimuth)."""
+    def _set_mask(self, uuid, texture_mask, uv):
+        if texture_mask is None:
+            return
+        m = np.ascontiguousarray(texture_mask, np.uint8)
+        if m.ndim != 2 or m.size == 0:
+            raise HeliosRuntimeError("ERROR (Context): a texture mask is a non-empty 2-D array.")
+        k = self._mask_index.get(id(texture_mask))
+        if k is None:
+            k = len(self.masks)
+            self.masks.append(m)
+            self._mask_index[id(texture_mask)] = k
+        self.mask_of[int(uuid)] = k
+        if uv is not None:
+            q = np.zeros(8, np.float32)
+            uv = np.asarray(uv, np.float32).reshape(-1, 2)
+            q[: 2 * len(uv)] = uv.ravel()
+            for j in range(len(uv), 4):  # pad to four corners with the last (as the reference does)
+                q[2 * j: 2 * j + 2] = uv[-1]
+            self.uv_of[int(uuid)] = q
+
+    def addPatch(self, center=(0, 0, 0), size=(1, 1), rotation=(0.0, 0.0), texture_mask=None, uv=None):
+        """rotation = (elevation, azimuth) radians, as SphericalCoord(1, elevation, azimuth).
+        texture_mask: 2-D array standing in for a texture's transparency channel (row 0 = top,
+        nonzero = opaque); uv: texture (u, v) of the corners (-x-y, +x-y, +x+y, -x+y)."""
         if size[0] < 1e-6 or size[1] < 1e-6:
             raise HeliosRuntimeError("ERROR (Context::addPatch): Size of patch must be greater than 1e-6 "
                                      "to avoid numerical precision issues.")
         T = scenes.helios_patch_T(center, size, rotation[0], rotation[1])
-        return self._add(T, scenes.PATCH, size[0] * size[1])
+        u = self._add(T, scenes.PATCH, size[0] * size[1])
+        self._set_mask(u, texture_mask, uv)
+        return u
 
-    def addTriangle(self, v0, v1, v2):
+    def addTriangle(self, v0, v1, v2, texture_mask=None, uv=None):
+        """texture_mask as for addPatch; uv: texture (u, v) of v0, v1, v2."""
         T = scenes.triangle_T(v0, v1, v2)[0]
         a = 0.5 * np.linalg.norm(np.cross(np.subtract(v1, v0), np.subtract(v2, v0)))
-        return self._add(T, scenes.TRIANGLE, a)
+        u = self._add(T, scenes.TRIANGLE, a)
+        self._set_mask(u, texture_mask, uv)
+        return u
+
+    def mask_arrays(self):
+        """Texture masks in the layout of hrt_geometry, or None without masks."""
+        if not self.mask_of:
+            return None
+        n = self._n
+        mid = np.full(n, -1, np.int32)
+        uvid = np.full(n, -1, np.int32)
+        uv = np.zeros((n, 8), np.float32)
+        for k, v in self.mask_of.items():
+            mid[k] = v
+        for k, q in self.uv_of.items():
+            uvid[k] = k
+            uv[k] = q
+        sizes = np.array([[m.shape[1], m.shape[0]] for m in self.masks], np.int32)
+        data = np.concatenate([m.ravel() for m in self.masks]).astype(np.uint8)
+        return {"mask_id": mid, "uv_id": uvid, "uv": uv, "sizes": sizes, "data": data}
 
     def addTile(self, center=(0, 0, 0), size=(1, 1), rotation=(0.0, 0.0), div=(1, 1)):
         s = scenes.tile_grid(center, size, div, twosided=1)
@@ -416,7 +465,8 @@ class RadiationModel:
     def updateGeometry(self):
         T, ty, ts = self.geometry_arrays()
         self._ts = ts
-        self.ctx.update_geometry(T, ty, ts, self._bbox_faces(), self.periodic, self.voxel_lad())
+        self.ctx.update_geometry(T, ty, ts, self._bbox_faces(), self.periodic, self.voxel_lad(),
+                                 self.context.mask_arrays())
         self.ctx.build_accel()
         self._geom_n = T.shape[0]
 

@@ -63,6 +63,15 @@ typedef struct {
     const float *bbox_vertices;   /* [nbbox*4*3] wall corners (bboxes.vertices) */
     float periodic_x, periodic_y; /* periodic_flag */
     const float *voxel_lad;       /* [n] leaf area density (m^2/m^3) read for voxels; may be NULL without voxels */
+    /* Texture masks (RayTracingGeometry mask_IDs / uv_IDs / uv_data / mask_sizes / mask_data,
+     * RayTracingTypes.h:72-77): a masked patch or triangle is hit, and launches rays, only
+     * where its mask texel is nonzero.  mask_id NULL or nmasks 0: no masks. */
+    const int32_t *mask_id;       /* [n] mask of each primitive, -1 none */
+    const int32_t *uv_id;         /* [n] >= 0: uv holds the primitive's texture coordinates, or NULL */
+    const float *uv;              /* [n*8] (u,v) of the canonical corners 0..3 (triangles: 0..2), or NULL */
+    int32_t nmasks;
+    const int32_t *mask_size;     /* [nmasks*2] width, height */
+    const uint8_t *mask_data;     /* masks one after another, each row-major [y][x] */
 } hrt_geometry;
 
 /* helios::RayTracingSource (RayTracingTypes.h:189-196) without the flux vectors,

@@ -441,12 +441,89 @@ inline bool voxel_hit(const Ray &ray, const V3 &inv, const Rec &r, uint32_t vid,
     return true;
 }
 
+// Texture masks (OptiX8DeviceCode.cu:173-187, 397-416, 457-476): a masked patch or triangle
+// is hit only where its mask texel is opaque.  (u, v) follow the reference: patches from
+// the local coordinates of the hit point, triangles from the Cramer barycentrics; custom
+// per-primitive UVs are mapped linearly (patches) or barycentrically (triangles).
+struct Masks {
+    std::vector<int32_t> id, uv_id, size;  // [n], [n], [nm*2]
+    std::vector<float> uv;                 // [n*8]: corners (u,v) 0..3
+    std::vector<uint32_t> offset;          // [nm]
+    std::vector<uint8_t> data;
+    const float *T = nullptr;              // transforms of the scene
+};
+
+inline bool mask_opaque(const Masks &m, int id, float u, float v) {
+    const int w = m.size[2 * id], h = m.size[2 * id + 1];
+    int ix = (int)std::floor((float)(w - 1) * u);
+    int iy = (int)std::floor((float)(h - 1) * (1.0f - v));
+    ix = ix < 0 ? 0 : (ix > w - 1 ? w - 1 : ix);
+    iy = iy < 0 ? 0 : (iy > h - 1 ? h - 1 : iy);
+    return m.data[m.offset[id] + (uint32_t)(iy * w + ix)] != 0;
+}
+
+// texture (u, v) of patch p at local coordinates (lu, lv) in [-0.5, 0.5]^2
+inline void patch_uv(const Masks &m, int p, float lu, float lv, float *uu, float *vv) {
+    if (m.uv_id[p] >= 0) {
+        const float *q = &m.uv[8 * (size_t)p];
+        *uu = q[0] + (lu + 0.5f) * (q[2] - q[0]);
+        *vv = q[1] + (lv + 0.5f) * (q[5] - q[1]);
+    } else {
+        *uu = lu + 0.5f;
+        *vv = lv + 0.5f;
+    }
+}
+
+// texture (u, v) of triangle p at barycentrics beta (vertex 1) and gamma (vertex 2)
+inline void tri_uv(const Masks &m, int p, float beta, float gamma, float *uu, float *vv) {
+    if (m.uv_id[p] >= 0) {
+        const float *q = &m.uv[8 * (size_t)p];
+        *uu = (q[0] + beta * (q[2] - q[0])) + gamma * (q[4] - q[0]);
+        *vv = 1.0f - ((q[1] + beta * (q[3] - q[1])) + gamma * (q[5] - q[1]));
+    } else {
+        *uu = beta + gamma;
+        *vv = gamma;
+    }
+}
+
+// Is the geometric hit at distance t on masked primitive p on an opaque texel?
+inline bool mask_hit_opaque(const Masks &m, int p, int type, const Ray &ray, float t) {
+    const float *T = m.T + 16 * (size_t)p;
+    V3 o = ray.o, d = ray.d;
+    float uu, vv;
+    if (type == PT_TRI) {
+        V3 v0 = v3(T[3], T[7], T[11]);
+        V3 v1 = xform(T, 0.f, 1.f), v2 = xform(T, 1.f, 1.f);
+        float a = v0.x - v1.x, b = v0.x - v2.x, c = d.x, dd = v0.x - o.x;
+        float e = v0.y - v1.y, f = v0.y - v2.y, g = d.y, h = v0.y - o.y;
+        float i = v0.z - v1.z, j = v0.z - v2.z, k = d.z, l = v0.z - o.z;
+        float mm = f * k - g * j, nn = h * k - g * l, pp = f * l - h * j;
+        float q = g * i - e * k, sq = e * j - f * i;
+        float den = a * mm + b * q + c * sq;
+        if (den == 0.f) return true;
+        float iv = 1.f / den;
+        float beta = (dd * mm - b * nn - c * pp) * iv;
+        float r = e * l - h * i;
+        float gamma = (a * nn + dd * q + c * r) * iv;
+        tri_uv(m, p, beta, gamma, &uu, &vv);
+    } else {
+        V3 hl = vsub(vadd(o, vscale(d, t)), v3(T[3], T[7], T[11]));
+        V3 lx = v3(T[0], T[4], T[8]), ly = v3(T[1], T[5], T[9]);
+        float lu = vdot(hl, lx) / vdot(lx, lx), lv = vdot(hl, ly) / vdot(ly, ly);
+        patch_uv(m, p, lu, lv, &uu, &vv);
+    }
+    return mask_opaque(m, m.id[p], uu, vv);
+}
+
 inline bool prim_hit(const WT &w, const Ray &ray, const V3 &inv, const Rec &r, uint32_t id, float tmax,
-                     float *t, int *face) {
+                     float *t, int *face, const Masks *mk = nullptr) {
     switch (r.type) {
         case PT_TRI:
-            return poly_hit(w, ray, r.p, 3, tmax, t, face);
+            if (!poly_hit(w, ray, r.p, 3, tmax, t, face)) return false;
+            return !(mk && mk->id[id] >= 0) || mask_hit_opaque(*mk, (int)id, PT_TRI, ray, *t);
         case PT_PATCH:
+            if (!poly_hit(w, ray, r.p, 4, tmax, t, face)) return false;
+            return !(mk && mk->id[id] >= 0) || mask_hit_opaque(*mk, (int)id, PT_PATCH, ray, *t);
         case PT_BBOX:
             return poly_hit(w, ray, r.p, 4, tmax, t, face);
         case PT_DISK:
@@ -541,6 +618,8 @@ struct Scene {
     std::vector<Rec> rec;       // original order
     std::vector<RGen> rgen;     // original order
     std::vector<double> area;   // original order (voxels: leaf area)
+    Masks masks;                // texture masks (empty: none)
+    const Masks *mk() const { return masks.id.empty() ? nullptr : &masks; }
     // BVH
     std::vector<uint64_t> codes;    // sorted Morton codes
     std::vector<uint32_t> perm;     // sorted slot -> original primitive
@@ -754,7 +833,7 @@ Hit trace_bvh(const Scene &s, const Ray &ray, bool anyhit, TraceStats *st) {
                 if (st) st->prims++;
                 float t;
                 int face;
-                if (prim_hit(w, ray, inv, s.rec[p], (uint32_t)p, best, &t, &face)) {
+                if (prim_hit(w, ray, inv, s.rec[p], (uint32_t)p, best, &t, &face, s.mk())) {
                     if (h.prim < 0 || better(t, p, h.t, h.prim)) {
                         h.t = t;
                         h.prim = p;
@@ -792,7 +871,7 @@ Hit trace_brute(const Scene &s, const Ray &ray, bool reference_formula) {
         int face;
         bool ok = reference_formula
                       ? prim_hit_reference(ray, &s.T[16 * (size_t)p], (int)s.type[p], ray.tmax, &t, &face)
-                      : prim_hit(w, ray, inv, s.rec[p], (uint32_t)p, ray.tmax, &t, &face);
+                      : prim_hit(w, ray, inv, s.rec[p], (uint32_t)p, ray.tmax, &t, &face, s.mk());
         if (ok && (h.prim < 0 || better(t, p, h.t, h.prim))) {
             h.t = t;
             h.prim = p;
@@ -998,14 +1077,36 @@ inline V3 diffuse_dir(V3 n, int ti, int pi, int dimx, int dimy, float j0, float 
 // Origin of direct ray r of primitive p; u = philox(r, p, c2, 0; seed, pass) with c2 =
 // source << 1.  Patches, disks and voxels are stratified in (u, v) over dimx x dimy cells
 // (OptiX8DeviceCode.cu:1270-1290); a voxel's third coordinate comes from counter c2 | 1.
+// Origins on masked primitives avoid transparent texels (OptiX8DeviceCode.cu:1252-1308):
+// up to ten redraws, uniform over the primitive, from Philox counters
+// (r, p, c2, 2^31 | attempt); the tenth redraw is kept unchecked, as in the reference.
+inline void mask_origin(const Masks *mk, int type, uint32_t r, uint32_t p, uint32_t c2, uint32_t seed,
+                        uint32_t pass, float *uu, float *vv) {
+    if (!mk || mk->id[p] < 0 || !(type == PT_PATCH || type == PT_TILE || type == PT_TRI)) return;
+    for (uint32_t a = 0; a < 10; ++a) {
+        float fu, fv;
+        if (type == PT_TRI) {
+            float lo = *uu < *vv ? *uu : *vv, hi = *uu < *vv ? *vv : *uu;
+            tri_uv(*mk, (int)p, hi - lo, lo, &fu, &fv);
+        } else {
+            patch_uv(*mk, (int)p, *uu - 0.5f, *vv - 0.5f, &fu, &fv);
+        }
+        if (mask_opaque(*mk, mk->id[p], fu, fv)) return;
+        U4 q = philox(r, p, c2, 0x80000000u | (a + 1u), seed, pass);
+        *uu = u01(q.v[0]);
+        *vv = u01(q.v[1]);
+    }
+}
+
 inline V3 direct_origin(const RGen &g, int type, uint32_t r, uint32_t p, uint32_t c2, int dimx, int dimy,
-                        uint32_t seed, uint32_t pass, const U4 &u) {
+                        uint32_t seed, uint32_t pass, const U4 &u, const Masks *mk = nullptr) {
     float uu = u01(u.v[0]), vv = u01(u.v[1]), ww = 0.f;
     if (type != PT_TRI) {
         int xi = (int)(r % (uint32_t)dimx), yi = (int)(r / (uint32_t)dimx);
         uu = ((float)xi + uu) / (float)dimx;
         vv = ((float)yi + vv) / (float)dimy;
     }
+    mask_origin(mk, type, r, p, c2, seed, pass, &uu, &vv);
     if (type == PT_VOXEL) ww = u01(philox(r, p, c2 | 1u, 0u, seed, pass).v[0]);
     return sample_point(g, type, uu, vv, ww);
 }
@@ -1015,7 +1116,7 @@ inline V3 direct_origin(const RGen &g, int type, uint32_t r, uint32_t p, uint32_
 // on voxels both faces share the sample of counter (r, p, 1, 0) (third coordinate from
 // (r, p, 2, 0)) and the bottom face flips the direction.
 inline void diffuse_ray(const RGen &g, int type, uint32_t r, uint32_t p, int face, int dimx, int dimy,
-                        uint32_t seed, uint32_t pass, V3 *org, V3 *dir) {
+                        uint32_t seed, uint32_t pass, V3 *org, V3 *dir, const Masks *mk = nullptr) {
     int ti = (int)(r % (uint32_t)dimx), pi = (int)(r / (uint32_t)dimx);
     V3 dd;
     if (type == PT_VOXEL) {
@@ -1026,7 +1127,9 @@ inline void diffuse_ray(const RGen &g, int type, uint32_t r, uint32_t p, int fac
     } else {
         U4 u = philox(r, p, (uint32_t)face, 0u, seed, pass);
         dd = diffuse_dir(g.N, ti, pi, dimx, dimy, u01(u.v[0]), u01(u.v[1]));
-        *org = sample_point(g, type, u01(u.v[2]), u01(u.v[3]), 0.f);
+        float uu = u01(u.v[2]), vv = u01(u.v[3]);
+        mask_origin(mk, type, r, p, (uint32_t)face, seed, pass, &uu, &vv);
+        *org = sample_point(g, type, uu, vv, 0.f);
     }
     *dir = (face == 0) ? v3(-dd.x, -dd.y, -dd.z) : dd;
 }
@@ -1072,6 +1175,12 @@ typedef struct {
     const float *bbox_verts;  // nbbox*4*3 world-space corners
     float periodic_x, periodic_y;
     const float *voxel_lad;   // n leaf area density (m^2/m^3), read for voxels; may be null without voxels
+    const int32_t *mask_id;   // n texture mask of each primitive (-1 none), or null: no masks
+    const int32_t *uv_id;     // n >= 0: uv holds the primitive's texture coordinates
+    const float *uv;          // n*8 corner (u,v) pairs, or null
+    int32_t nmasks;
+    const int32_t *mask_size; // nmasks*2 width, height
+    const uint8_t *mask_data; // all masks, row-major, nonzero = opaque
 } orc_geometry;
 
 typedef struct {
@@ -1124,6 +1233,23 @@ void *orc_scene_create(const orc_geometry *g) {
         s->rec[i] = make_rec(&s->T[16 * (size_t)i], (int)s->type[i], lad);
         s->rgen[i] = make_rgen(&s->T[16 * (size_t)i], (int)s->type[i]);
         s->area[i] = prim_area(&s->T[16 * (size_t)i], (int)s->type[i], lad);
+    }
+    if (g->mask_id && g->nmasks > 0) {
+        Masks &m = s->masks;
+        m.id.assign(g->mask_id, g->mask_id + g->n);
+        m.uv_id.assign(g->n, -1);
+        if (g->uv_id && g->uv) {
+            m.uv_id.assign(g->uv_id, g->uv_id + g->n);
+            m.uv.assign(g->uv, g->uv + 8 * (size_t)g->n);
+        }
+        m.size.assign(g->mask_size, g->mask_size + 2 * (size_t)g->nmasks);
+        uint32_t off = 0;
+        for (int k = 0; k < g->nmasks; ++k) {
+            m.offset.push_back(off);
+            off += (uint32_t)(m.size[2 * k] * m.size[2 * k + 1]);
+        }
+        m.data.assign(g->mask_data, g->mask_data + off);
+        m.T = s->T.data();
     }
     s->nbbox = g->nbbox;
     s->periodic[0] = g->periodic_x;
@@ -1224,10 +1350,11 @@ int orc_gen_rays(void *h, int kind, uint32_t seed, uint32_t pass, int32_t rpp, i
             if (kind == 0) {
                 U4 u = philox((uint32_t)r, (uint32_t)p, (uint32_t)face, 0u, seed, pass);
                 org = direct_origin(g, (int)s->type[p], (uint32_t)r, (uint32_t)p, (uint32_t)face, dimx, dimy, seed,
-                                    pass, u);
+                                    pass, u, s->mk());
                 dir = vnormalize(v3(dir3[0], dir3[1], dir3[2]));
             } else {
-                diffuse_ray(g, (int)s->type[p], (uint32_t)r, (uint32_t)p, face, dimx, dimy, seed, pass, &org, &dir);
+                diffuse_ray(g, (int)s->type[p], (uint32_t)r, (uint32_t)p, face, dimx, dimy, seed, pass, &org, &dir,
+                            s->mk());
             }
             size_t k = (size_t)p * nr + r;
             o[3 * k] = org.x;
@@ -1302,7 +1429,7 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
                 for (int k = 0; k < S; ++k) {
                     const uint32_t c2 = (uint32_t)(k << 1);
                     U4 u = philox((uint32_t)r, (uint32_t)p, c2, 0u, q->seed, 0u);
-                    V3 org = direct_origin(g, type, (uint32_t)r, (uint32_t)p, c2, dimx, dimy, q->seed, 0u, u);
+                    V3 org = direct_origin(g, type, (uint32_t)r, (uint32_t)p, c2, dimx, dimy, q->seed, 0u, u, s->mk());
                     V3 dir;
                     float tmax;
                     double strength;
@@ -1369,7 +1496,7 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
             std::vector<double> d_in(Bl, 0.0), d_top(Bl, 0.0), d_bot(Bl, 0.0);
             for (int r = 0; r < dimx * dimy; ++r) {
                 V3 org, dir;
-                diffuse_ray(g, type, (uint32_t)r, (uint32_t)p, face, dimx, dimy, q->seed, pass, &org, &dir);
+                diffuse_ray(g, type, (uint32_t)r, (uint32_t)p, face, dimx, dimy, q->seed, pass, &org, &dir, s->mk());
                 TraceStats st;
                 Hit hh = trace_full(
                     *s, Ray{org, dir, 1e-4f, 1e38f, VoxKey{(uint32_t)r, (uint32_t)p, (uint32_t)face, q->seed, pass}},

@@ -41,6 +41,12 @@ class _Geometry(C.Structure):
         ("periodic_x", C.c_float),
         ("periodic_y", C.c_float),
         ("voxel_lad", C.c_void_p),
+        ("mask_id", C.c_void_p),
+        ("uv_id", C.c_void_p),
+        ("uv", C.c_void_p),
+        ("nmasks", C.c_int32),
+        ("mask_size", C.c_void_p),
+        ("mask_data", C.c_void_p),
     ]
 
 
@@ -100,7 +106,9 @@ def _ptr(a):
 class OracleScene:
     """Host scene: primitive records, the host LBVH twin and the FP64 solver."""
 
-    def __init__(self, T, ptype, twosided, bbox_verts=None, periodic=(0.0, 0.0), voxel_lad=None):
+    def __init__(self, T, ptype, twosided, bbox_verts=None, periodic=(0.0, 0.0), voxel_lad=None, masks=None):
+        """masks: None or dict(mask_id [n] int, uv_id [n] int or None, uv [n, 8] or None,
+        sizes [m, 2] (width, height), data: concatenated row-major uint8 masks)."""
         lib = _load()
         self.T = np.ascontiguousarray(T, dtype=np.float32).reshape(-1, 16)
         self.n = self.T.shape[0]
@@ -111,6 +119,16 @@ class OracleScene:
         g = _Geometry(self.n, _ptr(self.T), _ptr(self.type), _ptr(self.twosided),
                       0 if self.bbox is None else self.bbox.shape[0], _ptr(self.bbox),
                       float(periodic[0]), float(periodic[1]), _ptr(self.lad))
+        self._mask_keep = []
+        if masks is not None:
+            mid = np.ascontiguousarray(masks["mask_id"], np.int32)
+            sizes = np.ascontiguousarray(masks["sizes"], np.int32).reshape(-1, 2)
+            data = np.ascontiguousarray(masks["data"], np.uint8)
+            uvid = None if masks.get("uv_id") is None else np.ascontiguousarray(masks["uv_id"], np.int32)
+            uv = None if masks.get("uv") is None else np.ascontiguousarray(masks["uv"], np.float32).reshape(-1, 8)
+            self._mask_keep = [mid, sizes, data, uvid, uv]
+            g.mask_id, g.uv_id, g.uv = _ptr(mid), _ptr(uvid), _ptr(uv)
+            g.nmasks, g.mask_size, g.mask_data = sizes.shape[0], _ptr(sizes), _ptr(data)
         self._h = lib.orc_scene_create(C.byref(g))
         if not self._h:
             raise ValueError("oracle scene rejected (voxels need voxel_lad)")

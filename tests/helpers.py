@@ -33,7 +33,7 @@ def oracle_solve(desc: dict, rotation=rotation_np) -> dict:
 def oracle_scene_for(rad, oracle_mod):
     T, ty, ts = rad.geometry_arrays()
     bb = rad._bbox_faces()
-    return oracle_mod.OracleScene(T, ty, ts, bb, rad.periodic, rad.voxel_lad())
+    return oracle_mod.OracleScene(T, ty, ts, bb, rad.periodic, rad.voxel_lad(), rad.context.mask_arrays())
 
 
 def run_oracle(rad, labels, oracle_mod, scene=None, seed=None, threads=0):

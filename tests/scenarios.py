@@ -337,6 +337,56 @@ def disk_view_factor(run, ensemble=4, rays=50000, r=0.5, h=0.5):
     return [("disk_view_0", f[0, 0], 1 - F12, 0.005), ("disk_view_1", f[1, 0], 1 - F12, 0.005)]
 
 
+def disk_mask(res=512):
+    """Transparency mask of a disk inscribed in its square (nonzero = opaque), standing in
+    for the reference's disk.png texture."""
+    c = (np.arange(res) + 0.5) / res * 2.0 - 1.0
+    X, Y = np.meshgrid(c, c)
+    return (X * X + Y * Y <= 1.0).astype(np.uint8)
+
+
+def parallel_disks_masked(run, ensemble=4, ndir=10000, ndiff=200000):
+    """selfTest.cpp:961-1060: square patches masked to disks by a transparency texture --
+    a lower disk (r 1, rho 0.3) under two upper disks (r 0.5, facing down) at 0.75 m; SW
+    sun with one scattering bounce, LW emission at 300 K."""
+    rho, r1, r2, h = 0.3, 1.0, 0.5, 0.75
+    A1, A2 = math.pi * r1 * r1, math.pi * r2 * r2
+    R1, R2 = r1 / h, r2 / h
+    X = 1.0 + (1.0 + R2 * R2) / (R1 * R1)
+    F12 = 0.5 * (X - math.sqrt(X * X - 4.0 * (R2 / R1) ** 2))
+    sw0 = (A1 - A2) / A1 * (1.0 - rho)
+    sw1 = (A1 - A2) / A1 * F12 * A1 / A2 * rho
+    lw0 = SIGMA * 300.0 ** 4 * F12
+    lw1 = SIGMA * 300.0 ** 4 * F12 * A1 / A2
+    m = disk_mask()
+    ctx = Context()
+    ctx.addPatch((0, 0, 0), (2 * r1, 2 * r1), (0.0, 0.0), texture_mask=m)
+    ctx.addPatch((0, 0, h), (2 * r2, 2 * r2), (math.pi, 0.0), texture_mask=m)
+    ctx.addPatch((0, 0, h + 0.01), (2 * r2, 2 * r2), (math.pi, 0.0), texture_mask=m)
+    ctx.setPrimitiveData(0, "reflectivity_SW", rho)
+    for k in range(3):
+        ctx.setPrimitiveData(k, "twosided_flag", 0)
+    ctx.setPrimitiveData(0, "temperature", 300.0)
+    ctx.setPrimitiveData(1, "temperature", 300.0)
+    rad = RadiationModel(ctx)
+    sun = rad.addCollimatedRadiationSource((0, 0, 1))
+    rad.addRadiationBand("SW")
+    rad.disableEmission("SW")
+    rad.setDirectRayCount("SW", ndir)
+    rad.setDiffuseRayCount("SW", ndiff)
+    rad.setSourceFlux(sun, "SW", 1.0)
+    rad.setDiffuseRadiationFlux("SW", 0.0)
+    rad.setScatteringDepth("SW", 1)
+    rad.addRadiationBand("LW")
+    rad.setDiffuseRayCount("LW", ndiff)
+    rad.setDiffuseRadiationFlux("LW", 0.0)
+    rad.setScatteringDepth("LW", 0)
+    sw = _ensemble(run, rad, ["SW"], ensemble, seed0=51)
+    lw = _ensemble(run, rad, ["LW"], ensemble, seed0=52)
+    return [("masked_sw_0", sw[0, 0], sw0, 0.01), ("masked_sw_1", sw[1, 0], sw1, 0.01),
+            ("masked_lw_0", lw[0, 0], lw0, 0.01), ("masked_lw_1", lw[1, 0], lw1, 0.01)]
+
+
 def check(results, abs_tol_names=()):
     bad = []
     for name, val, exp, tol in results:

@@ -229,7 +229,8 @@ def test_sources_all_types(oracle_mod):
 
 
 @pytest.mark.parametrize("name", ["simple_direct", "black_parallel_rectangles", "gray_parallel_rectangles",
-                                  "common_edge_squares", "launch_batching", "second_law_box"])
+                                  "common_edge_squares", "launch_batching", "second_law_box",
+                                  "parallel_disks_masked"])
 def test_known_answers_on_gpu(name):
     def run(rad, labels, seed):
         rad.setSeed(seed)
@@ -359,3 +360,68 @@ def test_ray_budget_keeps_results(oracle_mod):
         assert rad.last_stats["rays"] == rays
     rad.ctx.set_ray_budget(0)
     assert rad.ctx.device_status() == 0
+
+
+def _masked_canopy(n_leaves=1500, seed=3):
+    """Canopy of square leaves masked to disks (every second one with texture coordinates
+    that show only a quarter of the mask) and triangles masked to half, over a ground."""
+    rng = np.random.default_rng(seed)
+    ctx = Context()
+    ctx.addPatch((1.5, 1.5, 0.0), (3.0, 3.0))
+    ctx.setPrimitiveData(0, "twosided_flag", 0)
+    m = scenarios.disk_mask(64)
+    half = np.zeros((32, 32), np.uint8)
+    half[:, :16] = 1
+    for k in range(n_leaves):
+        c = rng.uniform((0.2, 0.2, 0.3), (2.8, 2.8, 2.5))
+        rot = (rng.uniform(0.0, 0.5 * math.pi), rng.uniform(0.0, 2.0 * math.pi))
+        uv = [(0.5, 0.5), (1.0, 0.5), (1.0, 1.0), (0.5, 1.0)] if k % 2 else None
+        ctx.addPatch(tuple(c), (0.2, 0.2), rot, texture_mask=m, uv=uv)
+    for k in range(n_leaves // 2):
+        p0 = rng.uniform((0.2, 0.2, 0.5), (2.8, 2.8, 2.5))
+        e1, e2 = rng.normal(size=3) * 0.1, rng.normal(size=3) * 0.1
+        uv = [(0.0, 0.0), (1.0, 0.0), (0.0, 1.0)] if k % 3 == 0 else None
+        ctx.addTriangle(tuple(p0), tuple(p0 + e1), tuple(p0 + e2), texture_mask=half, uv=uv)
+    n = ctx.getPrimitiveCount()
+    ctx.setPrimitiveData(np.arange(1, n), "reflectivity_SW", np.full(n - 1, 0.2))
+    ctx.setPrimitiveData(np.arange(1, n), "transmissivity_SW", np.full(n - 1, 0.1))
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("SW")
+    rad.disableEmission("SW")
+    sun = rad.addCollimatedRadiationSource(scenes.sun_direction(35, 10))
+    rad.setSourceFlux(sun, "SW", 800.0)
+    rad.setDiffuseRadiationFlux("SW", 100.0)
+    rad.setDirectRayCount("SW", 36)
+    rad.setDiffuseRayCount("SW", 64)
+    rad.setScatteringDepth("SW", 2)
+    return rad, ctx
+
+
+def test_masked_canopy_vs_oracle(oracle_mod):
+    """Texture-masked patches (with and without texture coordinates) and triangles: the
+    oracle's fluxes and ray counts."""
+    rad, _ = _masked_canopy()
+    rad.setSeed(9)
+    got = rad.runBand("SW")
+    ref, st = run_oracle(rad, ["SW"], oracle_mod, seed=9)
+    worst, _ = _flux_close(got, ref)
+    assert worst <= FLUX_RTOL, worst
+    assert rad.last_stats["rays"] == st["rays"]
+
+
+def test_masked_hits_and_rays_exact(oracle_mod):
+    """Hits through masked primitives and the ray sets of masked origins are bit-exact."""
+    rad, ctx = _masked_canopy(n_leaves=600, seed=4)
+    rad.updateGeometry()
+    sc = oracle_scene_for(rad, oracle_mod)
+    rng = np.random.default_rng(6)
+    n = 100000
+    o = np.stack([rng.uniform(-0.5, 3.5, n), rng.uniform(-0.5, 3.5, n), rng.uniform(0.0, 3.0, n)], 1)
+    d = scenes.uniform_sphere(rng, n)
+    h1, t1, f1 = rad.ctx.trace_rays(o.astype(np.float32), d.astype(np.float32))
+    h2, t2, f2, _ = sc.trace(o, d)
+    assert np.array_equal(h1, h2) and np.array_equal(t1[h1 >= 0], t2[h2 >= 0]) and np.array_equal(f1, f2)
+    for kind, face in ((0, 0), (1, 1), (1, 0)):
+        o1, d1 = rad.ctx.gen_rays(kind, 5, 2, 64, face, scenes.sun_direction(35, 10))
+        o2, d2 = sc.gen_rays(kind, 5, 2, 64, face, scenes.sun_direction(35, 10))
+        assert np.array_equal(o1, o2) and np.array_equal(d1, d2)
