@@ -26,7 +26,7 @@ EXPORTS = [
     "hrt_source_rotation", "hrt_set_measure", "hrt_get_measure", "hrt_build_accel_static", "hrt_run_sweep",
     "hrt_server_create", "hrt_server_add_scene", "hrt_server_submit", "hrt_server_start", "hrt_server_wait",
     "hrt_server_result", "hrt_server_stats", "hrt_server_destroy", "hrt_set_tuning", "hrt_tuning_report",
-    "hrt_set_ray_budget",
+    "hrt_set_ray_budget", "hrt_update_glass",
 ]
 
 
@@ -102,6 +102,7 @@ def load(path: str | None = None):
         "hrt_update_geometry": (C.c_int, [VP, C.POINTER(Geometry)]),
         "hrt_build_accel": (C.c_int, [VP]),
         "hrt_update_materials": (C.c_int, [VP, C.c_int32, C.c_int32, C.c_int32, VP, VP]),
+        "hrt_update_glass": (C.c_int, [VP, C.c_int32, C.c_int32, C.c_int32, VP, VP, VP]),
         "hrt_update_sources": (C.c_int, [VP, C.c_int32, VP]),
         "hrt_upload_source_fluxes": (C.c_int, [VP, VP, C.c_size_t]),
         "hrt_launch_direct": (C.c_int, [VP, C.POINTER(Launch)]),
@@ -227,6 +228,16 @@ class Context:
     def update_materials(self, rho, tau, nsources, nbands_global):
         rho, tau = f32(rho), f32(tau)
         self.check(self.lib.hrt_update_materials(self.h, nsources, self.n, nbands_global, ptr(rho), ptr(tau)))
+
+    def update_glass(self, is_glass=None, glass_n=None, glass_kl=None):
+        """Translucent covers [S, n, Bg] (is_glass None: none)."""
+        if is_glass is None:
+            self.check(self.lib.hrt_update_glass(self.h, 0, self.n, 0, None, None, None))
+            return
+        ig = np.ascontiguousarray(is_glass, np.int8)
+        gn, gk = f32(glass_n), f32(glass_kl)
+        S, n, Bg = ig.shape
+        self.check(self.lib.hrt_update_glass(self.h, S, n, Bg, ptr(ig), ptr(gn), ptr(gk)))
 
     @staticmethod
     def make_sources(sources):
@@ -356,6 +367,7 @@ class Context:
         return s, keep
 
     def run_band(self, solve: dict, out: bool = True):
+        self.update_glass(solve.get("is_glass"), solve.get("glass_n"), solve.get("glass_kl"))
         s, keep = self.band_solve(solve)
         bl = int(np.count_nonzero(np.asarray(solve["band_launch"])))
         flux = np.zeros((self.n, bl), np.float32) if out else None

@@ -104,6 +104,16 @@ void GB300Backend::updateMaterials(const RayTracingMaterial &m) {
     check(hrt_update_materials(ctx_, (int32_t)m.num_sources, (int32_t)m.num_primitives, (int32_t)m.num_bands,
                                m.reflectivity.data(), m.transmissivity.data()),
           "updateMaterials");
+    // translucent covers: is_glass / glass_n / glass_KL share the materials' layout
+    const size_t count = m.num_sources * m.num_primitives * m.num_bands;
+    const bool glass = m.is_glass.size() == count && m.glass_n.size() == count && m.glass_KL.size() == count &&
+                       std::any_of(m.is_glass.begin(), m.is_glass.end(), [](char g) { return g != 0; });
+    std::vector<int8_t> is_glass;
+    if (glass) is_glass.assign(m.is_glass.begin(), m.is_glass.end());
+    check(hrt_update_glass(ctx_, glass ? (int32_t)m.num_sources : 0, (int32_t)m.num_primitives,
+                           glass ? (int32_t)m.num_bands : 0, glass ? is_glass.data() : nullptr,
+                           glass ? m.glass_n.data() : nullptr, glass ? m.glass_KL.data() : nullptr),
+          "updateMaterials");
 }
 
 void GB300Backend::updateSources(const std::vector<RayTracingSource> &sources) {

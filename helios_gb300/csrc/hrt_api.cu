@@ -144,6 +144,15 @@ struct hrt_context {
     std::map<std::string, int> tuned;
     std::string tune_log;
     DevBuf tune_g;
+    // translucent covers: sheet optics [gS][n][gB] (gS 0: none), the cover bits of the
+    // current launch (key: band flags and source count) and the direct pass's per-band sums
+    int gS = 0, gB = 0;
+    std::vector<int8_t> h_glass;
+    DevBuf gn, gkl, cover, Gcov;
+    std::string cover_key;
+    bool cover_any = false;
+    std::vector<uint8_t> h_flags;  // band flags of the current launch
+    bool sky_any = false;          // some launched band of the current launch has sky flux
 };
 
 namespace {
@@ -187,6 +196,7 @@ TraceScene scene_of(hrt_context *ctx) {
         sc.masks.data = ctx->mask_data.as<uint8_t>();
         sc.masks.T = ctx->T.as<float>();
     }
+    sc.cover = nullptr;
     return sc;
 }
 
@@ -281,6 +291,8 @@ int upload_sky(hrt_context *ctx, int Bl, const float *flux, const float *K, cons
         for (int k = 0; k < 3; ++k) h[3 * Bn + 3 * b + k] = peak ? peak[3 * b + k] : (k == 2 ? 1.f : 0.f);
         for (int k = 0; k < 4; ++k) h[6 * Bn + 4 * b + k] = prague ? prague[4 * b + k] : 0.f;
     }
+    ctx->sky_any = false;
+    for (int b = 0; b < Bl; ++b) ctx->sky_any = ctx->sky_any || h[b] > 0.f;
     CU(ctx->sky.ensure(ctx->stream, h.size() * sizeof(float)));
     CU(cudaMemcpyAsync(ctx->sky.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
     float *d = ctx->sky.as<float>();
@@ -293,6 +305,7 @@ int upload_sky(hrt_context *ctx, int Bl, const float *flux, const float *K, cons
 }
 
 int upload_flags(hrt_context *ctx, int Bg, const uint8_t *flags) {
+    ctx->h_flags.assign(flags, flags + Bg);
     CU(ctx->flags.ensure(ctx->stream, (size_t)std::max(Bg, 1)));
     CU(cudaMemcpyAsync(ctx->flags.p, flags, (size_t)Bg, cudaMemcpyHostToDevice, ctx->stream));
     return HRT_OK;
@@ -302,6 +315,64 @@ void strata(uint32_t rpp, int *dimx, int *dimy) {
     int dx = (int)std::sqrt((float)rpp);
     *dimx = dx;
     *dimy = dx > 0 ? (int)(rpp / (uint32_t)dx) : 1;
+}
+
+// Cover bits of the current launch for rays of sources 0..nsrc-1: bit k of primitive p when p
+// is glass for source k in every launched band (RadiationModel.cpp:2759-2807 materials,
+// OptiX8DeviceCode.cu:838-850 rule); voxels never are.  *out stays null when no primitive is
+// a cover (the launch then runs the ordinary kernels).
+int covers_for(hrt_context *ctx, int Bg, int nsrc, const uint32_t **out) {
+    *out = nullptr;
+    if (ctx->gS == 0) return HRT_OK;
+    if (ctx->gB != Bg || ctx->h_glass.size() != (size_t)ctx->gS * ctx->n * ctx->gB)
+        return fail(ctx, HRT_EINVAL, "translucent-cover arrays do not match the geometry or bands; call hrt_update_glass()");
+    std::string key(ctx->h_flags.begin(), ctx->h_flags.end());
+    key += ":" + std::to_string(nsrc);
+    if (key != ctx->cover_key) {
+        const int n = ctx->n, ns = std::min(std::min(nsrc, ctx->gS), 32);
+        std::vector<uint8_t> vox((size_t)n, 0);
+        for (uint32_t v : ctx->h_voxels) vox[v] = 1;
+        std::vector<uint32_t> bits((size_t)std::max(n, 1), 0u);
+        bool any = false;
+        for (int p = 0; p < n; ++p) {
+            if (vox[p]) continue;
+            for (int k = 0; k < ns; ++k) {
+                bool launched = false, all = true;
+                for (int bg = 0; bg < Bg && all; ++bg) {
+                    if (!ctx->h_flags[bg]) continue;
+                    launched = true;
+                    all = ctx->h_glass[((size_t)k * n + p) * Bg + bg] != 0;
+                }
+                if (launched && all) {
+                    bits[p] |= 1u << k;
+                    any = true;
+                }
+            }
+        }
+        if (any) {
+            CU(ctx->cover.ensure(ctx->stream, bits.size() * sizeof(uint32_t)));
+            CU(cudaMemcpyAsync(ctx->cover.p, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                               ctx->stream));
+        }
+        ctx->cover_any = any;
+        ctx->cover_key = key;
+    }
+    if (ctx->cover_any) *out = ctx->cover.as<uint32_t>();
+    return HRT_OK;
+}
+
+GlassParams glass_params(hrt_context *ctx, int Bg, int Bl) {
+    GlassParams g{};
+    g.gn = ctx->gn.as<float>();
+    g.gkl = ctx->gkl.as<float>();
+    g.flags = ctx->flags.as<uint8_t>();
+    g.Bg = Bg;
+    g.Bl = Bl;
+    g.sky = ctx->sky_any ? 1 : 0;
+    g.rin = ctx->rin.as<double>();
+    g.stop = ctx->stop.as<double>();
+    g.sbot = ctx->sbot.as<double>();
+    return g;
 }
 
 // Direct pass + epilogue (__raygen__direct / __miss__direct).
@@ -328,7 +399,22 @@ int direct_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp,
     P.offset = offset;
     P.count = count;
     P.G = ctx->Gd.as<double>();
+    P.gl = GlassParams{};
+    const uint32_t *cov = nullptr;
+    int r;
+    if ((r = covers_for(ctx, Bg, ctx->S, &cov))) return r;
+    if (cov) {
+        if (Bc > kGlassBands) return fail(ctx, HRT_EUNSUPPORTED, "at most 16 bands can be launched with translucent covers");
+        const size_t nc = ng * (size_t)Bl;
+        CU(ctx->Gcov.ensure(ctx->stream, nc * sizeof(double)));
+        CU(cudaMemsetAsync(ctx->Gcov.p, 0, nc * sizeof(double), ctx->stream));
+        P.sc.cover = cov;
+        P.gl = glass_params(ctx, Bg, Bl);
+        P.gl.Gcov = ctx->Gcov.as<double>();
+        P.gl.src_flux = ctx->src_flux.as<float>();
+    }
     CU(timed_launch(ctx, 0, [&] {
+        if (cov) return launch_direct_glass(P, max_blocks(ctx), ctx->stream);
         return (ctx->measure & 1) ? launch_direct_stats(P, max_blocks(ctx), ctx->stream)
                                   : launch_direct(P, max_blocks(ctx), ctx->stream);
     }));
@@ -345,6 +431,7 @@ int direct_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp,
     E.stop = ctx->stop.as<double>();
     E.sbot = ctx->sbot.as<double>();
     E.Gd = ctx->Gd.as<double>();
+    E.Gcov = cov ? ctx->Gcov.as<double>() : nullptr;
     E.src_flux = ctx->src_flux.as<float>();
     CU(launch_epilogue_direct(E, ctx->stream));
     ctx->last_kernels += 2;
@@ -479,9 +566,18 @@ int diffuse_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp
     P.fetch = ctx->fetch.as<unsigned long long>();
     P.lane_budget = ctx->lane_budget;
     P.hits = nullptr;
+    P.gl = GlassParams{};
     int variant = DV_DEFAULT, r;
-    if ((r = tuned_variant(ctx, P, false, &variant))) return r;
+    const uint32_t *cov = nullptr;
+    if ((r = covers_for(ctx, Bg, 1, &cov))) return r;
+    if (cov) {
+        P.sc.cover = cov;
+        P.gl = glass_params(ctx, Bg, Bl);
+    } else if ((r = tuned_variant(ctx, P, false, &variant))) {
+        return r;
+    }
     CU(timed_launch(ctx, 1, [&] {
+        if (cov) return launch_diffuse_glass(P, max_blocks(ctx), ctx->stream);
         return (ctx->measure & 1)
                    ? launch_diffuse_stats(P, (ctx->measure & 4) ? DV_SIMPLE : DV_DEFAULT, max_blocks(ctx), ctx->stream)
                                   : launch_diffuse_variant(P, variant, max_blocks(ctx), ctx->stream);
@@ -584,6 +680,7 @@ int hrt_update_geometry(hrt_context *ctx, const hrt_geometry *g) {
         return fail(ctx, HRT_EINVAL, "null geometry array");
     if (!(g->nbbox == 0 || g->nbbox == 2 || g->nbbox == 4) || (g->nbbox > 0 && !g->bbox_vertices))
         return fail(ctx, HRT_EINVAL, "periodic walls must be 0, 2 or 4 quads");
+    ctx->cover_key.clear();
     std::vector<uint32_t> voxels;
     for (int i = 0; i < g->n; ++i) {
         if (g->type[i] > 4) return fail(ctx, HRT_EUNSUPPORTED, "unsupported primitive type " + std::to_string(g->type[i]));
@@ -744,6 +841,38 @@ int hrt_update_materials(hrt_context *ctx, int32_t nsources, int32_t nprims, int
     ctx->mS = nsources;
     ctx->mN = nprims;
     ctx->mB = nbands_global;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_update_glass(hrt_context *ctx, int32_t nsources, int32_t nprims, int32_t nbands_global, const int8_t *is_glass,
+                     const float *glass_n, const float *glass_kl) {
+    if (!ctx || nsources < 0 || nprims < 0 || nbands_global < 0) return HRT_EINVAL;
+    CU(cudaSetDevice(ctx->device));
+    ctx->cover_key.clear();
+    const size_t m = (size_t)nsources * nprims * nbands_global;
+    bool any = false;
+    for (size_t i = 0; is_glass && i < m && !any; ++i) any = is_glass[i] != 0;
+    if (!any) {
+        ctx->gS = 0;
+        ctx->h_glass.clear();
+        return HRT_OK;
+    }
+    if (!glass_n || !glass_kl) return fail(ctx, HRT_EINVAL, "null translucent-cover array");
+    if (nprims != ctx->n) return fail(ctx, HRT_EINVAL, "translucent-cover arrays do not match the geometry");
+    if (nsources > 32) return fail(ctx, HRT_EUNSUPPORTED, "translucent covers take at most 32 sources");
+    for (size_t i = 0; i < m; ++i) {
+        if (!is_glass[i]) continue;
+        if (!(glass_n[i] >= 1.f) || std::isinf(glass_n[i]) || !(glass_kl[i] >= 0.f) || std::isinf(glass_kl[i]))
+            return fail(ctx, HRT_EINVAL, "a translucent cover needs a refractive index >= 1 and K*L >= 0");
+    }
+    CU(ctx->gn.ensure(ctx->stream, m * sizeof(float)));
+    CU(ctx->gkl.ensure(ctx->stream, m * sizeof(float)));
+    CU(cudaMemcpyAsync(ctx->gn.p, glass_n, m * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(ctx->gkl.p, glass_kl, m * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->h_glass.assign(is_glass, is_glass + m);
+    ctx->gS = nsources;
+    ctx->gB = nbands_global;
     CU(cudaStreamSynchronize(ctx->stream));
     return HRT_OK;
 }
@@ -1098,6 +1227,7 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
     if (r) return r;
     CU(cudaSetDevice(ctx->device));
     if (!ctx->h_voxels.empty()) return fail(ctx, HRT_EUNSUPPORTED, "the batched sweep does not trace voxels");
+    if (ctx->gS > 0) return fail(ctx, HRT_EUNSUPPORTED, "the batched sweep does not trace translucent covers");
     const int n = ctx->n, nsun = s->nsun, Bl = s->nbands;
     if (nsun < 1 || Bl < 1 || !s->sun_dir || !s->direct_flux || !s->diffuse_flux || !s->rho || !s->tau)
         return fail(ctx, HRT_EINVAL, "sweep needs suns, bands, fluxes and materials");

@@ -552,6 +552,37 @@ static __device__ __noinline__ bool mask_hit_opaque(const MaskSet &m, uint32_t p
 }
 
 // Test record `slot`; on success returns t, face and the original primitive index.
+// Transmittance, reflectance and absorptance of one dielectric sheet (a translucent cover)
+// of refractive index n and absorption product K*L at incidence cosine c: Fresnel
+// reflection r at each face (s and p polarisation averaged), Bouguer attenuation ta along
+// the refracted path, incoherent multiple reflections T = ta (1-r)^2 / (1 - (r ta)^2),
+// R = r (1 + ta T).  The physics and clamps of the reference's glass_tau_rho_alpha
+// (OptiX8DeviceCode.cu:90-134), written in cosines (no trigonometric calls).
+__device__ __forceinline__ void glass_trs(float c, float n, float KL, float *tau, float *rho, float *alpha) {
+    c = fminf(1.f, fmaxf(1e-4f, c));
+    const float st = sqrtf(fmaxf(0.f, 1.f - c * c)) / n;
+    const float ct = sqrtf(fmaxf(0.f, 1.f - st * st));
+    const float as = (c - n * ct) / (c + n * ct);
+    const float ap = (n * c - ct) / (n * c + ct);
+    const float ta = KL > 0.f ? expf(-KL / fmaxf(1e-4f, ct)) : 1.f;
+    float T = 0.f, R = 0.f;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float r = k == 0 ? as * as : ap * ap;
+        const float q = r * ta;
+        const float den = fmaxf(1e-6f, 1.f - q * q);
+        const float ti = ta * (1.f - r) * (1.f - r) / den;
+        const float ri = r * (1.f + ta * ti);
+        T += 0.5f * ti;
+        R += 0.5f * ri;
+    }
+    T = fmaxf(0.f, fminf(1.f, T));
+    R = fmaxf(0.f, fminf(1.f, R));
+    *tau = T;
+    *rho = R;
+    *alpha = fmaxf(0.f, 1.f - T - R);
+}
+
 // VOX = false leaves voxels out (for scenes known to hold none).
 template <bool VOX = true>
 __device__ __forceinline__ bool rec_hit(const float4 *__restrict__ rec, uint32_t slot, const WT &w, f3 o, f3 d,

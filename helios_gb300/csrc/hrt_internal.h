@@ -25,6 +25,19 @@ struct TraceScene {
     unsigned long long *rays; // traced-ray counter
     unsigned long long *visits; // [2] node visits, primitive tests (statistics launches only)
     MaskSet masks;        // texture masks (masks.id null: none)
+    const uint32_t *cover; // [n] bit s: a translucent cover for this launch's rays of source s (null: none)
+};
+
+// Translucent covers of one launch: sheet optics and the cover deposits.
+constexpr int kGlassBands = 16;  // launched bands a launch with covers can carry
+struct GlassParams {
+    const float *gn, *gkl;     // [gS*n*Bg] refractive index, absorption product K*L
+    const uint8_t *flags;      // [Bg] band flags of this launch (device)
+    int Bg, Bl;
+    int sky;                   // diffuse: some launched band has sky flux (covers then take deposits)
+    double *rin, *stop, *sbot; // [n*Bl] absorbed / reflected shares deposited on covers
+    double *Gcov;              // direct: [n*S*2*Bl] strength x transmittance of unoccluded rays that crossed covers
+    const float *src_flux;     // direct: [S*Bl]
 };
 
 // Radiation source in device form (rotation pre-expanded to a 3x3 matrix on the host).
@@ -43,6 +56,7 @@ struct DirectParams {
     uint32_t seed, pass;
     uint32_t offset, count;   // primitive range
     double *G;                // [n*S*2] sums of strength of unoccluded rays, [p][s][face]
+    GlassParams gl;           // launches with covers (sc.cover non-null)
 };
 
 struct SkyParams {
@@ -68,6 +82,7 @@ struct DiffuseParams {
     uint32_t lane_budget;      // persistent kernel: rays a lane takes before its block retires
                                // (0 = no limit: one resident wave of blocks runs to the end)
     uint32_t *hits;            // record mode: hit code per ray id, else unused
+    GlassParams gl;            // launches with covers (sc.cover non-null)
 };
 
 // ---------------------------------------------------------------- BVH build
@@ -133,6 +148,9 @@ cudaError_t launch_direct_stats(const DirectParams &p, int max_blocks, cudaStrea
 // variant DV_SIMPLE counts on the binary tree (the structure the host oracle traverses),
 // DV_DEFAULT on the tree the default kernel traverses.
 cudaError_t launch_diffuse_stats(const DiffuseParams &p, int variant, int max_blocks, cudaStream_t s);
+// Launches whose scene holds translucent covers (sc.cover and the gl fields set).
+cudaError_t launch_direct_glass(const DirectParams &p, int max_blocks, cudaStream_t s);
+cudaError_t launch_diffuse_glass(const DiffuseParams &p, int max_blocks, cudaStream_t s);
 cudaError_t launch_trace_rays(const TraceScene &sc, int64_t nrays, const float *o, const float *d, float tmin,
                               float tmax, int anyhit, int32_t *hit, float *t, int32_t *face, cudaStream_t s);
 cudaError_t launch_gen_rays(const TraceScene &sc, int kind, uint32_t seed, uint32_t pass, int dimx, int dimy,
@@ -189,6 +207,7 @@ struct EpilogueParams {
     double *rin, *stop, *sbot; // [n*Bl]
     const double *Gt, *Gb;     // diffuse: [n*Bl]
     const double *Gd;          // direct: [n*S*2]
+    const double *Gcov;        // direct, launches with covers: [n*S*2*Bl] (null: none)
     const float *src_flux;     // direct: [S*Bl]
     double strength;           // diffuse: 1/(dimx*dimy)
 };

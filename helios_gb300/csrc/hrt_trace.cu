@@ -216,6 +216,171 @@ __global__ void __launch_bounds__(kBlock) k_diffuse(const DiffuseParams P) {
     }
 }
 
+// ------------------------------------------------------ translucent covers --
+// Launches whose scene holds covers (glass in every launched band; sc.cover) run these
+// one-ray-per-thread kernels: the ray passes every cover of its source, each cover crossed
+// before the ray's end attenuates it by the sheet transmittance per band and takes its
+// absorbed and reflected shares of the flux reaching it (OptiX8DeviceCode.cu:816-911), and
+// only sky or source deposits see the attenuation (:542, :630).
+
+// incidence cosine of direction d on primitive c (unit normal of its ray-origin record)
+__device__ __forceinline__ float cover_cos(const TraceScene &sc, uint32_t c, f3 d) {
+    const float4 n = __ldg(sc.rgen + 4 * (size_t)c + 3);
+    return fminf(1.f, fabsf(dot(d, xyz(n))));
+}
+
+__global__ void __launch_bounds__(kBlock) k_direct_glass(const DirectParams P) {
+    const uint32_t R = (uint32_t)(P.dimx * P.dimy);
+    const uint32_t total = P.count * R;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const double inv_nr = 1.0 / (double)R;
+    const GlassParams &gl = P.gl;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total; base += stride) {
+        const uint32_t id = base + (threadIdx.x & 31);
+        const bool active = id < total;
+        const uint32_t p = active ? P.offset + id / R : 0u;
+        const uint32_t r = active ? id % R : 0u;
+        float4 g[4];
+        int ts = 0;
+        uint32_t type = 0;
+        if (active) {
+            load_rgen(P.sc, p, g);
+            ts = P.sc.twosided[p];
+            type = __float_as_uint(g[0].w);
+        }
+        for (int k = 0; k < P.S; ++k) {
+            double v[2] = {0.0, 0.0};
+            bool live = active;
+            if (live) {
+                const uint32_t c2 = (uint32_t)(k << 1);
+                u4 u = philox(r, p, c2, 0u, P.seed, P.pass);
+                const bool vox = type == PT_VOXEL;
+                f3 org = direct_origin(g, type, r, p, c2, P.dimx, P.dimy, P.seed, P.pass, u, P.sc.masks);
+                f3 nrm = xyz(g[3]);
+                f3 dir;
+                float tmax;
+                double strength;
+                live = direct_ray(P.src[k], org, nrm, vox, u.c, u.d, inv_nr, &dir, &tmax, &strength);
+                if (live) {
+                    const int face = (vox || dot(dir, nrm) > 0.f) ? 1 : 0;
+                    if ((!face && ts == 0) || ts == 3) {
+                        live = false;
+                    } else {
+                        float T[kGlassBands];
+#pragma unroll
+                        for (int b = 0; b < kGlassBands; ++b) T[b] = 1.f;
+                        bool crossed = false;
+                        Hit h = trace_covers(P.sc, org, dir, 1e-4f, tmax, VoxKey{r, p, c2, P.seed, P.pass}, 1u << k, p,
+                                             true, [&](uint32_t c, int cface) {
+                                                 crossed = true;
+                                                 const float cs = cover_cos(P.sc, c, dir);
+                                                 int b = -1;
+                                                 for (int bg = 0; bg < gl.Bg && b + 1 < kGlassBands; ++bg) {
+                                                     if (!gl.flags[bg]) continue;
+                                                     ++b;
+                                                     const size_t m = ((size_t)k * P.sc.n + c) * gl.Bg + bg;
+                                                     float tc, rc, ac;
+                                                     glass_trs(cs, gl.gn[m], gl.gkl[m], &tc, &rc, &ac);
+                                                     cover_deposit(gl, c, cface, b,
+                                                                   strength * (double)gl.src_flux[k * gl.Bl + b] *
+                                                                       (double)T[b],
+                                                                   rc, ac);
+                                                     T[b] *= tc;
+                                                 }
+                                             });
+                        if (h.prim == 0xFFFFFFFFu) {
+                            if (!crossed) {
+                                v[face] = strength;
+                            } else {
+                                double *dst = gl.Gcov + (((size_t)p * P.S + k) * 2 + face) * gl.Bl;
+                                int b = -1;
+                                for (int bg = 0; bg < gl.Bg && b + 1 < kGlassBands; ++bg) {
+                                    if (!gl.flags[bg]) continue;
+                                    ++b;
+                                    atomicAdd(dst + b, strength * (double)T[b]);
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            count_rays(P.sc, live);
+            uint32_t key = active ? (p * (uint32_t)P.S + (uint32_t)k) : 0xFFFFFFFFu;
+            warp_segment_add<2>(key, v, 2, P.G, 2);
+        }
+    }
+}
+
+template <int NB>
+__global__ void __launch_bounds__(kBlock) k_diffuse_glass(const DiffuseParams P) {
+    const uint32_t R = (uint32_t)(P.dimx * P.dimy);
+    const uint32_t total = P.count * R;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const int face = (blockIdx.y == 0) ? 1 : 0;
+    if (!(P.faces & (1 << blockIdx.y))) return;
+    double *G = face ? P.Gt : P.Gb;
+    const double inv_r = 1.0 / (double)R;
+    const GlassParams &gl = P.gl;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total; base += stride) {
+        const uint32_t id = base + (threadIdx.x & 31);
+        bool active = id < total;
+        const uint32_t p = active ? P.offset + id / R : 0u;
+        const uint32_t r = active ? id % R : 0u;
+        if (active) {
+            int ts = P.sc.twosided[p];
+            if (face == 1 && ts == 3) active = false;
+            if (face == 0 && ts != 1) active = false;
+        }
+        double v[NB];
+#pragma unroll
+        for (int j = 0; j < NB; ++j) v[j] = 0.0;
+        if (active) {
+            float4 g[4];
+            load_rgen(P.sc, p, g);
+            uint32_t type = __float_as_uint(g[0].w);
+            f3 org, dir;
+            diffuse_ray<true>(g, type, r, p, face, P.dimx, P.dimy, P.seed, P.pass, &org, &dir, P.sc.masks);
+            float T[NB];
+#pragma unroll
+            for (int j = 0; j < NB; ++j) T[j] = 1.f;
+            // covers take the launch's isotropic sky flux (OptiX8DeviceCode.cu:871-880)
+            Hit h = trace_covers(P.sc, org, dir, 1e-4f, 1e38f, VoxKey{r, p, (uint32_t)face, P.seed, P.pass}, 1u, p,
+                                 gl.sky != 0, [&](uint32_t c, int cface) {
+                                     const float cs = cover_cos(P.sc, c, dir);
+                                     int b = -1;
+                                     for (int bg = 0; bg < gl.Bg && b + 1 < NB; ++bg) {
+                                         if (!gl.flags[bg]) continue;
+                                         ++b;
+                                         const size_t m = (size_t)c * gl.Bg + bg;
+                                         float tc, rc, ac;
+                                         glass_trs(cs, gl.gn[m], gl.gkl[m], &tc, &rc, &ac);
+                                         cover_deposit(gl, c, cface, b, inv_r * (double)P.sky.flux[b] * (double)T[b],
+                                                       rc, ac);
+                                         T[b] *= tc;
+                                     }
+                                 });
+            if (h.prim == kLost) {
+                // dropped ray: no deposit
+            } else if (h.prim != 0xFFFFFFFFu) {
+                const float *src = (h.face ? P.otop : P.obot) + (size_t)h.prim * P.Bl;
+#pragma unroll
+                for (int j = 0; j < NB; ++j)
+                    if (j < P.Bc) v[j] = (double)__ldg(src + j);
+            } else {
+#pragma unroll
+                for (int j = 0; j < NB; ++j)
+                    if (j < P.Bc) {
+                        float fl = P.sky.flux[j];
+                        if (fl > 0.f) v[j] = sky_fd(dir, P.sky, j) * (double)fl * (double)T[j];
+                    }
+            }
+        }
+        count_rays(P.sc, active);
+        uint32_t key = active ? p : 0xFFFFFFFFu;
+        warp_segment_add<NB>(key, v, P.Bc, G, P.Bl);
+    }
+}
+
 // ------------------------------------------------------------------ testing --
 __global__ void k_trace_rays(const TraceScene sc, int64_t nrays, const float *__restrict__ o,
                              const float *__restrict__ d, float tmin, float tmax, int anyhit, int32_t *hit, float *t,
@@ -296,6 +461,10 @@ __global__ void k_epilogue_direct(const EpilogueParams P) {
     for (int s = 0; s < P.S; ++s) {
         double flux = (double)P.src_flux[(size_t)s * P.Bl + b];
         double g0 = P.Gd[((size_t)p * P.S + s) * 2] * flux, g1 = P.Gd[((size_t)p * P.S + s) * 2 + 1] * flux;
+        if (P.Gcov) {
+            g0 += P.Gcov[(((size_t)p * P.S + s) * 2) * P.Bl + b] * flux;
+            g1 += P.Gcov[(((size_t)p * P.S + s) * 2 + 1) * P.Bl + b] * flux;
+        }
         size_t m = ((size_t)s * P.n + p) * P.Bg + bg;
         double rho = P.rho[m], tau = P.tau[m];
         in += (g0 + g1) * (1.0 - rho - tau);
@@ -580,6 +749,26 @@ cudaError_t launch_diffuse_variant(const DiffuseParams &p, int variant, int max_
 }
 cudaError_t launch_direct_stats(const DirectParams &p, int max_blocks, cudaStream_t s) {
     return direct_impl<true>(p, max_blocks, s);
+}
+cudaError_t launch_direct_glass(const DirectParams &p, int max_blocks, cudaStream_t s) {
+    int64_t total = (int64_t)p.count * p.dimx * p.dimy;
+    if (total <= 0 || p.S <= 0) return cudaSuccess;
+    unsigned nb = blocks_for(total, kBlock);
+    if ((int)nb > max_blocks) nb = (unsigned)max_blocks;
+    k_direct_glass<<<nb, kBlock, 0, s>>>(p);
+    return cudaGetLastError();
+}
+cudaError_t launch_diffuse_glass(const DiffuseParams &p, int max_blocks, cudaStream_t s) {
+    int64_t total = (int64_t)p.count * p.dimx * p.dimy;
+    if (total <= 0 || p.Bc <= 0) return cudaSuccess;
+    unsigned nb = blocks_for(total, kBlock);
+    if ((int)nb > max_blocks) nb = (unsigned)max_blocks;
+    dim3 grid(nb, 2);
+    if (p.Bc <= 1) k_diffuse_glass<1><<<grid, kBlock, 0, s>>>(p);
+    else if (p.Bc <= 4) k_diffuse_glass<4><<<grid, kBlock, 0, s>>>(p);
+    else if (p.Bc <= 16) k_diffuse_glass<16><<<grid, kBlock, 0, s>>>(p);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
 }
 cudaError_t launch_diffuse_stats(const DiffuseParams &p, int variant, int max_blocks, cudaStream_t s) {
     return diffuse_impl<true>(p, variant, max_blocks, s);

@@ -25,12 +25,25 @@ __device__ __forceinline__ void raise(uint32_t *status, uint32_t bit) {
     if (status) atomicOr(status, bit);
 }
 
+// Translucent-cover query of a launch with covers (sc.cover): mode 0 lets the ray pass
+// every cover of its source bit; mode 1 reports only covers after (tlo, ilo) in the order
+// (distance, primitive index), never the ray's own origin primitive.
+struct CoverQ {
+    uint32_t cbit;
+    int mode;
+    float tlo;
+    uint32_t ilo;
+    uint32_t self;
+};
+constexpr int kMaxCovers = 16;  // covers taken per periodic segment of a ray
+
 // Closest (or any) hit over the BVH.  Visiting order: both child boxes are
 // tested against the current best distance; leaf children are intersected at
 // once; of two internal children the nearer is entered and the farther pushed.
-template <bool STATS>
+// COV: apply the cover query cq to every geometric hit.
+template <bool STATS, bool COV = false>
 __device__ Hit trace_bvh(const TraceScene &sc, f3 o, f3 d, float tmin, float tmax, bool anyhit, const VoxKey &vk,
-                         uint32_t *nv, uint32_t *np) {
+                         uint32_t *nv, uint32_t *np, const CoverQ *cq = nullptr) {
     Hit h{tmax, 0xFFFFFFFFu, 0};
     if (sc.n == 0) return h;
     WT w = wt_setup(d);
@@ -72,6 +85,13 @@ __device__ Hit trace_bvh(const TraceScene &sc, f3 o, f3 d, float tmin, float tma
                 uint32_t orig;
                 if (STATS) ++*np;
                 if (rec_hit(sc.rec, (uint32_t)(~ck), w, o, d, inv, tmin, best, vk, &t, &face, &orig, sc.masks)) {
+                    if (COV) {
+                        const bool cov = (__ldg(sc.cover + orig) & cq->cbit) != 0u;
+                        if (cq->mode == 0 ? cov
+                                          : (!cov || orig == cq->self ||
+                                             !(t > cq->tlo || (t == cq->tlo && orig > cq->ilo))))
+                            continue;
+                    }
                     if (h.prim == 0xFFFFFFFFu || t < h.t || (t == h.t && orig < h.prim)) {
                         h.t = t;
                         h.prim = orig;
@@ -154,6 +174,61 @@ __device__ Hit trace_full(const TraceScene &sc, f3 o, f3 d, float tmin, float tm
     // The tenth trace ended on a wall again: the reference's loop stops there and no
     // miss or closest-hit program deposits anything for this ray.
     return Hit{tmax, kLost, 0};
+}
+
+// trace_full for a launch with covers (OptiX8DeviceCode.cu:816-911 any-hit semantics, made
+// deterministic): the closest opaque hit with every cover of source bit `cbit` passed, then,
+// when `collect`, the covers of each periodic segment before its end in the order
+// (distance, primitive index), each reported to on_cover(prim, face).
+template <class F>
+__device__ Hit trace_covers(const TraceScene &sc, f3 o, f3 d, float tmin, float tmax, VoxKey vk, uint32_t cbit,
+                            uint32_t self, bool collect, F &&on_cover) {
+    const uint32_t c2 = vk.c2;
+    const CoverQ q0{cbit, 0, -1.f, 0u, self};
+    for (int wrap = 0; wrap < 10; ++wrap) {
+        vk.c2 = c2 | ((uint32_t)wrap << 16);
+        Hit h = trace_bvh<false, true>(sc, o, d, tmin, tmax, false, vk, nullptr, nullptr, &q0);
+        const float lim = (h.prim != 0xFFFFFFFFu) ? h.t : tmax;
+        float tb = lim;
+        int which = -1;
+        const bool wall = sc.nbbox > 0 && wall_closest(sc, o, d, tmin, lim, &tb, &which) &&
+                          (h.prim == 0xFFFFFFFFu || tb < h.t);
+        if (collect) {
+            CoverQ q1{cbit, 1, -1.f, 0u, self};
+            const float end = wall ? tb : lim;
+            for (int c = 0; c < kMaxCovers; ++c) {
+                const Hit g = trace_bvh<false, true>(sc, o, d, tmin, end, false, vk, nullptr, nullptr, &q1);
+                if (g.prim == 0xFFFFFFFFu) break;
+                on_cover(g.prim, g.face);
+                q1.tlo = g.t;
+                q1.ilo = g.prim;
+            }
+        }
+        if (!wall) return h;
+        f3 hp = add(o, scl(d, tb));
+        bool xwall = (sc.periodic_x == 1.f) && which < 2;
+        if (xwall) {
+            float width = sc.bbox[4].x - sc.bbox[0].x;
+            hp.x = hp.x + ((which == 0) ? width : -width);
+        } else {
+            int yb = (sc.periodic_x == 1.f) ? 2 : 0;
+            float width = sc.bbox[4 * (yb + 1)].y - sc.bbox[4 * yb].y;
+            hp.y = hp.y + ((which == yb) ? width : -width);
+        }
+        o = hp;
+    }
+    return Hit{tmax, kLost, 0};
+}
+
+// A cover's absorbed and reflected shares of `incoming` for launched band b at sheet optics
+// (tau, rho, alpha): reflection leaves from the face the ray arrived on
+// (OptiX8DeviceCode.cu:874-895).
+__device__ __forceinline__ void cover_deposit(const GlassParams &gl, uint32_t c, int face, int b, double incoming,
+                                              float rho, float alpha) {
+    if (!(incoming > 0.0)) return;
+    const size_t i = (size_t)c * gl.Bl + b;
+    atomicAdd(gl.rin + i, incoming * (double)alpha);
+    atomicAdd((face ? gl.stop : gl.sbot) + i, incoming * (double)rho);
 }
 
 __device__ __forceinline__ void load_rgen(const TraceScene &sc, uint32_t p, float4 g[4]) {

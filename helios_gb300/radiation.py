@@ -479,24 +479,38 @@ class RadiationModel:
         rho = np.zeros((n, Bg))
         tau = np.zeros((n, Bg))
         eps_l = np.ones((n, len(band_labels)))
+        self._glass = None
         for bi, b in enumerate(all_bands):
             band = self.bands[b]
             r = self.context.primitive_array("reflectivity_" + b, self.rho_default)
             t = self.context.primitive_array("transmissivity_" + b, self.tau_default)
             e = self.context.primitive_array("emissivity_" + b, self.eps_default)
+            # translucent cover: glass_n_<band> >= 1 activates the sheet model, glass_KL_<band>
+            # (default 0, negative clamped) its absorption (RadiationModel.cpp:2759-2807); the
+            # constant rho/tau of a glass entry are kept as set and not checked (:2844-2846)
+            gn = self.context.primitive_array("glass_n_" + b, np.nan)
+            g = gn >= 1.0
+            if g.any():
+                if self._glass is None:
+                    self._glass = (np.zeros((n, Bg), np.int8), np.zeros((n, Bg), np.float32),
+                                   np.zeros((n, Bg), np.float32))
+                gkl = np.maximum(self.context.primitive_array("glass_KL_" + b, 0.0), 0.0)
+                self._glass[0][:, bi] = g
+                self._glass[1][:, bi] = np.where(g, gn, 0.0)
+                self._glass[2][:, bi] = np.where(g, gkl, 0.0)
             if band.emissionFlag:
-                m1 = (e != 1.0) & (r == 0) & (t == 0)
+                m1 = ~g & (e != 1.0) & (r == 0) & (t == 0)
                 r = np.where(m1, 1.0 - e, r)
-                bad = ~m1 & (np.abs(e + t + r - 1.0) > 1e-6) & (e > 0)
+                bad = ~g & ~m1 & (np.abs(e + t + r - 1.0) > 1e-6) & (e > 0)
                 if bad.any():
                     raise HeliosRuntimeError(f"ERROR (RadiationModel): emissivity, transmissivity, and reflectivity "
                                              f"must sum to 1 to ensure energy conservation. Band {b}. It is also "
                                              "possible that you forgot to disable emission for this band.")
-                m3 = ~m1 & (band.scatteringDepth == 0) & (e != 1.0)
+                m3 = ~g & ~m1 & (band.scatteringDepth == 0) & (e != 1.0)
                 e = np.where(m3, 1.0, e)
                 r = np.where(m3, 0.0, r)
                 t = np.where(m3, 0.0, t)
-            elif (t + r > 1.0 + 1e-6).any():
+            elif (~g & (t + r > 1.0 + 1e-6)).any():
                 raise HeliosRuntimeError("ERROR (RadiationModel): transmissivity and reflectivity cannot sum to "
                                          "greater than 1 ensure energy conservation.")
             rho[:, bi] = r
@@ -546,6 +560,10 @@ class RadiationModel:
             "scatter_tolerance": self.scatter_tolerance,
             "n": n,
         }
+        if self._glass is not None:
+            desc["is_glass"] = np.ascontiguousarray(np.broadcast_to(self._glass[0], (S, n, len(all_bands))))
+            desc["glass_n"] = np.ascontiguousarray(np.broadcast_to(self._glass[1], (S, n, len(all_bands))))
+            desc["glass_kl"] = np.ascontiguousarray(np.broadcast_to(self._glass[2], (S, n, len(all_bands))))
         return desc
 
     def runBand(self, labels):
@@ -594,6 +612,7 @@ def run_band_through_backend(ctx: "_hrt.Context", d: dict, twosided: np.ndarray)
     Bl = int(flags.sum())
     S = len(d["sources"])
     ctx.update_materials(d["rho"], d["tau"], S, Bg)
+    ctx.update_glass(d.get("is_glass"), d.get("glass_n"), d.get("glass_kl"))
     ctx.update_sources(d["sources"])
     scattering = bool((d["depth"] > 0).any())
     diffuse = bool((d["diffuse_flux"] > 0).any())

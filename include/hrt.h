@@ -148,6 +148,17 @@ int hrt_build_accel(hrt_context *ctx);
 /* ---- RayTracingBackend::updateMaterials (RayTracingBackend.h:90) */
 int hrt_update_materials(hrt_context *ctx, int32_t nsources, int32_t nprims, int32_t nbands_global,
                          const float *rho, const float *tau);
+/* ---- The glass part of RayTracingBackend::updateMaterials (RayTracingBackend.h:90): translucent
+ * covers (RayTracingMaterial glass_n / glass_KL / is_glass, RayTracingTypes.h:173-178, as
+ * OptiX8Backend::updateMaterials uploads them, OptiX8Backend.cpp:581-597).  Arrays are
+ * [nsources][nprims][nbands_global] like the materials.  A primitive that is glass in EVERY band of
+ * a launch is a cover for that launch's rays of the source: rays pass it, each cover crossed before
+ * a ray's end attenuates the ray by the Fresnel + Bouguer transmittance of one sheet per band and
+ * takes its absorbed and reflected shares of the flux reaching it; covers are taken in order of
+ * distance (the reference visits them in any-hit order).  is_glass NULL or all zero: no covers.
+ * At most 32 sources and 16 launched bands; the batched sweep refuses scenes with covers. */
+int hrt_update_glass(hrt_context *ctx, int32_t nsources, int32_t nprims, int32_t nbands_global, const int8_t *is_glass,
+                     const float *glass_n, const float *glass_kl);
 /* ---- RayTracingBackend::updateSources (RayTracingBackend.h:99) */
 int hrt_update_sources(hrt_context *ctx, int32_t nsources, const hrt_source *sources);
 /* ---- RayTracingBackend::uploadSourceFluxes (RayTracingBackend.h:247) [source*Bl + band] */

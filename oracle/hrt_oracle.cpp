@@ -792,6 +792,53 @@ void build_bvh(Scene &s) {
     (void)done;
 }
 
+// Translucent covers (glass / plastic sheets; OptiX8DeviceCode.cu:793-911, materials from
+// RadiationModel.cpp:2759-2807).  A primitive that is glass in EVERY band of a launch is a
+// cover for that launch's rays of the source: it never stops them; each cover a ray crosses
+// before its closest opaque hit (or the end of the periodic segment) attenuates the ray per
+// band and receives the cover's own absorbed and reflected share.  The reference visits
+// covers in OptiX any-hit order; here they are visited by increasing distance (ties: the
+// smaller primitive index), at most kMaxCovers per segment.
+constexpr int kMaxCovers = 16;
+struct CoverQ {
+    const uint32_t *bits = nullptr;  // [n] bit s: a cover for rays of source s (null: no covers)
+    uint32_t cbit = 0;               // the ray's source bit
+    int mode = 0;                    // 0: covers are transparent; 1: report only covers after (tlo, ilo)
+    float tlo = -1.f;
+    int32_t ilo = -1;
+    int32_t self = -1;               // the ray's origin primitive, never its own cover
+};
+
+// Transmittance, reflectance and absorptance of one dielectric sheet of refractive index n
+// and absorption product K*L at incidence cosine c: Fresnel reflection r at each face (s and
+// p polarisation averaged), Bouguer attenuation ta along the refracted path and incoherent
+// multiple reflections, T = ta (1-r)^2 / (1 - (r ta)^2), R = r (1 + ta T).  The physics of
+// the reference's glass_tau_rho_alpha (OptiX8DeviceCode.cu:90-134, clamps kept), written in
+// cosines.
+inline void glass_trs(float c, float n, float KL, float *tau, float *rho, float *alpha) {
+    c = std::fmin(1.f, std::fmax(1e-4f, c));
+    const float st = std::sqrt(std::fmax(0.f, 1.f - c * c)) / n;
+    const float ct = std::sqrt(std::fmax(0.f, 1.f - st * st));
+    const float as = (c - n * ct) / (c + n * ct);
+    const float ap = (n * c - ct) / (n * c + ct);
+    const float ta = KL > 0.f ? std::exp(-KL / std::fmax(1e-4f, ct)) : 1.f;
+    float T = 0.f, R = 0.f;
+    for (int k = 0; k < 2; ++k) {
+        const float r = k == 0 ? as * as : ap * ap;
+        const float q = r * ta;
+        const float den = std::fmax(1e-6f, 1.f - q * q);
+        const float ti = ta * (1.f - r) * (1.f - r) / den;
+        const float ri = r * (1.f + ta * ti);
+        T += 0.5f * ti;
+        R += 0.5f * ri;
+    }
+    T = std::fmax(0.f, std::fmin(1.f, T));
+    R = std::fmax(0.f, std::fmin(1.f, R));
+    *tau = T;
+    *rho = R;
+    *alpha = std::fmax(0.f, 1.f - T - R);
+}
+
 // Closest hit.  Ties in t go to the smaller original primitive index.
 struct TraceStats {
     uint64_t nodes = 0, prims = 0;
@@ -800,7 +847,7 @@ inline bool better(float t, int32_t p, float bt, int32_t bp) {
     return t < bt || (t == bt && (uint32_t)p < (uint32_t)bp);
 }
 
-Hit trace_bvh(const Scene &s, const Ray &ray, bool anyhit, TraceStats *st) {
+Hit trace_bvh(const Scene &s, const Ray &ray, bool anyhit, TraceStats *st, const CoverQ *cq = nullptr) {
     Hit h{ray.tmax, -1, 0};
     if (s.n == 0) return h;
     WT w = wt_setup(ray.d);
@@ -834,6 +881,12 @@ Hit trace_bvh(const Scene &s, const Ray &ray, bool anyhit, TraceStats *st) {
                 float t;
                 int face;
                 if (prim_hit(w, ray, inv, s.rec[p], (uint32_t)p, best, &t, &face, s.mk())) {
+                    if (cq && cq->bits) {
+                        const bool cov = (cq->bits[p] & cq->cbit) != 0;
+                        if (cq->mode == 0 ? cov
+                                          : (!cov || p == cq->self || !(t > cq->tlo || (t == cq->tlo && p > cq->ilo))))
+                            continue;
+                    }
                     if (h.prim < 0 || better(t, p, h.t, h.prim)) {
                         h.t = t;
                         h.prim = p;
@@ -928,6 +981,52 @@ Hit trace_full(const Scene &s, Ray ray, bool anyhit, TraceStats *st) {
     }
     // The tenth trace ended on a wall again: the reference's loop stops and neither a miss
     // nor a closest-hit program deposits energy for this ray (OptiX8DeviceCode.cu:1616-1653).
+    return Hit{ray.tmax, -2, 0};
+}
+
+// trace_full for a launch with covers: closest opaque hit (covers transparent), then the
+// covers of each periodic segment in order, reported to on_cover(prim, face).
+template <class F>
+Hit trace_covers(const Scene &s, Ray ray, const uint32_t *bits, uint32_t cbit, int32_t self, bool collect,
+                 TraceStats *st, F &&on_cover) {
+    const uint32_t c2 = ray.key.c2;
+    CoverQ q0;
+    q0.bits = bits;
+    q0.cbit = cbit;
+    for (int wrap = 0; wrap < 10; ++wrap) {
+        ray.key.c2 = c2 | ((uint32_t)wrap << 16);
+        Hit h = trace_bvh(s, ray, false, st, &q0);
+        const float lim = (h.prim >= 0) ? h.t : ray.tmax;
+        float tb = lim;
+        int which = -1;
+        const bool wall = s.nbbox > 0 && bbox_closest(s, ray, lim, &tb, &which) && (h.prim < 0 || tb < h.t);
+        if (collect) {
+            Ray seg = ray;
+            seg.tmax = wall ? tb : lim;
+            CoverQ q1 = q0;
+            q1.mode = 1;
+            q1.self = self;
+            for (int c = 0; c < kMaxCovers; ++c) {
+                Hit g = trace_bvh(s, seg, false, nullptr, &q1);
+                if (g.prim < 0) break;
+                on_cover(g.prim, g.face);
+                q1.tlo = g.t;
+                q1.ilo = g.prim;
+            }
+        }
+        if (!wall) return h;
+        V3 hp = vadd(ray.o, vscale(ray.d, tb));
+        bool xwall = (s.periodic[0] == 1.f) && which < 2;
+        if (xwall) {
+            float width = s.bbox[1].p[0].x - s.bbox[0].p[0].x;
+            hp.x = hp.x + ((which == 0) ? width : -width);
+        } else {
+            int ybase = (s.periodic[0] == 1.f) ? 2 : 0;
+            float width = s.bbox[ybase + 1].p[0].y - s.bbox[ybase].p[0].y;
+            hp.y = hp.y + ((which == ybase) ? width : -width);
+        }
+        ray.o = hp;
+    }
     return Hit{ray.tmax, -2, 0};
 }
 
@@ -1209,6 +1308,10 @@ typedef struct {
     int32_t threads;              // OpenMP threads (<=0: all)
     int32_t prim_limit;           // >0: launch rays only from the first prim_limit primitives (timing samples)
     double scatter_tol;           // >0: a band stops scattering once its residual falls to this value
+    int32_t glass_nsrc;           // sources of the glass arrays (0: no translucent covers)
+    const int8_t *is_glass;       // [glass_nsrc*n*Bg]
+    const float *glass_n;         // [glass_nsrc*n*Bg] refractive index
+    const float *glass_kl;        // [glass_nsrc*n*Bg] absorption product K*L
 } orc_solve;
 
 void *orc_scene_create(const orc_geometry *g) {
@@ -1280,6 +1383,10 @@ void orc_sincos2pi(int64_t n, const float *u, float *c, float *s) {
 }
 
 // ln_unit for a batch (accuracy tests against libm).
+void orc_glass_trs(int64_t m, const float *c, float n, float kl, float *out) {
+    for (int64_t i = 0; i < m; ++i) glass_trs(c[i], n, kl, &out[3 * i], &out[3 * i + 1], &out[3 * i + 2]);
+}
+
 void orc_ln_unit(int64_t n, const float *x, float *out) {
     for (int64_t i = 0; i < n; ++i) out[i] = ln_unit(x[i]);
 }
@@ -1412,17 +1519,56 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
     int iters = 0;
     const int nl = (q->prim_limit > 0 && q->prim_limit < n) ? q->prim_limit : n;
     auto matidx = [&](int srcid, int p, int bg) { return ((size_t)srcid * n + p) * Bg + bg; };
+    // Cover bits of one launch: bit k of primitive p when p is glass for source k in every
+    // launched band (voxels never are); empty when no primitive is a cover.
+    auto cover_bits = [&](const uint8_t *fl, int nsrc) {
+        std::vector<uint32_t> bits;
+        if (!q->is_glass || q->glass_nsrc <= 0) return bits;
+        bits.assign(n, 0u);
+        bool any = false;
+        const int ns = std::min(std::min(nsrc, q->glass_nsrc), 32);
+        for (int p = 0; p < n; ++p) {
+            if (s->type[p] == PT_VOXEL) continue;
+            for (int k = 0; k < ns; ++k) {
+                bool launched = false, all = true;
+                for (int bg = 0; bg < Bg && all; ++bg) {
+                    if (!fl[bg]) continue;
+                    launched = true;
+                    all = q->is_glass[matidx(k, p, bg)] != 0;
+                }
+                if (launched && all) {
+                    bits[p] |= 1u << k;
+                    any = true;
+                }
+            }
+        }
+        if (!any) bits.clear();
+        return bits;
+    };
+    // A cover's absorbed and reflected shares of `incoming` (OptiX8DeviceCode.cu:874-895).
+    auto cover_deposit = [&](int c, int face, int b, double incoming, float alpha, float rho) {
+        if (!(incoming > 0.0)) return;
+        const size_t i = (size_t)c * Bl + b;
+#pragma omp atomic
+        rin[i] += incoming * (double)alpha;
+        double *sc = face ? &stop[i] : &sbot[i];
+#pragma omp atomic
+        *sc += incoming * (double)rho;
+    };
 
     // ---- direct pass (OptiX8Backend::launchDirectRays + __raygen__direct + __miss__direct)
     if (S > 0 && rundirect && dirN > 0) {
         int dimx = (int)std::sqrt((float)dirN);
         int dimy = dimx > 0 ? dirN / dimx : 1;
         double inv_nr = 1.0 / (double)(dimx * dimy);
+        const std::vector<uint32_t> dbits = cover_bits(q->band_launch, S);
+        const uint32_t *cb = dbits.empty() ? nullptr : dbits.data();
 #pragma omp parallel for schedule(dynamic, 4) reduction(+ : n_rays, n_nodes, n_prims, n_hits)
         for (int p = 0; p < nl; ++p) {
             const RGen &g = s->rgen[p];
             int ts = s->twosided[p];
             std::vector<double> d_in(Bl, 0.0), d_top(Bl, 0.0), d_bot(Bl, 0.0);
+            std::vector<float> ctau(Bl, 1.f);
             const int type = (int)s->type[p];
             const bool vox = type == PT_VOXEL;
             for (int r = 0; r < dimx * dimy; ++r) {
@@ -1438,8 +1584,28 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
                     if (!face && ts == 0) continue;
                     if (ts == 3) continue;
                     TraceStats st;
-                    Hit hh = trace_full(*s, Ray{org, dir, 1e-4f, tmax, VoxKey{(uint32_t)r, (uint32_t)p, c2, q->seed, 0u}},
-                                        true, &st);
+                    const Ray ray{org, dir, 1e-4f, tmax, VoxKey{(uint32_t)r, (uint32_t)p, c2, q->seed, 0u}};
+                    Hit hh;
+                    if (!cb) {
+                        hh = trace_full(*s, ray, true, &st);
+                    } else {
+                        std::fill(ctau.begin(), ctau.end(), 1.f);
+                        hh = trace_covers(*s, ray, cb, 1u << k, p, true, &st, [&](int c, int cface) {
+                            const float cs = std::fmin(1.f, std::fabs(vdot(dir, s->rgen[c].N)));
+                            int b = -1;
+                            for (int bg = 0; bg < Bg; ++bg) {
+                                if (!q->band_launch[bg]) continue;
+                                ++b;
+                                float tau_c, rho_c, alpha_c;
+                                glass_trs(cs, q->glass_n[matidx(k, c, bg)], q->glass_kl[matidx(k, c, bg)], &tau_c,
+                                          &rho_c, &alpha_c);
+                                cover_deposit(c, cface, b,
+                                              strength * (double)q->source_flux[k * Bl + b] * (double)ctau[b],
+                                              alpha_c, rho_c);
+                                ctau[b] *= tau_c;
+                            }
+                        });
+                    }
                     n_rays++;
                     n_nodes += st.nodes;
                     n_prims += st.prims;
@@ -1452,6 +1618,7 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
                         float rho = q->rho[matidx(k, p, bg)], tau = q->tau[matidx(k, p, bg)];
                         eff_material(type, &rho, &tau);
                         double str = strength * (double)q->source_flux[k * Bl + b];
+                        if (cb) str *= (double)ctau[b];
                         d_in[b] += str * (1.0 - rho - tau);
                         if (rho > 0.f || tau > 0.f) {
                             if (face) {
@@ -1465,9 +1632,12 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
                     }
                 }
             }
-            for (int b = 0; b < Bl; ++b) {
+            for (int b = 0; b < Bl; ++b) {  // atomic: covers deposit on other primitives concurrently
+#pragma omp atomic
                 rin[(size_t)p * Bl + b] += d_in[b];
+#pragma omp atomic
                 stop[(size_t)p * Bl + b] += d_top[b];
+#pragma omp atomic
                 sbot[(size_t)p * Bl + b] += d_bot[b];
             }
         }
@@ -1483,6 +1653,10 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
         int dimx = (int)std::sqrt((float)rpp);
         int dimy = dimx > 0 ? rpp / dimx : 1;
         double strength = 1.0 / (double)(dimx * dimy);
+        const std::vector<uint32_t> fbits = cover_bits(flags.data(), 1);
+        const uint32_t *cb = fbits.empty() ? nullptr : fbits.data();
+        bool sky = false;
+        for (int b = 0; b < Bl; ++b) sky = sky || dflux[b] > 0.f;
 #pragma omp parallel for schedule(dynamic, 4) reduction(+ : n_rays, n_nodes, n_prims, n_hits)
         for (int p = 0; p < nl; ++p) {
             int ts = s->twosided[p];
@@ -1494,13 +1668,32 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
             // a voxel's two ray directions both deposit on its top face
             const int dface = (type == PT_VOXEL) ? 1 : face;
             std::vector<double> d_in(Bl, 0.0), d_top(Bl, 0.0), d_bot(Bl, 0.0);
+            std::vector<float> ctau(Bl, 1.f);
             for (int r = 0; r < dimx * dimy; ++r) {
                 V3 org, dir;
                 diffuse_ray(g, type, (uint32_t)r, (uint32_t)p, face, dimx, dimy, q->seed, pass, &org, &dir, s->mk());
                 TraceStats st;
-                Hit hh = trace_full(
-                    *s, Ray{org, dir, 1e-4f, 1e38f, VoxKey{(uint32_t)r, (uint32_t)p, (uint32_t)face, q->seed, pass}},
-                    false, &st);
+                const Ray ray{org, dir, 1e-4f, 1e38f, VoxKey{(uint32_t)r, (uint32_t)p, (uint32_t)face, q->seed, pass}};
+                Hit hh;
+                if (!cb) {
+                    hh = trace_full(*s, ray, false, &st);
+                } else {
+                    // covers deposit the isotropic sky flux of the launch (OptiX8DeviceCode.cu:871-880)
+                    std::fill(ctau.begin(), ctau.end(), 1.f);
+                    hh = trace_covers(*s, ray, cb, 1u, p, sky, &st, [&](int c, int cface) {
+                        const float cs = std::fmin(1.f, std::fabs(vdot(dir, s->rgen[c].N)));
+                        int b = -1;
+                        for (int bg = 0; bg < Bg; ++bg) {
+                            if (!flags[bg]) continue;
+                            ++b;
+                            float tau_c, rho_c, alpha_c;
+                            glass_trs(cs, q->glass_n[matidx(0, c, bg)], q->glass_kl[matidx(0, c, bg)], &tau_c, &rho_c,
+                                      &alpha_c);
+                            cover_deposit(c, cface, b, strength * (double)dflux[b] * (double)ctau[b], alpha_c, rho_c);
+                            ctau[b] *= tau_c;
+                        }
+                    });
+                }
                 n_rays++;
                 n_nodes += st.nodes;
                 n_prims += st.prims;
@@ -1524,6 +1717,7 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
                         float zero4[4] = {0, 0, 0, 0};
                         const float *pr = q->prague ? &q->prague[4 * b] : zero4;
                         val = sky_fd(dir, pk, K, kn, pr) * (double)dflux[b] * strength;
+                        if (cb) val *= (double)ctau[b];
                     }
                     float rho = q->rho[matidx(0, p, bg)], tau = q->tau[matidx(0, p, bg)];
                     eff_material(type, &rho, &tau);
@@ -1539,9 +1733,12 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
                     }
                 }
             }
-            for (int b = 0; b < Bl; ++b) {
+            for (int b = 0; b < Bl; ++b) {  // atomic: covers deposit on other primitives concurrently
+#pragma omp atomic
                 rin[(size_t)p * Bl + b] += d_in[b];
+#pragma omp atomic
                 stop[(size_t)p * Bl + b] += d_top[b];
+#pragma omp atomic
                 sbot[(size_t)p * Bl + b] += d_bot[b];
             }
         }

@@ -77,6 +77,10 @@ class _Solve(C.Structure):
         ("threads", C.c_int32),
         ("prim_limit", C.c_int32),
         ("scatter_tol", C.c_double),
+        ("glass_nsrc", C.c_int32),
+        ("is_glass", C.c_void_p),
+        ("glass_n", C.c_void_p),
+        ("glass_kl", C.c_void_p),
     ]
 
 
@@ -96,6 +100,7 @@ def _load():
         _lib.orc_philox.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_sincos2pi.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_ln_unit.argtypes = [C.c_int64, C.c_void_p, C.c_void_p]
+        _lib.orc_glass_trs.argtypes = [C.c_int64, C.c_void_p, C.c_float, C.c_float, C.c_void_p]
     return _lib
 
 
@@ -215,6 +220,12 @@ class OracleScene:
         s.threads = int(threads)
         s.prim_limit = int(prim_limit)
         s.scatter_tol = float(solve.get("scatter_tolerance", 0.0))
+        ig = arr("is_glass", np.int8)
+        if ig is not None:
+            s.glass_nsrc = ig.shape[0]
+            s.is_glass = _ptr(ig)
+            s.glass_n = _ptr(arr("glass_n", np.float32))
+            s.glass_kl = _ptr(arr("glass_kl", np.float32))
         flux = np.zeros((self.n, bl), np.float64)
         stats = np.zeros(5, np.uint64)
         _load().orc_run_band(self._h, C.byref(s), _ptr(flux), _ptr(stats))
@@ -242,4 +253,12 @@ def ln_unit(x):
     x = np.ascontiguousarray(x, np.float32)
     out = np.zeros_like(x)
     _load().orc_ln_unit(x.size, _ptr(x), _ptr(out))
+    return out
+
+
+def glass_trs(cos_theta, n, kl):
+    """(tau, rho, alpha) [m, 3] of one translucent sheet at the given incidence cosines."""
+    c = np.ascontiguousarray(cos_theta, np.float32).ravel()
+    out = np.zeros((c.size, 3), np.float32)
+    _load().orc_glass_trs(c.size, _ptr(c), float(n), float(kl), _ptr(out))
     return out

@@ -23,6 +23,8 @@ def oracle_solve(desc: dict, rotation=rotation_np) -> dict:
                               "diffuse_norm", "diffuse_peak", "prague", "direct_rays", "diffuse_rays", "depth",
                               "emission", "eps", "temperature", "seed")}
     d["scatter_tolerance"] = desc.get("scatter_tolerance", 0.0)
+    for k in ("is_glass", "glass_n", "glass_kl"):
+        d[k] = desc.get(k)
     d["source_type"] = np.array([s["type"] for s in srcs], np.int32)
     d["source_pos"] = np.array([s["position"] for s in srcs], np.float32)
     d["source_width"] = np.array([s["width"] for s in srcs], np.float32)
@@ -62,3 +64,29 @@ def view_factor_parallel(a, b, c):
                                       + X * math.sqrt(1 + Y2) * math.atan(X / math.sqrt(1 + Y2))
                                       + Y * math.sqrt(1 + X2) * math.atan(Y / math.sqrt(1 + X2))
                                       - X * math.atan(X) - Y * math.atan(Y))
+
+
+def glass_ref(cos_theta, n, KL):
+    """Single-sheet (tau, rho, alpha) in the angle form the reference's glass tests use as
+    their independent check (selfTest.cpp:9556-9591): Fresnel r_s = sin^2(t_r - t) /
+    sin^2(t_r + t), r_p = tan^2(t_r - t) / tan^2(t_r + t), Bouguer exp(-KL / cos t_r) and
+    incoherent multiple reflections; float64 here."""
+    c = min(1.0, max(1e-4, cos_theta))
+    th = math.acos(c)
+    st = math.sin(th) / n
+    ctr = math.sqrt(max(0.0, 1.0 - st * st))
+    tr = math.asin(min(1.0, st))
+    if th < 1e-3:
+        r_s = r_p = ((n - 1.0) / (n + 1.0)) ** 2
+    else:
+        r_s = math.sin(tr - th) ** 2 / max(1e-12, math.sin(tr + th) ** 2)
+        r_p = math.tan(tr - th) ** 2 / max(1e-12, math.tan(tr + th) ** 2)
+    ta = math.exp(-KL / max(1e-4, ctr)) if KL > 0 else 1.0
+    tau = rho = 0.0
+    for r in (r_s, r_p):
+        den = max(1e-6, 1.0 - (r * ta) ** 2)
+        ti = ta * (1.0 - r) ** 2 / den
+        tau += 0.5 * ti
+        rho += 0.5 * r * (1.0 + ta * ti)
+    tau, rho = min(1.0, max(0.0, tau)), min(1.0, max(0.0, rho))
+    return tau, rho, max(0.0, 1.0 - tau - rho)

@@ -12,7 +12,7 @@ import numpy as np
 from helios_gb300 import scenes
 from helios_gb300.radiation import SIGMA, Context, RadiationModel
 
-from helpers import beer_diffuse, view_factor_parallel
+from helpers import beer_diffuse, glass_ref, view_factor_parallel
 
 
 def _ensemble(run, rad, labels, k, seed0=11):
@@ -385,6 +385,115 @@ def parallel_disks_masked(run, ensemble=4, ndir=10000, ndiff=200000):
     lw = _ensemble(run, rad, ["LW"], ensemble, seed0=52)
     return [("masked_sw_0", sw[0, 0], sw0, 0.01), ("masked_sw_1", sw[1, 0], sw1, 0.01),
             ("masked_lw_0", lw[0, 0], lw0, 0.01), ("masked_lw_1", lw[1, 0], lw1, 0.01)]
+
+
+def _glass_model(ctx, bands=("SW",), sun=(0.0, 0.0, 1.0), rays=10000, depth=1):
+    rad = RadiationModel(ctx)
+    for b in bands:
+        rad.addRadiationBand(b)
+        rad.disableEmission(b)
+    s = rad.addCollimatedRadiationSource(sun)
+    for b in bands:
+        rad.setSourceFlux(s, b, 1000.0)
+        rad.setDirectRayCount(b, rays)
+        rad.setScatteringDepth(b, depth)
+    return rad
+
+
+def _cover_receiver(cover_size=4.0, covers=(1.0,)):
+    ctx = Context()
+    cov = [ctx.addPatch((0, 0, z), (cover_size, cover_size)) for z in covers]
+    rec = ctx.addPatch((0, 0, 0), (2, 2))
+    ctx.setPrimitiveData(rec, "twosided_flag", 0)
+    ctx.setPrimitiveData(rec, "reflectivity_SW", 0.0)
+    return ctx, cov, rec
+
+
+def glass_normal(run):
+    """selfTest.cpp:9617-9648: lossless cover (n 1.5) over an absorbing receiver, sun at the
+    zenith: the receiver gets 1000 tau(0)."""
+    ctx, (cov,), rec = _cover_receiver()
+    ctx.setPrimitiveData(cov, "glass_n_SW", 1.5)
+    f = run(_glass_model(ctx), ["SW"], 5)
+    return [("glass_normal", f[rec, 0], 1000.0 * glass_ref(1.0, 1.5, 0.0)[0], 0.02)]
+
+
+def glass_oblique(run):
+    """selfTest.cpp:9654-9684: sun 30 degrees from the zenith: 1000 cos(30) tau(30)."""
+    th = math.radians(30.0)
+    ctx, (cov,), rec = _cover_receiver(cover_size=8.0)
+    ctx.setPrimitiveData(cov, "glass_n_SW", 1.5)
+    f = run(_glass_model(ctx, sun=(math.sin(th), 0.0, math.cos(th)), rays=20000), ["SW"], 6)
+    return [("glass_oblique", f[rec, 0], 1000.0 * math.cos(th) * glass_ref(math.cos(th), 1.5, 0.0)[0], 0.03)]
+
+
+def glass_overrides_constant(run):
+    """selfTest.cpp:9689-9718: glass_n wins over a constant transmissivity 0.2."""
+    ctx, (cov,), rec = _cover_receiver()
+    ctx.setPrimitiveData(cov, "glass_n_SW", 1.5)
+    ctx.setPrimitiveData(cov, "transmissivity_SW", 0.2)
+    f = run(_glass_model(ctx), ["SW"], 7)
+    return [("glass_override", f[rec, 0], 1000.0 * glass_ref(1.0, 1.5, 0.0)[0], 0.02),
+            ("glass_override_not_constant", float(f[rec, 0] > 800.0), 1.0, 0.0)]
+
+
+def glass_beam_direction(run):
+    """selfTest.cpp:9724-9779: an opaque ceiling with a glass window, sun 45 degrees off the
+    zenith: the receiver whose sun ray passes the window gets 1000 cos(45) tau(45), the one
+    under the window is shaded by the ceiling."""
+    th, dz = math.radians(45.0), 2.0
+    shift = dz * math.tan(th)
+    ctx = Context()
+    cl = ctx.addPatch((-3.0, 0, dz), (4.0, 6.0))
+    cr = ctx.addPatch((3.0, 0, dz), (4.0, 6.0))
+    win = ctx.addPatch((0, 0, dz), (2.0, 6.0))
+    for c in (cl, cr):
+        ctx.setPrimitiveData(c, "twosided_flag", 1)
+        ctx.setPrimitiveData(c, "reflectivity_SW", 0.0)
+    ctx.setPrimitiveData(win, "glass_n_SW", 1.5)
+    rin = ctx.addPatch((-shift, 0, 0), (1.0, 1.0))
+    rbe = ctx.addPatch((0, 0, 0), (1.0, 1.0))
+    for r in (rin, rbe):
+        ctx.setPrimitiveData(r, "twosided_flag", 0)
+        ctx.setPrimitiveData(r, "reflectivity_SW", 0.0)
+    f = run(_glass_model(ctx, sun=(math.sin(th), 0.0, math.cos(th)), rays=40000), ["SW"], 8)
+    exp = 1000.0 * math.cos(th) * glass_ref(math.cos(th), 1.5, 0.0)[0]
+    return [("glass_window_inpath", f[rin, 0], exp, 0.08),
+            ("glass_window_below_shaded", float(f[rbe, 0] < 0.4 * f[rin, 0]), 1.0, 0.0)]
+
+
+def glass_inactive(run):
+    """selfTest.cpp:9783-9807: without glass_n the cover is an opaque absorber."""
+    ctx, (cov,), rec = _cover_receiver()
+    ctx.setPrimitiveData(cov, "twosided_flag", 0)
+    ctx.setPrimitiveData(cov, "reflectivity_SW", 0.0)
+    f = run(_glass_model(ctx, depth=0), ["SW"], 9)
+    return [("glass_inactive_blocked", float(f[rec, 0] < 5.0), 1.0, 0.0)]
+
+
+def glass_double_layer(run):
+    """selfTest.cpp:9811-9838: two stacked covers transmit tau(0)^2."""
+    ctx, cov, rec = _cover_receiver(covers=(2.0, 1.0))
+    for c in cov:
+        ctx.setPrimitiveData(c, "glass_n_SW", 1.5)
+    f = run(_glass_model(ctx), ["SW"], 10)
+    return [("glass_double", f[rec, 0], 1000.0 * glass_ref(1.0, 1.5, 0.0)[0] ** 2, 0.03)]
+
+
+def glass_mixed_bands(run):
+    """selfTest.cpp:9840-9882: glass in SW only, SW and LW launched together: the cover is
+    opaque for the whole ray, both bands are blocked."""
+    ctx, (cov,), rec = _cover_receiver()
+    ctx.setPrimitiveData(rec, "reflectivity_LW", 0.0)
+    ctx.setPrimitiveData(cov, "glass_n_SW", 1.5)
+    ctx.setPrimitiveData(cov, "reflectivity_LW", 0.0)
+    rad = _glass_model(ctx, bands=("LW", "SW"))
+    f = run(rad, ["SW", "LW"], 11)
+    return [("glass_mixed_blocked", float(f[rec, 0] < 5.0 and f[rec, 1] < 5.0), 1.0, 0.0)]
+
+
+GLASS = ["glass_normal", "glass_oblique", "glass_overrides_constant", "glass_beam_direction", "glass_inactive",
+         "glass_double_layer", "glass_mixed_bands"]
 
 
 def check(results, abs_tol_names=()):

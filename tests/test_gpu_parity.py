@@ -230,7 +230,7 @@ def test_sources_all_types(oracle_mod):
 
 @pytest.mark.parametrize("name", ["simple_direct", "black_parallel_rectangles", "gray_parallel_rectangles",
                                   "common_edge_squares", "launch_batching", "second_law_box",
-                                  "parallel_disks_masked"])
+                                  "parallel_disks_masked"] + scenarios.GLASS)
 def test_known_answers_on_gpu(name):
     def run(rad, labels, seed):
         rad.setSeed(seed)
@@ -425,3 +425,95 @@ def test_masked_hits_and_rays_exact(oracle_mod):
         o1, d1 = rad.ctx.gen_rays(kind, 5, 2, 64, face, scenes.sun_direction(35, 10))
         o2, d2 = sc.gen_rays(kind, 5, 2, 64, face, scenes.sun_direction(35, 10))
         assert np.array_equal(o1, o2) and np.array_equal(d1, d2)
+
+
+def _greenhouse(periodic=False, mode="device", n_leaves=1500, seed=0):
+    """A canopy under a roof of 16 slightly tilted glass panes (glass in PAR and NIR with
+    absorption, opaque in LW), two suns and a sky; leaves and ground emit in LW."""
+    sc = scenes.homogeneous_canopy(n_leaves=n_leaves, leaf=0.1, domain=3.0, zlo=0.5, zhi=2.0, seed=seed)
+    ctx = Context()
+    ctx.addScene(sc)
+    lv = sc.groups["leaves"]
+    roof = [ctx.addPatch((0.375 + 0.75 * i, 0.375 + 0.75 * j, 2.6 + 0.05 * ((i + j) % 2)), (0.75, 0.75),
+                         (0.08 * (i - 1.5), 0.3 * j)) for i in range(4) for j in range(4)]
+    ctx.setPrimitiveData(lv, "reflectivity_PAR", np.full(lv.size, 0.08))
+    ctx.setPrimitiveData(lv, "transmissivity_PAR", np.full(lv.size, 0.05))
+    ctx.setPrimitiveData(lv, "reflectivity_NIR", np.full(lv.size, 0.45))
+    ctx.setPrimitiveData(lv, "transmissivity_NIR", np.full(lv.size, 0.40))
+    ctx.setPrimitiveData(lv, "emissivity_LW", np.full(lv.size, 0.96))
+    for k, u in enumerate(roof):
+        ctx.setPrimitiveData(u, "glass_n_PAR", 1.5)
+        ctx.setPrimitiveData(u, "glass_KL_PAR", 0.05)
+        ctx.setPrimitiveData(u, "glass_n_NIR", 1.45 + 0.01 * k)
+        ctx.setPrimitiveData(u, "glass_KL_NIR", 0.2)
+        ctx.setPrimitiveData(u, "emissivity_LW", 0.9)
+    n = ctx.getPrimitiveCount()
+    rng = np.random.default_rng(seed)
+    ctx.setPrimitiveData(np.arange(n), "temperature", 273.15 + rng.normal(25.0, 2.0, n))
+    rad = RadiationModel(ctx, mode=mode)
+    if periodic:
+        rad.enforcePeriodicBoundary("xy")
+    s0 = rad.addCollimatedRadiationSource(scenes.sun_direction(35, 20))
+    s1 = rad.addCollimatedRadiationSource(scenes.sun_direction(60, 200))
+    for b in ("PAR", "NIR", "LW"):
+        rad.addRadiationBand(b)
+        rad.setDirectRayCount(b, 64)
+        rad.setDiffuseRayCount(b, 100)
+        rad.setScatteringDepth(b, 3)
+    for b, f0, f1 in (("PAR", 500.0, 120.0), ("NIR", 450.0, 90.0)):
+        rad.disableEmission(b)
+        rad.setDiffuseRadiationFlux(b, 100.0)
+        rad.setSourceFlux(s0, b, f0)
+        rad.setSourceFlux(s1, b, f1)
+    return rad
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_greenhouse_glass_vs_oracle(oracle_mod, periodic):
+    """Translucent covers: two suns and the sky through a glass roof (glass in every launched
+    band of the PAR + NIR launch), then LW with the roof opaque; fluxes of every primitive,
+    covers included, and the ray count against the oracle."""
+    rad = _greenhouse(periodic=periodic)
+    rad.setSeed(13)
+    got = rad.runBand(["PAR", "NIR"])
+    ref, st = run_oracle(rad, ["PAR", "NIR"], oracle_mod, seed=13)
+    worst, _ = _flux_close(got, ref)
+    assert worst <= FLUX_RTOL, worst
+    assert rad.last_stats["rays"] == st["rays"]
+    rad.setSeed(14)
+    got = rad.runBand("LW")
+    ref, _ = run_oracle(rad, ["LW"], oracle_mod, seed=14)
+    worst, _ = _flux_close(got, ref)
+    assert worst <= FLUX_RTOL, worst
+
+
+def test_greenhouse_backend_sequence():
+    """The backend entry points (hrt_update_glass with the materials) give the device solve's
+    fluxes for a scene with covers."""
+    a = _greenhouse(mode="device")
+    b = _greenhouse(mode="backend")
+    a.setSeed(3)
+    b.setSeed(3)
+    fa = a.runBand(["PAR", "NIR"])
+    fb = b.runBand(["PAR", "NIR"])
+    worst, _ = _flux_close(fb, fa, 1e-5)
+    assert worst <= 1e-5, worst
+
+
+def test_glass_errors(gpu):
+    T, ty, ts = _mixed(seed=2, n_leaf=50, n_tri=50)
+    gpu.update_geometry(T, ty, ts)
+    gpu.build_accel()
+    n = T.shape[0]
+    ig = np.zeros((1, n, 2), np.int8)
+    ig[0, :5] = 1
+    bad_n = np.ones((1, n, 2), np.float32) * 0.5
+    with pytest.raises(RuntimeError, match="refractive index"):
+        gpu.update_glass(ig, bad_n, np.zeros((1, n, 2), np.float32))
+    with pytest.raises(RuntimeError, match="geometry"):
+        gpu.update_glass(ig[:, :-1], np.full((1, n - 1, 2), 1.5, np.float32), np.zeros((1, n - 1, 2), np.float32))
+    gpu.update_glass(ig, np.full((1, n, 2), 1.5, np.float32), np.zeros((1, n, 2), np.float32))
+    with pytest.raises(RuntimeError, match="sweep"):
+        gpu.run_sweep(np.array([[0.0, 0.0, 1.0]]), np.ones((1, 2)), np.ones((1, 2)), np.full((n, 2), 0.1),
+                      np.full((n, 2), 0.05), 4, 4, 1, 0)
+    gpu.update_glass(None)
