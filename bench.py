@@ -33,6 +33,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "rays/s and solves/s (batched/served vs plain, 1 GB300) at <=1e-4 flux err; p50/p99"
 UNIT = "rays/s"
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the 4-wide persistent diffuse
+# kernel on the orchard (1 M triangles, 3 bands, 450 M rays per launch): mean of three
+# captured launches, 2.343 GB + 0.086 GB (profiles/k_diffuse_ps_wide4_orchard-1M_traffic.md)
+TRAFFIC_PER_LAUNCH = 2.429e9
 
 
 def peaks():
@@ -450,13 +454,18 @@ def run_gpu(args):
         return
     hbm, peak_kind = peaks()
     # algorithmic bytes of the diffuse kernel (dominant): per ray 64 B per node visit,
-    # 48 B per primitive test, origin record 64 B, per-band gather 4 B on hits and 8 B accumulate
-    n_launch = max(stats["diffuse_launches"] + stats["direct_launches"], 1)
+    # 48 B per primitive test, origin record 64 B, per-band gather 4 B on hits and 8 B accumulate;
+    # per launch: the mean bytes per ray of the statistics solve x the rays of one diffuse launch
     alg_bytes_total = 64.0 * stats["node_visits"] + 48.0 * stats["prim_tests"] + rays_per_step * (64 + 4 * 3)
+    bytes_per_ray = alg_bytes_total / max(rays_per_step, 1)
+    rays_per_launch = stats["diffuse_rays"] / max(stats["diffuse_launches"], 1)
     diff_ms = meas["diffuse_ms"] / max(meas["diffuse_launches"], 1)
     diff_share = meas["diffuse_ms"] / max(meas["diffuse_ms"] + meas["direct_ms"], 1e-9)
-    bytes_per_launch = alg_bytes_total / n_launch
+    bytes_per_launch = bytes_per_ray * rays_per_launch
     achieved = bytes_per_launch / (diff_ms * 1e-3) / 1e9
+    # DRAM bytes per launch of the same kernel on this workload, from one ncu capture
+    # (profiles/k_diffuse_ps_wide4_orchard-1M_traffic.md); the workload is fixed
+    traffic = TRAFFIC_PER_LAUNCH if sc.n == 1_000_000 else None
     rps = rays_per_step * world / (ms * 1e-3)
     cpu = None
     if not args.no_cpu:
@@ -474,8 +483,9 @@ def run_gpu(args):
                    "l2": "working set (BVH 64 MB + records 128 MB + buffers) larger than the 129 MB L2; no flush",
                    "setup_s": setup_s},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_kind": peak_kind, "traffic": None, "kernel": "k_diffuse",
-                     "kernel_ms": diff_ms, "kernel_share": diff_share,
+                     "peak_kind": peak_kind, "traffic": traffic, "kernel": "k_diffuse",
+                     "kernel_ms": diff_ms, "kernel_share": diff_share, "bytes_per_launch": bytes_per_launch,
+                     "rays_per_launch": rays_per_launch,
                      "node_visits_per_ray": stats["node_visits"] / max(rays_per_step, 1),
                      "prim_tests_per_ray": stats["prim_tests"] / max(rays_per_step, 1)},
         "autotune": [x for x in ctx.tuning_report().splitlines() if x.startswith("accumulate")],

@@ -26,7 +26,8 @@ EXPORTS = [
     "hrt_source_rotation", "hrt_set_measure", "hrt_get_measure", "hrt_build_accel_static", "hrt_run_sweep",
     "hrt_server_create", "hrt_server_add_scene", "hrt_server_submit", "hrt_server_start", "hrt_server_wait",
     "hrt_server_result", "hrt_server_stats", "hrt_server_destroy", "hrt_set_tuning", "hrt_tuning_report",
-    "hrt_set_ray_budget", "hrt_update_glass",
+    "hrt_set_ray_budget", "hrt_update_glass", "hrt_update_sky_model", "hrt_launch_camera",
+    "hrt_launch_pixel_labels", "hrt_zero_camera_pixel_buffers", "hrt_get_camera_results",
 ]
 
 
@@ -65,7 +66,68 @@ class BandSolve(C.Structure):
                 ("diffuse_dist_norm", C.c_void_p), ("sky_radiance_params", C.c_void_p),
                 ("direct_rays", C.c_void_p), ("diffuse_rays", C.c_void_p), ("scattering_depth", C.c_void_p),
                 ("emission", C.c_void_p), ("emissivity", C.c_void_p), ("temperature", C.c_void_p),
-                ("seed", C.c_uint32), ("scatter_tolerance", C.c_double)]
+                ("seed", C.c_uint32), ("scatter_tolerance", C.c_double), ("ncameras", C.c_int32),
+                ("cameras", C.c_void_p), ("camera_sky", C.c_void_p)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("direction", C.c_float * 2), ("focal_length", C.c_float),
+                ("lens_diameter", C.c_float), ("fov_aspect", C.c_float), ("viewplane_length", C.c_float),
+                ("resolution", C.c_int32 * 2), ("tile_offset", C.c_int32 * 2), ("tile_resolution", C.c_int32 * 2),
+                ("antialiasing", C.c_int32), ("seed", C.c_uint32), ("camera_id", C.c_uint32),
+                ("pixels", C.c_void_p), ("labels", C.c_void_p), ("depths", C.c_void_p)]
+
+
+class SkyModel(C.Structure):
+    _fields_ = [("sky_radiance_params", C.c_void_p), ("camera_sky_radiance", C.c_void_p),
+                ("sun_direction", C.c_float * 3), ("solar_disk_radiance", C.c_void_p),
+                ("solar_disk_cos_angle", C.c_float), ("camera_diffuse_flux", C.c_void_p),
+                ("band_emission_flag", C.c_void_p)]
+
+
+def make_camera(cam: dict) -> Camera:
+    """hrt_camera from a camera dict (the form the oracle takes)."""
+    c = Camera()
+    for k in range(3):
+        c.position[k] = float(cam["position"][k])
+    c.direction[0], c.direction[1] = float(cam["direction"][0]), float(cam["direction"][1])
+    c.focal_length = float(cam["focal_length"])
+    c.lens_diameter = float(cam["lens_diameter"])
+    c.fov_aspect = float(cam["fov_aspect"])
+    c.viewplane_length = float(cam["viewplane_length"])
+    c.resolution[0], c.resolution[1] = int(cam["resolution"][0]), int(cam["resolution"][1])
+    off = cam.get("tile_offset", (0, 0))
+    tr = cam.get("tile_resolution", (0, 0))
+    c.tile_offset[0], c.tile_offset[1] = int(off[0]), int(off[1])
+    c.tile_resolution[0], c.tile_resolution[1] = int(tr[0]), int(tr[1])
+    c.antialiasing = int(cam.get("antialiasing", 1))
+    c.seed = int(cam.get("seed", 0)) & 0xFFFFFFFF
+    c.camera_id = int(cam.get("camera_id", 0))
+    return c
+
+
+def make_sky_model(sky: dict, keep: list) -> SkyModel:
+    """hrt_sky_model from a camera-sky dict; arrays referenced are appended to keep."""
+    m = SkyModel()
+
+    def a(key, dt):
+        v = sky.get(key)
+        if v is None:
+            return None
+        arr = np.ascontiguousarray(v, dt).ravel()
+        keep.append(arr)
+        return ptr(arr)
+
+    m.sky_radiance_params = a("prague", np.float32)
+    m.camera_sky_radiance = a("sky_radiance", np.float32)
+    sun = sky.get("sun", (0.0, 0.0, 1.0))
+    for k in range(3):
+        m.sun_direction[k] = float(sun[k])
+    m.solar_disk_radiance = a("disk_radiance", np.float32)
+    m.solar_disk_cos_angle = float(sky.get("disk_cos", 0.0))
+    m.camera_diffuse_flux = a("diffuse_flux", np.float32)
+    m.band_emission_flag = a("emission", np.uint32)
+    return m
 
 
 class Sweep(C.Structure):
@@ -103,6 +165,11 @@ def load(path: str | None = None):
         "hrt_build_accel": (C.c_int, [VP]),
         "hrt_update_materials": (C.c_int, [VP, C.c_int32, C.c_int32, C.c_int32, VP, VP]),
         "hrt_update_glass": (C.c_int, [VP, C.c_int32, C.c_int32, C.c_int32, VP, VP, VP]),
+        "hrt_update_sky_model": (C.c_int, [VP, C.c_int32, VP]),
+        "hrt_launch_camera": (C.c_int, [VP, VP]),
+        "hrt_launch_pixel_labels": (C.c_int, [VP, VP]),
+        "hrt_zero_camera_pixel_buffers": (C.c_int, [VP, C.c_int32, C.c_int32]),
+        "hrt_get_camera_results": (C.c_int, [VP, VP, VP, VP, C.c_int32, C.c_int32]),
         "hrt_update_sources": (C.c_int, [VP, C.c_int32, VP]),
         "hrt_upload_source_fluxes": (C.c_int, [VP, VP, C.c_size_t]),
         "hrt_launch_direct": (C.c_int, [VP, C.POINTER(Launch)]),
@@ -364,7 +431,51 @@ class Context:
         s.temperature = a("temperature", np.float32)
         s.seed = int(solve.get("seed", 0)) & 0xFFFFFFFF
         s.scatter_tolerance = float(solve.get("scatter_tolerance", 0.0))
+        cams = solve.get("cameras") or []
+        self.last_cameras = []
+        if cams:
+            nb = int(np.count_nonzero(np.asarray(solve["band_launch"])))
+            arr = (Camera * len(cams))()
+            for i, cam in enumerate(cams):
+                arr[i] = make_camera(cam)
+                W, H = int(cam["resolution"][0]), int(cam["resolution"][1])
+                out = {"pixels": np.zeros((H, W, nb), np.float32), "labels": np.zeros((H, W), np.uint32),
+                       "depths": np.zeros((H, W), np.float32)}
+                arr[i].pixels, arr[i].labels, arr[i].depths = ptr(out["pixels"]), ptr(out["labels"]), ptr(out["depths"])
+                self.last_cameras.append(out)
+            keep.append(arr)
+            s.ncameras = len(cams)
+            s.cameras = C.cast(arr, C.c_void_p)
+            if solve.get("camera_sky") is not None:
+                m = make_sky_model(solve["camera_sky"], keep)
+                keep.append(m)
+                s.camera_sky = C.cast(C.pointer(m), C.c_void_p)
         return s, keep
+
+    # ---------------------------------------------------------------- cameras
+    def update_sky_model(self, nbands, sky=None):
+        keep = []
+        m = None if sky is None else make_sky_model(sky, keep)
+        self.check(self.lib.hrt_update_sky_model(self.h, int(nbands) if sky is not None else 0,
+                                                 None if m is None else C.byref(m)))
+
+    def launch_camera(self, cam: dict):
+        c = make_camera(cam)
+        self.check(self.lib.hrt_launch_camera(self.h, C.byref(c)))
+
+    def launch_pixel_labels(self, cam: dict):
+        c = make_camera(cam)
+        self.check(self.lib.hrt_launch_pixel_labels(self.h, C.byref(c)))
+
+    def zero_camera_pixel_buffers(self, width, height):
+        self.check(self.lib.hrt_zero_camera_pixel_buffers(self.h, int(width), int(height)))
+
+    def get_camera_results(self, width, height, nbands, pixels=True, labels=True):
+        pix = np.zeros((height, width, nbands), np.float32) if pixels else None
+        lab = np.zeros((height, width), np.uint32) if labels else None
+        dep = np.zeros((height, width), np.float32) if labels else None
+        self.check(self.lib.hrt_get_camera_results(self.h, ptr(pix), ptr(lab), ptr(dep), int(width), int(height)))
+        return pix, lab, dep
 
     def run_band(self, solve: dict, out: bool = True):
         self.update_glass(solve.get("is_glass"), solve.get("glass_n"), solve.get("glass_kl"))
@@ -444,7 +555,8 @@ class Context:
         out = np.zeros(8, np.float64)
         self.check(self.lib.hrt_get_measure(self.h, ptr(out), 8))
         return {"direct_launches": int(out[0]), "direct_ms": float(out[1]), "diffuse_launches": int(out[2]),
-                "diffuse_ms": float(out[3]), "node_visits": int(out[4]), "prim_tests": int(out[5])}
+                "diffuse_ms": float(out[3]), "node_visits": int(out[4]), "prim_tests": int(out[5]),
+                "direct_rays": int(out[6]), "diffuse_rays": int(out[7])}
 
     def device_status(self, reset=True):
         st = C.c_uint32()

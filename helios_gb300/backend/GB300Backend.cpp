@@ -8,6 +8,11 @@
  *   launchDiffuseRays         :872-1002  -> hrt_launch_diffuse (uploads radiation_out first)
  *   getRadiationResults       :1119-1143 -> hrt_get_results
  *   zero/copy/upload          :1168-1250 -> hrt_zero_* / hrt_copy_scatter_to_radiation / hrt_upload_radiation_out
+ *   updateSkyModel            :744       -> hrt_update_sky_model
+ *   launchCameraRays          :1004      -> hrt_launch_camera
+ *   launchPixelLabelRays      :1071      -> hrt_launch_pixel_labels
+ *   getCameraResults          :1145      -> hrt_get_camera_results
+ *   zeroCameraPixelBuffers    :1207      -> hrt_zero_camera_pixel_buffers
  */
 #include "GB300Backend.h"
 
@@ -137,10 +142,56 @@ void GB300Backend::updateDiffuseRadiation(const std::vector<float> &, const std:
                                           const std::vector<helios::vec3> &, const std::vector<float> &,
                                           const std::vector<float> &) {}
 
-// Sky radiance for cameras: cameras are not provided by this backend.
-void GB300Backend::updateSkyModel(const std::vector<helios::vec4> &, const std::vector<float> &, const helios::vec3 &,
-                                  const std::vector<float> &, float, const std::vector<float> &,
-                                  const std::vector<uint32_t> &) {}
+// What cameras see where their rays leave the scene.
+void GB300Backend::updateSkyModel(const std::vector<helios::vec4> &sky_radiance_params,
+                                  const std::vector<float> &camera_sky_radiance, const helios::vec3 &sun_direction,
+                                  const std::vector<float> &solar_disk_radiance, float solar_disk_cos_angle,
+                                  const std::vector<float> &camera_diffuse_flux,
+                                  const std::vector<uint32_t> &band_emission_flag) {
+    const size_t B = std::max(sky_radiance_params.size(), camera_sky_radiance.size());
+    std::vector<float> prague;
+    for (const auto &v : sky_radiance_params) {
+        prague.push_back(v.x);
+        prague.push_back(v.y);
+        prague.push_back(v.z);
+        prague.push_back(v.w);
+    }
+    auto arr = [B](const std::vector<float> &v) { return v.size() >= B && B > 0 ? v.data() : nullptr; };
+    hrt_sky_model m{};
+    m.sky_radiance_params = prague.size() >= 4 * B && B > 0 ? prague.data() : nullptr;
+    m.camera_sky_radiance = arr(camera_sky_radiance);
+    m.sun_direction[0] = sun_direction.x;
+    m.sun_direction[1] = sun_direction.y;
+    m.sun_direction[2] = sun_direction.z;
+    m.solar_disk_radiance = arr(solar_disk_radiance);
+    m.solar_disk_cos_angle = solar_disk_cos_angle;
+    m.camera_diffuse_flux = arr(camera_diffuse_flux);
+    m.band_emission_flag = band_emission_flag.size() >= B && B > 0 ? band_emission_flag.data() : nullptr;
+    check(hrt_update_sky_model(ctx_, (int32_t)B, B ? &m : nullptr), "updateSkyModel");
+}
+
+hrt_camera GB300Backend::makeCamera(const RayTracingLaunchParams &p) const {
+    hrt_camera c{};
+    c.position[0] = p.camera_position.x;
+    c.position[1] = p.camera_position.y;
+    c.position[2] = p.camera_position.z;
+    c.direction[0] = p.camera_direction.x;
+    c.direction[1] = p.camera_direction.y;
+    c.focal_length = p.camera_focal_length;
+    c.lens_diameter = p.camera_lens_diameter;
+    c.fov_aspect = p.camera_fov_aspect;
+    c.viewplane_length = p.camera_viewplane_length;
+    c.resolution[0] = p.camera_resolution_full.x;
+    c.resolution[1] = p.camera_resolution_full.y;
+    c.tile_offset[0] = p.camera_pixel_offset.x;
+    c.tile_offset[1] = p.camera_pixel_offset.y;
+    c.tile_resolution[0] = p.camera_resolution.x;
+    c.tile_resolution[1] = p.camera_resolution.y;
+    c.antialiasing = (int32_t)p.antialiasing_samples;
+    c.seed = p.random_seed;
+    c.camera_id = p.camera_id;
+    return c;
+}
 
 hrt_launch GB300Backend::makeLaunch(const RayTracingLaunchParams &p, std::vector<uint8_t> &flags,
                                     std::vector<float> &peak, std::vector<float> &sky) const {
@@ -191,12 +242,16 @@ void GB300Backend::launchDiffuseRays(const RayTracingLaunchParams &p) {
     check(hrt_launch_diffuse(ctx_, &L), "launchDiffuseRays");
 }
 
-void GB300Backend::launchCameraRays(const RayTracingLaunchParams &) {
-    helios_runtime_error("ERROR (GB300Backend::launchCameraRays): radiation cameras are not provided by the GB300 backend.");
+void GB300Backend::launchCameraRays(const RayTracingLaunchParams &p) {
+    hrt_camera c = makeCamera(p);
+    check(hrt_launch_camera(ctx_, &c), "launchCameraRays");
+    camera_image_ = p.camera_resolution_full;
 }
 
-void GB300Backend::launchPixelLabelRays(const RayTracingLaunchParams &) {
-    helios_runtime_error("ERROR (GB300Backend::launchPixelLabelRays): pixel labelling is not provided by the GB300 backend.");
+void GB300Backend::launchPixelLabelRays(const RayTracingLaunchParams &p) {
+    hrt_camera c = makeCamera(p);
+    check(hrt_launch_pixel_labels(ctx_, &c), "launchPixelLabelRays");
+    label_image_ = p.camera_resolution_full;
 }
 
 void GB300Backend::getRadiationResults(RayTracingResults &r) {
@@ -212,11 +267,28 @@ void GB300Backend::getRadiationResults(RayTracingResults &r) {
     check(hrt_get_results(ctx_, r.radiation_in.data(), r.radiation_out_top.data(), r.radiation_out_bottom.data(),
                           r.scatter_buff_top.data(), r.scatter_buff_bottom.data()),
           "getRadiationResults");
+    // Camera-weighted scatter: the camera materials are the band materials here, so a pass's
+    // camera scatter is its scatter (RadiationModel reads both right after the same launches).
+    r.scatter_buff_top_cam = r.scatter_buff_top;
+    r.scatter_buff_bottom_cam = r.scatter_buff_bottom;
 }
 
-void GB300Backend::getCameraResults(std::vector<float> &, std::vector<uint> &, std::vector<float> &, uint,
-                                    const helios::int2 &) {
-    helios_runtime_error("ERROR (GB300Backend::getCameraResults): radiation cameras are not provided by the GB300 backend.");
+void GB300Backend::getCameraResults(std::vector<float> &pixel_data, std::vector<uint> &pixel_labels,
+                                    std::vector<float> &pixel_depths, uint, const helios::int2 &resolution) {
+    const size_t npx = (size_t)std::max(resolution.x, 0) * (size_t)std::max(resolution.y, 0);
+    if (npx == 0) return;
+    if (camera_image_.x == resolution.x && camera_image_.y == resolution.y) {
+        pixel_data.assign(npx * launch_bands_, 0.f);
+        check(hrt_get_camera_results(ctx_, pixel_data.data(), nullptr, nullptr, resolution.x, resolution.y),
+              "getCameraResults");
+    }
+    if (label_image_.x == resolution.x && label_image_.y == resolution.y) {
+        std::vector<uint32_t> labels(npx, 0u);
+        pixel_depths.assign(npx, 0.f);
+        check(hrt_get_camera_results(ctx_, nullptr, labels.data(), pixel_depths.data(), resolution.x, resolution.y),
+              "getCameraResults");
+        pixel_labels.assign(labels.begin(), labels.end());
+    }
 }
 
 void GB300Backend::zeroRadiationBuffers(size_t launch_band_count) {
@@ -226,7 +298,10 @@ void GB300Backend::zeroRadiationBuffers(size_t launch_band_count) {
 
 void GB300Backend::zeroScatterBuffers() { check(hrt_zero_scatter_buffers(ctx_), "zeroScatterBuffers"); }
 
-void GB300Backend::zeroCameraPixelBuffers(const helios::int2 &) {}
+void GB300Backend::zeroCameraPixelBuffers(const helios::int2 &resolution) {
+    check(hrt_zero_camera_pixel_buffers(ctx_, resolution.x, resolution.y), "zeroCameraPixelBuffers");
+    label_image_ = resolution;
+}
 
 void GB300Backend::copyScatterToRadiation() { check(hrt_copy_scatter_to_radiation(ctx_), "copyScatterToRadiation"); }
 

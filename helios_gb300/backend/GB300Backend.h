@@ -8,7 +8,8 @@
  *     auto radiation = helios::RadiationModel::createWithBackend(&context, std::move(be));
  * (RadiationModel.h:730).  Every virtual forwards to one hrt_* call; a non-zero
  * return code becomes helios_runtime_error with the library's message.
- * Camera and pixel-label launches are not provided by this backend.
+ * Cameras render with the band materials (no per-camera spectral weighting) and without
+ * specular highlights.
  */
 #ifndef HELIOS_GB300_BACKEND_H
 #define HELIOS_GB300_BACKEND_H
@@ -63,12 +64,15 @@ private:
     void check(int rc, const char *where) const;
     hrt_launch makeLaunch(const RayTracingLaunchParams &p, std::vector<uint8_t> &flags, std::vector<float> &peak,
                           std::vector<float> &sky) const;
+    hrt_camera makeCamera(const RayTracingLaunchParams &p) const;
 
     int device_;
     hrt_context *ctx_ = nullptr;
     size_t nprims_ = 0;
     size_t launch_bands_ = 0;
     std::vector<float> voxel_lad_;
+    helios::int2 camera_image_{0, 0};  // resolution of the camera image on the device
+    helios::int2 label_image_{0, 0};   // resolution of the pixel labels on the device
 };
 
 }  // namespace helios

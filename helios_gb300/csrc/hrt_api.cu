@@ -153,6 +153,15 @@ struct hrt_context {
     bool cover_any = false;
     std::vector<uint8_t> h_flags;  // band flags of the current launch
     bool sky_any = false;          // some launched band of the current launch has sky flux
+    // cameras: radiance [W*H*Bl] (FP64), labels and depths [W*H], the camera sky model
+    // ([sky radiance B][solar disk B][sky flux B][Prague 4B][sun 3B], emission flags [B]) and
+    // the camera view of the primitives that hrt_run_band accumulates
+    DevBuf cam_pix, cam_lab, cam_dep, cam_sky, cam_em, ctop, cbot;
+    int cam_W = 0, cam_H = 0, cam_B = 0, lab_W = 0, lab_H = 0;
+    uint32_t cam_id_cur = 0xFFFFFFFFu;
+    int sky_B = 0;                 // bands of the camera sky model (0: none)
+    bool sky_has[5] = {false, false, false, false, false};  // sky radiance, disk, flux, Prague, emission
+    float sky_sun[3] = {0.f, 0.f, 1.f}, sky_cos = 0.f;
 };
 
 namespace {
@@ -202,9 +211,22 @@ TraceScene scene_of(hrt_context *ctx) {
 
 int max_blocks(hrt_context *ctx) { return ctx->sms * 8; }
 
-// Launch a trace kernel, bracketed by CUDA events when timing is on.
+// Launch a trace kernel, bracketed by CUDA events when timing is on.  With traversal counting
+// on (statistics launches, untimed), count the launch and the rays it traced instead:
+// meas[0] / meas[2] launches, meas[6] / meas[7] rays of direct / diffuse launches.
 template <class F>
 cudaError_t timed_launch(hrt_context *ctx, int kind, F &&launch) {
+    if (ctx->measure & 1) {
+        unsigned long long a = 0, b = 0;
+        cudaError_t e = cudaMemcpyAsync(&a, ctx->counter.p, sizeof a, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = launch();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&b, ctx->counter.p, sizeof b, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return e;
+        ctx->meas[kind == 0 ? 0 : 2] += 1.0;
+        ctx->meas[kind == 0 ? 6 : 7] += (double)(b - a);
+        return cudaSuccess;
+    }
     if (!(ctx->measure & 2)) return launch();
     hrt_context::Timed t{kind, nullptr, nullptr};
     cudaError_t e = cudaEventCreate(&t.a);
@@ -602,6 +624,85 @@ int diffuse_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp
     return HRT_OK;
 }
 
+// Camera parameters of a launch over the context's current radiation_out and sources.
+int camera_params(hrt_context *ctx, const hrt_camera *c, int Bl, CameraParams *P) {
+    if (!c) return fail(ctx, HRT_EINVAL, "null camera");
+    const int W = c->resolution[0], H = c->resolution[1];
+    const int tw = c->tile_resolution[0] > 0 ? c->tile_resolution[0] : W;
+    const int th = c->tile_resolution[1] > 0 ? c->tile_resolution[1] : H;
+    if (W <= 0 || H <= 0 || c->antialiasing < 1 || !(c->fov_aspect > 0.f) || !(c->viewplane_length > 0.f))
+        return fail(ctx, HRT_EINVAL, "camera needs a resolution, >= 1 antialiasing sample, a field of view and an aspect ratio");
+    if (c->tile_offset[0] < 0 || c->tile_offset[1] < 0 || c->tile_offset[0] + tw > W || c->tile_offset[1] + th > H)
+        return fail(ctx, HRT_EINVAL, "camera tile lies outside the image");
+    if ((long long)W * H > 0x7FFFFFFFLL || (long long)tw * th * c->antialiasing > 0xFFFFFFFFLL)
+        return fail(ctx, HRT_EUNSUPPORTED, "camera image or tile too large for one launch");
+    if (Bl <= 0 || Bl > 16) return fail(ctx, HRT_EINVAL, "a camera launch needs 1 to 16 bands in the radiation buffers");
+    if (ctx->S > 0 && ctx->src_flux_count < (size_t)ctx->S * Bl)
+        return fail(ctx, HRT_EINVAL, "source fluxes not uploaded for every source and launched band");
+    CameraParams &q = *P;
+    q = CameraParams{};
+    q.sc = scene_of(ctx);
+    for (int i = 0; i < 3; ++i) q.pos[i] = c->position[i];
+    camera_rotation(c->direction[0], c->direction[1], q.M);
+    q.focal = c->focal_length;
+    q.lens = c->lens_diameter;
+    q.inv_aspect = 1.0f / c->fov_aspect;
+    q.viewplane = c->viewplane_length;
+    q.W = W;
+    q.H = H;
+    q.ox = c->tile_offset[0];
+    q.oy = c->tile_offset[1];
+    q.tw = tw;
+    q.th = th;
+    q.aa = c->antialiasing;
+    q.seed = c->seed;
+    q.cam_id = c->camera_id;
+    q.Bl = Bl;
+    q.S = ctx->S;
+    q.src = ctx->src.as<SourceDev>();
+    q.src_flux = ctx->src_flux.as<float>();
+    q.otop = ctx->otop.as<float>();
+    q.obot = ctx->obot.as<float>();
+    q.sky = SkyParams{};
+    if (ctx->sky_B == Bl) {
+        const size_t B = (size_t)Bl;
+        float *d = ctx->cam_sky.as<float>();
+        q.sky_rad = ctx->sky_has[0] ? d : nullptr;
+        q.disk_rad = ctx->sky_has[1] ? d + B : nullptr;
+        q.dflux = ctx->sky_has[2] ? d + 2 * B : nullptr;
+        q.sky.prague = ctx->sky_has[3] ? d + 3 * B : nullptr;
+        q.sky.peak = d + 7 * B;
+        q.emission = ctx->sky_has[4] ? ctx->cam_em.as<uint32_t>() : nullptr;
+        for (int i = 0; i < 3; ++i) q.sun[i] = ctx->sky_sun[i];
+        q.disk_cos = ctx->sky_cos;
+    }
+    q.pix = ctx->cam_pix.as<double>();
+    q.labels = ctx->cam_lab.as<uint32_t>();
+    q.depths = ctx->cam_dep.as<float>();
+    return HRT_OK;
+}
+
+int ensure_camera_image(hrt_context *ctx, int W, int H, int Bl) {
+    const size_t npx = (size_t)W * H;
+    CU(ctx->cam_pix.ensure(ctx->stream, npx * Bl * sizeof(double)));
+    CU(cudaMemsetAsync(ctx->cam_pix.p, 0, npx * Bl * sizeof(double), ctx->stream));
+    ctx->cam_W = W;
+    ctx->cam_H = H;
+    ctx->cam_B = Bl;
+    return HRT_OK;
+}
+
+int ensure_camera_labels(hrt_context *ctx, int W, int H) {
+    const size_t npx = (size_t)W * H;
+    CU(ctx->cam_lab.ensure(ctx->stream, npx * sizeof(uint32_t)));
+    CU(ctx->cam_dep.ensure(ctx->stream, npx * sizeof(float)));
+    CU(cudaMemsetAsync(ctx->cam_lab.p, 0, npx * sizeof(uint32_t), ctx->stream));
+    CU(cudaMemsetAsync(ctx->cam_dep.p, 0, npx * sizeof(float), ctx->stream));
+    ctx->lab_W = W;
+    ctx->lab_H = H;
+    return HRT_OK;
+}
+
 int count_flags(int Bg, const uint8_t *f) {
     int c = 0;
     for (int b = 0; b < Bg; ++b) c += f[b] ? 1 : 0;
@@ -924,6 +1025,7 @@ int hrt_zero_radiation_buffers(hrt_context *ctx, size_t launch_band_count) {
     CU(cudaMemsetAsync(ctx->otop.p, 0, m * sizeof(float), ctx->stream));
     CU(cudaMemsetAsync(ctx->obot.p, 0, m * sizeof(float), ctx->stream));
     ctx->Bl = (int)launch_band_count;
+    ctx->cam_id_cur = 0xFFFFFFFFu;  // the next camera launch starts a fresh image
     CU(cudaStreamSynchronize(ctx->stream));
     return HRT_OK;
 }
@@ -976,6 +1078,106 @@ int hrt_get_results(hrt_context *ctx, float *radiation_in, float *out_top, float
     if ((r = dl_double(ctx->sbot, scatter_bottom))) return r;
     if (out_top) CU(cudaMemcpyAsync(out_top, ctx->otop.p, m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     if (out_bottom) CU(cudaMemcpyAsync(out_bottom, ctx->obot.p, m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_update_sky_model(hrt_context *ctx, int32_t nbands, const hrt_sky_model *m) {
+    if (!ctx || nbands < 0) return HRT_EINVAL;
+    CU(cudaSetDevice(ctx->device));
+    if (!m || nbands == 0) {
+        ctx->sky_B = 0;
+        return HRT_OK;
+    }
+    const size_t B = (size_t)nbands;
+    std::vector<float> h(10 * B, 0.f);
+    const float *arr[3] = {m->camera_sky_radiance, m->solar_disk_radiance, m->camera_diffuse_flux};
+    for (int k = 0; k < 3; ++k) {
+        ctx->sky_has[k] = arr[k] != nullptr;
+        if (arr[k]) std::copy(arr[k], arr[k] + B, h.begin() + k * B);
+    }
+    ctx->sky_has[3] = m->sky_radiance_params != nullptr;
+    if (m->sky_radiance_params) std::copy(m->sky_radiance_params, m->sky_radiance_params + 4 * B, h.begin() + 3 * B);
+    for (size_t b = 0; b < B; ++b)
+        for (int i = 0; i < 3; ++i) h[7 * B + 3 * b + i] = m->sun_direction[i];
+    CU(ctx->cam_sky.ensure(ctx->stream, h.size() * sizeof(float)));
+    CU(cudaMemcpyAsync(ctx->cam_sky.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->sky_has[4] = m->band_emission_flag != nullptr;
+    if (m->band_emission_flag) {
+        CU(ctx->cam_em.ensure(ctx->stream, B * sizeof(uint32_t)));
+        CU(cudaMemcpyAsync(ctx->cam_em.p, m->band_emission_flag, B * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                           ctx->stream));
+    }
+    for (int i = 0; i < 3; ++i) ctx->sky_sun[i] = m->sun_direction[i];
+    ctx->sky_cos = m->solar_disk_cos_angle;
+    ctx->sky_B = nbands;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_launch_camera(hrt_context *ctx, const hrt_camera *cam) {
+    if (!ctx || !cam) return HRT_EINVAL;
+    int r = check_built(ctx);
+    if (r) return r;
+    CU(cudaSetDevice(ctx->device));
+    CameraParams P;
+    if ((r = camera_params(ctx, cam, ctx->Bl, &P))) return r;
+    if (cam->camera_id != ctx->cam_id_cur || ctx->Bl != ctx->cam_B || P.W != ctx->cam_W || P.H != ctx->cam_H) {
+        if ((r = ensure_camera_image(ctx, P.W, P.H, ctx->Bl))) return r;
+        ctx->cam_id_cur = cam->camera_id;
+        P.pix = ctx->cam_pix.as<double>();
+    }
+    CU(cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), ctx->stream));
+    CU(launch_camera(P, max_blocks(ctx), ctx->stream));
+    return sync_and_status(ctx);
+}
+
+int hrt_zero_camera_pixel_buffers(hrt_context *ctx, int32_t width, int32_t height) {
+    if (!ctx || width < 0 || height < 0) return HRT_EINVAL;
+    if ((size_t)width * height == 0) return HRT_OK;
+    CU(cudaSetDevice(ctx->device));
+    int r = ensure_camera_labels(ctx, width, height);
+    if (r) return r;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_launch_pixel_labels(hrt_context *ctx, const hrt_camera *cam) {
+    if (!ctx || !cam) return HRT_EINVAL;
+    int r = check_built(ctx);
+    if (r) return r;
+    CU(cudaSetDevice(ctx->device));
+    CameraParams P;
+    if ((r = camera_params(ctx, cam, std::max(ctx->Bl, 1), &P))) return r;
+    if (P.W != ctx->lab_W || P.H != ctx->lab_H) {
+        if ((r = ensure_camera_labels(ctx, P.W, P.H))) return r;
+        P.labels = ctx->cam_lab.as<uint32_t>();
+        P.depths = ctx->cam_dep.as<float>();
+    }
+    CU(launch_pixel_labels(P, ctx->stream));
+    return sync_and_status(ctx);
+}
+
+int hrt_get_camera_results(hrt_context *ctx, float *pixels, uint32_t *labels, float *depths, int32_t width,
+                           int32_t height) {
+    if (!ctx || width < 0 || height < 0) return HRT_EINVAL;
+    CU(cudaSetDevice(ctx->device));
+    const size_t npx = (size_t)width * height;
+    if (npx == 0) return HRT_OK;
+    if (pixels) {
+        if (ctx->cam_W != width || ctx->cam_H != height)
+            return fail(ctx, HRT_EINVAL, "no camera image of this resolution; call hrt_launch_camera() first");
+        const size_t m = npx * ctx->cam_B;
+        CU(ctx->io_a.ensure(ctx->stream, m * sizeof(float)));
+        CU(launch_to_float(ctx->cam_pix.as<double>(), ctx->io_a.as<float>(), m, ctx->stream));
+        CU(cudaMemcpyAsync(pixels, ctx->io_a.p, m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if (labels || depths) {
+        if (ctx->lab_W != width || ctx->lab_H != height)
+            return fail(ctx, HRT_EINVAL, "no pixel labels of this resolution; call hrt_launch_pixel_labels() first");
+        if (labels) CU(cudaMemcpyAsync(labels, ctx->cam_lab.p, npx * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        if (depths) CU(cudaMemcpyAsync(depths, ctx->cam_dep.p, npx * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    }
     CU(cudaStreamSynchronize(ctx->stream));
     return HRT_OK;
 }
@@ -1094,6 +1296,23 @@ int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
     CU(cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), st));
     std::vector<uint8_t> flags(s->band_launch, s->band_launch + Bg);
     if ((r = upload_flags(ctx, Bg, flags.data()))) return r;
+    // Camera view of the primitives: the scatter of every pass plus emission, accumulated
+    // (RadiationModel.cpp:3992-4012, 4105-4131, 4211-4220, 4336-4345).
+    const bool cams = s->ncameras > 0 && s->cameras;
+    ctx->cam_id_cur = 0xFFFFFFFFu;
+    if (cams) {
+        CU(ctx->ctop.ensure(st, m * sizeof(double)));
+        CU(ctx->cbot.ensure(st, m * sizeof(double)));
+        CU(cudaMemsetAsync(ctx->ctop.p, 0, m * sizeof(double), st));
+        CU(cudaMemsetAsync(ctx->cbot.p, 0, m * sizeof(double), st));
+    }
+    auto cam_add_scatter = [&]() -> int {
+        if (!cams) return HRT_OK;
+        CU(launch_add(ctx->ctop.as<double>(), ctx->stop.as<double>(), m, st));
+        CU(launch_add(ctx->cbot.as<double>(), ctx->sbot.as<double>(), m, st));
+        ctx->last_kernels += 2;
+        return HRT_OK;
+    };
     if (emission) {
         // per-band flags and depths (small, every call); emissivity and temperature when given,
         // else the arrays resident from an earlier call are used
@@ -1120,6 +1339,7 @@ int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
     }
     // ---- scattered direct energy becomes the outgoing flux (one-sided prims fold top+bottom)
     if (scattering && rundirect) {
+        if ((r = cam_add_scatter())) return r;
         CU(launch_fold_onesided(n, Bl, ctx->twosided.as<int8_t>(), ctx->stop.as<double>(), ctx->sbot.as<double>(),
                                 ctx->ftop.as<double>(), ctx->fbot.as<double>(), st));
         CU(cudaMemsetAsync(ctx->stop.p, 0, m * sizeof(double), st));
@@ -1141,11 +1361,18 @@ int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
                                ctx->emis_eps.as<float>(), ctx->emis_T.as<float>(), ctx->twosided.as<int8_t>(),
                                ctx->ftop.as<double>(), ctx->fbot.as<double>(), st));
             ctx->last_kernels += 1;
+            if (cams) {
+                CU(launch_emission(n, Bl, ctx->emis.as<uint8_t>(), (const int32_t *)(ctx->emis.as<char>() + 64),
+                                   ctx->emis_eps.as<float>(), ctx->emis_T.as<float>(), ctx->twosided.as<int8_t>(),
+                                   ctx->ctop.as<double>(), ctx->cbot.as<double>(), st));
+                ctx->last_kernels += 1;
+            }
         }
         CU(launch_to_float(ctx->ftop.as<double>(), ctx->otop.as<float>(), m, st));
         CU(launch_to_float(ctx->fbot.as<double>(), ctx->obot.as<float>(), m, st));
         ctx->last_kernels += 2;
         if ((r = diffuse_pass(ctx, 0, (uint32_t)n, rpp_d, s->seed, 1u, 3, Bg, Bl, Bl, sky))) return r;
+        if ((r = cam_add_scatter())) return r;
     } else if (scattering && rundirect) {
         CU(launch_to_float(ctx->ftop.as<double>(), ctx->otop.as<float>(), m, st));
         CU(launch_to_float(ctx->fbot.as<double>(), ctx->obot.as<float>(), m, st));
@@ -1186,6 +1413,7 @@ int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
             CU(cudaMemsetAsync(ctx->sbot.p, 0, m * sizeof(double), st));
             int Bc = count_flags(Bg, sflags.data());
             if ((r = diffuse_pass(ctx, 0, (uint32_t)n, rpp_d, s->seed, 2u + (uint32_t)it, 3, Bg, Bc, Bl, sky0))) return r;
+            if ((r = cam_add_scatter())) return r;
             iters = it + 1;
             if (residual) {
                 // FP64 convergence check: a band stops once the power its last iteration
@@ -1212,6 +1440,43 @@ int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
     CU(launch_final_flux(m, ctx->rin.as<double>(), ctx->stop.as<double>(), ctx->sbot.as<double>(), ctx->fin.as<float>(), st));
     ctx->last_kernels += 1;
     if (flux_out) CU(cudaMemcpyAsync(flux_out, ctx->fin.p, m * sizeof(float), cudaMemcpyDeviceToHost, st));
+    // ---- cameras (RadiationModel.cpp:4358-4616), rendered from the accumulated camera view
+    if (cams) {
+        const bool render = scattering && (emission || diffuse || rundirect);
+        if (render) {
+            if ((r = hrt_update_sky_model(ctx, s->camera_sky ? Bl : 0, s->camera_sky))) return r;
+            CU(launch_to_float(ctx->ctop.as<double>(), ctx->otop.as<float>(), m, st));
+            CU(launch_to_float(ctx->cbot.as<double>(), ctx->obot.as<float>(), m, st));
+            ctx->last_kernels += 2;
+        }
+        for (int ci = 0; ci < s->ncameras; ++ci) {
+            hrt_camera c = s->cameras[ci];
+            c.tile_offset[0] = c.tile_offset[1] = 0;
+            c.tile_resolution[0] = c.tile_resolution[1] = 0;
+            CameraParams P;
+            if ((r = camera_params(ctx, &c, Bl, &P))) return r;
+            const size_t npx = (size_t)P.W * P.H;
+            if ((r = ensure_camera_image(ctx, P.W, P.H, Bl))) return r;
+            if ((r = ensure_camera_labels(ctx, P.W, P.H))) return r;
+            ctx->cam_id_cur = c.camera_id;
+            P.pix = ctx->cam_pix.as<double>();
+            P.labels = ctx->cam_lab.as<uint32_t>();
+            P.depths = ctx->cam_dep.as<float>();
+            if (render) {
+                CU(launch_camera(P, max_blocks(ctx), st));
+                CU(launch_pixel_labels(P, st));
+                ctx->last_kernels += 2;
+            }
+            if (c.pixels) {
+                CU(ctx->io_a.ensure(st, npx * Bl * sizeof(float)));
+                CU(launch_to_float(ctx->cam_pix.as<double>(), ctx->io_a.as<float>(), npx * Bl, st));
+                CU(cudaMemcpyAsync(c.pixels, ctx->io_a.p, npx * Bl * sizeof(float), cudaMemcpyDeviceToHost, st));
+                CU(cudaStreamSynchronize(st));
+            }
+            if (c.labels) CU(cudaMemcpyAsync(c.labels, ctx->cam_lab.p, npx * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+            if (c.depths) CU(cudaMemcpyAsync(c.depths, ctx->cam_dep.p, npx * sizeof(float), cudaMemcpyDeviceToHost, st));
+        }
+    }
     unsigned long long rays = 0;
     CU(cudaMemcpyAsync(&rays, ctx->counter.p, sizeof(rays), cudaMemcpyDeviceToHost, st));
     r = sync_and_status(ctx);

@@ -85,6 +85,34 @@ struct DiffuseParams {
     GlassParams gl;            // launches with covers (sc.cover non-null)
 };
 
+// ---------------------------------------------------------------- cameras
+struct CameraParams {
+    TraceScene sc;
+    float pos[3];
+    float M[9];                // camera-to-world rotation, row-major; column 0 is the view axis
+    float focal, lens, inv_aspect, viewplane;
+    int W, H;                  // full image
+    int ox, oy, tw, th;        // this launch's tile: first pixel and size
+    int aa;                    // rays per pixel
+    uint32_t seed, cam_id;
+    int Bl, S;
+    const SourceDev *src;      // [S]
+    const float *src_flux;     // [S*Bl]
+    const float *otop, *obot;  // radiation_out [n*Bl]
+    SkyParams sky;             // camera sky: peak = sun direction per band, Prague parameters
+    const float *sky_rad, *disk_rad, *dflux;  // [Bl] each, or null
+    const uint32_t *emission;  // [Bl] or null
+    float sun[3], disk_cos;
+    double *pix;               // [W*H*Bl] accumulated radiance
+    uint32_t *labels;          // [W*H]
+    float *depths;             // [W*H]
+};
+cudaError_t launch_camera(const CameraParams &p, int max_blocks, cudaStream_t s);
+cudaError_t launch_pixel_labels(const CameraParams &p, cudaStream_t s);
+cudaError_t launch_add(double *dst, const double *src, size_t n, cudaStream_t s);
+// Camera-to-world rotation for a view axis of the given zenith and azimuth (host, FP64 rounded to FP32).
+void camera_rotation(float zenith, float azimuth, float M[9]);
+
 // ---------------------------------------------------------------- BVH build
 struct BvhBuffers {
     float4 *rec;        // out: sorted records [n*4]

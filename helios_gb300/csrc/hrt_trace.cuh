@@ -147,12 +147,14 @@ __device__ __forceinline__ bool wall_closest(const TraceScene &sc, f3 o, f3 d, f
 }
 
 // Trace with periodic wrapping (<= 10 wraps; OptiX8DeviceCode.cu:763-789, 1440-1459).
+// o_last (optional): origin of the last segment traced.
 template <bool STATS>
 __device__ Hit trace_full(const TraceScene &sc, f3 o, f3 d, float tmin, float tmax, bool anyhit, VoxKey vk,
-                          uint32_t *nv, uint32_t *np) {
+                          uint32_t *nv, uint32_t *np, f3 *o_last = nullptr) {
     const uint32_t c2 = vk.c2;
     for (int wrap = 0; wrap < 10; ++wrap) {
         vk.c2 = c2 | ((uint32_t)wrap << 16);
+        if (o_last) *o_last = o;
         Hit h = trace_bvh<STATS>(sc, o, d, tmin, tmax, anyhit && sc.nbbox == 0, vk, nv, np);
         if (sc.nbbox == 0) return h;
         float tb;

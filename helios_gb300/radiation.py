@@ -288,6 +288,8 @@ class RadiationModel:
         self.temperature_default = 300.0
         self.scatter_tolerance = 0.0
         self.last_stats = {}
+        self.cameras: dict[str, dict] = {}
+        self.camera_sky_radiance: dict[str, float] = {}
 
     @property
     def ctx(self) -> "_hrt.Context":
@@ -321,6 +323,102 @@ class RadiationModel:
             raise HeliosRuntimeError(f"ERROR (RadiationModel::{fn}): Cannot {fn} for band '{label}' because it "
                                      "is not a valid band.")
         return self.bands[label]
+
+    # -------------------------------------------------------------- cameras
+    def addRadiationCamera(self, label, band_labels, position, lookat, properties=None, antialiasing_samples=1):
+        """A radiation camera (RadiationCamera.cpp:30-88).  properties: dict with the
+        CameraProperties fields this solve uses -- camera_resolution (512, 512),
+        focal_plane_distance 1, lens_diameter 0.05, HFOV 20 degrees, camera_zoom 1.  Pixel data
+        is radiance (the reference's "manual" exposure); exposure and white balance are not
+        applied."""
+        p = {"camera_resolution": (512, 512), "focal_plane_distance": 1.0, "lens_diameter": 0.05, "HFOV": 20.0,
+             "camera_zoom": 1.0}
+        p.update(properties or {})
+        W, H = int(p["camera_resolution"][0]), int(p["camera_resolution"][1])
+        if int(antialiasing_samples) == 0:
+            raise HeliosRuntimeError("ERROR (RadiationModel::addRadiationCamera): The model requires at least 1 "
+                                     "antialiasing sample to run.")
+        if W <= 0 or H <= 0:
+            raise HeliosRuntimeError("ERROR (RadiationModel::addRadiationCamera): Camera resolution must be at "
+                                     "least 1x1.")
+        if p["HFOV"] < 0 or p["HFOV"] > 180.0:
+            raise HeliosRuntimeError("ERROR (RadiationModel::addRadiationCamera): Camera horizontal field of view "
+                                     "must be between 0 and 180 degrees.")
+        self.cameras[label] = {"bands": list(band_labels), "position": tuple(map(float, position)),
+                               "lookat": tuple(map(float, lookat)), "props": p, "aa": int(antialiasing_samples),
+                               "pixels": {}, "labels": None, "depths": None}
+
+    def setCameraSkyRadiance(self, band, radiance):
+        """Sky radiance cameras see on a miss that meets no source, for one band.  The reference
+        computes it with its atmospheric sky model (RadiationModel.cpp:2928-3050), which runs only
+        when atmospheric global data are set; this sets its output directly (default 0)."""
+        self.camera_sky_radiance[band] = float(radiance)
+
+    @staticmethod
+    def _view_direction(position, lookat):
+        """(zenith, azimuth) of lookat - position as cart2sphere gives them (global.cpp:818-831)."""
+        d = np.asarray(lookat, np.float32) - np.asarray(position, np.float32)
+        r = np.float32(math.sqrt(float(d[0]) ** 2 + float(d[1]) ** 2 + float(d[2]) ** 2))
+        x, y = float(d[0]), float(d[1])
+        if abs(x) < 1e-7 and abs(y) < 1e-7:
+            y = 1e-7
+        elev = math.asin(max(-1.0, min(1.0, float(d[2]) / float(r))))
+        az = math.atan2(x, y)
+        if az < 0:
+            az += 2.0 * math.pi
+        return 0.5 * math.pi - elev, az
+
+    def _camera_dicts(self, band_labels, seed):
+        """Cameras whose bands meet this dispatch (RadiationModel.cpp:4431-4448), in label order."""
+        out, labels = [], []
+        for cid, (label, cam) in enumerate(sorted(self.cameras.items())):
+            if not any(b in band_labels for b in cam["bands"]):
+                continue
+            p = cam["props"]
+            W, H = int(p["camera_resolution"][0]), int(p["camera_resolution"][1])
+            hfov = float(p["HFOV"]) / float(p["camera_zoom"])
+            zen, az = self._view_direction(cam["position"], cam["lookat"])
+            out.append({"position": cam["position"], "direction": (zen, az),
+                        "focal_length": float(p["focal_plane_distance"]), "lens_diameter": float(p["lens_diameter"]),
+                        "fov_aspect": float(np.float32(W) / np.float32(H)),
+                        "viewplane_length": float(0.5 / math.tan(0.5 * hfov * math.pi / 180.0)),
+                        "resolution": (W, H), "antialiasing": cam["aa"], "seed": seed, "camera_id": cid})
+            labels.append(label)
+        return out, labels
+
+    def _camera_sky_dict(self, band_labels):
+        """The camera sky of a dispatch (the updateSkyModel inputs, RadiationModel.cpp:4368-4428):
+        Prague parameters (none in this mirror), the sky radiance, the first collimated or
+        sun-sphere source as the solar disk (collimated: flux / 6.74e-5 sr; sun sphere: flux / pi;
+        cos 0.999989), and the sky flux of every band with its emission flag."""
+        sky = {"sky_radiance": np.array([self.camera_sky_radiance.get(b, 0.0) for b in band_labels], np.float32),
+               "prague": np.zeros((len(band_labels), 4), np.float32), "sun": (0.0, 0.0, 1.0), "disk_cos": 0.0,
+               "disk_radiance": np.zeros(len(band_labels), np.float32),
+               "diffuse_flux": np.array([self.getDiffuseFlux(b) for b in band_labels], np.float32),
+               "emission": np.array([1 if self.bands[b].emissionFlag else 0 for b in band_labels], np.uint32)}
+        for k, src in enumerate(self.sources):
+            if src["type"] in (0, 2):
+                v = np.asarray(src["position"], np.float32)
+                sky["sun"] = tuple(float(x) for x in v / np.float32(math.sqrt(float(np.dot(v, v)))))
+                fl = np.array([self.getSourceFlux(k, b) for b in band_labels], np.float32)
+                sky["disk_radiance"] = (fl / np.float32(math.pi) if src["type"] == 2 else fl / np.float32(6.74e-5))
+                sky["disk_cos"] = 0.999989
+                break
+        return sky
+
+    def getCameraPixelData(self, label, band):
+        if label not in self.cameras:
+            raise HeliosRuntimeError(f"ERROR (RadiationModel::getCameraPixelData): Camera '{label}' does not exist.")
+        if band not in self.cameras[label]["pixels"]:
+            raise HeliosRuntimeError(f"ERROR (RadiationModel::getCameraPixelData): Band '{band}' has no pixel data "
+                                     f"for camera '{label}'.")
+        return self.cameras[label]["pixels"][band]
+
+    def getCameraPixelLabels(self, label):
+        return self.cameras[label]["labels"]
+
+    def getCameraPixelDepths(self, label):
+        return self.cameras[label]["depths"]
 
     def disableEmission(self, label):
         self._band(label, "disableEmission").emissionFlag = False
@@ -560,6 +658,12 @@ class RadiationModel:
             "scatter_tolerance": self.scatter_tolerance,
             "n": n,
         }
+        if self.cameras:
+            cams, labels = self._camera_dicts(band_labels, desc["seed"])
+            if cams:
+                desc["cameras"] = cams
+                desc["camera_labels"] = labels
+                desc["camera_sky"] = self._camera_sky_dict(band_labels)
         if self._glass is not None:
             desc["is_glass"] = np.ascontiguousarray(np.broadcast_to(self._glass[0], (S, n, len(all_bands))))
             desc["glass_n"] = np.ascontiguousarray(np.broadcast_to(self._glass[1], (S, n, len(all_bands))))
@@ -587,9 +691,26 @@ class RadiationModel:
         uu = np.arange(n)
         for i, b in enumerate(desc["band_labels"]):
             self.context.setPrimitiveData(uu, "radiation_flux_" + b, flux[:, i].astype(np.float64))
+        self._store_cameras(desc, self.ctx.last_cameras if desc.get("cameras") else [])
         if self.auto_seed:
             self.seed = (self.seed + 0x9E3779B9) & 0xFFFFFFFF
         return flux
+
+    def _store_cameras(self, desc, outs):
+        """Pixel data, labels and depths of the rendered cameras as the reference stores them
+        (global data camera_<label>_<band>, _pixel_UUID, _pixel_depth; RadiationModel.cpp:4527-4605).
+        Labels are primitive UUID + 1 (0 = sky)."""
+        for label, out in zip(desc.get("camera_labels", []), outs):
+            cam = self.cameras[label]
+            H, W = out["labels"].shape
+            for i, b in enumerate(desc["band_labels"]):
+                px = out["pixels"][:, :, i].reshape(-1).astype(np.float32)
+                cam["pixels"][b] = px
+                self.context.setGlobalData(f"camera_{label}_{b}", px)
+            cam["labels"] = out["labels"].reshape(-1).copy()
+            cam["depths"] = out["depths"].reshape(-1).copy()
+            self.context.setGlobalData(f"camera_{label}_pixel_UUID", cam["labels"])
+            self.context.setGlobalData(f"camera_{label}_pixel_depth", cam["depths"])
 
     def getTotalAbsorbedFlux(self):
         """Per-primitive sum over bands of radiation_flux_<band> times area (RadiationModel.cpp:4686-4708)."""
@@ -620,6 +741,15 @@ def run_band_through_backend(ctx: "_hrt.Context", d: dict, twosided: np.ndarray)
     dirN, difN, depth = int(d["direct_rays"].max()), int(d["diffuse_rays"].max()), int(d["depth"].max())
     seed = d["seed"]
     ctx.zero_radiation_buffers(Bl)
+    cams = d.get("cameras") or []
+    # camera view of the primitives, accumulated on the host as RadiationModel::runBand does
+    ctop = np.zeros((n, Bl)) if cams else None
+    cbot = np.zeros((n, Bl)) if cams else None
+
+    def cam_add(res):
+        if cams:
+            ctop[...] += res["scatter_buff_top"].reshape(n, Bl)
+            cbot[...] += res["scatter_buff_bottom"].reshape(n, Bl)
     rundirect = bool((d["source_flux"] > 0).any())
     ctx.upload_source_fluxes(d["source_flux"])
     common = dict(launch_offset=0, launch_count=n, random_seed=seed, nbands_global=Bg, nbands_launch=Bl)
@@ -629,6 +759,7 @@ def run_band_through_backend(ctx: "_hrt.Context", d: dict, twosided: np.ndarray)
     fbot = np.zeros((n, Bl), np.float32)
     if scattering and rundirect:
         res = ctx.get_results(Bl)
+        cam_add(res)
         ftop = res["scatter_buff_top"].reshape(n, Bl).copy()
         fbot = res["scatter_buff_bottom"].reshape(n, Bl).copy()
         one = twosided == 0
@@ -652,10 +783,15 @@ def run_band_through_backend(ctx: "_hrt.Context", d: dict, twosided: np.ndarray)
                 out = ((SIGMA_F32 * e).astype(np.float64) * (T * T * T * T)).astype(np.float32)
                 ftop[:, b] += out
                 fbot[twosided != 0, b] += out[twosided != 0]
+                if cams:
+                    ctop[:, b] += out
+                    cbot[twosided != 0, b] += out[twosided != 0]
         for face in (1, 0):
             ctx.launch_diffuse(rays_per_primitive=rpp, pass_id=1, band_launch_flag=flags, launch_face=face,
                                diffuse_flux=d["diffuse_flux"], radiation_out_top=ftop, radiation_out_bottom=fbot,
                                **sky, **common)
+        if cams:
+            cam_add(ctx.get_results(Bl))
     if scattering and (emission or diffuse) and not rundirect:
         ctx.copy_scatter_to_radiation()
         ctx.zero_scatter_buffers()
@@ -678,8 +814,28 @@ def run_band_through_backend(ctx: "_hrt.Context", d: dict, twosided: np.ndarray)
                 ctx.launch_diffuse(rays_per_primitive=rpp, pass_id=2 + it, band_launch_flag=sflags, launch_face=face,
                                    diffuse_flux=zero, radiation_out_top=res["radiation_out_top"],
                                    radiation_out_bottom=res["radiation_out_bottom"], **sky, **common)
+            if cams:
+                cam_add(ctx.get_results(Bl))
     res = ctx.get_results(Bl)
     flux = (res["radiation_in"] + res["scatter_buff_top"] + res["scatter_buff_bottom"]).reshape(n, Bl)
+    # cameras (RadiationModel.cpp:4358-4616): launchCameraRays / launchPixelLabelRays per camera
+    ctx.last_cameras = []
+    if cams:
+        render = scattering and (emission or diffuse or rundirect)
+        if render:
+            ctx.upload_radiation_out(ctop.astype(np.float32), cbot.astype(np.float32))
+            ctx.update_sky_model(Bl, d.get("camera_sky"))
+        for cam in cams:
+            W, H = cam["resolution"]
+            out = {"pixels": np.zeros((H, W, Bl), np.float32), "labels": np.zeros((H, W), np.uint32),
+                   "depths": np.zeros((H, W), np.float32)}
+            if render:
+                ctx.launch_camera(cam)
+                out["pixels"] = ctx.get_camera_results(W, H, Bl, labels=False)[0]
+                ctx.zero_camera_pixel_buffers(W, H)
+                ctx.launch_pixel_labels(cam)
+                _, out["labels"], out["depths"] = ctx.get_camera_results(W, H, Bl, pixels=False)
+            ctx.last_cameras.append(out)
     return flux
 
 

@@ -106,6 +106,40 @@ typedef struct {
 /* One whole RadiationModel::runBand() (RadiationModel.cpp:3470-4663) executed on
  * the device: direct pass, emission source term, primary diffuse pass and the
  * scattering iterations, with every intermediate buffer kept in HBM. */
+/* Camera of a launch (the camera fields of RayTracingLaunchParams, RayTracingTypes.h:220-234).
+ * A camera ray of pixel (ii, jj) leaves a point of the lens toward the focal plane through
+ * the pixel's sub-pixel sample (OptiX8DeviceCode.cu:1665-1738); pixel (0, 0) is the top left.
+ * The outputs are read by hrt_run_band only (the granular calls use hrt_get_camera_results). */
+typedef struct {
+    float position[3];            /* camera_position */
+    float direction[2];           /* camera_direction: zenith and azimuth (radians) of lookat - position */
+    float focal_length;           /* camera_focal_length: distance to the focal plane */
+    float lens_diameter;          /* camera_lens_diameter; 0 = pinhole */
+    float fov_aspect;             /* camera_fov_aspect = HFOV / VFOV */
+    float viewplane_length;       /* camera_viewplane_length = 0.5 / tan(HFOV / 2) */
+    int32_t resolution[2];        /* camera_resolution_full: width, height */
+    int32_t tile_offset[2];       /* camera_pixel_offset: first pixel of this launch */
+    int32_t tile_resolution[2];   /* camera_resolution: pixels of this launch; 0 = the whole image */
+    int32_t antialiasing;         /* antialiasing_samples: rays per pixel */
+    uint32_t seed;                /* random_seed */
+    uint32_t camera_id;           /* camera_id */
+    float *pixels;                /* out [height*width*Bl] radiance, pixel-major, or NULL */
+    uint32_t *labels;             /* out [height*width] hit primitive + 1 (0 = sky), or NULL */
+    float *depths;                /* out [height*width] depth along the view axis (-1 = sky), or NULL */
+} hrt_camera;
+
+/* What cameras see where their rays leave the scene (RayTracingBackend::updateSkyModel,
+ * RayTracingBackend.h:129): per launched band.  Any array may be NULL (nothing seen). */
+typedef struct {
+    const float *sky_radiance_params;   /* [Bl*4] Prague parameters of the camera sky */
+    const float *camera_sky_radiance;   /* [Bl] sky radiance on a miss that sees no source */
+    float sun_direction[3];             /* unit vector toward the sun */
+    const float *solar_disk_radiance;   /* [Bl] radiance of the solar disk (collimated / sun-sphere sources) */
+    float solar_disk_cos_angle;         /* a miss within this cosine of the sun sees the disk */
+    const float *camera_diffuse_flux;   /* [Bl] sky flux of emission bands, seen as isotropic radiance */
+    const uint32_t *band_emission_flag; /* [Bl] */
+} hrt_sky_model;
+
 typedef struct {
     int32_t nbands_global;
     const uint8_t *band_launch;         /* [nbands_global] bands run by this call */
@@ -131,6 +165,13 @@ typedef struct {
      * scatter_tolerance times its total (absorbed + that); that power stays in the flux
      * as at the depth limit.  0 runs the reference's fixed iteration count. */
     double scatter_tolerance;
+    /* Cameras rendered after the solve (RadiationModel.cpp:4358-4616): each sees every
+     * primitive's scattered and emitted radiation accumulated over all passes.  Rendered only
+     * when scattering is enabled and something radiates, as in the reference; else the pixels
+     * are zero.  camera_sky NULL: the cameras see nothing where their rays leave the scene. */
+    int32_t ncameras;
+    const hrt_camera *cameras;
+    const hrt_sky_model *camera_sky;
 } hrt_band_solve;
 
 /* ---- lifecycle: RayTracingBackend::initialize / shutdown (RayTracingBackend.h:54,61) */
@@ -167,6 +208,22 @@ int hrt_upload_source_fluxes(hrt_context *ctx, const float *fluxes, size_t count
 int hrt_launch_direct(hrt_context *ctx, const hrt_launch *p);
 /* ---- RayTracingBackend::launchDiffuseRays (RayTracingBackend.h:146) */
 int hrt_launch_diffuse(hrt_context *ctx, const hrt_launch *p);
+/* ---- RayTracingBackend::updateSkyModel (RayTracingBackend.h:129) */
+int hrt_update_sky_model(hrt_context *ctx, int32_t nbands, const hrt_sky_model *m);
+/* ---- RayTracingBackend::launchCameraRays (RayTracingBackend.h:153): adds the radiance of every
+ * pixel of the launch's tile, as seen through radiation_out and the sources, to the camera buffer.
+ * The buffer is zeroed when the camera id or band count differs from the previous launch, or after
+ * hrt_zero_radiation_buffers (the OptiX8Backend rule, OptiX8Backend.cpp:1023-1037). */
+int hrt_launch_camera(hrt_context *ctx, const hrt_camera *cam);
+/* ---- RayTracingBackend::launchPixelLabelRays (RayTracingBackend.h:160): one ray through each
+ * pixel centre of the tile; label = hit primitive + 1, depth along the view axis, -1 on a miss. */
+int hrt_launch_pixel_labels(hrt_context *ctx, const hrt_camera *cam);
+/* ---- RayTracingBackend::zeroCameraPixelBuffers (RayTracingBackend.h:210) */
+int hrt_zero_camera_pixel_buffers(hrt_context *ctx, int32_t width, int32_t height);
+/* ---- RayTracingBackend::getCameraResults (RayTracingBackend.h:182): pixels [height*width*Bl]
+ * (pixel-major), labels and depths [height*width]; any pointer may be NULL. */
+int hrt_get_camera_results(hrt_context *ctx, float *pixels, uint32_t *labels, float *depths, int32_t width,
+                           int32_t height);
 /* ---- RayTracingBackend::getRadiationResults (RayTracingBackend.h:171): any pointer may be NULL */
 int hrt_get_results(hrt_context *ctx, float *radiation_in, float *radiation_out_top, float *radiation_out_bottom,
                     float *scatter_top, float *scatter_bottom);
@@ -286,7 +343,8 @@ int hrt_get_bvh(hrt_context *ctx, uint64_t *codes, uint32_t *perm, uint32_t *nod
  * also set, of the binary tree); bit 1: time every trace-kernel launch with CUDA
  * events on the context's stream.  Setting flags also resets the accumulators.
  * hrt_get_measure: [0] direct launches, [1] direct ms, [2] diffuse launches,
- * [3] diffuse ms, [4] node visits, [5] primitive tests. */
+ * [3] diffuse ms, [4] node visits, [5] primitive tests, [6] rays of direct launches,
+ * [7] rays of diffuse launches ([6] and [7] with bit 0, which syncs after every launch). */
 int hrt_set_measure(hrt_context *ctx, int flags);
 int hrt_get_measure(hrt_context *ctx, double *out, int count);
 /* ---- BVH build that allocates nothing (no counterpart in the reference).

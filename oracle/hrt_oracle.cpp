@@ -956,10 +956,11 @@ inline bool bbox_closest(const Scene &s, const Ray &ray, float tmax, float *t_ou
 }
 
 // Full trace with periodic wrapping (<= 10 wraps, OptiX8DeviceCode.cu:1440-1459, 763-789).
-Hit trace_full(const Scene &s, Ray ray, bool anyhit, TraceStats *st) {
+Hit trace_full(const Scene &s, Ray ray, bool anyhit, TraceStats *st, V3 *o_last = nullptr) {
     const uint32_t c2 = ray.key.c2;
     for (int wrap = 0; wrap < 10; ++wrap) {
         ray.key.c2 = c2 | ((uint32_t)wrap << 16);
+        if (o_last) *o_last = ray.o;
         Hit h = trace_bvh(s, ray, anyhit && s.nbbox == 0, st);
         if (s.nbbox == 0) return h;
         float tb;
@@ -1260,6 +1261,161 @@ inline double sky_fd(V3 dir, V3 peak, float K, float knorm, const float *prague)
     return 1.0;
 }
 
+// ---------------------------------------------------------------- cameras ---
+// Camera and pixel-label rays (OptiX8DeviceCode.cu:1665-1812 generation, :673-741 miss,
+// :1007-1170 closest hit, :743-748 and :1176-1199 pixel labels).  A camera ray of pixel
+// (ii, jj), sample s, draws its sub-pixel offset and lens point from Philox counter
+// (pixel, s, kCamCounter, 0) keyed by (seed, camera id), so images do not depend on tiling.
+constexpr uint32_t kCamCounter = 0xCA3E0001u;
+constexpr float kPiF = 3.14159265358979323846f;
+
+struct Cam {
+    V3 pos;
+    float M[9];  // camera-to-world rotation, row-major; column 0 is the view axis
+    float focal, lens, inv_aspect, L;
+    int W, H, aa;
+    uint32_t seed, id;
+};
+
+// Rotation of camera space (x = view axis) to the world for a view direction of the given
+// zenith and azimuth: about y by zenith - pi/2, then about z by pi/2 - azimuth (the
+// reference's d_rotatePoint), evaluated in FP64 and rounded to FP32.
+inline void camera_rotation(float zenith, float azimuth, float M[9]) {
+    const double th = -0.5 * M_PI + (double)zenith, ph = 0.5 * M_PI - (double)azimuth;
+    const double st = std::sin(th), ct = std::cos(th), sp = std::sin(ph), cp = std::cos(ph);
+    const double m[9] = {cp * ct, -sp, cp * st, sp * ct, cp, sp * st, -st, 0.0, ct};
+    for (int i = 0; i < 9; ++i) M[i] = (float)m[i];
+}
+
+inline V3 mrot(const float M[9], V3 v) {
+    return v3((M[0] * v.x + M[1] * v.y) + M[2] * v.z, (M[3] * v.x + M[4] * v.y) + M[5] * v.z,
+              (M[6] * v.x + M[7] * v.y) + M[8] * v.z);
+}
+
+// Ray of pixel (ii, jj), sample s; centre: the pixel centre through the lens centre (labels).
+inline void camera_ray(const Cam &c, uint32_t ii, uint32_t jj, uint32_t smp, bool centre, V3 *o, V3 *d) {
+    float rx = 0.5f, ry = 0.5f, lx = 0.f, ly = 0.f;
+    if (!centre) {
+        U4 u = philox(jj * (uint32_t)c.W + ii, smp, kCamCounter, 0u, c.seed, c.id);
+        rx = u01(u.v[0]);
+        ry = u01(u.v[1]);
+        if (c.lens > 0.f) concentric(u01(u.v[2]), u01(u.v[3]), &lx, &ly);
+    }
+    const float spy = -0.5f + ((float)ii + rx) / (float)c.W;
+    const float spz = (0.5f - ((float)jj + ry) / (float)c.H) * c.inv_aspect;
+    const V3 p = v3(c.focal, spy / c.L * c.focal, spz / c.L * c.focal);
+    const V3 org = v3(0.f, 0.5f * lx * c.lens, 0.5f * ly * c.lens);
+    *o = vadd(mrot(c.M, org), c.pos);
+    *d = vnormalize(mrot(c.M, vsub(p, org)));
+}
+
+// Radiance of a sphere, rectangle or disk source seen along (o, d) before distance tlim
+// (front faces only for rectangles and disks; OptiX8DeviceCode.cu:249-309, 1049-1126).
+inline float source_radiance(const Source &sr, float flux, V3 o, V3 d, float tlim) {
+    if (sr.type == 1) {
+        const float r = 0.5f * sr.w0;
+        const V3 oc = vsub(o, sr.pos);
+        const float b = vdot(oc, d), cc = vdot(oc, oc) - r * r, disc = b * b - cc;
+        if (disc < 0.f) return 0.f;
+        const float t = -b - std::sqrt(disc);
+        if (!(t > 0.f && t < tlim)) return 0.f;
+        return flux / (4.f * kPiF * r * r) / kPiF;
+    }
+    if (sr.type == 3 || sr.type == 4) {
+        const V3 n = v3(sr.R[2], sr.R[5], sr.R[8]);
+        const float den = vdot(d, n);
+        if (!(den < -1e-6f)) return 0.f;
+        const float t = vdot(vsub(sr.pos, o), n) / den;
+        if (!(t > 0.f && t < tlim)) return 0.f;
+        const V3 hp = vsub(vadd(o, vscale(d, t)), sr.pos);
+        float area;
+        if (sr.type == 3) {
+            const float lx = (sr.R[0] * hp.x + sr.R[3] * hp.y) + sr.R[6] * hp.z;
+            const float ly = (sr.R[1] * hp.x + sr.R[4] * hp.y) + sr.R[7] * hp.z;
+            if (std::fabs(lx) > 0.5f * sr.w0 || std::fabs(ly) > 0.5f * sr.w1) return 0.f;
+            area = sr.w0 * sr.w1;
+        } else {
+            if (vdot(hp, hp) > sr.w0 * sr.w0) return 0.f;
+            area = kPiF * sr.w0 * sr.w0;
+        }
+        return flux / area * (-den) / kPiF;
+    }
+    return 0.f;
+}
+
+// Camera view of the sky (RayTracingBackend::updateSkyModel): per launched band the sky
+// radiance and Prague parameters, the solar disk, and the isotropic sky flux of emission bands.
+struct CamSky {
+    const float *sky_radiance = nullptr, *disk_radiance = nullptr, *diffuse_flux = nullptr, *prague = nullptr;
+    const uint32_t *emission = nullptr;
+    V3 sun = {0.f, 0.f, 1.f};
+    float disk_cos = 0.f;
+};
+
+// Render one camera into pixels [W*H*Bl] (accumulated, FP64) and labels / depths [W*H].
+void render_camera(const Scene &s, const Cam &c, int Bl, const std::vector<Source> &src, const float *src_flux,
+                   const float *rtop, const float *rbot, const CamSky &sky, double *pix, uint32_t *labels,
+                   float *depths) {
+    const int S = (int)src.size();
+    const float strength = 1.0f / (float)c.aa;
+    const int np = c.W * c.H;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int q = 0; q < np; ++q) {
+        const uint32_t ii = (uint32_t)(q % c.W), jj = (uint32_t)(q / c.W);
+        for (int smp = 0; smp < c.aa; ++smp) {
+            V3 o, d, ol;
+            camera_ray(c, ii, jj, (uint32_t)smp, false, &o, &d);
+            Hit h = trace_full(s, Ray{o, d, 1e-5f, 1e30f, VoxKey{(uint32_t)q, (uint32_t)smp, 0x40000000u, c.seed, c.id}},
+                               false, nullptr, &ol);
+            if (h.prim == -2) continue;
+            for (int b = 0; b < Bl; ++b) {
+                if (h.prim >= 0) {
+                    const size_t ih = (size_t)h.prim * Bl + b;
+                    float val = strength * (h.face ? rtop[ih] : rbot[ih]);
+                    for (int k = 0; k < S; ++k) {
+                        const float fl = src_flux[k * Bl + b];
+                        if (!(fl > 0.f)) continue;
+                        const float r = source_radiance(src[k], fl, ol, d, h.t);
+                        if (r > 0.f) val += r * strength;
+                    }
+                    pix[(size_t)q * Bl + b] += (double)(val / kPiF);
+                } else {
+                    float rad = 0.f;
+                    for (int k = 0; k < S; ++k) {
+                        const float fl = src_flux[k * Bl + b];
+                        if (!(fl > 0.f)) continue;
+                        if (src[k].type == 0 || src[k].type == 2) {
+                            if (sky.disk_radiance && sky.disk_radiance[b] > 0.f && vdot(d, sky.sun) >= sky.disk_cos)
+                                rad += sky.disk_radiance[b];
+                        } else {
+                            rad += source_radiance(src[k], fl, ol, d, INFINITY);
+                        }
+                    }
+                    if (rad <= 0.f && sky.sky_radiance && sky.sky_radiance[b] > 0.f) {
+                        const float zero4[4] = {0.f, 0.f, 0.f, 0.f};
+                        rad = sky.sky_radiance[b] * (float)sky_fd(d, sky.sun, 0.f, 1.f, sky.prague ? sky.prague + 4 * b : zero4);
+                    }
+                    if (sky.emission && sky.emission[b] && sky.diffuse_flux && sky.diffuse_flux[b] > 0.f)
+                        rad += sky.diffuse_flux[b] / kPiF;
+                    if (rad > 0.f) pix[(size_t)q * Bl + b] += (double)(rad * strength);
+                }
+            }
+        }
+        // pixel label and depth: the pixel centre through the lens centre
+        V3 o, d, ol;
+        camera_ray(c, ii, jj, 0u, true, &o, &d);
+        Hit h = trace_full(s, Ray{o, d, 1e-5f, 1e30f, VoxKey{(uint32_t)q, 0xFFFFFFFFu, 0x40000000u, c.seed, c.id}},
+                           false, nullptr, &ol);
+        if (h.prim >= 0) {
+            labels[q] = (uint32_t)h.prim + 1u;
+            depths[q] = std::fabs(vdot(v3(c.M[0], c.M[3], c.M[6]), d)) * h.t;
+        } else if (h.prim == -1) {
+            labels[q] = 0u;
+            depths[q] = -1.f;
+        }
+    }
+}
+
 }  // namespace
 
 // ==================================================================== C API ===
@@ -1312,7 +1468,27 @@ typedef struct {
     const int8_t *is_glass;       // [glass_nsrc*n*Bg]
     const float *glass_n;         // [glass_nsrc*n*Bg] refractive index
     const float *glass_kl;        // [glass_nsrc*n*Bg] absorption product K*L
+    int32_t ncameras;             // cameras rendered after the solve (needs scattering enabled)
+    const struct orc_camera *cameras;
+    const float *cam_sky_radiance;  // [Bl] camera sky model, each may be null
+    const float *cam_disk_radiance; // [Bl]
+    const float *cam_diffuse_flux;  // [Bl]
+    const float *cam_prague;        // [Bl*4]
+    const uint32_t *cam_emission;   // [Bl]
+    float cam_sun[3];
+    float cam_disk_cos;
 } orc_solve;
+
+typedef struct orc_camera {
+    float position[3];
+    float direction[2];           // zenith, azimuth of the view axis (radians)
+    float focal_length, lens_diameter, fov_aspect, viewplane_length;
+    int32_t width, height, antialiasing;
+    uint32_t seed, camera_id;
+    float *pixels;                // out [W*H*Bl] radiance
+    uint32_t *labels;             // out [W*H] primitive index + 1 (0: sky)
+    float *depths;                // out [W*H] depth along the view axis (-1: sky)
+} orc_camera;
 
 void *orc_scene_create(const orc_geometry *g) {
     Scene *s = new Scene();
@@ -1747,7 +1923,23 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
     std::vector<uint8_t> flags(q->band_launch, q->band_launch + Bg);
     std::vector<float> dflux(q->diffuse_flux, q->diffuse_flux + Bl);
     std::vector<double> ftop((size_t)n * Bl, 0.0), fbot((size_t)n * Bl, 0.0);
+    // Camera view of the primitives: the scatter of every pass plus emission, accumulated
+    // (RadiationModel.cpp:3992-4012, 4105-4131, 4211-4220, 4336-4345).
+    const bool cams = q->ncameras > 0 && q->cameras;
+    std::vector<double> ctop, cbot;
+    if (cams) {
+        ctop.assign((size_t)n * Bl, 0.0);
+        cbot.assign((size_t)n * Bl, 0.0);
+    }
+    auto cam_add_scatter = [&]() {
+        if (!cams) return;
+        for (size_t i = 0; i < ctop.size(); ++i) {
+            ctop[i] += stop[i];
+            cbot[i] += sbot[i];
+        }
+    };
     if (scattering && rundirect) {
+        cam_add_scatter();
         ftop = stop;
         fbot = sbot;
         for (int p = 0; p < n; ++p) {
@@ -1777,6 +1969,10 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
                     size_t i = (size_t)p * Bl + b;
                     ftop[i] += out;
                     if (s->twosided[p] != 0) fbot[i] += out;
+                    if (cams) {
+                        ctop[i] += out;
+                        if (s->twosided[p] != 0) cbot[i] += out;
+                    }
                 }
             }
         }
@@ -1784,6 +1980,7 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
         obot = fbot;
         diffuse_pass(1, 1u, flags, dflux);
         diffuse_pass(0, 1u, flags, dflux);
+        cam_add_scatter();
     }
     if (scattering && (emission || diffuse) && !rundirect) {
         otop = stop;
@@ -1810,6 +2007,7 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
             std::fill(sbot.begin(), sbot.end(), 0.0);
             diffuse_pass(1, 2u + (uint32_t)it, sflags, dflux);
             diffuse_pass(0, 2u + (uint32_t)it, sflags, dflux);
+            cam_add_scatter();
             iters = it + 1;
             if (q->scatter_tol > 0.0) {
                 // Residual of band column c: area-weighted power scattered by this
@@ -1834,6 +2032,46 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
                 if (all) break;
             }
         }
+    }
+    // ---- cameras (RadiationModel.cpp:4358-4616): rendered from the accumulated camera view
+    for (int ci = 0; cams && ci < q->ncameras; ++ci) {
+        const orc_camera &oc = q->cameras[ci];
+        const size_t npx = (size_t)oc.width * oc.height;
+        std::vector<double> pix(npx * Bl, 0.0);
+        std::vector<uint32_t> lab(npx, 0u);
+        std::vector<float> dep(npx, 0.f);
+        if (scattering && (emission || diffuse || rundirect)) {
+            Cam c;
+            c.pos = v3(oc.position[0], oc.position[1], oc.position[2]);
+            camera_rotation(oc.direction[0], oc.direction[1], c.M);
+            c.focal = oc.focal_length;
+            c.lens = oc.lens_diameter;
+            c.inv_aspect = 1.0f / oc.fov_aspect;
+            c.L = oc.viewplane_length;
+            c.W = oc.width;
+            c.H = oc.height;
+            c.aa = std::max(oc.antialiasing, 1);
+            c.seed = oc.seed;
+            c.id = oc.camera_id;
+            std::vector<float> rt(ctop.size()), rb(cbot.size());
+            for (size_t i = 0; i < ctop.size(); ++i) {
+                rt[i] = (float)ctop[i];
+                rb[i] = (float)cbot[i];
+            }
+            CamSky sky;
+            sky.sky_radiance = q->cam_sky_radiance;
+            sky.disk_radiance = q->cam_disk_radiance;
+            sky.diffuse_flux = q->cam_diffuse_flux;
+            sky.prague = q->cam_prague;
+            sky.emission = q->cam_emission;
+            sky.sun = v3(q->cam_sun[0], q->cam_sun[1], q->cam_sun[2]);
+            sky.disk_cos = q->cam_disk_cos;
+            render_camera(*s, c, Bl, src, q->source_flux, rt.data(), rb.data(), sky, pix.data(), lab.data(), dep.data());
+        }
+        if (oc.pixels)
+            for (size_t i = 0; i < pix.size(); ++i) oc.pixels[i] = (float)pix[i];
+        if (oc.labels) std::copy(lab.begin(), lab.end(), oc.labels);
+        if (oc.depths) std::copy(dep.begin(), dep.end(), oc.depths);
     }
     for (size_t i = 0; i < (size_t)n * Bl; ++i) flux_out[i] = rin[i] + stop[i] + sbot[i];
     if (stats) {

@@ -81,6 +81,34 @@ class _Solve(C.Structure):
         ("is_glass", C.c_void_p),
         ("glass_n", C.c_void_p),
         ("glass_kl", C.c_void_p),
+        ("ncameras", C.c_int32),
+        ("cameras", C.c_void_p),
+        ("cam_sky_radiance", C.c_void_p),
+        ("cam_disk_radiance", C.c_void_p),
+        ("cam_diffuse_flux", C.c_void_p),
+        ("cam_prague", C.c_void_p),
+        ("cam_emission", C.c_void_p),
+        ("cam_sun", C.c_float * 3),
+        ("cam_disk_cos", C.c_float),
+    ]
+
+
+class _Camera(C.Structure):
+    _fields_ = [
+        ("position", C.c_float * 3),
+        ("direction", C.c_float * 2),
+        ("focal_length", C.c_float),
+        ("lens_diameter", C.c_float),
+        ("fov_aspect", C.c_float),
+        ("viewplane_length", C.c_float),
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("antialiasing", C.c_int32),
+        ("seed", C.c_uint32),
+        ("camera_id", C.c_uint32),
+        ("pixels", C.c_void_p),
+        ("labels", C.c_void_p),
+        ("depths", C.c_void_p),
     ]
 
 
@@ -226,11 +254,57 @@ class OracleScene:
             s.is_glass = _ptr(ig)
             s.glass_n = _ptr(arr("glass_n", np.float32))
             s.glass_kl = _ptr(arr("glass_kl", np.float32))
+        cams = solve.get("cameras") or []
+        cam_out = []
+        if cams:
+            arr = (_Camera * len(cams))()
+            for i, cam in enumerate(cams):
+                c = arr[i]
+                for k in range(3):
+                    c.position[k] = float(cam["position"][k])
+                c.direction[0], c.direction[1] = float(cam["direction"][0]), float(cam["direction"][1])
+                c.focal_length = float(cam["focal_length"])
+                c.lens_diameter = float(cam["lens_diameter"])
+                c.fov_aspect = float(cam["fov_aspect"])
+                c.viewplane_length = float(cam["viewplane_length"])
+                W, H = int(cam["resolution"][0]), int(cam["resolution"][1])
+                c.width, c.height = W, H
+                c.antialiasing = int(cam.get("antialiasing", 1))
+                c.seed = int(cam.get("seed", 0)) & 0xFFFFFFFF
+                c.camera_id = int(cam.get("camera_id", 0))
+                out = {"pixels": np.zeros((H, W, bl), np.float32), "labels": np.zeros((H, W), np.uint32),
+                       "depths": np.zeros((H, W), np.float32)}
+                c.pixels, c.labels, c.depths = _ptr(out["pixels"]), _ptr(out["labels"]), _ptr(out["depths"])
+                cam_out.append(out)
+            keep.append(arr)
+            s.ncameras = len(cams)
+            s.cameras = C.cast(arr, C.c_void_p)
+            sky = solve.get("camera_sky")
+            if sky is not None:
+                def sk(key, dtype):
+                    v = sky.get(key)
+                    if v is None:
+                        return None
+                    a = np.ascontiguousarray(v, dtype).ravel()
+                    keep.append(a)
+                    return _ptr(a)
+                s.cam_sky_radiance = sk("sky_radiance", np.float32)
+                s.cam_disk_radiance = sk("disk_radiance", np.float32)
+                s.cam_diffuse_flux = sk("diffuse_flux", np.float32)
+                s.cam_prague = sk("prague", np.float32)
+                s.cam_emission = sk("emission", np.uint32)
+                sun = sky.get("sun", (0.0, 0.0, 1.0))
+                for k in range(3):
+                    s.cam_sun[k] = float(sun[k])
+                s.cam_disk_cos = float(sky.get("disk_cos", 0.0))
         flux = np.zeros((self.n, bl), np.float64)
         stats = np.zeros(5, np.uint64)
         _load().orc_run_band(self._h, C.byref(s), _ptr(flux), _ptr(stats))
-        return flux, {"rays": int(stats[0]), "nodes": int(stats[1]), "prims": int(stats[2]),
-                      "hits": int(stats[3]), "iterations": int(stats[4])}
+        st = {"rays": int(stats[0]), "nodes": int(stats[1]), "prims": int(stats[2]),
+              "hits": int(stats[3]), "iterations": int(stats[4])}
+        if cams:
+            st["cameras"] = cam_out
+        return flux, st
 
 
 def philox(ctr, key):

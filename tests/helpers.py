@@ -23,7 +23,7 @@ def oracle_solve(desc: dict, rotation=rotation_np) -> dict:
                               "diffuse_norm", "diffuse_peak", "prague", "direct_rays", "diffuse_rays", "depth",
                               "emission", "eps", "temperature", "seed")}
     d["scatter_tolerance"] = desc.get("scatter_tolerance", 0.0)
-    for k in ("is_glass", "glass_n", "glass_kl"):
+    for k in ("is_glass", "glass_n", "glass_kl", "cameras", "camera_sky"):
         d[k] = desc.get(k)
     d["source_type"] = np.array([s["type"] for s in srcs], np.int32)
     d["source_pos"] = np.array([s["position"] for s in srcs], np.float32)
@@ -90,3 +90,27 @@ def glass_ref(cos_theta, n, KL):
         rho += 0.5 * r * (1.0 + ta * ti)
     tau, rho = min(1.0, max(0.0, tau)), min(1.0, max(0.0, rho))
     return tau, rho, max(0.0, 1.0 - tau - rho)
+
+
+def run_oracle_cameras(rad, labels, oracle_mod, seed=None):
+    """(flux, {camera label: dict(pixels, labels, depths)}) of one runBand by the oracle."""
+    desc = rad.solve_description(labels, seed=seed)
+    sc = oracle_scene_for(rad, oracle_mod)
+    flux, stats = sc.run_band(oracle_solve(desc))
+    cams = dict(zip(desc.get("camera_labels", []), stats.get("cameras", [])))
+    return flux, cams
+
+
+def run_device_cameras(rad, labels, seed):
+    """(flux, {camera label: dict(pixels, labels, depths)}) of one runBand on the device."""
+    rad.setSeed(seed)
+    flux = rad.runBand(labels)
+    cams = {}
+    for label, cam in rad.cameras.items():
+        if cam["labels"] is None:
+            continue
+        W, H = cam["props"]["camera_resolution"]
+        bands = [b for b in sorted(rad.bands) if b in labels]
+        pix = np.stack([cam["pixels"][b].reshape(H, W) for b in bands], axis=-1)
+        cams[label] = {"pixels": pix, "labels": cam["labels"].reshape(H, W), "depths": cam["depths"].reshape(H, W)}
+    return flux, cams

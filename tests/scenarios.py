@@ -496,6 +496,125 @@ GLASS = ["glass_normal", "glass_oblique", "glass_overrides_constant", "glass_bea
          "glass_double_layer", "glass_mixed_bands"]
 
 
+# ---------------------------------------------------------------- cameras
+# Camera scenarios take run_cam(rad, labels, seed) -> (flux, {camera label: dict(pixels [H, W, Bl],
+# labels [H, W], depths [H, W])}).
+
+def camera_stefan_boltzmann(run_cam):
+    """selfTest.cpp:5586-5650: one blackbody patch (350 K) under a pinhole camera; the pixels
+    on the patch read sigma T^4 / pi, on every one of three renders."""
+    ctx = Context()
+    p = ctx.addPatch((0, 0, 0), (2, 2))
+    ctx.setPrimitiveData(p, "temperature", 350.0)
+    ctx.setPrimitiveData(p, "emissivity_TH", 1.0)
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("TH")
+    rad.enableEmission("TH")
+    rad.setScatteringDepth("TH", 1)
+    rad.setDiffuseRayCount("TH", 100)
+    rad.addRadiationCamera("thermal_cam", ["TH"], (0, 0, 10), (0, 0, 0),
+                           {"camera_resolution": (64, 64), "HFOV": 30.0, "lens_diameter": 0.0}, 1)
+    exp = SIGMA * 350.0 ** 4 / math.pi
+    out = []
+    for k in range(3):
+        _, cams = run_cam(rad, ["TH"], 21 + k)
+        out.append((f"camera_sb_run{k}", float(cams["thermal_cam"]["pixels"].max()), exp, 1e-5))
+    return out
+
+
+def _camera_source_scene(kind):
+    ctx = Context()
+    g = ctx.addPatch((0, 0, 0), (2.0, 2.0))
+    ctx.setPrimitiveData(g, "twosided_flag", 0)
+    ctx.setPrimitiveData(g, "reflectivity_test_band", 0.0)
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("test_band")
+    rad.disableEmission("test_band")
+    rad.setDirectRayCount("test_band", 100)
+    rad.setDiffuseRayCount("test_band", 0)
+    rad.setScatteringDepth("test_band", 1)
+    if kind == "sphere":
+        src = rad.addSphereRadiationSource((0, 0, 0.5), 0.2)
+        area = 4.0 * math.pi * 0.2 ** 2
+    elif kind == "rectangle":
+        src = rad.addRectangleRadiationSource((0, 0, 0.5), (0.4, 0.4), (0, 0, 0))
+        area = 0.4 * 0.4
+    else:
+        src = rad.addDiskRadiationSource((0, 0, 0.5), 0.2, (0, 0, 0))
+        area = math.pi * 0.2 ** 2
+    rad.setSourceFlux(src, "test_band", 1000.0)
+    rad.addRadiationCamera(kind + "_cam", ["test_band"], (0, 0, 2), (0, 0, 0),
+                           {"camera_resolution": (32, 32), "HFOV": 45.0, "lens_diameter": 0.0}, 10)
+    return rad, area
+
+
+def camera_source_rendering(run_cam):
+    """selfTest.cpp:7321-7427: sphere, rectangle and disk sources between a camera and a black
+    ground show in the centre pixel.  The value is the source radiance flux / area / pi (facing
+    the camera) divided by pi once more, as the reference's closest-hit program divides the sum
+    of the surface and source terms by pi."""
+    out = []
+    for kind in ("sphere", "rectangle", "disk"):
+        rad, area = _camera_source_scene(kind)
+        _, cams = run_cam(rad, ["test_band"], 31)
+        px = cams[kind + "_cam"]["pixels"][16, 16, 0]
+        # rectangles and disks show radiance x the cosine of the ray on their normal, which
+        # the centre pixel's rays keep within 1e-3 of 1
+        out.append((f"camera_{kind}_source", float(px), 1000.0 / area / math.pi ** 2, 1e-5 if kind == "sphere" else 1e-3))
+    return out
+
+
+def camera_pixel_labels(run_cam):
+    """selfTest.cpp:7429-7528: three patches under a camera looking down; the pixel labels
+    (UUID + 1) put the world-left patch on the right of the raw image (the reference's label
+    map writer flips it horizontally), and the centre depth is the distance to the plane."""
+    ctx = Context()
+    for x in (-1.5, 0.0, 1.5):
+        ctx.addPatch((x, 0, 0), (0.8, 2))
+    rad = RadiationModel(ctx)
+    rad.addRadiationCamera("test_cam", ["SW"], (0, 0, 5), (0, 0, 0),
+                           {"camera_resolution": (64, 64), "HFOV": 90.0, "focal_plane_distance": 10.0,
+                            "lens_diameter": 0.0}, 1)
+    rad.addRadiationBand("SW")
+    rad.setScatteringDepth("SW", 1)
+    s = rad.addCollimatedRadiationSource((0, 0, 1))
+    rad.setSourceFlux(s, "SW", 1000.0)
+    _, cams = run_cam(rad, ["SW"], 41)
+    lab, dep = cams["test_cam"]["labels"], cams["test_cam"]["depths"]
+    right_region = lab[26:38, 20:25]   # raw columns 20-24: world x > 0
+    left_region = lab[26:38, 39:44]    # raw columns 39-43: world x < 0
+    frac_left = float(np.mean(left_region == 1))
+    frac_right = float(np.mean(right_region == 3))
+    return [("camera_labels_left", frac_left, 1.0, 0.0), ("camera_labels_right", frac_right, 1.0, 0.0),
+            ("camera_depth_centre", float(dep[32, 32]), 5.0, 1e-5), ("camera_sky_label", float(lab[0, 0]), 0.0, 0.0),
+            ("camera_sky_depth", float(dep[0, 0]), -1.0, 0.0)]
+
+
+def camera_sky_longwave(run_cam):
+    """selfTest.cpp:6387-6439: a camera looking at an empty longwave sky sees the band's sky
+    flux as isotropic radiance, 400 / pi."""
+    ctx = Context()
+    d = ctx.addPatch((100, 100, -1000), (0.01, 0.01))
+    ctx.setPrimitiveData(d, "twosided_flag", 0)
+    ctx.setPrimitiveData(d, "emissivity_LW", 0.0)
+    ctx.setPrimitiveData(d, "temperature", 0.0)
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("LW")
+    rad.setDirectRayCount("LW", 0)
+    rad.setDiffuseRayCount("LW", 0)
+    rad.setScatteringDepth("LW", 1)
+    rad.setDiffuseRadiationFlux("LW", 400.0)
+    rad.addRadiationCamera("sky_cam", ["LW"], (0, 0, 0), (0, 0, 1),
+                           {"camera_resolution": (8, 8), "HFOV": 30.0, "lens_diameter": 0.0}, 1)
+    _, cams = run_cam(rad, ["LW"], 51)
+    px = cams["sky_cam"]["pixels"]
+    return [("camera_lw_sky_min", float(px.min()), 400.0 / math.pi, 1e-6),
+            ("camera_lw_sky_max", float(px.max()), 400.0 / math.pi, 1e-6)]
+
+
+CAMERAS = ["camera_stefan_boltzmann", "camera_source_rendering", "camera_pixel_labels", "camera_sky_longwave"]
+
+
 def check(results, abs_tol_names=()):
     bad = []
     for name, val, exp, tol in results:

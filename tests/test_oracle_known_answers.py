@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import scenarios
-from helpers import glass_ref, run_oracle
+from helpers import glass_ref, run_oracle, run_oracle_cameras
 
 
 @pytest.fixture(scope="module")
@@ -46,3 +46,12 @@ def test_glass_sheet_optics_reference_values(oracle_mod):
         got = oracle_mod.glass_trs(c, n, kl)
         ref = np.array([glass_ref(float(x), n, kl) for x in c])
         assert np.abs(got - ref).max() <= 2e-5, (n, kl, np.abs(got - ref).max())
+
+
+@pytest.mark.parametrize("name", scenarios.CAMERAS)
+def test_camera_known_answer(oracle_mod, name):
+    def run_cam(rad, labels, seed):
+        return run_oracle_cameras(rad, labels, oracle_mod, seed=seed)
+    res = getattr(scenarios, name)(run_cam)
+    assert not scenarios.check(res, abs_tol_names=[r[0] for r in res if r[0].startswith("camera_labels")
+                                                   or r[0].startswith("camera_sky_")]), scenarios.check(res)
