@@ -162,6 +162,11 @@ struct hrt_context {
     int sky_B = 0;                 // bands of the camera sky model (0: none)
     bool sky_has[5] = {false, false, false, false, false};  // sky radiance, disk, flux, Prague, emission
     float sky_sun[3] = {0.f, 0.f, 1.f}, sky_cos = 0.f;
+    // energy balance: surface arrays (10 x [n] float + [n] sides), R, new temperatures, outputs
+    DevBuf eb_surf, eb_sides, eb_R, eb_T, eb_out, eb_status;
+    int eb_n = 0;
+    float eb_dt = 0.f, eb_Tdef = 300.f;
+    uint64_t eb_unconverged = 0;
 };
 
 namespace {
@@ -703,6 +708,63 @@ int ensure_camera_labels(hrt_context *ctx, int W, int H) {
     return HRT_OK;
 }
 
+// Energy balance: upload the surface arrays of n primitives.
+int upload_surface(hrt_context *ctx, int n, const hrt_surface *s) {
+    if (!s) return fail(ctx, HRT_EINVAL, "null surface");
+    const float *a[10] = {s->air_temperature, s->air_vapor_pressure, s->air_pressure, s->bl_conductance,
+                          s->moisture_conductance, s->emissivity, s->other_flux, s->heat_capacity,
+                          s->surface_humidity, s->stomatal_sidedness};
+    for (const float *x : a)
+        if (!x) return fail(ctx, HRT_EINVAL, "null surface array");
+    if (!s->nsides) return fail(ctx, HRT_EINVAL, "null surface array");
+    if (!(s->dt >= 0.f)) return fail(ctx, HRT_EINVAL, "dt must be >= 0");
+    const size_t N = (size_t)n;
+    CU(ctx->eb_surf.ensure(ctx->stream, 10 * N * sizeof(float)));
+    CU(ctx->eb_sides.ensure(ctx->stream, N));
+    for (int k = 0; k < 10; ++k)
+        CU(cudaMemcpyAsync(ctx->eb_surf.as<float>() + k * N, a[k], N * sizeof(float), cudaMemcpyHostToDevice,
+                           ctx->stream));
+    CU(cudaMemcpyAsync(ctx->eb_sides.p, s->nsides, N, cudaMemcpyHostToDevice, ctx->stream));
+    CU(ctx->eb_R.ensure(ctx->stream, N * sizeof(float)));
+    CU(ctx->eb_T.ensure(ctx->stream, N * sizeof(float)));
+    CU(ctx->eb_out.ensure(ctx->stream, 5 * N * sizeof(float)));
+    CU(ctx->eb_status.ensure(ctx->stream, 2 * sizeof(unsigned)));
+    ctx->eb_n = n;
+    ctx->eb_dt = s->dt;
+    ctx->eb_Tdef = s->temperature_default;
+    return HRT_OK;
+}
+
+// One energy-balance solve over the uploaded surface: R (device [n]) and Tin (device [n]) to
+// ctx->eb_T; counts unconverged primitives into eb_status[0].
+int eb_solve(hrt_context *ctx, const float *R, const float *Tin, bool outputs) {
+    const size_t N = (size_t)ctx->eb_n;
+    EnergyParams P{};
+    P.n = ctx->eb_n;
+    P.R = R;
+    P.Tin = Tin;
+    const float *f = ctx->eb_surf.as<float>();
+    P.Ta = f;
+    P.ea = f + N;
+    P.press = f + 2 * N;
+    P.gH = f + 3 * N;
+    P.gS = f + 4 * N;
+    P.eps = f + 5 * N;
+    P.Qother = f + 6 * N;
+    P.cap = f + 7 * N;
+    P.hs = f + 8 * N;
+    P.sided = f + 9 * N;
+    P.nsides = ctx->eb_sides.as<uint8_t>();
+    P.dt = ctx->eb_dt;
+    P.T_default = ctx->eb_Tdef;
+    P.Tout = ctx->eb_T.as<float>();
+    P.out = outputs ? ctx->eb_out.as<float>() : nullptr;
+    P.status = ctx->eb_status.as<unsigned>();
+    CU(cudaMemsetAsync(ctx->eb_status.p, 0, 2 * sizeof(unsigned), ctx->stream));
+    CU(launch_energy_balance(P, ctx->stream));
+    return HRT_OK;
+}
+
 int count_flags(int Bg, const uint8_t *f) {
     int c = 0;
     for (int b = 0; b < Bg; ++b) c += f[b] ? 1 : 0;
@@ -1079,6 +1141,86 @@ int hrt_get_results(hrt_context *ctx, float *radiation_in, float *out_top, float
     if (out_top) CU(cudaMemcpyAsync(out_top, ctx->otop.p, m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     if (out_bottom) CU(cudaMemcpyAsync(out_bottom, ctx->obot.p, m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaStreamSynchronize(ctx->stream));
+    return HRT_OK;
+}
+
+int hrt_energy_balance(hrt_context *ctx, int32_t n, const hrt_surface *s, const float *net_radiation,
+                       const float *temperature, float *temperature_out, float *fluxes_out) {
+    if (!ctx || n < 0) return HRT_EINVAL;
+    if (n == 0) return HRT_OK;
+    CU(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    int r = upload_surface(ctx, n, s);
+    if (r) return r;
+    const size_t N = (size_t)n;
+    if (net_radiation) {
+        CU(cudaMemcpyAsync(ctx->eb_R.p, net_radiation, N * sizeof(float), cudaMemcpyHostToDevice, st));
+    } else {
+        if (n != ctx->n || ctx->Bl <= 0 || !ctx->fin.p)
+            return fail(ctx, HRT_EINVAL, "no device fluxes of this scene; call hrt_run_band() first or pass net_radiation");
+        CU(launch_net_radiation(n, ctx->Bl, ctx->fin.as<float>(), ctx->eb_R.as<float>(), st));
+    }
+    if (temperature) {
+        CU(ctx->emis_T.ensure(st, N * sizeof(float)));
+        CU(cudaMemcpyAsync(ctx->emis_T.p, temperature, N * sizeof(float), cudaMemcpyHostToDevice, st));
+        ctx->emis_T_count = N;
+    } else if (ctx->emis_T_count != N) {
+        return fail(ctx, HRT_EINVAL, "no resident temperatures for these primitives; pass temperature");
+    }
+    if ((r = eb_solve(ctx, ctx->eb_R.as<float>(), ctx->emis_T.as<float>(), fluxes_out != nullptr))) return r;
+    CU(cudaMemcpyAsync(ctx->emis_T.p, ctx->eb_T.p, N * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    unsigned bad = 0;
+    CU(cudaMemcpyAsync(&bad, ctx->eb_status.p, sizeof bad, cudaMemcpyDeviceToHost, st));
+    if (temperature_out) CU(cudaMemcpyAsync(temperature_out, ctx->eb_T.p, N * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (fluxes_out) CU(cudaMemcpyAsync(fluxes_out, ctx->eb_out.p, 5 * N * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    ctx->eb_unconverged = bad;
+    return HRT_OK;
+}
+
+int hrt_run_coupled(hrt_context *ctx, const hrt_band_solve *s, const hrt_surface *surface, int32_t max_iterations,
+                    float tolerance_K, float *flux_out, float *temperature_out, int32_t *iterations_out) {
+    if (!ctx || !s || max_iterations < 1 || !(tolerance_K >= 0.f)) return HRT_EINVAL;
+    int r = check_built(ctx);
+    if (r) return r;
+    CU(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const int n = ctx->n;
+    const size_t N = (size_t)n;
+    if ((r = upload_surface(ctx, n, surface))) return r;
+    hrt_band_solve later = *s;
+    later.temperature = nullptr;
+    later.emissivity = nullptr;
+    later.rho = nullptr;
+    later.tau = nullptr;
+    later.sources = nullptr;
+    later.source_flux = nullptr;
+    later.ncameras = 0;
+    int it = 0;
+    uint64_t bad_total = 0;
+    for (; it < max_iterations;) {
+        if ((r = hrt_run_band(ctx, it == 0 ? s : &later, nullptr))) return r;
+        if (ctx->emis_T_count != N)
+            return fail(ctx, HRT_EINVAL, "the coupled solve needs temperatures (hrt_band_solve.temperature)");
+        CU(launch_net_radiation(n, ctx->Bl, ctx->fin.as<float>(), ctx->eb_R.as<float>(), st));
+        if ((r = eb_solve(ctx, ctx->eb_R.as<float>(), ctx->emis_T.as<float>(), false))) return r;
+        CU(launch_max_abs_diff(n, ctx->eb_T.as<float>(), ctx->emis_T.as<float>(), ctx->eb_status.as<unsigned>() + 1, st));
+        CU(cudaMemcpyAsync(ctx->emis_T.p, ctx->eb_T.p, N * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        unsigned h[2] = {0, 0};
+        CU(cudaMemcpyAsync(h, ctx->eb_status.p, sizeof h, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        ++it;
+        bad_total = h[0];
+        float dmax;
+        std::memcpy(&dmax, &h[1], sizeof dmax);
+        if (dmax <= tolerance_K) break;
+    }
+    ctx->eb_unconverged = bad_total;
+    const size_t m = N * (size_t)ctx->Bl;
+    if (flux_out) CU(cudaMemcpyAsync(flux_out, ctx->fin.p, m * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (temperature_out) CU(cudaMemcpyAsync(temperature_out, ctx->emis_T.p, N * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (iterations_out) *iterations_out = it;
     return HRT_OK;
 }
 
@@ -1724,6 +1866,7 @@ int hrt_last_stats(const hrt_context *ctx, uint64_t *stats, int count) {
     if (count > 0) stats[0] = ctx->last_rays;
     if (count > 1) stats[1] = ctx->last_kernels;
     if (count > 2) stats[2] = ctx->last_iters;
+    if (count > 3) stats[3] = ctx->eb_unconverged;
     return HRT_OK;
 }
 

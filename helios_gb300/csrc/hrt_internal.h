@@ -113,6 +113,23 @@ cudaError_t launch_add(double *dst, const double *src, size_t n, cudaStream_t s)
 // Camera-to-world rotation for a view axis of the given zenith and azimuth (host, FP64 rounded to FP32).
 void camera_rotation(float zenith, float azimuth, float M[9]);
 
+// ---------------------------------------------------------------- energy balance
+struct EnergyParams {
+    int n;
+    const float *R;            // [n] absorbed radiation, sum over bands
+    const float *Tin;          // [n] previous / initial surface temperature
+    const float *Ta, *ea, *press, *gH, *gS, *eps, *Qother, *cap, *hs, *sided;  // [n] each
+    const uint8_t *nsides;     // [n] 1 or 2
+    float dt;                  // > 0: storage term over this time step
+    float T_default;           // temperature of a primitive whose solve is not finite
+    float *Tout;               // [n]
+    float *out;                // [n*5] sensible, latent, storage, net radiation, VPD (or null)
+    unsigned *status;          // primitives not converged (or null)
+};
+cudaError_t launch_energy_balance(const EnergyParams &p, cudaStream_t s);
+cudaError_t launch_net_radiation(int n, int Bl, const float *flux, float *R, cudaStream_t s);
+cudaError_t launch_max_abs_diff(int n, const float *a, const float *b, unsigned *out, cudaStream_t s);
+
 // ---------------------------------------------------------------- BVH build
 struct BvhBuffers {
     float4 *rec;        // out: sorted records [n*4]

@@ -208,6 +208,44 @@ int hrt_upload_source_fluxes(hrt_context *ctx, const float *fluxes, size_t count
 int hrt_launch_direct(hrt_context *ctx, const hrt_launch *p);
 /* ---- RayTracingBackend::launchDiffuseRays (RayTracingBackend.h:146) */
 int hrt_launch_diffuse(hrt_context *ctx, const hrt_launch *p);
+/* ---- Surface energy balance: the step after the radiation solve (EnergyBalanceModel::run,
+ * plugins/energybalance/src/EnergyBalanceModel.cu:34-125 and :466-505).  Per primitive, the
+ * temperature T that closes R = Nsides eps sigma T^4 + QH + QL + Qother + storage, by the
+ * reference's secant iteration (from the previous temperature and 400 K, relative step 1e-4,
+ * at most 100 steps).  All arrays [n]. */
+typedef struct {
+    const float *air_temperature;      /* Ta (K) */
+    const float *air_vapor_pressure;   /* ea (Pa) */
+    const float *air_pressure;         /* Pa */
+    const float *bl_conductance;       /* gH: boundary-layer conductance to heat (mol/m^2/s) */
+    const float *moisture_conductance; /* gS: surface / stomatal conductance to vapour (mol/m^2/s) */
+    const float *emissivity;           /* thermal emissivity */
+    const float *other_flux;           /* Qother (W/m^2) */
+    const float *heat_capacity;        /* J/m^2/K, used when dt > 0 */
+    const float *surface_humidity;     /* relative humidity at the evaporating surface */
+    const float *stomatal_sidedness;   /* fraction of the stomata on the second face */
+    const uint8_t *nsides;             /* emitting faces: 1 or 2 */
+    float dt;                          /* s; > 0 adds the heat-storage term */
+    float temperature_default;         /* K, kept where the solution is not finite */
+} hrt_surface;
+
+/* net_radiation NULL: the sum over bands of the last hrt_run_band's fluxes (device-resident).
+ * temperature NULL: the context's resident emission temperature.  The solved temperature
+ * becomes the resident emission temperature, which the next hrt_run_band with temperature =
+ * NULL emits with.  temperature_out [n] and fluxes_out [n*5] (sensible, latent, storage, net
+ * radiation, vapour pressure deficit / P) may be NULL.  hrt_last_stats [3]: primitives whose
+ * iteration did not converge. */
+int hrt_energy_balance(hrt_context *ctx, int32_t n, const hrt_surface *s, const float *net_radiation,
+                       const float *temperature, float *temperature_out, float *fluxes_out);
+
+/* Radiation and energy balance coupled on the device: repeat { hrt_run_band(s) with the
+ * resident temperatures; hrt_energy_balance on its fluxes } until no temperature changes by
+ * more than tolerance_K or max_iterations solves have run.  The first solve uses s as given
+ * (its temperature, if any); later ones keep materials, sources and emissivities resident.
+ * flux_out [n*Bl] is the last solve's flux, temperature_out [n] the final temperatures. */
+int hrt_run_coupled(hrt_context *ctx, const hrt_band_solve *s, const hrt_surface *surface, int32_t max_iterations,
+                    float tolerance_K, float *flux_out, float *temperature_out, int32_t *iterations_out);
+
 /* ---- RayTracingBackend::updateSkyModel (RayTracingBackend.h:129) */
 int hrt_update_sky_model(hrt_context *ctx, int32_t nbands, const hrt_sky_model *m);
 /* ---- RayTracingBackend::launchCameraRays (RayTracingBackend.h:153): adds the radiance of every
@@ -325,7 +363,7 @@ int hrt_set_ray_budget(hrt_context *ctx, uint32_t rays_per_thread);
  * needed (including the terminating zero); buf may be NULL. */
 size_t hrt_tuning_report(const hrt_context *ctx, char *buf, size_t len);
 /* Statistics of the last hrt_run_band: [0] rays traced, [1] kernels launched,
- * [2] scattering iterations run. */
+ * [2] scattering iterations run; [3] primitives whose last energy balance did not converge. */
 int hrt_last_stats(const hrt_context *ctx, uint64_t *stats, int count);
 /* Device status word (HRT error bits) accumulated since the last reset. */
 int hrt_device_status(hrt_context *ctx, uint32_t *status, int reset);
