@@ -28,6 +28,7 @@ EXPORTS = [
     "hrt_server_result", "hrt_server_stats", "hrt_server_destroy", "hrt_set_tuning", "hrt_tuning_report",
     "hrt_set_ray_budget", "hrt_update_glass", "hrt_update_sky_model", "hrt_launch_camera",
     "hrt_launch_pixel_labels", "hrt_zero_camera_pixel_buffers", "hrt_get_camera_results",
+    "hrt_energy_balance", "hrt_run_coupled",
 ]
 
 
@@ -68,6 +69,33 @@ class BandSolve(C.Structure):
                 ("emission", C.c_void_p), ("emissivity", C.c_void_p), ("temperature", C.c_void_p),
                 ("seed", C.c_uint32), ("scatter_tolerance", C.c_double), ("ncameras", C.c_int32),
                 ("cameras", C.c_void_p), ("camera_sky", C.c_void_p)]
+
+
+class Surface(C.Structure):
+    _fields_ = [("air_temperature", C.c_void_p), ("air_vapor_pressure", C.c_void_p), ("air_pressure", C.c_void_p),
+                ("bl_conductance", C.c_void_p), ("moisture_conductance", C.c_void_p), ("emissivity", C.c_void_p),
+                ("other_flux", C.c_void_p), ("heat_capacity", C.c_void_p), ("surface_humidity", C.c_void_p),
+                ("stomatal_sidedness", C.c_void_p), ("nsides", C.c_void_p), ("dt", C.c_float),
+                ("temperature_default", C.c_float)]
+
+
+SURFACE_FIELDS = ("air_temperature", "air_vapor_pressure", "air_pressure", "bl_conductance", "moisture_conductance",
+                  "emissivity", "other_flux", "heat_capacity", "surface_humidity", "stomatal_sidedness")
+
+
+def make_surface(surf: dict, keep: list) -> Surface:
+    """hrt_surface from a dict of [n] arrays (SURFACE_FIELDS, nsides) plus dt and temperature_default."""
+    s = Surface()
+    for k in SURFACE_FIELDS:
+        a = np.ascontiguousarray(surf[k], np.float32).ravel()
+        keep.append(a)
+        setattr(s, k, ptr(a))
+    ns = np.ascontiguousarray(surf["nsides"], np.uint8).ravel()
+    keep.append(ns)
+    s.nsides = ptr(ns)
+    s.dt = float(surf.get("dt", 0.0))
+    s.temperature_default = float(surf.get("temperature_default", 300.0))
+    return s
 
 
 class Camera(C.Structure):
@@ -170,6 +198,8 @@ def load(path: str | None = None):
         "hrt_launch_pixel_labels": (C.c_int, [VP, VP]),
         "hrt_zero_camera_pixel_buffers": (C.c_int, [VP, C.c_int32, C.c_int32]),
         "hrt_get_camera_results": (C.c_int, [VP, VP, VP, VP, C.c_int32, C.c_int32]),
+        "hrt_energy_balance": (C.c_int, [VP, C.c_int32, VP, VP, VP, VP, VP]),
+        "hrt_run_coupled": (C.c_int, [VP, VP, VP, C.c_int32, C.c_float, VP, VP, VP]),
         "hrt_update_sources": (C.c_int, [VP, C.c_int32, VP]),
         "hrt_upload_source_fluxes": (C.c_int, [VP, VP, C.c_size_t]),
         "hrt_launch_direct": (C.c_int, [VP, C.POINTER(Launch)]),
@@ -470,6 +500,33 @@ class Context:
     def zero_camera_pixel_buffers(self, width, height):
         self.check(self.lib.hrt_zero_camera_pixel_buffers(self.h, int(width), int(height)))
 
+    # --------------------------------------------------------- energy balance
+    def energy_balance(self, surf: dict, net_radiation=None, temperature=None, outputs=False):
+        """Surface temperatures [n] (and fluxes [n, 5]: sensible, latent, storage, net radiation,
+        VPD) of hrt_energy_balance; net_radiation / temperature None use the device-resident ones."""
+        keep = []
+        s = make_surface(surf, keep)
+        n = int(np.asarray(surf["air_temperature"]).size)
+        R = None if net_radiation is None else f32(net_radiation).ravel()
+        T0 = None if temperature is None else f32(temperature).ravel()
+        T = np.zeros(n, np.float32)
+        out = np.zeros((n, 5), np.float32) if outputs else None
+        self.check(self.lib.hrt_energy_balance(self.h, n, C.byref(s), ptr(R), ptr(T0), ptr(T), ptr(out)))
+        return (T, out) if outputs else T
+
+    def run_coupled(self, solve: dict, surf: dict, max_iterations=20, tolerance=1e-3):
+        """hrt_run_coupled: (flux [n, Bl], temperature [n], iterations)."""
+        self.update_glass(solve.get("is_glass"), solve.get("glass_n"), solve.get("glass_kl"))
+        b, keep = self.band_solve(solve)
+        s = make_surface(surf, keep)
+        bl = int(np.count_nonzero(np.asarray(solve["band_launch"])))
+        flux = np.zeros((self.n, bl), np.float32)
+        T = np.zeros(self.n, np.float32)
+        it = C.c_int32(0)
+        self.check(self.lib.hrt_run_coupled(self.h, C.byref(b), C.byref(s), int(max_iterations), float(tolerance),
+                                            ptr(flux), ptr(T), C.byref(it)))
+        return flux, T, it.value
+
     def get_camera_results(self, width, height, nbands, pixels=True, labels=True):
         pix = np.zeros((height, width, nbands), np.float32) if pixels else None
         lab = np.zeros((height, width), np.uint32) if labels else None
@@ -516,9 +573,10 @@ class Context:
         return buf.value.decode()
 
     def last_stats(self):
-        st = np.zeros(3, np.uint64)
-        self.check(self.lib.hrt_last_stats(self.h, ptr(st), 3))
-        return {"rays": int(st[0]), "kernels": int(st[1]), "iterations": int(st[2])}
+        st = np.zeros(4, np.uint64)
+        self.check(self.lib.hrt_last_stats(self.h, ptr(st), 4))
+        return {"rays": int(st[0]), "kernels": int(st[1]), "iterations": int(st[2]),
+                "eb_unconverged": int(st[3])}
 
     # -------------------------------------------------------------- inspection
     def trace_rays(self, o, d, tmin=1e-4, tmax=1e38, anyhit=False):
