@@ -205,6 +205,10 @@ class Context:
             vals = np.broadcast_to(np.asarray(value), uuids.shape)
             arr = self._bulk(label, vals.dtype)
             arr[uuids] = vals
+            d = self.primitive_data.get(label)
+            if d:  # values set one by one earlier are replaced
+                for u in uuids.tolist():
+                    d.pop(u, None)
             return
         d = self.primitive_data.setdefault(label, {})
         d[int(uuid)] = value

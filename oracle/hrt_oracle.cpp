@@ -1559,6 +1559,66 @@ void orc_sincos2pi(int64_t n, const float *u, float *c, float *s) {
 }
 
 // ln_unit for a batch (accuracy tests against libm).
+// Surface energy balance (plugins/energybalance/src/EnergyBalanceModel.cu:34-125, outputs
+// :466-505): per primitive, the secant root from (Tin, 400 K) of R - Nsides eps sigma T^4 - QH -
+// QL - Qother - storage, relative step 1e-4, at most 100 steps, in FP32 as the reference computes
+// it.  in: [11][n] Ta, ea, P, gH, gS, eps, Qother, C, hs, sidedness, R; returns the number of
+// primitives that did not converge.  out5 (may be null): [n][5] sensible, latent, storage, net
+// radiation, vapour pressure deficit / P.
+int orc_energy_balance(int32_t n, const float *in, const uint8_t *nsides, const float *Tin, float dt, float Tdef,
+                       float *Tout, float *out5) {
+    const float cp = 29.25f, lam = 44000.f, sig = 5.67e-8f;
+    const size_t N = (size_t)n;
+    int bad = 0;
+    for (int32_t p = 0; p < n; ++p) {
+        const float Ta = in[p], ea = in[N + p], P = in[2 * N + p], gH = in[3 * N + p], gS = in[4 * N + p],
+                    eps = in[5 * N + p], Qo = in[6 * N + p], C = in[7 * N + p], hs = in[8 * N + p],
+                    sd = in[9 * N + p], R = in[10 * N + p];
+        const float ns = (float)nsides[p];
+        const float gM = (gH == 0.f || gS == 0.f)
+                             ? 0.f
+                             : 1.08f * gH * gS * (sd / (1.08f * gH + gS * sd) + (1.f - sd) / (1.08f * gH + gS * (1.f - sd)));
+        const float Tprev = Tin[p];
+        auto res = [&](float T) {
+            const float Rout = ns * eps * sig * T * T * T * T;
+            const float QH = cp * gH * (T - Ta);
+            const float es = 611.0f * std::exp(17.502f * (T - 273.f) / (T - 273.f + 240.97f));
+            const float QL = gM * lam * (es - ea * hs) / P;
+            const float st = dt > 0.f ? C * (T - Tprev) / dt : 0.f;
+            return R - Rout - QH - QL - Qo - st;
+        };
+        float T0 = Tprev, T1 = 400.f;
+        if (T1 == T0) T1 = T0 + 100.f;
+        float T = T0, r0 = res(T0), r1 = res(T1), err = 100.f;
+        for (int it = 0; it < 100 && err > 1e-4f; ++it) {
+            if (r0 == r1) {
+                err = 0.f;
+                break;
+            }
+            T = std::fabs((T1 * r0 - T0 * r1) / (r0 - r1));
+            const float r = res(T);
+            err = std::fabs(T - T0) / std::fabs(T0);
+            r1 = r0;
+            r0 = r;
+            T1 = T0;
+            T0 = T;
+        }
+        if (!std::isfinite(T)) T = Tdef;
+        if (err > 1e-4f) ++bad;
+        Tout[p] = T;
+        if (out5) {
+            const float es = 611.0f * std::exp(17.502f * (T - 273.15f) / (T - 273.15f + 240.97f));
+            float *o = out5 + 5 * (size_t)p;
+            o[0] = cp * gH * (T - Ta);
+            o[1] = lam * gM * (es - ea) / P;
+            o[2] = dt > 0.f ? C * (T - Tprev) / dt : 0.f;
+            o[3] = R - ns * eps * sig * T * T * T * T;
+            o[4] = (es - ea) / P;
+        }
+    }
+    return bad;
+}
+
 void orc_glass_trs(int64_t m, const float *c, float n, float kl, float *out) {
     for (int64_t i = 0; i < m; ++i) glass_trs(c[i], n, kl, &out[3 * i], &out[3 * i + 1], &out[3 * i + 2]);
 }

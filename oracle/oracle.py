@@ -129,6 +129,8 @@ def _load():
         _lib.orc_sincos2pi.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_ln_unit.argtypes = [C.c_int64, C.c_void_p, C.c_void_p]
         _lib.orc_glass_trs.argtypes = [C.c_int64, C.c_void_p, C.c_float, C.c_float, C.c_void_p]
+        _lib.orc_energy_balance.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float,
+                                            C.c_void_p, C.c_void_p]
     return _lib
 
 
@@ -336,3 +338,22 @@ def glass_trs(cos_theta, n, kl):
     out = np.zeros((c.size, 3), np.float32)
     _load().orc_glass_trs(c.size, _ptr(c), float(n), float(kl), _ptr(out))
     return out
+
+
+EB_FIELDS = ("air_temperature", "air_vapor_pressure", "air_pressure", "bl_conductance", "moisture_conductance",
+             "emissivity", "other_flux", "heat_capacity", "surface_humidity", "stomatal_sidedness")
+
+
+def energy_balance(surf, net_radiation, temperature):
+    """(T [n], fluxes [n, 5], unconverged) of the surface energy balance on the CPU (FP32)."""
+    n = int(np.asarray(net_radiation).size)
+    rows = [np.ascontiguousarray(surf[k], np.float32).ravel() for k in EB_FIELDS]
+    rows.append(np.ascontiguousarray(net_radiation, np.float32).ravel())
+    inp = np.ascontiguousarray(np.concatenate(rows), np.float32)
+    ns = np.ascontiguousarray(surf["nsides"], np.uint8).ravel()
+    Tin = np.ascontiguousarray(temperature, np.float32).ravel()
+    T = np.zeros(n, np.float32)
+    out = np.zeros((n, 5), np.float32)
+    bad = _load().orc_energy_balance(n, _ptr(inp), _ptr(ns), _ptr(Tin), float(surf.get("dt", 0.0)),
+                                     float(surf.get("temperature_default", 300.0)), _ptr(T), _ptr(out))
+    return T, out, int(bad)

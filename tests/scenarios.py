@@ -615,6 +615,155 @@ def camera_sky_longwave(run_cam):
 CAMERAS = ["camera_stefan_boltzmann", "camera_source_rendering", "camera_pixel_labels", "camera_sky_longwave"]
 
 
+# ---------------------------------------------------------------- energy balance
+# Scenarios take run_eb(model, dt) that solves EnergyBalanceModel `model` once (its surface
+# inputs from primitive data) and writes the outputs as primitive data.
+# plugins/energybalance/tests/selfTest.cpp, err_tol = 1e-3.
+SIGMA_EB = 5.67e-8
+
+
+def _eb_model(ctx, bands):
+    from helios_gb300.energybalance import EnergyBalanceModel
+    m = EnergyBalanceModel(ctx)
+    m.disableMessages()
+    m.addRadiationBand(bands)
+    return m
+
+
+def eb_equilibrium(run_eb):
+    """selfTest.cpp:11-31: R = 2 sigma Tref^4 with air at Tref gives T = Tref."""
+    ctx = Context()
+    u = [ctx.addPatch((1, 2, 3), (3, 2)), ctx.addTriangle((4, 5, 6), (5, 5, 6), (5, 6, 6))]
+    ctx.setPrimitiveData(np.array(u), "radiation_flux_LW", np.full(2, 2.0 * SIGMA_EB * 350.0 ** 4))
+    ctx.setPrimitiveData(np.array(u), "air_temperature", np.full(2, 350.0))
+    m = _eb_model(ctx, "LW")
+    run_eb(m, 0.0)
+    return [(f"eb_equilibrium_{k}", ctx.getPrimitiveData(k, "temperature"), 350.0, 1e-3) for k in u]
+
+
+def eb_budget_closure(run_eb):
+    """selfTest.cpp:33-66: Rin - Rout - QH - QL = 0 at the solved temperature."""
+    ctx = Context()
+    u = np.array([ctx.addPatch((1, 2, 3), (3, 2)), ctx.addTriangle((4, 5, 6), (5, 5, 6), (5, 6, 6))])
+    ctx.setPrimitiveData(u, "radiation_flux_LW", np.full(2, 2.0 * SIGMA_EB * 300.0 ** 4))
+    ctx.setPrimitiveData(u, "radiation_flux_SW", np.full(2, 300.0))
+    ctx.setPrimitiveData(u, "air_temperature", np.full(2, 300.0))
+    m = _eb_model(ctx, ["LW", "SW"])
+    run_eb(m, 0.0)
+    out = []
+    for k in u:
+        T = ctx.getPrimitiveData(k, "temperature")
+        rin = ctx.getPrimitiveData(k, "radiation_flux_LW") + ctx.getPrimitiveData(k, "radiation_flux_SW")
+        resid = rin - 2.0 * SIGMA_EB * T ** 4 - ctx.getPrimitiveData(k, "sensible_flux") - \
+            ctx.getPrimitiveData(k, "latent_flux")
+        out.append((f"eb_closure_{k}", resid, 0.0, 1e-2))
+    return out
+
+
+def _eb_check_scene(extra=None):
+    ctx = Context()
+    u = ctx.addPatch((1, 2, 3), (3, 2))
+    T = 312.0
+    for k, v in (("radiation_flux_LW", SIGMA_EB * T ** 4), ("radiation_flux_SW", 350.0), ("wind_speed", 1.244),
+                 ("moisture_conductance", 0.05), ("air_humidity", 0.4), ("air_pressure", 956789.0),
+                 ("other_surface_flux", 150.0), ("air_temperature", T), ("twosided_flag", 0)):
+        ctx.setPrimitiveData(u, k, v)
+    for k, v in (extra or {}).items():
+        ctx.setPrimitiveData(u, k, v)
+    return ctx, u
+
+
+def eb_solution_checks(run_eb):
+    """selfTest.cpp:68-177: temperature, sensible and latent flux of one patch with wind,
+    stomata, other fluxes and reduced pressure; with the object length; with a given
+    boundary-layer conductance (the reference's values, relative 1e-3)."""
+    out = []
+    for tag, extra, (qh, ql, t) in (("len_sqrt_area", None, (48.7017, 21.6094, 329.307)),
+                                    ("object_length", {"object_length": 0.374}, (89.2024, 20.0723, 324.386)),
+                                    ("given_gH", {"boundarylayer_conductance": 0.134}, (61.5411, 21.6718, 327.701))):
+        ctx, u = _eb_check_scene(extra)
+        run_eb(_eb_model(ctx, ["LW", "SW"]), 0.0)
+        out += [(f"eb_{tag}_sensible", ctx.getPrimitiveData(u, "sensible_flux"), qh, 1e-3),
+                (f"eb_{tag}_latent", ctx.getPrimitiveData(u, "latent_flux"), ql, 1e-3),
+                (f"eb_{tag}_temperature", ctx.getPrimitiveData(u, "temperature"), t, 1e-3)]
+    return out
+
+
+def eb_dynamic(run_eb):
+    """selfTest.cpp:196-249: heat storage; after a step in radiation the temperature relaxes
+    exponentially with time constant C / (gH cp); RMS deviation below 0.2 K."""
+    ctx = Context()
+    u = ctx.addPatch((0, 0, 0), (1, 1))
+    dt, Tend, To, cp = 1.0, 3600.0, 300.0, 2000.0
+    Rlow, Rhigh = 50.0, 500.0
+    for k, v in (("radiation_flux_SW", Rlow), ("temperature", To), ("heat_capacity", cp), ("twosided_flag", 0),
+                 ("emissivity_SW", 0.0)):
+        ctx.setPrimitiveData(u, k, v)
+    m = _eb_model(ctx, "SW")
+    m.optionalOutputPrimitiveData("boundarylayer_conductance_out")
+    N = int(round(Tend / dt))
+    temps = []
+    for t in range(N):
+        if t > 0.5 * N:
+            ctx.setPrimitiveData(u, "radiation_flux_SW", Rhigh)
+        run_eb(m, dt)
+        temps.append(ctx.getPrimitiveData(u, "temperature"))
+    gH = ctx.getPrimitiveData(u, "boundarylayer_conductance_out")
+    tau = cp / gH / 29.25
+    ctx.setPrimitiveData(u, "radiation_flux_SW", Rlow)
+    run_eb(m, 0.0)
+    Tlow = ctx.getPrimitiveData(u, "temperature")
+    ctx.setPrimitiveData(u, "radiation_flux_SW", Rhigh)
+    run_eb(m, 0.0)
+    Thigh = ctx.getPrimitiveData(u, "temperature")
+    err = 0.0
+    h = int(round(0.5 * N))
+    for t in range(h, N):
+        ref = Tlow + (Thigh - Tlow) * (1.0 - math.exp(-(dt * (t - h)) / tau))
+        err += (ref - temps[t]) ** 2
+    return [("eb_dynamic_rms", math.sqrt(err / N), 0.0, 0.2)]
+
+
+def eb_regressions(run_eb):
+    """selfTest.cpp:588-704: an initial temperature equal to the second secant guess (400 K),
+    zero boundary-layer conductance with stomatal conductance, and the emissivity of the one
+    emission-enabled band (or the first of several)."""
+    out = []
+    ctx = Context()
+    u = ctx.addPatch((0, 0, 0), (1, 1))
+    for k, v in (("radiation_flux_LW", 2.0 * SIGMA_EB * 350.0 ** 4), ("air_temperature", 300.0),
+                 ("boundarylayer_conductance", 0.0), ("temperature", 400.0)):
+        ctx.setPrimitiveData(u, k, v)
+    run_eb(_eb_model(ctx, "LW"), 0.0)
+    out.append(("eb_guess_400", ctx.getPrimitiveData(u, "temperature"), 350.0, 1e-3))
+    ctx = Context()
+    u = ctx.addPatch((0, 0, 0), (1, 1))
+    for k, v in (("radiation_flux_LW", 400.0), ("air_temperature", 300.0), ("boundarylayer_conductance", 0.0),
+                 ("moisture_conductance", 0.1)):
+        ctx.setPrimitiveData(u, k, v)
+    run_eb(_eb_model(ctx, "LW"), 0.0)
+    ql, T = ctx.getPrimitiveData(u, "latent_flux"), ctx.getPrimitiveData(u, "temperature")
+    out.append(("eb_zero_gH_latent", ql, 0.0, 0.0))
+    out.append(("eb_zero_gH_finite", float(math.isfinite(T)), 1.0, 0.0))
+    for bands, flags in ((("LW", "SW"), (1, 0)), (("LW", "LW2"), (1, 1))):
+        ctx = Context()
+        u = ctx.addPatch((0, 0, 0), (1, 1))
+        ctx.setPrimitiveData(u, "radiation_flux_" + bands[0], 500.0)
+        ctx.setPrimitiveData(u, "radiation_flux_" + bands[1], 0.0)
+        for k, v in (("air_temperature", 300.0), ("boundarylayer_conductance", 0.0),
+                     ("emissivity_" + bands[0], 0.8), ("emissivity_" + bands[1], 0.4)):
+            ctx.setPrimitiveData(u, k, v)
+        for b, f in zip(bands, flags):
+            ctx.setGlobalData("emission_enabled_" + b, f)
+        run_eb(_eb_model(ctx, list(bands)), 0.0)
+        exp = (500.0 / (2.0 * 0.8 * SIGMA_EB)) ** 0.25
+        out.append((f"eb_emissivity_{bands[1]}", ctx.getPrimitiveData(u, "temperature"), exp, 1e-3))
+    return out
+
+
+ENERGY = ["eb_equilibrium", "eb_budget_closure", "eb_solution_checks", "eb_dynamic", "eb_regressions"]
+
+
 def check(results, abs_tol_names=()):
     bad = []
     for name, val, exp, tol in results:
