@@ -57,8 +57,9 @@ def test_energy_balance_vs_oracle(oracle_mod):
         T2, o2, bad = oracle_mod.energy_balance(surf, R, To)
         assert np.abs(T1 - T2).max() <= T_ATOL
         assert ctx.last_stats()["eb_unconverged"] == bad
-        scale = np.maximum(np.abs(o2), 1e-2)
-        assert (np.abs(o1 - o2) / scale).max() <= 1e-3
+        # fluxes follow T: within 1e-3 relative or 0.05 W/m^2 (storage amplifies T by C / dt)
+        assert np.allclose(o1[:, :4], o2[:, :4], rtol=1e-3, atol=5e-2)
+        assert np.allclose(o1[:, 4], o2[:, 4], rtol=1e-3, atol=1e-6)
 
 
 def _coupled_scene(seed=0, n_leaves=1500):
@@ -103,6 +104,9 @@ def test_coupled_loop_vs_oracle_loop(oracle_mod):
     assert 2 <= it < 30
     T_gpu = ctx.primitive_array("temperature", np.nan).astype(np.float32)
     rad2, eb2, ctx2 = _coupled_scene()
+    n = ctx2.getPrimitiveCount()
+    for b in ("SW", "LW"):  # surface inputs only; the loop below computes the fluxes
+        ctx2.setPrimitiveData(np.arange(n), "radiation_flux_" + b, np.zeros(n))
     surf, _, To, _ = eb2.surface_arrays()
     sc = oracle_scene_for(rad2, oracle_mod)
     T = To.copy()
