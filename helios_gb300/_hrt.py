@@ -28,7 +28,8 @@ EXPORTS = [
     "hrt_server_result", "hrt_server_stats", "hrt_server_destroy", "hrt_set_tuning", "hrt_tuning_report",
     "hrt_set_ray_budget", "hrt_update_glass", "hrt_update_sky_model", "hrt_launch_camera",
     "hrt_launch_pixel_labels", "hrt_zero_camera_pixel_buffers", "hrt_get_camera_results",
-    "hrt_energy_balance", "hrt_run_coupled",
+    "hrt_energy_balance", "hrt_run_coupled", "hrt_scene_load", "hrt_scene_last_error", "hrt_scene_count",
+    "hrt_scene_arrays", "hrt_scene_data_labels", "hrt_scene_data", "hrt_scene_free",
 ]
 
 
@@ -96,6 +97,53 @@ def make_surface(surf: dict, keep: list) -> Surface:
     s.dt = float(surf.get("dt", 0.0))
     s.temperature_default = float(surf.get("temperature_default", 300.0))
     return s
+
+
+class LoadOptions(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("height", C.c_float), ("rotation", C.c_float * 2),
+                ("up_axis", C.c_int32), ("default_color", C.c_float * 3)]
+
+
+UP_AXES = {"XUP": 0, "YUP": 1, "ZUP": 2}
+
+
+def load_scene_file(path, origin=(0.0, 0.0, 0.0), height=0.0, rotation=(0.0, 0.0), up_axis="ZUP",
+                    default_color=(0.0, 0.0, 1.0)):
+    """Primitive arrays of a PLY / OBJ / XML file (hrt_scene_load): dict with T [n, 16], type [n],
+    twosided [n], color [n, 3] and data {label: [n] float64 (NaN where absent)}."""
+    lib = load()
+    if up_axis not in UP_AXES:
+        raise ValueError(f"{up_axis} is not a valid up-axis. Please specify a value of XUP, YUP, or ZUP.")
+    o = LoadOptions()
+    for k in range(3):
+        o.origin[k] = float(origin[k])
+        o.default_color[k] = float(default_color[k])
+    o.height = float(height)
+    o.rotation[0], o.rotation[1] = float(rotation[0]), float(rotation[1])
+    o.up_axis = UP_AXES[up_axis]
+    h = C.c_void_p()
+    rc = lib.hrt_scene_load(os.fsencode(path), C.byref(o), C.byref(h))
+    if rc != HRT_OK:
+        raise HrtError(rc, lib.hrt_scene_last_error().decode())
+    try:
+        n = int(lib.hrt_scene_count(h))
+        T = np.zeros((n, 16), np.float32)
+        ty = np.zeros(n, np.uint32)
+        ts = np.zeros(n, np.int8)
+        col = np.zeros((n, 3), np.float32)
+        lib.hrt_scene_arrays(h, ptr(T), ptr(ty), ptr(ts), ptr(col))
+        need = lib.hrt_scene_data_labels(h, None, 0)
+        buf = C.create_string_buffer(int(need))
+        lib.hrt_scene_data_labels(h, buf, need)
+        data = {}
+        for lab in buf.value.decode().split("\n"):
+            if lab:
+                v = np.zeros(n, np.float64)
+                lib.hrt_scene_data(h, lab.encode(), ptr(v))
+                data[lab] = v
+    finally:
+        lib.hrt_scene_free(h)
+    return {"T": T, "type": ty, "twosided": ts, "color": col, "data": data}
 
 
 class Camera(C.Structure):
@@ -199,6 +247,13 @@ def load(path: str | None = None):
         "hrt_zero_camera_pixel_buffers": (C.c_int, [VP, C.c_int32, C.c_int32]),
         "hrt_get_camera_results": (C.c_int, [VP, VP, VP, VP, C.c_int32, C.c_int32]),
         "hrt_energy_balance": (C.c_int, [VP, C.c_int32, VP, VP, VP, VP, VP]),
+        "hrt_scene_load": (C.c_int, [C.c_char_p, VP, C.POINTER(C.c_void_p)]),
+        "hrt_scene_last_error": (C.c_char_p, []),
+        "hrt_scene_count": (C.c_int64, [VP]),
+        "hrt_scene_arrays": (C.c_int, [VP, VP, VP, VP, VP]),
+        "hrt_scene_data_labels": (C.c_size_t, [VP, VP, C.c_size_t]),
+        "hrt_scene_data": (C.c_int, [VP, C.c_char_p, VP]),
+        "hrt_scene_free": (None, [VP]),
         "hrt_run_coupled": (C.c_int, [VP, VP, VP, C.c_int32, C.c_float, VP, VP, VP]),
         "hrt_update_sources": (C.c_int, [VP, C.c_int32, VP]),
         "hrt_upload_source_fluxes": (C.c_int, [VP, VP, C.c_size_t]),

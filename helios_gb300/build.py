@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libhrt.so")
-SOURCES = ["hrt_bvh.cu", "hrt_bvh4.cu", "hrt_trace.cu", "hrt_ps_accumulate.cu", "hrt_ps_special.cu", "hrt_camera.cu", "hrt_energy.cu", "hrt_api.cu",
+SOURCES = ["hrt_bvh.cu", "hrt_bvh4.cu", "hrt_trace.cu", "hrt_ps_accumulate.cu", "hrt_ps_special.cu", "hrt_camera.cu", "hrt_energy.cu", "hrt_ingest.cpp", "hrt_api.cu",
            "hrt_static.cu", "hrt_serve.cu"]
 HEADERS = ["hrt_device.cuh", "hrt_internal.h", "hrt_trace.cuh", os.path.join("..", "..", "include", "hrt.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -47,7 +47,7 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> str:
     objs, jobs = [], []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s, *headers, __file__]):
             cmd = [cc, *ARCH, *NVFLAGS, *(extra or []), "-c", s, "-o", o]

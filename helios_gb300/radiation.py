@@ -141,6 +141,52 @@ class Context:
             self.setPrimitiveData(uuids, "twosided_flag", np.broadcast_to(np.asarray(twosided, np.float64), uuids.shape))
         return uuids
 
+    # ------------------------------------------------------------ file input
+    def _add_loaded(self, f):
+        """Add the primitives of a loaded file (helios_gb300._hrt.load_scene_file)."""
+        T, ty = f["T"].astype(np.float64), f["type"]
+        c0, c1, c2 = T[:, [0, 4, 8]], T[:, [1, 5, 9]], T[:, [2, 6, 10]]
+        a, b, c = (np.linalg.norm(x, axis=1) for x in (c0, c1, c2))
+        cr = np.linalg.norm(np.cross(c0, c1), axis=1)
+        area = np.select([ty == scenes.TRIANGLE, ty == 2, ty == 4], [0.5 * cr, math.pi * a * b, 2.0 * (a * b + b * c + c * a)],
+                         cr)
+        uu = self.addPrimitives(f["T"], ty, area, f["twosided"])
+        for lab, v in f["data"].items():
+            m = ~np.isnan(v)
+            if m.any():
+                self.setPrimitiveData(uu[m], lab, v[m])
+        return uu
+
+    def loadPLY(self, filename, origin=(0.0, 0.0, 0.0), height=0.0, rotation=(0.0, 0.0), default_color=(0.0, 0.0, 1.0),
+                upaxis="YUP"):
+        """Context::loadPLY (core/src/Context_fileIO.cpp:3617-3908): triangles of a PLY file
+        (rotation = (elevation, azimuth)); returns their UUIDs."""
+        if not str(filename).lower().endswith(".ply"):
+            raise HeliosRuntimeError(f"ERROR (Context::loadPLY): File {filename} is not PLY format.")
+        return self._load_file(filename, origin, height, rotation, default_color, upaxis, "loadPLY")
+
+    def loadOBJ(self, filename, origin=(0.0, 0.0, 0.0), height=0.0, rotation=(0.0, 0.0), default_color=(0.0, 0.0, 1.0),
+                upaxis="ZUP"):
+        """Context::loadOBJ (core/src/Context_fileIO.cpp:3983-4340): triangles of an OBJ file."""
+        if not str(filename).lower().endswith(".obj"):
+            raise HeliosRuntimeError(f"ERROR (Context::loadOBJ): File {filename} is not OBJ format.")
+        return self._load_file(filename, origin, height, rotation, default_color, upaxis, "loadOBJ")
+
+    def loadXML(self, filename):
+        """Context::loadXML (core/src/Context_fileIO.cpp:1260-2230): patches, triangles, voxels
+        and disks with their transforms and scalar primitive data."""
+        if not str(filename).lower().endswith(".xml"):
+            raise HeliosRuntimeError(f"failed.\n File {filename} is not XML format.")
+        return self._load_file(filename, (0, 0, 0), 0.0, (0, 0), (0, 0, 1), "ZUP", "loadXML")
+
+    def _load_file(self, filename, origin, height, rotation, color, upaxis, fn):
+        from . import _hrt
+        try:
+            f = _hrt.load_scene_file(filename, origin, height, rotation, upaxis, color)
+        except (ValueError, _hrt.HrtError) as e:
+            raise HeliosRuntimeError(f"ERROR (Context::{fn}): {e}") from None
+        return self._add_loaded(f)
+
     def addScene(self, sc: "scenes.Scene"):
         uuids = self.addPrimitives(sc.T, sc.ptype, sc.area, sc.twosided)
         if sc.lad is not None:

@@ -246,6 +246,36 @@ int hrt_energy_balance(hrt_context *ctx, int32_t n, const hrt_surface *s, const 
 int hrt_run_coupled(hrt_context *ctx, const hrt_band_solve *s, const hrt_surface *surface, int32_t max_iterations,
                     float tolerance_K, float *flux_out, float *temperature_out, int32_t *iterations_out);
 
+/* ---- Scene ingestion: the geometry of Context::loadPLY / loadOBJ / loadXML
+ * (core/src/Context_fileIO.cpp:3633-3908, 3995-4340, 1260-2230) as primitive arrays for
+ * hrt_update_geometry or hrt_server_add_scene.  PLY (ascii and binary little-endian) and OBJ
+ * give triangles: up-axis remap, base moved to z = 0 (PLY), scaled to `height` (> 0), rotated
+ * by (elevation, azimuth) as rotatePoint does, moved to `origin`, polygons fan-triangulated and
+ * degenerate triangles dropped; OBJ triangles are grouped by material name, with the material's
+ * Kd colour.  XML gives patches, triangles, voxels and disks with their <transform> (triangles
+ * also from <vertices>) and scalar primitive data (<data_float>, <data_double>, <data_int>,
+ * <data_uint>).  Texture images, compound objects and materials beyond Kd are not read. */
+typedef struct hrt_scene_file hrt_scene_file;
+typedef struct {
+    float origin[3];
+    float height;                 /* > 0: scale the model to this height (PLY, OBJ) */
+    float rotation[2];            /* elevation, azimuth (radians) */
+    int32_t up_axis;              /* 0 XUP, 1 YUP, 2 ZUP */
+    float default_color[3];       /* colour of triangles without one */
+} hrt_load_options;
+/* opt NULL: origin 0, no scaling or rotation, ZUP, blue.  On failure *out is NULL and
+ * hrt_scene_last_error() (per thread) says why. */
+int hrt_scene_load(const char *path, const hrt_load_options *opt, hrt_scene_file **out);
+const char *hrt_scene_last_error(void);
+int64_t hrt_scene_count(const hrt_scene_file *f);
+/* transform [n*16], type [n], twosided [n], color [n*3]; any may be NULL */
+int hrt_scene_arrays(const hrt_scene_file *f, float *transform, uint32_t *type, int8_t *twosided, float *color);
+/* primitive data labels, one per line; returns the buffer size needed */
+size_t hrt_scene_data_labels(const hrt_scene_file *f, char *buf, size_t len);
+/* values [n] of a primitive data label (NaN where a primitive has none) */
+int hrt_scene_data(const hrt_scene_file *f, const char *label, double *values);
+void hrt_scene_free(hrt_scene_file *f);
+
 /* ---- RayTracingBackend::updateSkyModel (RayTracingBackend.h:129) */
 int hrt_update_sky_model(hrt_context *ctx, int32_t nbands, const hrt_sky_model *m);
 /* ---- RayTracingBackend::launchCameraRays (RayTracingBackend.h:153): adds the radiance of every

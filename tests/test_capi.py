@@ -9,7 +9,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared():
     src = open(os.path.join(ROOT, "include", "hrt.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|void|size_t|const char \*)\s*(hrt_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|void|size_t|int64_t|const char \*)\s*(hrt_\w+)\s*\(", src, re.M)))
 
 
 def test_header_matches_binding():
