@@ -49,6 +49,11 @@ struct DevBuf {
     T *as() const {
         return (T *)p;
     }
+    void free_on(cudaStream_t s) {
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+        cap = 0;
+    }
     void release() {
         if (p) {
             if (g_release_stream) cudaFreeAsync(p, g_release_stream);
@@ -964,8 +969,20 @@ int hrt_build_accel(hrt_context *ctx) {
     CU(ctx->nodes4.ensure(ctx->stream, ni * 4 * sizeof(float4)));
     if (bvh4_scratch_bytes(n) > ctx->bvh_scratch.cap) CU(ctx->bvh_scratch.ensure(ctx->stream, bvh4_scratch_bytes(n)));
     int n4 = 0;
-    CU(bvh4_build(ctx->nodes.as<float4>(), n, ctx->nodes4.as<float4>(), ctx->bvh_scratch.p, ctx->status.as<uint32_t>(),
-                  &n4, ctx->stream));
+    // the 4-wide nodes come from the clustered binary tree (fewer node visits than the
+    // Morton split); its nodes and scratch live only for the build
+    const float4 *src2 = ctx->nodes.as<float4>();
+    DevBuf ploc_nodes, ploc_scratch;
+    if (n >= 2) {
+        CU(ploc_nodes.ensure(ctx->stream, ni * 4 * sizeof(float4)));
+        CU(ploc_scratch.ensure(ctx->stream, ploc_scratch_bytes(n)));
+        CU(ploc_build(b.leafbox, n, ploc_nodes.as<float4>(), ploc_scratch.p, ctx->stream));
+        src2 = ploc_nodes.as<float4>();
+    }
+    CU(bvh4_build(src2, n, ctx->nodes4.as<float4>(), ctx->bvh_scratch.p, ctx->status.as<uint32_t>(), &n4,
+                  ctx->stream));
+    ploc_nodes.free_on(ctx->stream);
+    ploc_scratch.free_on(ctx->stream);
     if ((r = sync_and_status(ctx))) return r;
     ctx->n4 = n4;
     ctx->built = true;

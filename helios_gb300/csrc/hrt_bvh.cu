@@ -420,6 +420,102 @@ __global__ void k_single(const float *__restrict__ leafbox, float4 *__restrict__
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// ---------------------------------------------------------------- PLOC
+// Agglomerative clustering of the Morton-ordered leaves (Meister & Bittner, "Parallel
+// Locally-Ordered Clustering for Bounding Volume Hierarchy Construction", TVCG 2018): each
+// cluster finds the neighbour within +-kPlocRadius places whose merged box has the least
+// surface area (ties: the smaller index); mutual pairs merge into a new binary node; the
+// survivors are compacted in order; repeat until one cluster is left.  Node indices are
+// handed out from n-2 downwards by a prefix sum, so the root is node 0 and the tree does not
+// depend on scheduling.  The leaves are the same record slots as the LBVH's.
+constexpr int kPlocRadius = 16;
+
+__device__ __forceinline__ float merged_area(const float *a, const float *b) {
+    const float dx = fmaxf(a[3], b[3]) - fminf(a[0], b[0]);
+    const float dy = fmaxf(a[4], b[4]) - fminf(a[1], b[1]);
+    const float dz = fmaxf(a[5], b[5]) - fminf(a[2], b[2]);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__global__ void k_ploc_init(int n, const float *__restrict__ leafbox, float *__restrict__ cbox,
+                            int32_t *__restrict__ cid) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) cbox[6 * (size_t)i + k] = leafbox[6 * (size_t)i + k];
+    cid[i] = ~i;
+}
+
+__global__ void k_ploc_nn(int m, const float *__restrict__ cbox, int32_t *__restrict__ nn) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    float a[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) a[k] = cbox[6 * (size_t)i + k];
+    float best = INFINITY;
+    int bj = -1;
+    const int lo = i - kPlocRadius < 0 ? 0 : i - kPlocRadius;
+    const int hi = i + kPlocRadius > m - 1 ? m - 1 : i + kPlocRadius;
+    for (int j = lo; j <= hi; ++j) {
+        if (j == i) continue;
+        float b[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) b[k] = __ldg(cbox + 6 * (size_t)j + k);
+        const float d = merged_area(a, b);
+        if (d < best) {  // j ascends: equal areas keep the smaller index
+            best = d;
+            bj = j;
+        }
+    }
+    nn[i] = bj;
+}
+
+// create[i] = 1 when cluster i starts a mutual pair (i < nn[i]); keep[i] = 0 for the partner.
+__global__ void k_ploc_flags(int m, const int32_t *__restrict__ nn, uint32_t *__restrict__ create,
+                             uint32_t *__restrict__ keep) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int j = nn[i];
+    const bool mutual = j >= 0 && j < m && nn[j] == i;
+    create[i] = (mutual && i < j) ? 1u : 0u;
+    keep[i] = (mutual && i > j) ? 0u : 1u;
+}
+
+__global__ void k_ploc_merge(int m, const int32_t *__restrict__ nn, const uint32_t *__restrict__ create,
+                             const uint32_t *__restrict__ rank, int next_free, float *__restrict__ cbox,
+                             int32_t *__restrict__ cid, float4 *__restrict__ nodes) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m || !create[i]) return;
+    const int j = nn[i];
+    const int node = next_free - (int)rank[i];
+    float a[6], b[6], u[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        a[k] = cbox[6 * (size_t)i + k];
+        b[k] = cbox[6 * (size_t)j + k];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        u[k] = fminf(a[k], b[k]);
+        u[3 + k] = fmaxf(a[3 + k], b[3 + k]);
+    }
+    write_node(nodes, node, a, b, cid[i], cid[j]);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) cbox[6 * (size_t)i + k] = u[k];
+    cid[i] = node;
+}
+
+__global__ void k_ploc_compact(int m, const uint32_t *__restrict__ keep, const uint32_t *__restrict__ pos,
+                               const float *__restrict__ cbox, const int32_t *__restrict__ cid,
+                               float *__restrict__ cbox2, int32_t *__restrict__ cid2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m || !keep[i]) return;
+    const uint32_t o = pos[i];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) cbox2[6 * (size_t)o + k] = cbox[6 * (size_t)i + k];
+    cid2[o] = cid[i];
+}
+
 }  // namespace
 
 size_t bvh_scratch_bytes(int n) { return bvh_scratch_bytes_c(n); }
@@ -494,6 +590,83 @@ cudaError_t bvh_build(const float *T, const uint32_t *type, const float *lad, in
     k_refit<<<grid, kThreads, 0, s>>>(n, b.parent_leaf, b.parent_int, b.child, b.leafbox, b.nodebox, b.flags,
                                       b.nodes, b.status);
     return cudaGetLastError();
+}
+
+// Exclusive scan of any length (tiles of kSortTile, sums scanned recursively); tmp holds
+// ploc_scan_tmp(count) words.
+static size_t scan_tmp_words(int count) {
+    size_t w = 64;
+    for (int c = count; c > kSortTile;) {
+        const int nb = (c + kSortTile - 1) / kSortTile;
+        w += 2 * (size_t)nb;
+        c = nb;
+    }
+    return w;
+}
+
+static cudaError_t scan_any(const uint32_t *in, uint32_t *out, int count, uint32_t *tmp, cudaStream_t s) {
+    const int nb = (count + kSortTile - 1) / kSortTile;
+    if (nb <= 1) {
+        k_scan_blocks<<<1, kThreads, 0, s>>>(in, out, count, nullptr);
+        return cudaGetLastError();
+    }
+    uint32_t *sums = tmp, *sums_scan = tmp + nb;
+    k_scan_blocks<<<nb, kThreads, 0, s>>>(in, out, count, sums);
+    cudaError_t e = scan_any(sums, sums_scan, nb, tmp + 2 * nb, s);
+    if (e != cudaSuccess) return e;
+    k_scan_add<<<nb, kThreads, 0, s>>>(out, count, sums_scan);
+    return cudaGetLastError();
+}
+
+size_t ploc_scratch_bytes(int n) {
+    const size_t nn = (size_t)(n > 1 ? n : 1);
+    return 2 * align256(nn * 6 * sizeof(float)) + 2 * align256(nn * sizeof(int32_t)) +
+           4 * align256(nn * sizeof(uint32_t)) + align256(scan_tmp_words(n) * sizeof(uint32_t));
+}
+
+cudaError_t ploc_build(const float *leafbox, int n, float4 *nodes, void *scratch, cudaStream_t s) {
+    if (n <= 1) return cudaSuccess;
+    const size_t nn = (size_t)n;
+    char *p = (char *)scratch;
+    auto take = [&](size_t bytes) {
+        char *r = p;
+        p += align256(bytes);
+        return (void *)r;
+    };
+    float *box[2] = {(float *)take(nn * 6 * sizeof(float)), (float *)take(nn * 6 * sizeof(float))};
+    int32_t *cid[2] = {(int32_t *)take(nn * sizeof(int32_t)), (int32_t *)take(nn * sizeof(int32_t))};
+    int32_t *nn_idx = (int32_t *)take(nn * sizeof(int32_t));
+    uint32_t *create = (uint32_t *)take(nn * sizeof(uint32_t));
+    uint32_t *rank = (uint32_t *)take(nn * sizeof(uint32_t));
+    uint32_t *keep = (uint32_t *)take(nn * sizeof(uint32_t));
+    uint32_t *tmp = (uint32_t *)take(scan_tmp_words(n) * sizeof(uint32_t));
+    uint32_t *pos = create;  // reused after the merge
+    k_ploc_init<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(n, leafbox, box[0], cid[0]);
+    int m = n, cur = 0, next_free = n - 2;
+    for (int iter = 0; m > 1; ++iter) {
+        if (iter > 4 * 1024) return cudaErrorInvalidValue;  // each round merges at least one pair
+        const int g = (m + kThreads - 1) / kThreads;
+        k_ploc_nn<<<g, kThreads, 0, s>>>(m, box[cur], nn_idx);
+        k_ploc_flags<<<g, kThreads, 0, s>>>(m, nn_idx, create, keep);
+        cudaError_t e = scan_any(create, rank, m, tmp, s);
+        if (e != cudaSuccess) return e;
+        uint32_t h[2];  // merges this round: last rank + last flag
+        if ((e = cudaMemcpyAsync(&h[0], rank + (m - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            return e;
+        if ((e = cudaMemcpyAsync(&h[1], create + (m - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            return e;
+        k_ploc_merge<<<g, kThreads, 0, s>>>(m, nn_idx, create, rank, next_free, box[cur], cid[cur], nodes);
+        if ((e = scan_any(keep, pos, m, tmp, s)) != cudaSuccess) return e;
+        k_ploc_compact<<<g, kThreads, 0, s>>>(m, keep, pos, box[cur], cid[cur], box[1 - cur], cid[1 - cur]);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+        const int merged = (int)(h[0] + h[1]);
+        if (merged <= 0) return cudaErrorInvalidValue;
+        next_free -= merged;
+        m -= merged;
+        cur = 1 - cur;
+    }
+    return next_free == -1 ? cudaSuccess : cudaErrorInvalidValue;
 }
 
 }  // namespace hrt

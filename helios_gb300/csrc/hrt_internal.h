@@ -168,6 +168,11 @@ constexpr size_t bvh_scratch_bytes_c(int n) {
 size_t bvh_scratch_bytes(int n);
 void bvh_carve(BvhBuffers &b, void *scratch, int n);
 // Compressed 4-wide BVH collapsed from the binary nodes (hrt_bvh4.cu): nodes4 holds
+// Binary BVH over the LBVH's leaf slots by locally-ordered agglomerative clustering (better
+// surface-area cost than the Morton split; the 4-wide nodes are collapsed from it).  leafbox:
+// [n*6] padded leaf boxes of bvh_build; nodes: [n-1] binary nodes, root 0; n >= 2.
+size_t ploc_scratch_bytes(int n);
+cudaError_t ploc_build(const float *leafbox, int n, float4 *nodes, void *scratch, cudaStream_t s);
 // max(n-1,1) * 4 float4, scratch bvh4_scratch_bytes(n); *count_out = nodes written.
 size_t bvh4_scratch_bytes(int n);
 cudaError_t bvh4_build(const float4 *nodes2, int n, float4 *nodes4, void *scratch, uint32_t *status, int *count_out,
