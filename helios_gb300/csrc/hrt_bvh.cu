@@ -428,7 +428,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // survivors are compacted in order; repeat until one cluster is left.  Node indices are
 // handed out from n-2 downwards by a prefix sum, so the root is node 0 and the tree does not
 // depend on scheduling.  The leaves are the same record slots as the LBVH's.
-constexpr int kPlocRadius = 16;
+constexpr int kPlocRadius = 32;
 
 __device__ __forceinline__ float merged_area(const float *a, const float *b) {
     const float dx = fmaxf(a[3], b[3]) - fminf(a[0], b[0]);
