@@ -1,4 +1,4 @@
-// hrt_bvh4.cu -- compressed 4-wide BVH from the binary LBVH.
+// hrt_bvh4.cu -- compressed 4-wide BVH from a binary BVH (the clustered tree of ploc_build).
 //
 // The diffuse trace is bound by L1 traffic of node fetches (64 B per visit of a binary
 // node).  A 4-wide node with 8-bit child boxes (node format in hrt_device.cuh) is also
