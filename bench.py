@@ -35,8 +35,8 @@ METRIC = "rays/s and solves/s (batched/served vs plain, 1 GB300) at <=1e-4 flux 
 UNIT = "rays/s"
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the 4-wide persistent diffuse
 # kernel on the orchard (1 M triangles, 3 bands, 450 M rays per launch): mean of three
-# captured launches, 2.343 GB + 0.086 GB (profiles/k_diffuse_ps_wide4_orchard-1M_traffic.md)
-TRAFFIC_PER_LAUNCH = 2.429e9
+# captured launches, 2.490 GB + 0.091 GB (profiles/k_diffuse_ps_wide4_orchard-1M_traffic.md)
+TRAFFIC_PER_LAUNCH = 2.581e9
 
 
 def peaks():
@@ -333,6 +333,10 @@ def stress_model(scale=1.0, device=0):
     return rad, sc
 
 
+# kernel variants by the tuner's names (hrt_set_tuning: 16 + v forces variant v)
+TUNER_VARIANTS = {"binary4": 1, "binary3": 2, "simple": 3, "wide4": 4, "wide4-3": 5}
+
+
 def run_stress(args, stream, device=0):
     """One timed solve of the deep-scattering stress workload (after one untimed solve)."""
     import torch
@@ -355,10 +359,14 @@ def run_stress(args, stream, device=0):
     t = ev0.elapsed_time(ev1) / 1e3
     st = ctx.last_stats()
     tuning = [x for x in ctx.tuning_report().splitlines() if x.startswith("accumulate")]
-    # traversal counts (untimed) on the same workload scaled to 5 % of the primitives
+    # traversal counts (untimed) on the same workload scaled to 5 % of the primitives, with
+    # the kernel variant and tree the tuner chose for the full workload
     small, _ = stress_model(0.05 * args.stress_scale, device=device)
     small.setSeed(99)
     small.updateGeometry()
+    chosen = tuning[-1].rsplit("-> ", 1)[-1].strip() if tuning else ""
+    if chosen in TUNER_VARIANTS:
+        small.ctx.set_tuning(16 + TUNER_VARIANTS[chosen])
     small.ctx.set_measure(1)
     small.ctx.run_band(small.solve_description(["NIR"]), out=False)
     meas = small.ctx.get_measure()
@@ -370,7 +378,8 @@ def run_stress(args, stream, device=0):
             "primitives": int(sc.n), "s_per_solve": t, "rays_per_solve": st["rays"], "rays_per_s": st["rays"] / t,
             "scattering_iterations": st["iterations"], "kernels": st["kernels"], "setup_build_s": t_build,
             "node_visits_per_ray_5pct": meas["node_visits"] / small_rays,
-            "prim_tests_per_ray_5pct": meas["prim_tests"] / small_rays, "autotune": tuning}
+            "prim_tests_per_ray_5pct": meas["prim_tests"] / small_rays, "counted_variant": chosen,
+            "autotune": tuning}
 
 
 def run_gpu(args):

@@ -502,7 +502,7 @@ int tuned_variant(hrt_context *ctx, const DiffuseParams &P0, bool record, int *v
         if (!(record && v == DV_SIMPLE)) *variant = v;
         return HRT_OK;
     }
-    if (!ctx->tune || rays < kTuneMinRays || (ctx->measure & 1)) return HRT_OK;
+    if (!ctx->tune || rays < kTuneMinRays) return HRT_OK;
     char key[160];
     std::snprintf(key, sizeof key, "%s n=%d count=%u rays_per_face=%d faces=%d bands=%d voxels=%d",
                   record ? "record" : "accumulate", ctx->n, P0.count, P0.dimx * P0.dimy, P0.faces, P0.Bc,
@@ -512,6 +512,7 @@ int tuned_variant(hrt_context *ctx, const DiffuseParams &P0, bool record, int *v
         *variant = it->second;
         return HRT_OK;
     }
+    if (ctx->measure & 1) return HRT_OK;  // statistics launches count on a tuned choice, never time one
     std::vector<int> cand;
     const bool w4 = P0.sc.nodes4 != nullptr;
     if (record) cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_PS3, DV_PS4} : std::vector<int>{DV_PS3, DV_PS4};
@@ -611,7 +612,7 @@ int diffuse_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp
     CU(timed_launch(ctx, 1, [&] {
         if (cov) return launch_diffuse_glass(P, max_blocks(ctx), ctx->stream);
         return (ctx->measure & 1)
-                   ? launch_diffuse_stats(P, (ctx->measure & 4) ? DV_SIMPLE : DV_DEFAULT, max_blocks(ctx), ctx->stream)
+                   ? launch_diffuse_stats(P, (ctx->measure & 4) ? DV_SIMPLE : variant, max_blocks(ctx), ctx->stream)
                                   : launch_diffuse_variant(P, variant, max_blocks(ctx), ctx->stream);
     }));
     EpilogueParams E{};

@@ -341,6 +341,31 @@ __device__ __forceinline__ float q_float(uint32_t w, int k) {
     return __uint_as_float(__byte_perm(w, 0x4B000000u, (uint32_t)k | 0x7540u)) - 8388608.0f;
 }
 
+// Packed FP32 pairs (PTX .f32x2 on sm_100 and later): one instruction applies the same
+// IEEE operation (round to nearest) to both halves of a 64-bit register pair.
+__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(unsigned long long r, float *lo, float *hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(*lo), "=f"(*hi) : "l"(r));
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b, unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// Byte k of w as the float 2^23 + q (q_float before its subtraction).
+__device__ __forceinline__ float q_biased(uint32_t w, int k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, (uint32_t)k | 0x7540u));
+}
+
 // Leaf-box padding: each face moves out by (|x| + extent) * 2^-20.
 __device__ __forceinline__ float pad_lo(float x, float ext) { return x - (fabsf(x) + ext) * 9.5367431640625e-07f; }
 __device__ __forceinline__ float pad_hi(float x, float ext) { return x + (fabsf(x) + ext) * 9.5367431640625e-07f; }

@@ -719,7 +719,7 @@ static cudaError_t diffuse_impl(const DiffuseParams &p, int variant, int max_blo
     if ((variant == DV_W4 || variant == DV_W43) && !p.sc.nodes4) variant = DV_PS4;
     if (p.fetch && variant != DV_SIMPLE) {
         if (STATS) {
-            if (p.Bc <= 4 && variant == DV_W4) return launch_ps_stats(p, s);
+            if (p.Bc <= 4 && (variant == DV_W4 || variant == DV_W43)) return launch_ps_stats(p, s);
         } else if (p.sc.voxels) {
             return launch_ps_voxels(p, variant, s);
         } else {

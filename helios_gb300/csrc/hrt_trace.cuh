@@ -529,13 +529,19 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
                 // leaf-box padding, so no box holding an accepted hit is culled.
                 const float ax = inv.x * sx, ay = inv.y * sy, az = inv.z * sz;
                 const float bx = (q0.x - o.x) * inv.x, by = (q0.y - o.y) * inv.y, bz = (q0.z - o.z) * inv.z;
+                // near and far plane of one axis as one packed pair: the same two subtractions
+                // (exact) and fused multiply-adds as the scalar form, in half the instructions
+                const unsigned long long bias = f2_pack(8388608.0f, 8388608.0f);
+                const unsigned long long ax2 = f2_pack(ax, ax), ay2 = f2_pack(ay, ay), az2 = f2_pack(az, az);
+                const unsigned long long bx2 = f2_pack(bx, bx), by2 = f2_pack(by, by), bz2 = f2_pack(bz, bz);
                 float tk[4];
                 int32_t ck[4];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const float tnx = __fmaf_rn(q_float(nx, k), ax, bx), tfx = __fmaf_rn(q_float(fx, k), ax, bx);
-                    const float tny = __fmaf_rn(q_float(ny, k), ay, by), tfy = __fmaf_rn(q_float(fy, k), ay, by);
-                    const float tnz = __fmaf_rn(q_float(nz, k), az, bz), tfz = __fmaf_rn(q_float(fz, k), az, bz);
+                    float tnx, tfx, tny, tfy, tnz, tfz;
+                    f2_unpack(f2_fma(f2_sub(f2_pack(q_biased(nx, k), q_biased(fx, k)), bias), ax2, bx2), &tnx, &tfx);
+                    f2_unpack(f2_fma(f2_sub(f2_pack(q_biased(ny, k), q_biased(fy, k)), bias), ay2, by2), &tny, &tfy);
+                    f2_unpack(f2_fma(f2_sub(f2_pack(q_biased(nz, k), q_biased(fz, k)), bias), az2, bz2), &tnz, &tfz);
                     const float tn = fmax3(tnx, tny, fmaxf(tnz, 1e-4f));
                     const float tf = fmin3(tfx, tfy, fminf(tfz, best));
                     const bool hit = cref[k] != kEmptyChild && tn <= tf;

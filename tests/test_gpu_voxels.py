@@ -129,6 +129,32 @@ def test_stress_flux_vs_oracle(oracle_mod, tol):
     assert worst <= FLUX_RTOL, worst
 
 
+def test_stress_variants_agree(oracle_mod):
+    """On a scene with voxels every diffuse-kernel variant (persistent over binary nodes,
+    one ray per thread, persistent over compressed 4-wide nodes) gives the oracle's fluxes
+    and ray count, and the statistics launches count on the forced variant's tree (the
+    binary and 4-wide node-visit counts differ)."""
+    sc = _stress()
+    visits = {}
+    for variant in (1, 3, 4):
+        rad = _stress_model(sc, depth=6)
+        rad.ctx.set_tuning(16 + variant)
+        rad.setSeed(23)
+        got = rad.runBand("NIR")
+        rays = rad.last_stats["rays"]
+        rad.ctx.set_measure(1)
+        rad.setSeed(23)
+        rad.runBand("NIR")
+        visits[variant] = rad.ctx.get_measure()["node_visits"]
+        rad.ctx.set_measure(0)
+        ref, st = run_oracle(rad, ["NIR"], oracle_mod, seed=23)
+        assert rays == st["rays"]
+        worst = _flux_close(got, ref)
+        assert worst <= FLUX_RTOL, (variant, worst)
+        assert rad.ctx.device_status() == 0
+    assert visits[1] > 0 and visits[4] > 0 and visits[1] != visits[4]
+
+
 def test_stress_backend_sequence_matches_device():
     """The RayTracingBackend-shaped call sequence gives the device solve's numbers on a
     scene with disks and voxels (fixed depth: that sequence has no residual stop)."""
