@@ -90,6 +90,42 @@ inline U4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0
 }
 inline float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
 
+// ------------------------------------------------- reference random numbers ---
+// Statistical parity only (orc_set_rng(1)): the reference seeds each ray's stream with
+// TEA, 16 rounds (Wheeler & Needham, FSE 1994; the reference's keys), of (ray index,
+// launch seed) and draws 24-bit uniforms from a linear congruential generator with the
+// Numerical Recipes constants (OptiX8DeviceCode.cu:29-49; per-ray seeding :1232, :1497).
+// The four uniforms of one call are four consecutive draws of that stream, consumed in the
+// reference's order (direction jitter, then origin).  The reference's launch seed comes from
+// the wall clock (RadiationModel.cpp:3961); here it is TEA of (seed, pass, counter words),
+// and the ray index is TEA-mixed from (ray, primitive).
+int g_rng_mode = 0;  // 0 Philox (the product's stream), 1 reference TEA + LCG
+
+inline uint32_t tea16(uint32_t a, uint32_t b) {
+    uint32_t sum = 0;
+    for (int round = 0; round < 16; ++round) {
+        sum += 0x9E3779B9u;
+        a += ((b << 4) + 0xA341316Cu) ^ (b + sum) ^ ((b >> 5) + 0xC8013EA4u);
+        b += ((a << 4) + 0xAD90777Du) ^ (a + sum) ^ ((a >> 5) + 0x7E95761Eu);
+    }
+    return a;
+}
+
+inline uint32_t lcg24(uint32_t *state) {
+    *state = 1664525u * *state + 1013904223u;
+    return *state & 0x00FFFFFFu;
+}
+
+// Four uniforms for counter (c0 ray, c1 primitive, c2, c3) and key (k0 seed, k1 pass).
+inline U4 draw(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1) {
+    if (g_rng_mode == 0) return philox(c0, c1, c2, c3, k0, k1);
+    const uint32_t launch = tea16(tea16(k0, k1), tea16(c2, c3));
+    uint32_t st = tea16(tea16(c0, c1), launch);
+    U4 u;
+    for (int k = 0; k < 4; ++k) u.v[k] = lcg24(&st) << 8;  // u01 keeps the top 24 bits
+    return u;
+}
+
 // cos(2*pi*u), sin(2*pi*u) for u in [0,1): quadrant/octant reduction and
 // Taylor polynomials on [0, pi/4] (coefficients are 1/k!), evaluated in a fixed order.
 inline void sincos2pi(float u, float *c_out, float *s_out) {
@@ -432,7 +468,7 @@ inline bool voxel_hit(const Ray &ray, const V3 &inv, const Rec &r, uint32_t vid,
                          std::fmax(std::fmin(t0z, t1z), ray.tmin));
     float tf = std::fmin(std::fmin(std::fmax(t0x, t1x), std::fmax(t0y, t1y)), std::fmax(t0z, t1z));
     if (!(tn < tf)) return false;
-    U4 u = philox(ray.key.c0, ray.key.c1, ray.key.c2, vid + 1u, ray.key.k0, ray.key.k1);
+    U4 u = draw(ray.key.c0, ray.key.c1, ray.key.c2, vid + 1u, ray.key.k0, ray.key.k1);
     float s = -ln_unit(1.0f - u01(u.v[0])) / r.k;
     float t = tn + s;
     if (!(t < tf) || !(t <= tmax)) return false;
@@ -1192,7 +1228,7 @@ inline void mask_origin(const Masks *mk, int type, uint32_t r, uint32_t p, uint3
             patch_uv(*mk, (int)p, *uu - 0.5f, *vv - 0.5f, &fu, &fv);
         }
         if (mask_opaque(*mk, mk->id[p], fu, fv)) return;
-        U4 q = philox(r, p, c2, 0x80000000u | (a + 1u), seed, pass);
+        U4 q = draw(r, p, c2, 0x80000000u | (a + 1u), seed, pass);
         *uu = u01(q.v[0]);
         *vv = u01(q.v[1]);
     }
@@ -1207,7 +1243,7 @@ inline V3 direct_origin(const RGen &g, int type, uint32_t r, uint32_t p, uint32_
         vv = ((float)yi + vv) / (float)dimy;
     }
     mask_origin(mk, type, r, p, c2, seed, pass, &uu, &vv);
-    if (type == PT_VOXEL) ww = u01(philox(r, p, c2 | 1u, 0u, seed, pass).v[0]);
+    if (type == PT_VOXEL) ww = u01(draw(r, p, c2 | 1u, 0u, seed, pass).v[0]);
     return sample_point(g, type, uu, vv, ww);
 }
 
@@ -1220,12 +1256,12 @@ inline void diffuse_ray(const RGen &g, int type, uint32_t r, uint32_t p, int fac
     int ti = (int)(r % (uint32_t)dimx), pi = (int)(r / (uint32_t)dimx);
     V3 dd;
     if (type == PT_VOXEL) {
-        U4 u = philox(r, p, 1u, 0u, seed, pass);
-        U4 uw = philox(r, p, 2u, 0u, seed, pass);
+        U4 u = draw(r, p, 1u, 0u, seed, pass);
+        U4 uw = draw(r, p, 2u, 0u, seed, pass);
         dd = voxel_dir(ti, pi, dimx, dimy, u01(u.v[0]), u01(u.v[1]));
         *org = sample_point(g, type, u01(u.v[2]), u01(u.v[3]), u01(uw.v[0]));
     } else {
-        U4 u = philox(r, p, (uint32_t)face, 0u, seed, pass);
+        U4 u = draw(r, p, (uint32_t)face, 0u, seed, pass);
         dd = diffuse_dir(g.N, ti, pi, dimx, dimy, u01(u.v[0]), u01(u.v[1]));
         float uu = u01(u.v[2]), vv = u01(u.v[3]);
         mask_origin(mk, type, r, p, (uint32_t)face, seed, pass, &uu, &vv);
@@ -1296,7 +1332,7 @@ inline V3 mrot(const float M[9], V3 v) {
 inline void camera_ray(const Cam &c, uint32_t ii, uint32_t jj, uint32_t smp, bool centre, V3 *o, V3 *d) {
     float rx = 0.5f, ry = 0.5f, lx = 0.f, ly = 0.f;
     if (!centre) {
-        U4 u = philox(jj * (uint32_t)c.W + ii, smp, kCamCounter, 0u, c.seed, c.id);
+        U4 u = draw(jj * (uint32_t)c.W + ii, smp, kCamCounter, 0u, c.seed, c.id);
         rx = u01(u.v[0]);
         ry = u01(u.v[1]);
         if (c.lens > 0.f) concentric(u01(u.v[2]), u01(u.v[3]), &lx, &ly);
@@ -1548,6 +1584,13 @@ void *orc_scene_create(const orc_geometry *g) {
 void orc_scene_destroy(void *h) { delete (Scene *)h; }
 
 // Philox4x32-10 block (for known-answer tests).
+// Random-number stream of the ray generators: 0 Philox (default), 1 the reference's TEA + LCG.
+int orc_set_rng(int mode) {
+    if (mode != 0 && mode != 1) return -1;
+    g_rng_mode = mode;
+    return 0;
+}
+
 void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
     U4 u = philox(ctr[0], ctr[1], ctr[2], ctr[3], key[0], key[1]);
     for (int i = 0; i < 4; ++i) out[i] = u.v[i];
@@ -1691,7 +1734,7 @@ int orc_gen_rays(void *h, int kind, uint32_t seed, uint32_t pass, int32_t rpp, i
         for (int r = 0; r < nr; ++r) {
             V3 org, dir;
             if (kind == 0) {
-                U4 u = philox((uint32_t)r, (uint32_t)p, (uint32_t)face, 0u, seed, pass);
+                U4 u = draw((uint32_t)r, (uint32_t)p, (uint32_t)face, 0u, seed, pass);
                 org = direct_origin(g, (int)s->type[p], (uint32_t)r, (uint32_t)p, (uint32_t)face, dimx, dimy, seed,
                                     pass, u, s->mk());
                 dir = vnormalize(v3(dir3[0], dir3[1], dir3[2]));
@@ -1810,7 +1853,7 @@ int orc_run_band(void *h, const orc_solve *q, double *flux_out, uint64_t *stats)
             for (int r = 0; r < dimx * dimy; ++r) {
                 for (int k = 0; k < S; ++k) {
                     const uint32_t c2 = (uint32_t)(k << 1);
-                    U4 u = philox((uint32_t)r, (uint32_t)p, c2, 0u, q->seed, 0u);
+                    U4 u = draw((uint32_t)r, (uint32_t)p, c2, 0u, q->seed, 0u);
                     V3 org = direct_origin(g, type, (uint32_t)r, (uint32_t)p, c2, dimx, dimy, q->seed, 0u, u, s->mk());
                     V3 dir;
                     float tmax;

@@ -126,6 +126,7 @@ def _load():
                                       C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_run_band.argtypes = [C.c_void_p, C.POINTER(_Solve), C.c_void_p, C.c_void_p]
         _lib.orc_philox.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_set_rng.argtypes = [C.c_int]
         _lib.orc_sincos2pi.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_ln_unit.argtypes = [C.c_int64, C.c_void_p, C.c_void_p]
         _lib.orc_glass_trs.argtypes = [C.c_int64, C.c_void_p, C.c_float, C.c_float, C.c_void_p]
@@ -307,6 +308,21 @@ class OracleScene:
         if cams:
             st["cameras"] = cam_out
         return flux, st
+
+
+class reference_rng:
+    """Context manager: the ray generators draw from the reference's random-number stream
+    (TEA-16 seeded 24-bit LCG per ray, OptiX8DeviceCode.cu:29-49) instead of Philox.  Results
+    then agree with the product only in distribution (statistical parity)."""
+
+    def __enter__(self):
+        if _load().orc_set_rng(1):
+            raise RuntimeError("orc_set_rng failed")
+        return self
+
+    def __exit__(self, *exc):
+        _load().orc_set_rng(0)
+        return False
 
 
 def philox(ctr, key):

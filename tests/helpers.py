@@ -114,3 +114,19 @@ def run_device_cameras(rad, labels, seed):
         pix = np.stack([cam["pixels"][b].reshape(H, W) for b in bands], axis=-1)
         cams[label] = {"pixels": pix, "labels": cam["labels"].reshape(H, W), "depths": cam["depths"].reshape(H, W)}
     return flux, cams
+
+
+def ensemble(solve, seeds):
+    """[K, n] fluxes of solve(seed) over the seeds (first band)."""
+    return np.stack([np.asarray(solve(s), np.float64)[:, 0] for s in seeds])
+
+
+def z_scores(a, b, floor_frac=1e-3):
+    """Per-primitive difference of the ensemble means of a and b [K, n] in units of its
+    standard error; primitives whose mean flux is below floor_frac of the average, or whose
+    samples do not vary, are left out."""
+    ka, kb = a.shape[0], b.shape[0]
+    ma, mb = a.mean(0), b.mean(0)
+    se = np.sqrt(a.var(0, ddof=1) / ka + b.var(0, ddof=1) / kb)
+    keep = (np.abs(0.5 * (ma + mb)) > floor_frac * np.abs(0.5 * (ma + mb)).mean()) & (se > 0)
+    return (ma - mb)[keep] / se[keep]
