@@ -82,6 +82,9 @@ struct DiffuseParams {
     uint32_t lane_budget;      // persistent kernel: rays a lane takes before its block retires
                                // (0 = no limit: one resident wave of blocks runs to the end)
     uint32_t *hits;            // record mode: hit code per ray id, else unused
+    int refill = 0;            // persistent kernel: a warp leaves its node loop to give idle lanes new
+                               // rays when fewer than this many lanes are still in it (0: never);
+                               // set by the launcher
     GlassParams gl;            // launches with covers (sc.cover non-null)
 };
 

@@ -22,7 +22,9 @@ cudaError_t ps_launch(const DiffuseParams &p, cudaStream_t s) {
     }
     cudaError_t e = cudaMemsetAsync(p.fetch, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
-    k_diffuse_ps<NB, RECORD, MINB, VOX, W4, STATS><<<ps_grid(p, sms * blocks_per_sm), kBlock, 0, s>>>(p);
+    DiffuseParams q = p;
+    q.refill = refill_threshold(VOX);
+    k_diffuse_ps<NB, RECORD, MINB, VOX, W4, STATS><<<ps_grid(q, sms * blocks_per_sm), kBlock, 0, s>>>(q);
     return cudaGetLastError();
 }
 
