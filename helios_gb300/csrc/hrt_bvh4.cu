@@ -128,9 +128,12 @@ __global__ void __launch_bounds__(kThreads4) k_collapse(int n2count, const float
     }
     uint32_t wlo[3] = {0, 0, 0}, whi[3] = {0, 0, 0};
     int32_t outref[4] = {kEmptyChild, kEmptyChild, kEmptyChild, kEmptyChild};
-    for (int k = 0; k < cnt; ++k) {
-        const int32_t c = ref[k];
-        if (c == kEmptyChild) continue;
+    for (int k = 0; k < 4; ++k) {
+        const int32_t c = k < cnt ? ref[k] : kEmptyChild;
+        if (c == kEmptyChild) {  // inverted box: lo bytes 255, hi bytes 0
+            for (int a = 0; a < 3; ++a) wlo[a] |= 0xFFu << (8 * k);
+            continue;
+        }
         for (int a = 0; a < 3; ++a) {
             wlo[a] |= quant_lo(lo[a], box[k].lo[a], s[a]) << (8 * k);
             whi[a] |= quant_hi(lo[a], box[k].hi[a], s[a]) << (8 * k);

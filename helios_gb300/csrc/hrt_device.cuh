@@ -316,6 +316,10 @@ __device__ __forceinline__ f3 sample_point(const float4 g[4], uint32_t type, flo
 //   q1 = (lox, loy, loz, hix)   quantised child boxes, byte k = child k (0 <= q <= 255)
 //   q2 = (hiy, hiz, c0, c1)     child refs c_k: >= 0 node, ~slot leaf, kEmptyChild none
 //   q3 = (c2, c3, 0, 0)
+// An empty child slot has lo bytes 255 and hi bytes 0: an inverted box that no ray enters.
+// On every axis the slab slope a = inv * s is nonzero (|inv| >= 1 for a unit direction,
+// s >= 2^-126), so the near plane lies beyond the far plane; an infinite slope gives a NaN
+// plane, which the min/max skip, and an infinite near or far plane, which fails the test.
 // Child k's box per axis: [p + lo_k * s, p + hi_k * s] in FP32 (q * s is exact; one rounded
 // add).  The build picks the bytes so that these values enclose the child's FP32 box (itself
 // padded), so a slab test on the decoded box never culls an accepted hit (after Ylitie,

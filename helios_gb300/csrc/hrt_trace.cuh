@@ -562,7 +562,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
                     f2_unpack(f2_fma(f2_sub(f2_pack(q_biased(nz, k), q_biased(fz, k)), bias), az2, bz2), &tnz, &tfz);
                     const float tn = fmax3(tnx, tny, fmaxf(tnz, 1e-4f));
                     const float tf = fmin3(tfx, tfy, fminf(tfz, best));
-                    const bool hit = cref[k] != kEmptyChild && tn <= tf;
+                    const bool hit = tn <= tf;  // empty slots hold inverted boxes
                     tk[k] = hit ? tn : INFINITY;
                     ck[k] = hit ? cref[k] : kSentinel;
                 }
