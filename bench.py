@@ -35,8 +35,8 @@ METRIC = "rays/s and solves/s (batched/served vs plain, 1 GB300) at <=1e-4 flux 
 UNIT = "rays/s"
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the 4-wide persistent diffuse
 # kernel on the orchard (1 M triangles, 3 bands, 450 M rays per launch): mean of three
-# captured launches, 2.450 GB + 0.088 GB (profiles/k_diffuse_ps_wide4_orchard-1M_traffic.md)
-TRAFFIC_PER_LAUNCH = 2.538e9
+# captured launches, 2.460 GB + 0.091 GB (profiles/k_diffuse_ps_wide4_orchard-1M_traffic.md)
+TRAFFIC_PER_LAUNCH = 2.551e9
 
 
 def peaks():
