@@ -629,12 +629,11 @@ size_t ploc_scratch_bytes(int n) {
 }
 
 static int ploc_radius() {
-    static int v = 0;
-    if (v == 0) {
+    static const int v = [] {  // initialised once, thread-safe
         const char *e = getenv("HRT_PLOC_RADIUS");
-        v = e ? atoi(e) : kPlocRadius;
-        if (v < 1 || v > 256) v = kPlocRadius;
-    }
+        const int r = e ? atoi(e) : kPlocRadius;
+        return (r < 1 || r > 256) ? kPlocRadius : r;
+    }();
     return v;
 }
 

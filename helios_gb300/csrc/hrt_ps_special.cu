@@ -11,20 +11,20 @@ namespace {
 
 template <int NB, bool RECORD, int MINB, bool VOX, bool W4, bool STATS>
 cudaError_t ps_launch(const DiffuseParams &p, cudaStream_t s) {
-    static int blocks_per_sm = 0, sms = 0;
-    if (blocks_per_sm == 0) {
-        int dev = 0;
+    // resident blocks of one wave (SMs x blocks per SM); initialised once per instantiation,
+    // thread-safe (the server launches from several threads)
+    static const int resident = [] {
+        int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_diffuse_ps<NB, RECORD, MINB, VOX, W4, STATS>,
-                                                      kBlock, 0);
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
-    }
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_diffuse_ps<NB, RECORD, MINB, VOX, W4, STATS>, kBlock, 0);
+        return (sms < 1 ? 1 : sms) * (per_sm < 1 ? 1 : per_sm);
+    }();
     cudaError_t e = cudaMemsetAsync(p.fetch, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     DiffuseParams q = p;
     q.refill = refill_threshold(VOX);
-    k_diffuse_ps<NB, RECORD, MINB, VOX, W4, STATS><<<ps_grid(q, sms * blocks_per_sm), kBlock, 0, s>>>(q);
+    k_diffuse_ps<NB, RECORD, MINB, VOX, W4, STATS><<<ps_grid(q, resident), kBlock, 0, s>>>(q);
     return cudaGetLastError();
 }
 

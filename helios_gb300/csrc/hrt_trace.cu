@@ -702,11 +702,10 @@ static cudaError_t direct_impl(const DirectParams &p, int max_blocks, cudaStream
 // Default diffuse variant: the persistent 4-wide traversal; HRT_TRAVERSAL=simple selects
 // the one-ray-per-thread kernel and HRT_TRAVERSAL=bvh2 the persistent binary traversal.
 static int default_variant() {
-    static int v = -1;
-    if (v < 0) {
+    static const int v = [] {  // initialised once, thread-safe
         const char *e = getenv("HRT_TRAVERSAL");
-        v = (e && e[0] == 's') ? DV_SIMPLE : ((e && e[0] == 'b') ? DV_PS4 : DV_W4);
-    }
+        return (e && e[0] == 's') ? DV_SIMPLE : ((e && e[0] == 'b') ? DV_PS4 : DV_W4);
+    }();
     return v;
 }
 
