@@ -464,9 +464,11 @@ def run_gpu(args):
     hbm, peak_kind = peaks()
     # algorithmic bytes of the diffuse kernel (dominant): per ray 64 B per node visit,
     # 48 B per primitive test, origin record 64 B, per-band gather 4 B on hits and 8 B accumulate;
-    # per launch: the mean bytes per ray of the statistics solve x the rays of one diffuse launch
-    alg_bytes_total = 64.0 * stats["node_visits"] + 48.0 * stats["prim_tests"] + rays_per_step * (64 + 4 * 3)
-    bytes_per_ray = alg_bytes_total / max(rays_per_step, 1)
+    # per launch: the mean bytes per diffuse ray of the statistics solve (visits and tests of
+    # its diffuse launches only) x the rays of one diffuse launch
+    diffuse_rays = max(stats["diffuse_rays"], 1)
+    bytes_per_ray = (64.0 * stats["diffuse_node_visits"] + 48.0 * stats["diffuse_prim_tests"]) / diffuse_rays \
+        + (64 + 4 * 3)
     rays_per_launch = stats["diffuse_rays"] / max(stats["diffuse_launches"], 1)
     diff_ms = meas["diffuse_ms"] / max(meas["diffuse_launches"], 1)
     diff_share = meas["diffuse_ms"] / max(meas["diffuse_ms"] + meas["direct_ms"], 1e-9)
@@ -496,7 +498,9 @@ def run_gpu(args):
                      "kernel_ms": diff_ms, "kernel_share": diff_share, "bytes_per_launch": bytes_per_launch,
                      "rays_per_launch": rays_per_launch,
                      "node_visits_per_ray": stats["node_visits"] / max(rays_per_step, 1),
-                     "prim_tests_per_ray": stats["prim_tests"] / max(rays_per_step, 1)},
+                     "prim_tests_per_ray": stats["prim_tests"] / max(rays_per_step, 1),
+                     "diffuse_node_visits_per_ray": stats["diffuse_node_visits"] / diffuse_rays,
+                     "diffuse_prim_tests_per_ray": stats["diffuse_prim_tests"] / diffuse_rays},
         "autotune": [x for x in ctx.tuning_report().splitlines() if x.startswith("accumulate")],
         "clocks": clk.summary(),
         "e2e": {"value": rays_per_step / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

@@ -665,11 +665,12 @@ class Context:
         self.check(self.lib.hrt_set_measure(self.h, int(flags)))
 
     def get_measure(self):
-        out = np.zeros(8, np.float64)
-        self.check(self.lib.hrt_get_measure(self.h, ptr(out), 8))
+        out = np.zeros(10, np.float64)
+        self.check(self.lib.hrt_get_measure(self.h, ptr(out), 10))
         return {"direct_launches": int(out[0]), "direct_ms": float(out[1]), "diffuse_launches": int(out[2]),
                 "diffuse_ms": float(out[3]), "node_visits": int(out[4]), "prim_tests": int(out[5]),
-                "direct_rays": int(out[6]), "diffuse_rays": int(out[7])}
+                "direct_rays": int(out[6]), "diffuse_rays": int(out[7]), "diffuse_node_visits": int(out[8]),
+                "diffuse_prim_tests": int(out[9])}
 
     def device_status(self, reset=True):
         st = C.c_uint32()

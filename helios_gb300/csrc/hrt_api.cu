@@ -136,7 +136,7 @@ struct hrt_context {
         cudaEvent_t a, b;
     };
     std::vector<Timed> timed;
-    double meas[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double meas[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     // batched sweep: inputs, accumulators, recorded hits and the captured graph
     DevBuf sw_in, sw_mat, sw_acc, sw_out, sw_hits;
     cudaGraphExec_t sw_exec = nullptr;
@@ -227,14 +227,21 @@ int max_blocks(hrt_context *ctx) { return ctx->sms * 8; }
 template <class F>
 cudaError_t timed_launch(hrt_context *ctx, int kind, F &&launch) {
     if (ctx->measure & 1) {
-        unsigned long long a = 0, b = 0;
+        // rays, node visits and primitive tests of this launch: counters before and after
+        unsigned long long a = 0, b = 0, va[2] = {0, 0}, vb[2] = {0, 0};
         cudaError_t e = cudaMemcpyAsync(&a, ctx->counter.p, sizeof a, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(va, ctx->visits.p, sizeof va, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = launch();
         if (e == cudaSuccess) e = cudaMemcpyAsync(&b, ctx->counter.p, sizeof b, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(vb, ctx->visits.p, sizeof vb, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) return e;
         ctx->meas[kind == 0 ? 0 : 2] += 1.0;
         ctx->meas[kind == 0 ? 6 : 7] += (double)(b - a);
+        if (kind != 0) {
+            ctx->meas[8] += (double)(vb[0] - va[0]);
+            ctx->meas[9] += (double)(vb[1] - va[1]);
+        }
         return cudaSuccess;
     }
     if (!(ctx->measure & 2)) return launch();
@@ -445,6 +452,7 @@ int direct_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp,
         P.gl.Gcov = ctx->Gcov.as<double>();
         P.gl.src_flux = ctx->src_flux.as<float>();
     }
+    if (ctx->measure & 4) P.sc.nodes4 = nullptr;  // counting on the binary tree, as the oracle does
     CU(timed_launch(ctx, 0, [&] {
         if (cov) return launch_direct_glass(P, max_blocks(ctx), ctx->stream);
         return (ctx->measure & 1) ? launch_direct_stats(P, max_blocks(ctx), ctx->stream)
@@ -1974,7 +1982,7 @@ int hrt_get_measure(hrt_context *ctx, double *out, int count) {
     if (ctx->visits.p) CU(cudaMemcpy(v, ctx->visits.p, sizeof v, cudaMemcpyDeviceToHost));
     ctx->meas[4] = (double)v[0];
     ctx->meas[5] = (double)v[1];
-    for (int i = 0; i < count && i < 8; ++i) out[i] = ctx->meas[i];
+    for (int i = 0; i < count && i < 10; ++i) out[i] = ctx->meas[i];
     return HRT_OK;
 }
 

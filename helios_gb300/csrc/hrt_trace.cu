@@ -109,8 +109,9 @@ __device__ __forceinline__ bool direct_ray(const SourceDev &src, f3 org, f3 nrm,
     return false;
 }
 
-template <bool STATS>
-__global__ void __launch_bounds__(kBlock) k_direct(const DirectParams P) {
+// W4: shadow rays over the compressed 4-wide nodes (sc.nodes4 set), else the binary nodes.
+template <bool STATS, bool W4>
+__global__ void __launch_bounds__(kBlock, 3) k_direct(const DirectParams P) {
     const uint32_t R = (uint32_t)(P.dimx * P.dimy);
     const uint32_t total = P.count * R;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -147,8 +148,8 @@ __global__ void __launch_bounds__(kBlock) k_direct(const DirectParams P) {
                     if ((!face && ts == 0) || ts == 3) {
                         live = false;
                     } else {
-                        Hit h = trace_full<STATS>(P.sc, org, dir, 1e-4f, tmax, true, VoxKey{r, p, c2, P.seed, P.pass},
-                                                  &nv, &np);
+                        Hit h = trace_full<STATS, W4>(P.sc, org, dir, 1e-4f, tmax, true,
+                                                      VoxKey{r, p, c2, P.seed, P.pass}, &nv, &np);
                         if (h.prim == 0xFFFFFFFFu) v[face ? 1 : 0] = strength;
                     }
                 }
@@ -695,7 +696,8 @@ static cudaError_t direct_impl(const DirectParams &p, int max_blocks, cudaStream
     if (total <= 0 || p.S <= 0) return cudaSuccess;
     unsigned nb = blocks_for(total, kBlock);
     if ((int)nb > max_blocks) nb = (unsigned)max_blocks;
-    k_direct<STATS><<<nb, kBlock, 0, s>>>(p);
+    if (p.sc.nodes4) k_direct<STATS, true><<<nb, kBlock, 0, s>>>(p);
+    else k_direct<STATS, false><<<nb, kBlock, 0, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -37,6 +37,65 @@ struct CoverQ {
 };
 constexpr int kMaxCovers = 16;  // covers taken per periodic segment of a ray
 
+constexpr int32_t kSentinel = 0x7FFFFFF0;  // no node (empty stack, missed child)
+constexpr int kStack4 = 128;               // a 4-wide node pushes up to three children
+
+// The four child boxes of a compressed 4-wide node (q0..q3, format in hrt_device.cuh) against
+// a ray (origin o, inverse direction inv) within [tmin, tmax]: entry distances tk (INFINITY:
+// missed) and child references ck (kSentinel: missed), sorted nearest first.
+__device__ __forceinline__ void node4_test(const float4 q0, const float4 q1, const float4 q2, const float4 q3, f3 o,
+                                           f3 inv, float tmin, float tmax, float tk[4], int32_t ck[4]) {
+    const uint32_t eb = __float_as_uint(q0.w);
+    const float sx = q_step(eb & 0xFFu), sy = q_step((eb >> 8) & 0xFFu), sz = q_step((eb >> 16) & 0xFFu);
+    // near / far plane bytes per axis from the sign of the ray direction: with inv >= 0 the
+    // lower plane is entered first (q_lo <= q_hi, fma is monotone)
+    const uint32_t nx = inv.x >= 0.f ? __float_as_uint(q1.x) : __float_as_uint(q1.w);
+    const uint32_t fx = inv.x >= 0.f ? __float_as_uint(q1.w) : __float_as_uint(q1.x);
+    const uint32_t ny = inv.y >= 0.f ? __float_as_uint(q1.y) : __float_as_uint(q2.x);
+    const uint32_t fy = inv.y >= 0.f ? __float_as_uint(q2.x) : __float_as_uint(q1.y);
+    const uint32_t nz = inv.z >= 0.f ? __float_as_uint(q1.z) : __float_as_uint(q2.y);
+    const uint32_t fz = inv.z >= 0.f ? __float_as_uint(q2.y) : __float_as_uint(q1.z);
+    const int32_t cref[4] = {__float_as_int(q2.z), __float_as_int(q2.w), __float_as_int(q3.x), __float_as_int(q3.y)};
+    // slab planes in the node's quantised frame: t = q * (inv s) + (p - o) inv, one fused
+    // multiply-add per plane (inv s is exact: s is a power of two).  The rounding is of the
+    // same order as the binary test's and is covered by the leaf-box padding, so no box
+    // holding an accepted hit is culled.
+    const float ax = inv.x * sx, ay = inv.y * sy, az = inv.z * sz;
+    const float bx = (q0.x - o.x) * inv.x, by = (q0.y - o.y) * inv.y, bz = (q0.z - o.z) * inv.z;
+    // near and far plane of one axis as one packed pair: the same two subtractions (exact)
+    // and fused multiply-adds as the scalar form, in half the instructions
+    const unsigned long long bias = f2_pack(8388608.0f, 8388608.0f);
+    const unsigned long long ax2 = f2_pack(ax, ax), ay2 = f2_pack(ay, ay), az2 = f2_pack(az, az);
+    const unsigned long long bx2 = f2_pack(bx, bx), by2 = f2_pack(by, by), bz2 = f2_pack(bz, bz);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float tnx, tfx, tny, tfy, tnz, tfz;
+        f2_unpack(f2_fma(f2_sub(f2_pack(q_biased(nx, k), q_biased(fx, k)), bias), ax2, bx2), &tnx, &tfx);
+        f2_unpack(f2_fma(f2_sub(f2_pack(q_biased(ny, k), q_biased(fy, k)), bias), ay2, by2), &tny, &tfy);
+        f2_unpack(f2_fma(f2_sub(f2_pack(q_biased(nz, k), q_biased(fz, k)), bias), az2, bz2), &tnz, &tfz);
+        const float tn = fmax3(tnx, tny, fmaxf(tnz, tmin));
+        const float tf = fmin3(tfx, tfy, fminf(tfz, tmax));
+        const bool hit = tn <= tf;  // empty slots hold inverted boxes
+        tk[k] = hit ? tn : INFINITY;
+        ck[k] = hit ? cref[k] : kSentinel;
+    }
+#define HRT_CSWAP(a, b)                                  \
+    if (tk[b] < tk[a]) {                                 \
+        const float tt = tk[a];                          \
+        tk[a] = tk[b];                                   \
+        tk[b] = tt;                                      \
+        const int32_t cc = ck[a];                        \
+        ck[a] = ck[b];                                   \
+        ck[b] = cc;                                      \
+    }
+    HRT_CSWAP(0, 1)
+    HRT_CSWAP(2, 3)
+    HRT_CSWAP(0, 2)
+    HRT_CSWAP(1, 3)
+    HRT_CSWAP(1, 2)
+#undef HRT_CSWAP
+}
+
 // Closest (or any) hit over the BVH.  Visiting order: both child boxes are
 // tested against the current best distance; leaf children are intersected at
 // once; of two internal children the nearer is entered and the farther pushed.
@@ -124,6 +183,77 @@ __device__ Hit trace_bvh(const TraceScene &sc, f3 o, f3 d, float tmin, float tma
     return h;
 }
 
+// Closest (or any) hit over the compressed 4-wide nodes (sc.nodes4).  Each visit tests the four
+// child boxes against the current best distance; leaf children are intersected at once, nearest
+// first; of the internal children the nearest is entered and the others pushed farthest first.
+// The closest hit (ties to the smaller original index) is the binary trace's; an any-hit trace
+// may report another occluder.
+template <bool STATS>
+__device__ Hit trace_bvh4(const TraceScene &sc, f3 o, f3 d, float tmin, float tmax, bool anyhit, const VoxKey &vk,
+                          uint32_t *nv, uint32_t *np) {
+    Hit h{tmax, 0xFFFFFFFFu, 0};
+    if (sc.n == 0) return h;
+    WT w = wt_setup(d);
+    f3 inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+    int32_t stack[kStack4];
+    int sp = 0;
+    int32_t cur = 0;
+    float best = tmax;
+    const uint32_t n4 = (uint32_t)sc.n4;
+    uint32_t budget = 2u * (uint32_t)sc.n + 64u;  // a ray visits each node at most once
+    for (;;) {
+        if ((uint32_t)cur >= n4 || budget-- == 0u) {
+            raise(sc.status, ERR_BOUNDS);
+            return h;
+        }
+        if (STATS) ++*nv;
+        const float4 *nd = sc.nodes4 + 4 * (size_t)cur;
+        float tk[4];
+        int32_t ck[4];
+        node4_test(__ldg(nd), __ldg(nd + 1), __ldg(nd + 2), __ldg(nd + 3), o, inv, tmin, best, tk, ck);
+        int32_t inner[4];
+        int ni = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int32_t c = ck[k];
+            if (c == kSentinel) continue;
+            if (c >= 0) {
+                inner[ni++] = c;
+                continue;
+            }
+            if ((uint32_t)(~c) >= (uint32_t)sc.n) {
+                raise(sc.status, ERR_BOUNDS);
+                continue;
+            }
+            float t;
+            int face;
+            uint32_t orig;
+            if (STATS) ++*np;
+            if (rec_hit(sc.rec, (uint32_t)(~c), w, o, d, inv, tmin, best, vk, &t, &face, &orig, sc.masks)) {
+                if (h.prim == 0xFFFFFFFFu || t < h.t || (t == h.t && orig < h.prim)) {
+                    h.t = t;
+                    h.prim = orig;
+                    h.face = face;
+                    best = t;
+                }
+                if (anyhit) return h;
+            }
+        }
+        if (ni > 0) {
+            if (sp + ni - 1 > kStack4) {
+                raise(sc.status, ERR_STACK);
+                return h;
+            }
+            for (int k = ni - 1; k >= 1; --k) stack[sp++] = inner[k];
+            cur = inner[0];
+        } else {
+            if (sp == 0) break;
+            cur = stack[--sp];
+        }
+    }
+    return h;
+}
+
 // Periodic walls: closest wall before `lim`.
 __device__ __forceinline__ bool wall_closest(const TraceScene &sc, f3 o, f3 d, float tmin, float lim, float *tb,
                                              int *which) {
@@ -147,15 +277,18 @@ __device__ __forceinline__ bool wall_closest(const TraceScene &sc, f3 o, f3 d, f
 }
 
 // Trace with periodic wrapping (<= 10 wraps; OptiX8DeviceCode.cu:763-789, 1440-1459).
-// o_last (optional): origin of the last segment traced.
-template <bool STATS>
+// o_last (optional): origin of the last segment traced.  W4: over the compressed 4-wide nodes
+// (the caller checks that sc.nodes4 is set).
+template <bool STATS, bool W4 = false>
 __device__ Hit trace_full(const TraceScene &sc, f3 o, f3 d, float tmin, float tmax, bool anyhit, VoxKey vk,
                           uint32_t *nv, uint32_t *np, f3 *o_last = nullptr) {
     const uint32_t c2 = vk.c2;
     for (int wrap = 0; wrap < 10; ++wrap) {
         vk.c2 = c2 | ((uint32_t)wrap << 16);
         if (o_last) *o_last = o;
-        Hit h = trace_bvh<STATS>(sc, o, d, tmin, tmax, anyhit && sc.nbbox == 0, vk, nv, np);
+        const bool any = anyhit && sc.nbbox == 0;
+        Hit h = W4 ? trace_bvh4<STATS>(sc, o, d, tmin, tmax, any, vk, nv, np)
+                   : trace_bvh<STATS>(sc, o, d, tmin, tmax, any, vk, nv, np);
         if (sc.nbbox == 0) return h;
         float tb;
         int which = -1;
@@ -416,8 +549,6 @@ inline unsigned ps_grid(const DiffuseParams &p, int resident) {
 // equal those of trace_bvh (same tests, same tie rule; only the order differs).
 // Each lane keeps a running FP64 sum for its current origin (primitive, face) and
 // adds it to G only when the origin changes.
-constexpr int32_t kSentinel = 0x7FFFFFF0;
-constexpr int kStack4 = 128;  // a 4-wide node pushes up to three children
 
 // MINB: resident blocks per SM the register allocation must allow (4, the default: 64
 // registers; 3: more registers, fewer warps).  VOX: the scene holds voxels (turbid media
@@ -528,58 +659,9 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
                 if (STATS) ++nvis;
                 const float4 *nd = sc.nodes4 + 4 * (size_t)cur;
                 const float4 q0 = __ldg(nd), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2), q3 = __ldg(nd + 3);
-                const uint32_t eb = __float_as_uint(q0.w);
-                const float sx = q_step(eb & 0xFFu), sy = q_step((eb >> 8) & 0xFFu), sz = q_step((eb >> 16) & 0xFFu);
-                // near / far plane bytes per axis from the sign of the ray direction: with
-                // inv >= 0 the lower plane is entered first (q_lo <= q_hi, fma is monotone)
-                const uint32_t nx = inv.x >= 0.f ? __float_as_uint(q1.x) : __float_as_uint(q1.w);
-                const uint32_t fx = inv.x >= 0.f ? __float_as_uint(q1.w) : __float_as_uint(q1.x);
-                const uint32_t ny = inv.y >= 0.f ? __float_as_uint(q1.y) : __float_as_uint(q2.x);
-                const uint32_t fy = inv.y >= 0.f ? __float_as_uint(q2.x) : __float_as_uint(q1.y);
-                const uint32_t nz = inv.z >= 0.f ? __float_as_uint(q1.z) : __float_as_uint(q2.y);
-                const uint32_t fz = inv.z >= 0.f ? __float_as_uint(q2.y) : __float_as_uint(q1.z);
-                const int32_t cref[4] = {__float_as_int(q2.z), __float_as_int(q2.w), __float_as_int(q3.x),
-                                         __float_as_int(q3.y)};
-                // slab planes in the node's quantised frame: t = q * (inv s) + (p - o) inv, one
-                // fused multiply-add per plane (inv s is exact: s is a power of two).  The
-                // rounding is of the same order as the binary test's and is covered by the
-                // leaf-box padding, so no box holding an accepted hit is culled.
-                const float ax = inv.x * sx, ay = inv.y * sy, az = inv.z * sz;
-                const float bx = (q0.x - o.x) * inv.x, by = (q0.y - o.y) * inv.y, bz = (q0.z - o.z) * inv.z;
-                // near and far plane of one axis as one packed pair: the same two subtractions
-                // (exact) and fused multiply-adds as the scalar form, in half the instructions
-                const unsigned long long bias = f2_pack(8388608.0f, 8388608.0f);
-                const unsigned long long ax2 = f2_pack(ax, ax), ay2 = f2_pack(ay, ay), az2 = f2_pack(az, az);
-                const unsigned long long bx2 = f2_pack(bx, bx), by2 = f2_pack(by, by), bz2 = f2_pack(bz, bz);
                 float tk[4];
                 int32_t ck[4];
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    float tnx, tfx, tny, tfy, tnz, tfz;
-                    f2_unpack(f2_fma(f2_sub(f2_pack(q_biased(nx, k), q_biased(fx, k)), bias), ax2, bx2), &tnx, &tfx);
-                    f2_unpack(f2_fma(f2_sub(f2_pack(q_biased(ny, k), q_biased(fy, k)), bias), ay2, by2), &tny, &tfy);
-                    f2_unpack(f2_fma(f2_sub(f2_pack(q_biased(nz, k), q_biased(fz, k)), bias), az2, bz2), &tnz, &tfz);
-                    const float tn = fmax3(tnx, tny, fmaxf(tnz, 1e-4f));
-                    const float tf = fmin3(tfx, tfy, fminf(tfz, best));
-                    const bool hit = tn <= tf;  // empty slots hold inverted boxes
-                    tk[k] = hit ? tn : INFINITY;
-                    ck[k] = hit ? cref[k] : kSentinel;
-                }
-#define HRT_CSWAP(a, b)                                  \
-    if (tk[b] < tk[a]) {                                 \
-        const float tt = tk[a];                          \
-        tk[a] = tk[b];                                   \
-        tk[b] = tt;                                      \
-        const int32_t cc = ck[a];                        \
-        ck[a] = ck[b];                                   \
-        ck[b] = cc;                                      \
-    }
-                HRT_CSWAP(0, 1)
-                HRT_CSWAP(2, 3)
-                HRT_CSWAP(0, 2)
-                HRT_CSWAP(1, 3)
-                HRT_CSWAP(1, 2)
-#undef HRT_CSWAP
+                node4_test(q0, q1, q2, q3, o, inv, 1e-4f, best, tk, ck);
                 if (ck[0] == kSentinel) {
                     cur = POP();
                 } else {

@@ -412,7 +412,8 @@ int hrt_get_bvh(hrt_context *ctx, uint64_t *codes, uint32_t *perm, uint32_t *nod
  * events on the context's stream.  Setting flags also resets the accumulators.
  * hrt_get_measure: [0] direct launches, [1] direct ms, [2] diffuse launches,
  * [3] diffuse ms, [4] node visits, [5] primitive tests, [6] rays of direct launches,
- * [7] rays of diffuse launches ([6] and [7] with bit 0, which syncs after every launch). */
+ * [7] rays of diffuse launches, [8] node visits and [9] primitive tests of diffuse launches
+ * ([6]-[9] with bit 0, which syncs after every launch). */
 int hrt_set_measure(hrt_context *ctx, int flags);
 int hrt_get_measure(hrt_context *ctx, double *out, int count);
 /* ---- BVH build that allocates nothing (no counterpart in the reference).

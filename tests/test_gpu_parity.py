@@ -325,6 +325,9 @@ def test_traversal_counts_match_oracle(gpu, oracle_mod):
     _, st = run_oracle(rad, ["SW"], oracle_mod, seed=4)
     assert m["node_visits"] == st["nodes"]
     assert m["prim_tests"] == st["prims"]
+    # the diffuse launches' share of the counts (the bench's roofline reads it)
+    assert 0 < m["diffuse_node_visits"] < m["node_visits"]
+    assert 0 < m["diffuse_prim_tests"] <= m["prim_tests"]
 
 
 @pytest.mark.parametrize("variant", [1, 2, 3, 4, 5])
