@@ -526,8 +526,10 @@ __global__ void k_final(size_t nb, const double *__restrict__ rin, const double 
 // ---------------------------------------------------------------- batched sweep --
 // Shadow rays of many suns in one launch.  Ray ids are sun-major, so a warp holds
 // 32 strata of one primitive toward ONE sun (coherent rays).  Origins and strengths
-// are exactly those of a plain direct pass with the same seed (source slot 0).
-__global__ void __launch_bounds__(kBlock) k_direct_sweep(const SweepDirectParams P) {
+// are exactly those of a plain direct pass with the same seed (source slot 0).  W4: shadow rays
+// over the compressed 4-wide nodes (sc.nodes4 set), else the binary nodes.
+template <bool W4>
+__global__ void __launch_bounds__(kBlock, 3) k_direct_sweep(const SweepDirectParams P) {
     const uint32_t R = (uint32_t)(P.dimx * P.dimy);
     const unsigned long long per_sun = (unsigned long long)P.sc.n * R;
     const unsigned long long total = per_sun * (unsigned long long)P.nsun;
@@ -560,7 +562,8 @@ __global__ void __launch_bounds__(kBlock) k_direct_sweep(const SweepDirectParams
             if (!((!face && ts == 0) || ts == 3)) {
                 live = true;
                 uint32_t nv = 0, np = 0;
-                const Hit h = trace_full<false>(P.sc, org, dd, 1e-4f, 1e38f, true, VoxKey{r, p, 0u, P.seed, 0u}, &nv, &np);
+                const Hit h =
+                    trace_full<false, W4>(P.sc, org, dd, 1e-4f, 1e38f, true, VoxKey{r, p, 0u, P.seed, 0u}, &nv, &np);
                 if (h.prim == 0xFFFFFFFFu) v[face ? 1 : 0] = strength;
             }
         }
@@ -894,7 +897,8 @@ cudaError_t launch_direct_sweep(const SweepDirectParams &p, int max_blocks, cuda
     if (total <= 0) return cudaSuccess;
     unsigned nb = blocks_for(total, kBlock);
     if ((int)nb > max_blocks) nb = (unsigned)max_blocks;
-    k_direct_sweep<<<nb, kBlock, 0, s>>>(p);
+    if (p.sc.nodes4) k_direct_sweep<true><<<nb, kBlock, 0, s>>>(p);
+    else k_direct_sweep<false><<<nb, kBlock, 0, s>>>(p);
     return cudaGetLastError();
 }
 
