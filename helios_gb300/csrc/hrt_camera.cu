@@ -112,7 +112,9 @@ __device__ float cam_value(const CameraParams &P, const Hit &h, f3 ol, f3 d, int
     return rad > 0.f ? rad * strength : 0.f;
 }
 
-template <int NB>
+// W4: camera rays over the compressed 4-wide nodes (sc.nodes4 set), else the binary nodes; the
+// closest hit does not depend on the tree.
+template <int NB, bool W4>
 __global__ void __launch_bounds__(kBlock) k_camera(const CameraParams P) {
     const uint32_t aa = (uint32_t)P.aa;
     const uint32_t total = (uint32_t)(P.tw * P.th) * aa;
@@ -131,8 +133,8 @@ __global__ void __launch_bounds__(kBlock) k_camera(const CameraParams P) {
             q = jj * (uint32_t)P.W + ii;
             f3 o, d, ol;
             camera_ray(P, ii, jj, smp, false, &o, &d);
-            const Hit h = trace_full<false>(P.sc, o, d, 1e-5f, 1e30f, false, VoxKey{q, smp, 0x40000000u, P.seed, P.cam_id},
-                                            nullptr, nullptr, &ol);
+            const Hit h = trace_full<false, W4>(P.sc, o, d, 1e-5f, 1e30f, false,
+                                                VoxKey{q, smp, 0x40000000u, P.seed, P.cam_id}, nullptr, nullptr, &ol);
             if (h.prim != kLost) {
 #pragma unroll
                 for (int j = 0; j < NB; ++j)
@@ -144,6 +146,7 @@ __global__ void __launch_bounds__(kBlock) k_camera(const CameraParams P) {
     }
 }
 
+template <bool W4>
 __global__ void k_pixel_label(const CameraParams P) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (uint32_t)(P.tw * P.th)) return;
@@ -151,8 +154,8 @@ __global__ void k_pixel_label(const CameraParams P) {
     const uint32_t q = jj * (uint32_t)P.W + ii;
     f3 o, d, ol;
     camera_ray(P, ii, jj, 0u, true, &o, &d);
-    const Hit h = trace_full<false>(P.sc, o, d, 1e-5f, 1e30f, false, VoxKey{q, 0xFFFFFFFFu, 0x40000000u, P.seed, P.cam_id},
-                                    nullptr, nullptr, &ol);
+    const Hit h = trace_full<false, W4>(P.sc, o, d, 1e-5f, 1e30f, false,
+                                        VoxKey{q, 0xFFFFFFFFu, 0x40000000u, P.seed, P.cam_id}, nullptr, nullptr, &ol);
     if (h.prim == 0xFFFFFFFFu) {
         P.labels[q] = 0u;
         P.depths[q] = -1.f;
@@ -174,9 +177,10 @@ cudaError_t launch_camera(const CameraParams &p, int max_blocks, cudaStream_t s)
     if (total <= 0 || p.Bl <= 0) return cudaSuccess;
     long long nb = (total + kBlock - 1) / kBlock;
     if (nb > max_blocks) nb = max_blocks;
-    if (p.Bl <= 1) k_camera<1><<<(unsigned)nb, kBlock, 0, s>>>(p);
-    else if (p.Bl <= 4) k_camera<4><<<(unsigned)nb, kBlock, 0, s>>>(p);
-    else if (p.Bl <= 16) k_camera<16><<<(unsigned)nb, kBlock, 0, s>>>(p);
+    const bool w4 = p.sc.nodes4 != nullptr;
+    if (p.Bl <= 1) w4 ? k_camera<1, true><<<(unsigned)nb, kBlock, 0, s>>>(p) : k_camera<1, false><<<(unsigned)nb, kBlock, 0, s>>>(p);
+    else if (p.Bl <= 4) w4 ? k_camera<4, true><<<(unsigned)nb, kBlock, 0, s>>>(p) : k_camera<4, false><<<(unsigned)nb, kBlock, 0, s>>>(p);
+    else if (p.Bl <= 16) w4 ? k_camera<16, true><<<(unsigned)nb, kBlock, 0, s>>>(p) : k_camera<16, false><<<(unsigned)nb, kBlock, 0, s>>>(p);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
@@ -184,7 +188,8 @@ cudaError_t launch_camera(const CameraParams &p, int max_blocks, cudaStream_t s)
 cudaError_t launch_pixel_labels(const CameraParams &p, cudaStream_t s) {
     const long long total = (long long)p.tw * p.th;
     if (total <= 0) return cudaSuccess;
-    k_pixel_label<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(p);
+    if (p.sc.nodes4) k_pixel_label<true><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(p);
+    else k_pixel_label<false><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(p);
     return cudaGetLastError();
 }
 
