@@ -30,7 +30,20 @@ EXPORTS = [
     "hrt_launch_pixel_labels", "hrt_zero_camera_pixel_buffers", "hrt_get_camera_results",
     "hrt_energy_balance", "hrt_run_coupled", "hrt_scene_load", "hrt_scene_last_error", "hrt_scene_count",
     "hrt_scene_arrays", "hrt_scene_data_labels", "hrt_scene_data", "hrt_scene_free",
+    "hrt_plan_launch_chunks", "hrt_set_launch_ray_limit", "hrt_set_visit_budget",
 ]
+
+
+def plan_launch_chunks(count: int, rays_per_primitive: int, max_rays: int = 0):
+    """(launches, primitives per launch) for a pass (hrt_plan_launch_chunks; host arithmetic only).
+
+    Raises HrtError(HRT_EUNSUPPORTED) when one primitive's rays exceed a launch."""
+    lib = load()
+    per = C.c_uint32()
+    k = lib.hrt_plan_launch_chunks(int(count), int(rays_per_primitive), int(max_rays), C.byref(per))
+    if k < 0:
+        raise HrtError(int(k), "the rays of one primitive exceed the rays one launch can carry")
+    return int(k), int(per.value)
 
 
 class HrtError(RuntimeError):
@@ -270,6 +283,9 @@ def load(path: str | None = None):
         "hrt_last_stats": (C.c_int, [VP, VP, C.c_int]),
         "hrt_set_tuning": (C.c_int, [VP, C.c_int]),
         "hrt_set_ray_budget": (C.c_int, [VP, C.c_uint32]),
+        "hrt_plan_launch_chunks": (C.c_int64, [C.c_uint32, C.c_uint64, C.c_uint64, C.POINTER(C.c_uint32)]),
+        "hrt_set_launch_ray_limit": (C.c_int, [VP, C.c_uint64]),
+        "hrt_set_visit_budget": (C.c_int, [VP, C.c_uint32]),
         "hrt_tuning_report": (C.c_size_t, [VP, VP, C.c_size_t]),
         "hrt_device_status": (C.c_int, [VP, C.POINTER(C.c_uint32), C.c_int]),
         "hrt_trace_rays": (C.c_int, [VP, C.c_int64, VP, VP, C.c_float, C.c_float, C.c_int, VP, VP, VP]),
@@ -620,6 +636,14 @@ class Context:
     def set_ray_budget(self, rays_per_thread: int):
         """Rays a thread of the persistent trace takes before its block retires (0: no limit)."""
         self.check(self.lib.hrt_set_ray_budget(self.h, int(rays_per_thread)))
+
+    def set_launch_ray_limit(self, max_rays: int):
+        """Rays one trace launch may carry; larger passes run as primitive chunks (tests lower it)."""
+        self.check(self.lib.hrt_set_launch_ray_limit(self.h, int(max_rays)))
+
+    def set_visit_budget(self, visits: int):
+        """Node visits a ray segment may make before traversal ends it with a device error (0: 2n+64)."""
+        self.check(self.lib.hrt_set_visit_budget(self.h, int(visits)))
 
     def tuning_report(self) -> str:
         k = self.lib.hrt_tuning_report(self.h, None, 0)

@@ -144,6 +144,10 @@ struct hrt_context {
     int sw_kernels = 0;
     // rays a lane of the persistent trace takes before its block retires (0: no limit)
     uint32_t lane_budget = 0;
+    // rays one trace launch may carry (passes above it run as primitive chunks) and the
+    // node-visit budget of a ray segment (0: 2n+64); both lowered only by tests
+    uint64_t ray_limit = kLaunchRayLimit;
+    uint32_t visit_budget = 0;
     // kernel-variant tuner: choice per pass shape, and a log of the trials
     int tune = 1;
     std::map<std::string, int> tuned;
@@ -216,7 +220,17 @@ TraceScene scene_of(hrt_context *ctx) {
         sc.masks.T = ctx->T.as<float>();
     }
     sc.cover = nullptr;
+    const uint64_t vb = 2ull * (uint64_t)std::max(ctx->n, 0) + 64ull;
+    sc.visit_budget = ctx->visit_budget ? ctx->visit_budget : (uint32_t)std::min<uint64_t>(vb, 0xFFFFFFFFull);
     return sc;
+}
+
+// Primitives per trace launch of a pass with `rays_per_primitive` rays per primitive (all
+// faces), or 0 with the context's error set when one primitive's rays exceed a launch.
+uint32_t chunk_prims(hrt_context *ctx, uint64_t rays_per_primitive) {
+    const uint32_t per = launch_chunk_prims(rays_per_primitive, ctx->ray_limit);
+    if (per == 0) fail(ctx, HRT_EUNSUPPORTED, "the rays of one primitive exceed the rays one launch can carry (2^31)");
+    return per;
 }
 
 int max_blocks(hrt_context *ctx) { return ctx->sms * 8; }
@@ -294,9 +308,11 @@ int sync_and_status(hrt_context *ctx) {
     CU(cudaStreamSynchronize(ctx->stream));
     if (st) {
         CU(cudaMemsetAsync(ctx->status.p, 0, sizeof(uint32_t), ctx->stream));
-        char buf[160];
-        std::snprintf(buf, sizeof buf, "device error word 0x%x (%s%s%s)", st, (st & ERR_STACK) ? "traversal stack overflow " : "",
-                      (st & ERR_WRAP) ? "periodic wrap limit " : "", (st & ERR_BOUNDS) ? "index out of range" : "");
+        char buf[200];
+        std::snprintf(buf, sizeof buf, "device error word 0x%x (%s%s%s%s)", st,
+                      (st & ERR_STACK) ? "traversal stack overflow " : "", (st & ERR_WRAP) ? "periodic wrap limit " : "",
+                      (st & ERR_BOUNDS) ? "index out of range " : "",
+                      (st & ERR_BUDGET) ? "traversal visit budget exhausted" : "");
         return fail(ctx, HRT_EDEVICE, buf);
     }
     return HRT_OK;
@@ -424,6 +440,8 @@ int direct_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp,
         return fail(ctx, HRT_EINVAL, "materials do not match the geometry/sources; call hrt_update_materials()");
     if (ctx->src_flux_count < (size_t)ctx->S * Bl)
         return fail(ctx, HRT_EINVAL, "source fluxes not uploaded for every source and launched band");
+    if ((uint64_t)ctx->n * (uint64_t)ctx->S >= 0xFFFFFFFFull)  // (primitive, source) sum keys are 32-bit
+        return fail(ctx, HRT_EUNSUPPORTED, "primitives x sources of a direct pass must stay below 2^32");
     size_t ng = (size_t)ctx->n * ctx->S * 2;
     CU(ctx->Gd.ensure(ctx->stream, ng * sizeof(double)));
     CU(cudaMemsetAsync(ctx->Gd.p, 0, ng * sizeof(double), ctx->stream));
@@ -453,10 +471,20 @@ int direct_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp,
         P.gl.src_flux = ctx->src_flux.as<float>();
     }
     if (ctx->measure & 4) P.sc.nodes4 = nullptr;  // counting on the binary tree, as the oracle does
+    const uint32_t per = chunk_prims(ctx, (uint64_t)dimx * (uint64_t)dimy);
+    if (per == 0) return HRT_EUNSUPPORTED;
+    uint32_t chunks = 0;
     CU(timed_launch(ctx, 0, [&] {
-        if (cov) return launch_direct_glass(P, max_blocks(ctx), ctx->stream);
-        return (ctx->measure & 1) ? launch_direct_stats(P, max_blocks(ctx), ctx->stream)
-                                  : launch_direct(P, max_blocks(ctx), ctx->stream);
+        DirectParams Q = P;
+        for (uint32_t done = 0; done < count; done += Q.count, ++chunks) {
+            Q.offset = offset + done;
+            Q.count = std::min(per, count - done);
+            const cudaError_t e = cov ? launch_direct_glass(Q, max_blocks(ctx), ctx->stream)
+                                      : ((ctx->measure & 1) ? launch_direct_stats(Q, max_blocks(ctx), ctx->stream)
+                                                            : launch_direct(Q, max_blocks(ctx), ctx->stream));
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
     }));
     EpilogueParams E{};
     E.n = ctx->n;
@@ -474,7 +502,7 @@ int direct_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp,
     E.Gcov = cov ? ctx->Gcov.as<double>() : nullptr;
     E.src_flux = ctx->src_flux.as<float>();
     CU(launch_epilogue_direct(E, ctx->stream));
-    ctx->last_kernels += 2;
+    ctx->last_kernels += 1 + chunks;
     return HRT_OK;
 }
 
@@ -529,6 +557,8 @@ int tuned_variant(hrt_context *ctx, const DiffuseParams &P0, bool record, int *v
                    : std::vector<int>{DV_PS4, DV_PS3, DV_SIMPLE};
     DiffuseParams P = P0;
     P.count = std::min(P0.count, std::max(P0.count / 32u, 4096u));
+    // the sample is one launch: keep it within the per-launch ray limit
+    P.count = std::min(P.count, std::max(launch_chunk_prims((uint64_t)P0.dimx * P0.dimy * nf, ctx->ray_limit), 1u));
     P.sc.rays = nullptr;
     P.sc.visits = nullptr;
     if (!record) {
@@ -584,6 +614,9 @@ int diffuse_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp
     if (ctx->mS < 1 || ctx->mN != ctx->n)
         return fail(ctx, HRT_EINVAL, "materials do not match the geometry; call hrt_update_materials()");
     if (Bc > 16) return fail(ctx, HRT_EUNSUPPORTED, "at most 16 bands can be launched together");
+    const int nfaces = ((faces & 1) ? 1 : 0) + ((faces & 2) ? 1 : 0);
+    const uint32_t per = chunk_prims(ctx, (uint64_t)dimx * (uint64_t)dimy * (uint64_t)nfaces);
+    if (per == 0) return HRT_EUNSUPPORTED;
     size_t m = (size_t)ctx->n * Bl;
     CU(cudaMemsetAsync(ctx->Gt.p, 0, m * sizeof(double), ctx->stream));
     CU(cudaMemsetAsync(ctx->Gb.p, 0, m * sizeof(double), ctx->stream));
@@ -617,11 +650,20 @@ int diffuse_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp
     } else if ((r = tuned_variant(ctx, P, false, &variant))) {
         return r;
     }
+    uint32_t chunks = 0;
     CU(timed_launch(ctx, 1, [&] {
-        if (cov) return launch_diffuse_glass(P, max_blocks(ctx), ctx->stream);
-        return (ctx->measure & 1)
-                   ? launch_diffuse_stats(P, (ctx->measure & 4) ? DV_SIMPLE : variant, max_blocks(ctx), ctx->stream)
-                                  : launch_diffuse_variant(P, variant, max_blocks(ctx), ctx->stream);
+        DiffuseParams Q = P;
+        for (uint32_t done = 0; done < count; done += Q.count, ++chunks) {
+            Q.offset = offset + done;
+            Q.count = std::min(per, count - done);
+            const cudaError_t e =
+                cov ? launch_diffuse_glass(Q, max_blocks(ctx), ctx->stream)
+                    : ((ctx->measure & 1) ? launch_diffuse_stats(Q, (ctx->measure & 4) ? DV_SIMPLE : variant,
+                                                                 max_blocks(ctx), ctx->stream)
+                                          : launch_diffuse_variant(Q, variant, max_blocks(ctx), ctx->stream));
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
     }));
     EpilogueParams E{};
     E.n = ctx->n;
@@ -639,7 +681,7 @@ int diffuse_pass(hrt_context *ctx, uint32_t offset, uint32_t count, uint32_t rpp
     E.Gb = ctx->Gb.as<double>();
     E.strength = 1.0 / (double)(dimx * dimy);
     CU(launch_epilogue_diffuse(E, ctx->stream));
-    ctx->last_kernels += 2;
+    ctx->last_kernels += 1 + chunks;
     return HRT_OK;
 }
 
@@ -1720,6 +1762,11 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
     CU(ctx->sw_out.ensure(ctx->stream, 3 * m * sizeof(float)));
     float *otop = ctx->sw_out.as<float>(), *obot = otop + m, *fin = obot + m;
     const size_t nhits = 2 * (size_t)n * (size_t)std::max(Rd, 1);
+    // recording launches over primitive chunks of at most rec_per primitives (32-bit ray ids)
+    const uint32_t rec_per = chunk_prims(ctx, 2ull * (uint64_t)std::max(Rd, 1));
+    if (rec_per == 0) return HRT_EUNSUPPORTED;
+    if ((uint64_t)n * (uint64_t)nsun >= 0xFFFFFFFFull)  // (primitive, sun) sum keys are 32-bit
+        return fail(ctx, HRT_EUNSUPPORTED, "primitives x suns of a sweep must stay below 2^32");
     CU(ctx->sw_hits.ensure(ctx->stream, nhits * sizeof(uint32_t)));
     CU(ctx->Gd.ensure(ctx->stream, std::max<size_t>((size_t)n * nsun * 2, 1) * sizeof(double)));
     CU(ctx->fetch.ensure(ctx->stream, sizeof(unsigned long long)));
@@ -1748,8 +1795,8 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
                   ctx->sw_acc.p, ctx->sw_hits.p);
     {
         char more[128];
-        std::snprintf(more, sizeof more, "/%p/%p/%p/%p/%p/v%d", ctx->sw_in.p, ctx->sw_mat.p, ctx->sw_out.p, ctx->Gd.p,
-                      (void *)ctx->stream, rec_variant);
+        std::snprintf(more, sizeof more, "/%p/%p/%p/%p/%p/v%d/c%u", ctx->sw_in.p, ctx->sw_mat.p, ctx->sw_out.p,
+                      ctx->Gd.p, (void *)ctx->stream, rec_variant, rec_per);
         std::strncat(key, more, sizeof key - std::strlen(key) - 1);
     }
     if (!ctx->sw_exec || ctx->sw_key != key) {
@@ -1803,14 +1850,20 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
             E.strength = 1.0 / (double)std::max(Rd, 1);
             auto pass = [&](uint32_t pass_id, const float *sky, const uint8_t *mask) -> cudaError_t {
                 cudaError_t e2;
-                P.pass = pass_id;
-                if ((e2 = launch_diffuse_record(P, ctx->sw_hits.as<uint32_t>(), rec_variant, st)) != cudaSuccess)
-                    return e2;
+                DiffuseParams Q = P;
+                Q.pass = pass_id;
+                for (uint32_t done = 0; done < (uint32_t)n; done += Q.count) {
+                    Q.offset = done;
+                    Q.count = std::min(rec_per, (uint32_t)n - done);
+                    if ((e2 = launch_diffuse_record(Q, ctx->sw_hits.as<uint32_t>(), rec_variant, st)) != cudaSuccess)
+                        return e2;
+                    ++nk;
+                }
                 Gp.sky = sky;
                 if ((e2 = launch_gather(Gp, st)) != cudaSuccess) return e2;
                 E.mask = mask;
                 if ((e2 = launch_epilogue_diffuse_channels(E, st)) != cudaSuccess) return e2;
-                nk += 3;
+                nk += 2;
                 return cudaSuccess;
             };
             if (any_diffuse && Rd > 0) {
@@ -1857,6 +1910,28 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
     ctx->last_rays = rays;
     ctx->last_iters = (uint64_t)s->scattering_depth;
     return r;
+}
+
+int hrt_set_launch_ray_limit(hrt_context *ctx, uint64_t max_rays) {
+    if (!ctx || max_rays == 0) return HRT_EINVAL;
+    ctx->ray_limit = std::min<uint64_t>(max_rays, kLaunchRayLimit);
+    return HRT_OK;
+}
+
+int64_t hrt_plan_launch_chunks(uint32_t count, uint64_t rays_per_primitive, uint64_t max_rays,
+                               uint32_t *prims_per_chunk) {
+    if (max_rays == 0) max_rays = kLaunchRayLimit;
+    const uint32_t per = launch_chunk_prims(rays_per_primitive, max_rays);
+    if (prims_per_chunk) *prims_per_chunk = per;
+    if (per == 0) return HRT_EUNSUPPORTED;
+    if (count == 0) return 0;
+    return (int64_t)(((uint64_t)count + per - 1) / per);
+}
+
+int hrt_set_visit_budget(hrt_context *ctx, uint32_t visits) {
+    if (!ctx) return HRT_EINVAL;
+    ctx->visit_budget = visits;
+    return HRT_OK;
 }
 
 int hrt_set_ray_budget(hrt_context *ctx, uint32_t rays_per_thread) {

@@ -17,7 +17,7 @@ namespace hrt {
 enum : uint32_t { PT_PATCH = 0, PT_TRI = 1, PT_DISK = 2, PT_TILE = 3, PT_VOXEL = 4, PT_BBOX = 5 };
 
 // Error bits of the per-context device status word.
-enum : uint32_t { ERR_STACK = 1u, ERR_WRAP = 2u, ERR_TIMEOUT = 4u, ERR_BOUNDS = 8u };
+enum : uint32_t { ERR_STACK = 1u, ERR_WRAP = 2u, ERR_TIMEOUT = 4u, ERR_BOUNDS = 8u, ERR_BUDGET = 16u };
 
 constexpr int kStack = 64;           // traversal stack entries per ray
 constexpr int32_t kEmptyChild = ~0x7FFFFFFF;

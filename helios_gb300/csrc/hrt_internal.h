@@ -26,6 +26,8 @@ struct TraceScene {
     unsigned long long *visits; // [2] node visits, primitive tests (statistics launches only)
     MaskSet masks;        // texture masks (masks.id null: none)
     const uint32_t *cover; // [n] bit s: a translucent cover for this launch's rays of source s (null: none)
+    uint32_t visit_budget; // node visits one ray segment may make before it is ended with ERR_BOUNDS
+                           // (2n+64 by default: a ray visits each node at most once)
 };
 
 // Translucent covers of one launch: sheet optics and the cover deposits.
@@ -47,6 +49,21 @@ struct SourceDev {
     float w0, w1;
     float R[9];
 };
+
+// Ray ids inside one trace launch are 32-bit (primitive x stratum x face, and the
+// persistent kernel's per-face id range).  A pass whose primitives x rays per primitive x
+// faces reaches kLaunchRayLimit runs as consecutive launches over primitive chunks, so
+// every launch's ids stay below 2^31 and no 32-bit product or grid-stride step wraps.
+constexpr uint64_t kLaunchRayLimit = 1ull << 31;
+
+// Primitives per launch for `rays_per_primitive` rays each under `limit` rays per launch;
+// 0 when a single primitive's rays alone exceed the limit (or the limit is 0).
+inline uint32_t launch_chunk_prims(uint64_t rays_per_primitive, uint64_t limit) {
+    if (limit > kLaunchRayLimit) limit = kLaunchRayLimit;
+    if (rays_per_primitive == 0) return 0xFFFFFFFFu;
+    const uint64_t c = limit / rays_per_primitive;
+    return c > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)c;
+}
 
 struct DirectParams {
     TraceScene sc;

@@ -113,7 +113,7 @@ __device__ __forceinline__ bool direct_ray(const SourceDev &src, f3 org, f3 nrm,
 template <bool STATS, bool W4>
 __global__ void __launch_bounds__(kBlock, 3) k_direct(const DirectParams P) {
     const uint32_t R = (uint32_t)(P.dimx * P.dimy);
-    const uint32_t total = P.count * R;
+    const uint32_t total = P.count * R;  // < 2^31: the host plans primitive chunks
     const uint32_t stride = gridDim.x * blockDim.x;
     const double inv_nr = 1.0 / (double)R;
     for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total; base += stride) {
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_direct(const DirectParams P) {
 template <int NB, bool STATS>
 __global__ void __launch_bounds__(kBlock) k_diffuse(const DiffuseParams P) {
     const uint32_t R = (uint32_t)(P.dimx * P.dimy);
-    const uint32_t total = P.count * R;
+    const uint32_t total = P.count * R;  // < 2^31: the host plans primitive chunks
     const uint32_t stride = gridDim.x * blockDim.x;
     // blockIdx.y: 0 = top face (launch_face 1), 1 = bottom face (launch_face 0)
     const int face = (blockIdx.y == 0) ? 1 : 0;
@@ -232,7 +232,7 @@ __device__ __forceinline__ float cover_cos(const TraceScene &sc, uint32_t c, f3 
 
 __global__ void __launch_bounds__(kBlock) k_direct_glass(const DirectParams P) {
     const uint32_t R = (uint32_t)(P.dimx * P.dimy);
-    const uint32_t total = P.count * R;
+    const uint32_t total = P.count * R;  // < 2^31: the host plans primitive chunks
     const uint32_t stride = gridDim.x * blockDim.x;
     const double inv_nr = 1.0 / (double)R;
     const GlassParams &gl = P.gl;
@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(kBlock) k_direct_glass(const DirectParams P) {
 template <int NB>
 __global__ void __launch_bounds__(kBlock) k_diffuse_glass(const DiffuseParams P) {
     const uint32_t R = (uint32_t)(P.dimx * P.dimy);
-    const uint32_t total = P.count * R;
+    const uint32_t total = P.count * R;  // < 2^31: the host plans primitive chunks
     const uint32_t stride = gridDim.x * blockDim.x;
     const int face = (blockIdx.y == 0) ? 1 : 0;
     if (!(P.faces & (1 << blockIdx.y))) return;

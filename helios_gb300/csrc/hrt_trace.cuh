@@ -113,10 +113,10 @@ __device__ Hit trace_bvh(const TraceScene &sc, f3 o, f3 d, float tmin, float tma
     int32_t cur = 0;
     float best = tmax;
     const uint32_t ni = (uint32_t)(sc.n > 1 ? sc.n - 1 : 1);
-    uint32_t budget = 2u * (uint32_t)sc.n + 64u;  // a ray visits each node at most once
+    uint32_t budget = sc.visit_budget;
     for (;;) {
         if ((uint32_t)cur >= ni || budget-- == 0u) {
-            raise(sc.status, ERR_BOUNDS);
+            raise(sc.status, budget == 0xFFFFFFFFu ? ERR_BUDGET : ERR_BOUNDS);
             return h;
         }
         if (STATS) ++*nv;
@@ -200,10 +200,10 @@ __device__ Hit trace_bvh4(const TraceScene &sc, f3 o, f3 d, float tmin, float tm
     int32_t cur = 0;
     float best = tmax;
     const uint32_t n4 = (uint32_t)sc.n4;
-    uint32_t budget = 2u * (uint32_t)sc.n + 64u;  // a ray visits each node at most once
+    uint32_t budget = sc.visit_budget;
     for (;;) {
         if ((uint32_t)cur >= n4 || budget-- == 0u) {
-            raise(sc.status, ERR_BOUNDS);
+            raise(sc.status, budget == 0xFFFFFFFFu ? ERR_BUDGET : ERR_BOUNDS);
             return h;
         }
         if (STATS) ++*nv;
@@ -558,6 +558,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
     unsigned long long *fetch = P.fetch;
     const int lane = threadIdx.x & 31;
     const uint32_t R = (uint32_t)(P.dimx * P.dimy);
+    // count x R x faces < 2^31: the host splits larger passes into primitive chunks
     const uint32_t per_face = P.count * R;
     const int nf = ((P.faces & 1) ? 1 : 0) + ((P.faces & 2) ? 1 : 0);
     const unsigned long long total = (unsigned long long)per_face * (unsigned long long)nf;
@@ -609,12 +610,14 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
                     exhausted = true;
                 } else {
                     ++taken;
-                    rid = id;
                     const uint32_t fi = (uint32_t)(id / per_face);
                     const uint32_t rem = (uint32_t)(id - (unsigned long long)fi * per_face);
                     face = (nf == 2) ? (fi == 0 ? 1 : 0) : ((P.faces & 1) ? 1 : 0);
                     p = P.offset + rem / R;
                     const uint32_t r = rem % R;
+                    // recorded hits are laid out [face][primitive][ray] over the whole scene,
+                    // whatever primitive chunk this launch covers
+                    if (RECORD) rid = ((unsigned long long)fi * (unsigned long long)sc.n + p) * R + r;
                     const int ts = sc.twosided[p];
                     const bool skip = (face == 1 && ts == 3) || (face == 0 && ts != 1);
                     if (!skip) {
@@ -632,7 +635,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
                         cur = (sc.n > 0) ? 0 : kSentinel;
                         leaf = 0;
                         sp = 0;
-                        budget = 2u * (uint32_t)sc.n + 64u;
+                        budget = sc.visit_budget;
                         wraps = 0;
                         live = true;
                         ++nrays;
@@ -651,7 +654,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
             // children farthest first and continue with the nearest
             while (cur >= 0 && cur != kSentinel) {
                 if ((uint32_t)cur >= n4 || budget-- == 0u) {
-                    raise(sc.status, ERR_BOUNDS);
+                    raise(sc.status, budget == 0xFFFFFFFFu ? ERR_BUDGET : ERR_BOUNDS);
                     cur = kSentinel;
                     leaf = 0;
                     break;
@@ -686,7 +689,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
         } else {
             while (cur >= 0 && cur != kSentinel) {
                 if ((uint32_t)cur >= ni || budget-- == 0u) {
-                    raise(sc.status, ERR_BOUNDS);
+                    raise(sc.status, budget == 0xFFFFFFFFu ? ERR_BUDGET : ERR_BOUNDS);
                     cur = kSentinel;
                     leaf = 0;
                     break;
@@ -779,7 +782,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
                     bprim = 0xFFFFFFFFu;
                     cur = 0;
                     sp = 0;
-                    budget = 2u * (uint32_t)sc.n + 64u;
+                    budget = sc.visit_budget;
                     ++wraps;
                     continue;
                 }

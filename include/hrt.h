@@ -389,6 +389,24 @@ int hrt_set_tuning(hrt_context *ctx, int mode);
  * the hardware interleaves them with other streams' blocks (by stream priority).
  * Results do not change.  0 restores the default. */
 int hrt_set_ray_budget(hrt_context *ctx, uint32_t rays_per_thread);
+/* Launch planning (the reference likewise splits a pass into launches of at most 65,535
+ * primitives, the OptiX depth limit: OptiX8Backend.cpp:854-868, 985-1000).  Ray ids inside one trace launch
+ * are 32-bit, so a pass whose primitives x rays per primitive x faces reaches 2^31 runs as
+ * consecutive launches over primitive chunks; results do not depend on the chunking
+ * beyond the order of FP64 sums.  hrt_plan_launch_chunks returns the number of launches
+ * for `count` primitives of `rays_per_primitive` rays each (all faces) under `max_rays`
+ * rays per launch (0: the library's 2^31), and the primitives per launch in
+ * *prims_per_chunk; HRT_EUNSUPPORTED when one primitive's rays exceed a launch.  It is
+ * pure host arithmetic.  hrt_set_launch_ray_limit lowers a context's limit (tests force
+ * small scenes through several chunks with it); values above 2^31 are clamped. */
+int64_t hrt_plan_launch_chunks(uint32_t count, uint64_t rays_per_primitive, uint64_t max_rays,
+                               uint32_t *prims_per_chunk);
+int hrt_set_launch_ray_limit(hrt_context *ctx, uint64_t max_rays);
+/* Node visits one ray segment may make before traversal ends it and sets the bounds
+ * bit of the device error word (a ray visits each node at most once, so the default,
+ * 0, means 2n+64 and never fires on a valid tree).  Tests set a tiny budget to drive
+ * the device error path: the next solve returns HRT_EDEVICE and clears the word. */
+int hrt_set_visit_budget(hrt_context *ctx, uint32_t visits);
 /* Text log of the tuner's trials and choices, one line per shape; returns the bytes
  * needed (including the terminating zero); buf may be NULL. */
 size_t hrt_tuning_report(const hrt_context *ctx, char *buf, size_t len);
