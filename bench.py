@@ -47,37 +47,10 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def orchard_model(leaves_per_tree=5000, nx=20, ny=10, mode="device", device=0):
-    from helios_gb300 import scenes
-    from helios_gb300.radiation import Context, RadiationModel
+def orchard_model(nx=20, ny=10, device=0, **kw):
+    from helios_gb300 import workloads
 
-    sc = scenes.orchard(nx=nx, ny=ny, leaves_per_tree=leaves_per_tree, side=0.03, seed=0)
-    ctx = Context()
-    ctx.addScene(sc)
-    n = sc.n
-    rng = np.random.default_rng(0)
-    uu = np.arange(n)
-    ctx.setPrimitiveData(uu, "reflectivity_PAR", np.full(n, 0.08))
-    ctx.setPrimitiveData(uu, "transmissivity_PAR", np.full(n, 0.05))
-    ctx.setPrimitiveData(uu, "reflectivity_NIR", np.full(n, 0.45))
-    ctx.setPrimitiveData(uu, "transmissivity_NIR", np.full(n, 0.40))
-    ctx.setPrimitiveData(uu, "emissivity_LW", np.full(n, 0.96))
-    ctx.setPrimitiveData(uu, "temperature", 273.15 + rng.normal(25.0, 2.0, n))
-    rad = RadiationModel(ctx, device=device, mode=mode)
-    sun = rad.addCollimatedRadiationSource(scenes.sun_direction(30.0, 0.0))
-    for b in ("PAR", "NIR", "LW"):
-        rad.addRadiationBand(b)
-        rad.setDirectRayCount(b, 100)
-        rad.setDiffuseRayCount(b, 200)
-        rad.setScatteringDepth(b, 5)
-    rad.disableEmission("PAR")
-    rad.disableEmission("NIR")
-    rad.setSourceFlux(sun, "PAR", 500.0)
-    rad.setSourceFlux(sun, "NIR", 450.0)
-    rad.setDiffuseRadiationFlux("PAR", 50.0)
-    rad.setDiffuseRadiationFlux("NIR", 45.0)
-    rad.setDiffuseRadiationFlux("LW", 350.0)
-    return rad, sc
+    return workloads.orchard_model(nx=nx, ny=ny, device=device, **kw)
 
 
 BANDS = ["LW", "NIR", "PAR"]
