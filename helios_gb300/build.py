@@ -17,9 +17,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libhrt.so")
-SOURCES = ["hrt_bvh.cu", "hrt_bvh4.cu", "hrt_trace.cu", "hrt_ps_accumulate.cu", "hrt_ps_special.cu", "hrt_camera.cu", "hrt_energy.cu", "hrt_ingest.cpp", "hrt_api.cu",
+SOURCES = ["hrt_bvh.cu", "hrt_bvh4.cu", "hrt_trace.cu", "hrt_ps_accumulate.cu", "hrt_ps_special.cu", "hrt_ps_w4.cu", "hrt_camera.cu", "hrt_energy.cu", "hrt_ingest.cpp", "hrt_api.cu",
            "hrt_static.cu", "hrt_serve.cu"]
-HEADERS = ["hrt_device.cuh", "hrt_internal.h", "hrt_trace.cuh", os.path.join("..", "..", "include", "hrt.h")]
+HEADERS = ["hrt_device.cuh", "hrt_internal.h", "hrt_trace.cuh", "hrt_trace_w4.cuh", os.path.join("..", "..", "include", "hrt.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
            "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "-Xcompiler", "-ffp-contract=off",

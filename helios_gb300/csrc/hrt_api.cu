@@ -522,6 +522,11 @@ const char *variant_name(int v) {
     switch (v) {
         case DV_W4: return "wide4";
         case DV_W43: return "wide4-3";
+        case DV_W4S4: return "lean4";
+        case DV_W4S5: return "lean5";
+        case DV_W4S4D16: return "lean4-s16";
+        case DV_W4B128: return "lean4-b128";
+        case DV_W4B512: return "lean4-b512";
         case DV_PS4: return "binary4";
         case DV_PS3: return "binary3";
         case DV_SIMPLE: return "simple";
@@ -551,9 +556,12 @@ int tuned_variant(hrt_context *ctx, const DiffuseParams &P0, bool record, int *v
     if (ctx->measure & 1) return HRT_OK;  // statistics launches count on a tuned choice, never time one
     std::vector<int> cand;
     const bool w4 = P0.sc.nodes4 != nullptr;
-    if (record) cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_PS3, DV_PS4} : std::vector<int>{DV_PS3, DV_PS4};
+    if (record)
+        cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_W4S4, DV_W4S5, DV_W4S4D16, DV_W4B128, DV_W4B512, DV_PS3, DV_PS4}
+                  : std::vector<int>{DV_PS3, DV_PS4};
     else if (P0.sc.voxels) cand = w4 ? std::vector<int>{DV_W4, DV_PS4, DV_SIMPLE} : std::vector<int>{DV_PS4, DV_SIMPLE};
-    else cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_PS4, DV_PS3, DV_SIMPLE}
+    else cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_W4S4, DV_W4S5, DV_W4S4D16, DV_W4B128, DV_W4B512, DV_PS4, DV_PS3,
+                                      DV_SIMPLE}
                    : std::vector<int>{DV_PS4, DV_PS3, DV_SIMPLE};
     DiffuseParams P = P0;
     P.count = std::min(P0.count, std::max(P0.count / 32u, 4096u));
@@ -1017,7 +1025,7 @@ int hrt_build_accel(hrt_context *ctx) {
     if (r) return r;
     // compressed 4-wide nodes for the persistent diffuse trace (scratch reuses the build's)
     ctx->n4 = 0;
-    CU(ctx->nodes4.ensure(ctx->stream, ni * 4 * sizeof(float4)));
+    CU(ctx->nodes4.ensure(ctx->stream, bvh4_node_capacity(n) * 4 * sizeof(float4)));
     if (bvh4_scratch_bytes(n) > ctx->bvh_scratch.cap) CU(ctx->bvh_scratch.ensure(ctx->stream, bvh4_scratch_bytes(n)));
     int n4 = 0;
     // the 4-wide nodes come from the clustered binary tree (fewer node visits than the
@@ -1942,7 +1950,7 @@ int hrt_set_ray_budget(hrt_context *ctx, uint32_t rays_per_thread) {
 }
 
 int hrt_set_tuning(hrt_context *ctx, int mode) {
-    if (!ctx || mode < 0 || (mode > 2 && !(mode >= 16 + DV_PS4 && mode <= 16 + DV_W43))) return HRT_EINVAL;
+    if (!ctx || mode < 0 || (mode > 2 && !(mode >= 16 + DV_PS4 && mode <= 16 + DV_LAST))) return HRT_EINVAL;
     if (mode == 2) {
         ctx->tuned.clear();
         ctx->tune_log.clear();

@@ -65,10 +65,12 @@ __device__ __forceinline__ uint32_t quant_hi(float p, float v, float s) {
 }
 
 // One wave: item i turns binary node in[i].x into 4-wide node in[i].y.
+// cap: 4-wide nodes n4 holds; qcap: items the wave queues hold.
 __global__ void __launch_bounds__(kThreads4) k_collapse(int n2count, const float4 *__restrict__ n2,
                                                         const int2 *__restrict__ in, int nin, int2 *__restrict__ out,
                                                         unsigned *__restrict__ nout, unsigned *__restrict__ nnodes,
-                                                        int cap, float4 *__restrict__ n4, uint32_t *__restrict__ status) {
+                                                        int cap, int qcap, float4 *__restrict__ n4,
+                                                        uint32_t *__restrict__ status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nin) return;
     const int32_t b = in[i].x, q = in[i].y;
@@ -128,6 +130,17 @@ __global__ void __launch_bounds__(kThreads4) k_collapse(int n2count, const float
     }
     uint32_t wlo[3] = {0, 0, 0}, whi[3] = {0, 0, 0};
     int32_t outref[4] = {kEmptyChild, kEmptyChild, kEmptyChild, kEmptyChild};
+    // The internal children of a node get consecutive indices from one allocation, padded to
+    // an even count: every allocation starts on an even index, i.e. on a 128-byte line of two
+    // 64-byte nodes, so siblings (which rays tend to visit one after another) share lines.
+    int nint = 0;
+    for (int k = 0; k < cnt; ++k) nint += ref[k] >= 0 ? 1 : 0;
+    unsigned nq0 = 0, slot0 = 0;
+    if (nint > 0) {
+        nq0 = atomicAdd(nnodes, (unsigned)((nint + 1) & ~1));
+        slot0 = atomicAdd(nout, (unsigned)nint);
+    }
+    int j = 0;
     for (int k = 0; k < 4; ++k) {
         const int32_t c = k < cnt ? ref[k] : kEmptyChild;
         if (c == kEmptyChild) {  // inverted box: lo bytes 255, hi bytes 0
@@ -141,9 +154,9 @@ __global__ void __launch_bounds__(kThreads4) k_collapse(int n2count, const float
         if (c < 0) {
             outref[k] = c;  // leaf: ~slot
         } else {
-            const unsigned nq = atomicAdd(nnodes, 1u);
-            const unsigned slot = atomicAdd(nout, 1u);
-            if ((int)nq >= cap || (int)slot >= cap) {
+            const unsigned nq = nq0 + (unsigned)j, slot = slot0 + (unsigned)j;
+            ++j;
+            if ((int)nq >= cap || (int)slot >= qcap) {
                 atomicOr(status, ERR_BOUNDS);
                 continue;
             }
@@ -167,6 +180,8 @@ size_t bvh4_scratch_bytes(int n) {
     return 2 * ni * sizeof(int2) + 256;
 }
 
+size_t bvh4_node_capacity(int n) { return (size_t)(n > 1 ? n - 1 : 1) + 8; }
+
 cudaError_t bvh4_build(const float4 *nodes2, int n, float4 *nodes4, void *scratch, uint32_t *status, int *count_out,
                        cudaStream_t s) {
     *count_out = 0;
@@ -177,14 +192,16 @@ cudaError_t bvh4_build(const float4 *nodes2, int n, float4 *nodes4, void *scratc
     const int2 root = make_int2(0, 0);
     cudaError_t e;
     if ((e = cudaMemcpyAsync(qa, &root, sizeof(int2), cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
-    const unsigned one = 1;
-    if ((e = cudaMemcpyAsync(counters + 1, &one, sizeof(unsigned), cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+    // node 0 is the root; node 1 pads the root's line, so the first allocation starts at 2
+    const unsigned first = 2;
+    if ((e = cudaMemcpyAsync(counters + 1, &first, sizeof(unsigned), cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+    const int cap = (int)bvh4_node_capacity(n);
     int nin = 1, waves = 0;
     while (nin > 0) {
         if (++waves > 4 * 64 + 8) return cudaErrorInvalidValue;  // deeper than any LBVH of 2^32 leaves
         if ((e = cudaMemsetAsync(counters, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
         k_collapse<<<(nin + kThreads4 - 1) / kThreads4, kThreads4, 0, s>>>(ni, nodes2, qa, nin, qb, counters,
-                                                                           counters + 1, ni, nodes4, status);
+                                                                           counters + 1, cap, ni, nodes4, status);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         unsigned next = 0;
         if ((e = cudaMemcpyAsync(&next, counters, sizeof(unsigned), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
@@ -197,7 +214,7 @@ cudaError_t bvh4_build(const float4 *nodes2, int n, float4 *nodes4, void *scratc
     unsigned total = 0;
     if ((e = cudaMemcpyAsync(&total, counters + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-    *count_out = (int)std::min<unsigned>(total, (unsigned)ni);
+    *count_out = (int)std::min<unsigned>(total, (unsigned)cap);
     return cudaSuccess;
 }
 

@@ -187,14 +187,16 @@ constexpr size_t bvh_scratch_bytes_c(int n) {
 }
 size_t bvh_scratch_bytes(int n);
 void bvh_carve(BvhBuffers &b, void *scratch, int n);
-// Compressed 4-wide BVH collapsed from the binary nodes (hrt_bvh4.cu): nodes4 holds
 // Binary BVH over the LBVH's leaf slots by locally-ordered agglomerative clustering (better
 // surface-area cost than the Morton split; the 4-wide nodes are collapsed from it).  leafbox:
 // [n*6] padded leaf boxes of bvh_build; nodes: [n-1] binary nodes, root 0; n >= 2.
 size_t ploc_scratch_bytes(int n);
 cudaError_t ploc_build(const float *leafbox, int n, float4 *nodes, void *scratch, cudaStream_t s);
-// max(n-1,1) * 4 float4, scratch bvh4_scratch_bytes(n); *count_out = nodes written.
+// Compressed 4-wide BVH collapsed from the binary nodes (hrt_bvh4.cu): nodes4 holds
+// bvh4_node_capacity(n) nodes of 4 float4, scratch bvh4_scratch_bytes(n); *count_out = the
+// highest node index used + 1 (node 1 and the odd tail of some sibling groups are padding).
 size_t bvh4_scratch_bytes(int n);
+size_t bvh4_node_capacity(int n);
 cudaError_t bvh4_build(const float4 *nodes2, int n, float4 *nodes4, void *scratch, uint32_t *status, int *count_out,
                        cudaStream_t s);
 // lad: [n] leaf area density of voxels (original order), or null (voxels then hold no leaves).
@@ -207,7 +209,17 @@ cudaError_t launch_diffuse(const DiffuseParams &p, int max_blocks, cudaStream_t 
 // Diffuse kernel variants the tuner chooses between: persistent threads over binary nodes
 // (PS4 / PS3: 4 or 3 resident blocks per SM), over compressed 4-wide nodes (W4 / W43), or
 // one ray per thread over binary nodes (SIMPLE).
-enum DiffuseVariant { DV_DEFAULT = 0, DV_PS4 = 1, DV_PS3 = 2, DV_SIMPLE = 3, DV_W4 = 4, DV_W43 = 5 };
+enum DiffuseVariant {
+    DV_DEFAULT = 0, DV_PS4 = 1, DV_PS3 = 2, DV_SIMPLE = 3, DV_W4 = 4, DV_W43 = 5,
+    // lean 4-wide trace (k_diffuse_w4): threads per block x resident blocks per SM, shared
+    // stack entries per lane -- 256 x 4, 8; 256 x 5, 8; 256 x 4, 16; 128 x 8, 8; 512 x 2, 8
+    DV_W4S4 = 6, DV_W4S5 = 7, DV_W4S4D16 = 8, DV_W4B128 = 9, DV_W4B512 = 10,
+    DV_LAST = DV_W4B512
+};
+bool is_w4s_variant(int v);
+cudaError_t launch_w4s(const DiffuseParams &p, int variant, cudaStream_t s);
+cudaError_t launch_w4s_record(const DiffuseParams &p, uint32_t *hits, int variant, cudaStream_t s);
+cudaError_t launch_w4s_stats(const DiffuseParams &p, int variant, cudaStream_t s);
 cudaError_t launch_diffuse_variant(const DiffuseParams &p, int variant, int max_blocks, cudaStream_t s);
 // persistent-kernel launchers (hrt_ps_accumulate.cu, hrt_ps_special.cu)
 cudaError_t launch_ps_accumulate(const DiffuseParams &p, int variant, cudaStream_t s);

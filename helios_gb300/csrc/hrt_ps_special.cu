@@ -62,10 +62,11 @@ cudaError_t launch_ps_stats(const DiffuseParams &p, cudaStream_t s) {
 // Recording mode (one hit code per ray id, no sums) for the batched sweep.
 cudaError_t launch_diffuse_record(const DiffuseParams &p, uint32_t *hits, int variant, cudaStream_t s) {
     if ((long long)p.count * p.dimx * p.dimy <= 0) return cudaSuccess;
+    if (is_w4s_variant(variant) && p.sc.nodes4 && !p.sc.voxels) return launch_w4s_record(p, hits, variant, s);
     DiffuseParams q = p;
     q.hits = hits;
     q.Bc = 1;
-    if ((variant == DV_W4 || variant == DV_W43) && !q.sc.nodes4) variant = DV_PS3;
+    if ((variant == DV_W4 || variant == DV_W43 || is_w4s_variant(variant)) && !q.sc.nodes4) variant = DV_PS3;
     switch (variant) {
         case DV_W4: return ps_launch<1, true, 4, false, true, false>(q, s);
         case DV_W43: return ps_launch<1, true, 3, false, true, false>(q, s);

@@ -720,12 +720,16 @@ static cudaError_t diffuse_impl(const DiffuseParams &p, int variant, int max_blo
     int64_t total = (int64_t)p.count * p.dimx * p.dimy;
     if (total <= 0 || p.Bc <= 0) return cudaSuccess;
     if (variant == DV_DEFAULT) variant = default_variant();
-    if ((variant == DV_W4 || variant == DV_W43) && !p.sc.nodes4) variant = DV_PS4;
+    if ((variant == DV_W4 || variant == DV_W43 || is_w4s_variant(variant)) && !p.sc.nodes4) variant = DV_PS4;
+    if (is_w4s_variant(variant) && p.sc.voxels) variant = DV_W4;  // the lean kernel has no voxel code
     if (p.fetch && variant != DV_SIMPLE) {
         if (STATS) {
+            if (p.Bc <= 4 && is_w4s_variant(variant)) return launch_w4s_stats(p, variant, s);
             if (p.Bc <= 4 && (variant == DV_W4 || variant == DV_W43)) return launch_ps_stats(p, s);
         } else if (p.sc.voxels) {
             return launch_ps_voxels(p, variant, s);
+        } else if (is_w4s_variant(variant)) {
+            return launch_w4s(p, variant, s);
         } else {
             return launch_ps_accumulate(p, variant, s);
         }

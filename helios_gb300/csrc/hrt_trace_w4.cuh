@@ -1,0 +1,311 @@
+// hrt_trace_w4.cuh -- the persistent diffuse trace over compressed 4-wide nodes for scenes
+// without voxels, laid out for occupancy.
+//
+// The trace is bound by the latency of node fetches (L1/L2 hits) and by issue slots, not by
+// DRAM.  More resident warps hide more of that latency, so this kernel keeps only the state
+// of the node loop in registers -- ray origin, inverse direction, best distance, current
+// node, postponed leaf, stack pointer and visit budget -- and moves the rest of each lane's
+// state to shared memory, where it is touched only when a ray starts, reaches a leaf or
+// ends: the direction and the watertight-test set-up (kx, ky, kz, Sx, Sy, Sz), the best hit
+// so far, the origin primitive and face, the wrap count, the running-sum key and sums.
+// The traversal stack is a ring of SD entries per lane in shared memory (indexed
+// [entry][lane], so the 32 lanes of a warp always hit 32 different banks) over a local
+// overflow array: entries deeper than SD below the top are moved to local memory on push
+// and brought back on pop, so local memory is touched only by rays whose stack is deeper
+// than SD.
+//
+// Hits equal those of trace_bvh / k_diffuse_ps: the same node and primitive tests, the same
+// tie rule (closest, then smaller original index); only the order of work differs.
+#pragma once
+#include "hrt_trace.cuh"
+
+namespace hrt {
+
+namespace {
+
+template <int SD, int BLOCK>
+struct RingStack {
+    static_assert((SD & (SD - 1)) == 0 && SD >= 2, "shared stack depth must be a power of two");
+    int32_t (*ring)[BLOCK];   // [SD][BLOCK] in shared memory
+    int tid;
+    int32_t spill[kStack4];   // local memory, entries below the top SD
+    __device__ __forceinline__ void push(int sp, int32_t v) {
+        const int slot = sp & (SD - 1);
+        if (sp >= SD) spill[sp - SD] = ring[slot][tid];
+        ring[slot][tid] = v;
+    }
+    // value of entry sp (the entry just below the old top), restoring the ring window
+    __device__ __forceinline__ int32_t pop(int sp) {
+        const int slot = sp & (SD - 1);
+        const int32_t v = ring[slot][tid];
+        if (sp >= SD) ring[slot][tid] = spill[sp - SD];
+        return v;
+    }
+};
+
+// BLOCK: threads per block; MINB: resident blocks per SM the register allocation must allow.
+// SD: stack entries per lane in shared memory (a power of two).
+template <int NB, bool RECORD, bool STATS, int MINB, int SD, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams P) {
+    __shared__ double s_sum[RECORD ? 1 : NB][BLOCK];            // running sums of the lane's origin
+    __shared__ float s_ray[6][BLOCK];                            // d.xyz, Sx, Sy, Sz
+    __shared__ uint32_t s_lane[5][BLOCK];                        // see the L_* slots below
+    __shared__ int32_t s_stack[SD][BLOCK];
+    __shared__ unsigned long long s_rid[RECORD ? BLOCK : 1];     // record: hit-buffer index
+    constexpr int L_AXES = 0;  // kx | ky << 2 | kz << 4 | face << 6 | wraps << 8
+    constexpr int L_P = 1;     // origin primitive
+    constexpr int L_HIT = 2;   // best hit so far: prim << 1 | face, or kMissCode
+    constexpr int L_KEY = 3;   // running-sum key 2p + face, or 0xFFFFFFFF
+    constexpr int L_TAKEN = 4; // rays taken (lane budget)
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const TraceScene &sc = P.sc;
+    const uint32_t R = (uint32_t)(P.dimx * P.dimy);
+    // count x R x faces < 2^31: the host splits larger passes into primitive chunks
+    const uint32_t per_face = P.count * R;
+    const int nf = ((P.faces & 1) ? 1 : 0) + ((P.faces & 2) ? 1 : 0);
+    const unsigned long long total = (unsigned long long)per_face * (unsigned long long)nf;
+    const uint32_t n4 = (uint32_t)sc.n4;
+
+    RingStack<SD, BLOCK> stk;
+    stk.ring = s_stack;
+    stk.tid = tid;
+    uint32_t nvis = 0, ntest = 0;  // statistics builds only
+    uint32_t nrays = 0;
+    bool live = false, exhausted = false;
+    f3 o = mk(0.f, 0.f, 0.f), inv = o;
+    float best = 1e38f;
+    int32_t cur = kSentinel, leaf = 0;
+    int sp = 0;
+    uint32_t budget = 0;
+    if (!RECORD) {
+#pragma unroll
+        for (int j = 0; j < NB; ++j) s_sum[j][tid] = 0.0;
+    }
+    s_lane[L_KEY][tid] = 0xFFFFFFFFu;
+    s_lane[L_TAKEN][tid] = 0u;
+#define POP() (sp > 0 ? stk.pop(--sp) : kSentinel)
+
+    for (;;) {
+        // ---- refill lanes without a ray (warp-vote compaction of the fetch)
+        if (!live && P.lane_budget && s_lane[L_TAKEN][tid] >= P.lane_budget) exhausted = true;
+        const bool need = !live && !exhausted;
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(P.fetch, (unsigned long long)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                const unsigned long long id = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
+                if (id >= total) {
+                    exhausted = true;
+                } else {
+                    s_lane[L_TAKEN][tid] += 1u;
+                    const uint32_t fi = (uint32_t)(id / per_face);
+                    const uint32_t rem = (uint32_t)(id - (unsigned long long)fi * per_face);
+                    const int face = (nf == 2) ? (fi == 0 ? 1 : 0) : ((P.faces & 1) ? 1 : 0);
+                    const uint32_t p = P.offset + rem / R;
+                    const uint32_t r = rem % R;
+                    if (RECORD) s_rid[tid] = ((unsigned long long)fi * (unsigned long long)sc.n + p) * R + r;
+                    const int ts = sc.twosided[p];
+                    const bool skip = (face == 1 && ts == 3) || (face == 0 && ts != 1);
+                    if (!skip) {
+                        float4 g[4];
+                        load_rgen(sc, p, g);
+                        const uint32_t type = __float_as_uint(g[0].w);
+                        f3 d;
+                        diffuse_ray<false>(g, type, r, p, face, P.dimx, P.dimy, P.seed, P.pass, &o, &d, sc.masks);
+                        const WT w = wt_setup(d);
+                        s_ray[0][tid] = d.x;
+                        s_ray[1][tid] = d.y;
+                        s_ray[2][tid] = d.z;
+                        s_ray[3][tid] = w.Sx;
+                        s_ray[4][tid] = w.Sy;
+                        s_ray[5][tid] = w.Sz;
+                        s_lane[L_AXES][tid] = (uint32_t)(w.kx | (w.ky << 2) | (w.kz << 4) | (face << 6));
+                        s_lane[L_P][tid] = p;
+                        s_lane[L_HIT][tid] = kMissCode;
+                        inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+                        best = 1e38f;
+                        cur = (sc.n > 0) ? 0 : kSentinel;
+                        leaf = 0;
+                        sp = 0;
+                        budget = sc.visit_budget;
+                        live = true;
+                        ++nrays;
+                    }
+                }
+            }
+        }
+        // A lane may be idle because its id was skipped by the face rule; only when every
+        // lane has run past the end of the id range is the warp done.
+        if (__all_sync(0xffffffffu, exhausted && !live)) break;
+        if (!live) continue;
+
+        // ---- internal nodes; leaves are postponed until every active lane has one
+        while (cur >= 0 && cur != kSentinel) {
+            if ((uint32_t)cur >= n4 || budget-- == 0u) {
+                raise(sc.status, budget == 0xFFFFFFFFu ? ERR_BUDGET : ERR_BOUNDS);
+                cur = kSentinel;
+                leaf = 0;
+                sp = 0;
+                break;
+            }
+            if (STATS) ++nvis;
+            const float4 *nd = sc.nodes4 + 4 * (size_t)cur;
+            const float4 q0 = __ldg(nd), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2), q3 = __ldg(nd + 3);
+            float tk[4];
+            int32_t ck[4];
+            node4_test(q0, q1, q2, q3, o, inv, 1e-4f, best, tk, ck);
+            if (ck[0] == kSentinel) {
+                cur = POP();
+            } else {
+                if (sp + 3 > SD + kStack4) {
+                    raise(sc.status, ERR_STACK);
+                    cur = kSentinel;
+                    leaf = 0;
+                    sp = 0;
+                    break;
+                }
+#pragma unroll
+                for (int k = 3; k >= 1; --k)
+                    if (ck[k] != kSentinel) stk.push(sp++, ck[k]);
+                cur = ck[0];
+            }
+            if (cur < 0 && leaf == 0) {
+                leaf = cur;
+                cur = POP();
+            }
+            const unsigned am = __activemask();
+            if (__all_sync(am, leaf != 0) || __popc(am) < P.refill) break;
+        }
+        // ---- primitive tests (direction and watertight set-up come back from shared memory)
+        if (leaf != 0) {
+            const f3 d = mk(s_ray[0][tid], s_ray[1][tid], s_ray[2][tid]);
+            const uint32_t ax = s_lane[L_AXES][tid];
+            WT w;
+            w.kx = (int)(ax & 3u);
+            w.ky = (int)((ax >> 2) & 3u);
+            w.kz = (int)((ax >> 4) & 3u);
+            w.Sx = s_ray[3][tid];
+            w.Sy = s_ray[4][tid];
+            w.Sz = s_ray[5][tid];
+            uint32_t bcode = s_lane[L_HIT][tid];
+            const VoxKey vk{0u, 0u, 0u, 0u, 0u};  // no voxels in this kernel's scenes
+            while (leaf != 0) {
+                const uint32_t slot = (uint32_t)(~leaf);
+                if (STATS) ++ntest;
+                if (slot < (uint32_t)sc.n) {
+                    float t;
+                    int fc;
+                    uint32_t orig;
+                    if (rec_hit<false>(sc.rec, slot, w, o, d, inv, 1e-4f, best, vk, &t, &fc, &orig, sc.masks)) {
+                        if (bcode == kMissCode || t < best || (t == best && orig < (bcode >> 1))) {
+                            best = t;
+                            bcode = (orig << 1) | (uint32_t)fc;
+                        }
+                    }
+                } else {
+                    raise(sc.status, ERR_BOUNDS);
+                }
+                leaf = 0;
+                if (cur < 0) {
+                    leaf = cur;
+                    cur = POP();
+                }
+            }
+            s_lane[L_HIT][tid] = bcode;
+        }
+        if (cur != kSentinel || leaf != 0) continue;  // traversal of this ray goes on next round
+
+        // ---- periodic walls: wrap and restart, or finish the ray
+        const uint32_t bcode = s_lane[L_HIT][tid];
+        bool lost = false;
+        if (sc.nbbox > 0) {
+            const f3 d = mk(s_ray[0][tid], s_ray[1][tid], s_ray[2][tid]);
+            float tb;
+            int which = -1;
+            if (wall_closest(sc, o, d, 1e-4f, (bcode != kMissCode) ? best : 1e38f, &tb, &which) &&
+                (bcode == kMissCode || tb < best)) {
+                const uint32_t ax = s_lane[L_AXES][tid];
+                const uint32_t wraps = ax >> 8;
+                if (wraps >= 9) {
+                    lost = true;
+                } else {
+                    f3 hp = add(o, scl(d, tb));
+                    if ((sc.periodic_x == 1.f) && which < 2) {
+                        const float width = sc.bbox[4].x - sc.bbox[0].x;
+                        hp.x = hp.x + ((which == 0) ? width : -width);
+                    } else {
+                        const int yb = (sc.periodic_x == 1.f) ? 2 : 0;
+                        const float width = sc.bbox[4 * (yb + 1)].y - sc.bbox[4 * yb].y;
+                        hp.y = hp.y + ((which == yb) ? width : -width);
+                    }
+                    o = hp;
+                    best = 1e38f;
+                    s_lane[L_HIT][tid] = kMissCode;
+                    s_lane[L_AXES][tid] = (ax & 0xFFu) | ((wraps + 1u) << 8);
+                    cur = 0;
+                    sp = 0;
+                    budget = sc.visit_budget;
+                    continue;
+                }
+            }
+        }
+        // ---- value of the finished ray, added to the lane's running sum
+        live = false;
+        if (RECORD) {
+            P.hits[s_rid[tid]] = lost ? kLostCode : bcode;
+            continue;
+        }
+        if (lost) continue;
+        const uint32_t face = (s_lane[L_AXES][tid] >> 6) & 1u;
+        const uint32_t key = 2u * s_lane[L_P][tid] + face;
+        const uint32_t akey = s_lane[L_KEY][tid];
+        if (key != akey) {
+            if (akey != 0xFFFFFFFFu) {
+                double *dst = ((akey & 1u) ? P.Gt : P.Gb) + (size_t)(akey >> 1) * P.Bl;
+#pragma unroll
+                for (int j = 0; j < NB; ++j)
+                    if (j < P.Bc && s_sum[j][tid] != 0.0) atomicAdd(dst + j, s_sum[j][tid]);
+            }
+            s_lane[L_KEY][tid] = key;
+#pragma unroll
+            for (int j = 0; j < NB; ++j) s_sum[j][tid] = 0.0;
+        }
+        if (bcode != kMissCode) {
+            const float *src = ((bcode & 1u) ? P.otop : P.obot) + (size_t)(bcode >> 1) * P.Bl;
+#pragma unroll
+            for (int j = 0; j < NB; ++j)
+                if (j < P.Bc) s_sum[j][tid] += (double)__ldg(src + j);
+        } else {
+            const f3 d = mk(s_ray[0][tid], s_ray[1][tid], s_ray[2][tid]);
+#pragma unroll
+            for (int j = 0; j < NB; ++j)
+                if (j < P.Bc) {
+                    const float fl = P.sky.flux[j];
+                    if (fl > 0.f) s_sum[j][tid] += sky_fd(d, P.sky, j) * (double)fl;
+                }
+        }
+    }
+    if (!RECORD) {
+        const uint32_t akey = s_lane[L_KEY][tid];
+        if (akey != 0xFFFFFFFFu) {
+            double *dst = ((akey & 1u) ? P.Gt : P.Gb) + (size_t)(akey >> 1) * P.Bl;
+#pragma unroll
+            for (int j = 0; j < NB; ++j)
+                if (j < P.Bc && s_sum[j][tid] != 0.0) atomicAdd(dst + j, s_sum[j][tid]);
+        }
+    }
+    if (sc.rays && nrays) atomicAdd(sc.rays, (unsigned long long)nrays);
+    if (STATS && sc.visits) {
+        atomicAdd(sc.visits, (unsigned long long)nvis);
+        atomicAdd(sc.visits + 1, (unsigned long long)ntest);
+    }
+#undef POP
+}
+
+}  // namespace
+
+}  // namespace hrt

@@ -57,3 +57,23 @@ def test_sweep_channels_equal_plain_solves():
     # a replay of the captured graph gives the same numbers
     again = rad.ctx.run_sweep(dirs, direct[:, ::-1], diffuse[:, ::-1], rho, tau, 49, 64, 3, seed=123)
     np.testing.assert_allclose(again, sweep, rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("variant", [4, 6, 7, 8, 9, 10])
+def test_sweep_recording_variants_agree(variant):
+    """The recording trace of the sweep gives the same channels whichever 4-wide kernel
+    records the hits (the generic persistent kernel or the lean one in each of its block
+    shapes and shared stack depths)."""
+    rad, sc = _orchard()
+    dirs, direct, diffuse, _ = scenes.day_sweep(n=4)
+    rad.updateGeometry()
+    desc = rad.solve_description(["PAR", "NIR"])
+    rho, tau = desc["rho"][0], desc["tau"][0]
+    base = rad.ctx.run_sweep(dirs, direct, diffuse, rho, tau, 49, 64, 2, seed=7).astype(np.float64)
+    rad.ctx.set_tuning(16 + variant)
+    try:
+        got = rad.ctx.run_sweep(dirs, direct, diffuse, rho, tau, 49, 64, 2, seed=7).astype(np.float64)
+    finally:
+        rad.ctx.set_tuning(1)
+    np.testing.assert_allclose(got, base, rtol=1e-6, atol=1e-9)
+    assert rad.ctx.device_status() == 0
