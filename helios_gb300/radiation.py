@@ -308,6 +308,58 @@ class Context:
     def getGlobalData(self, label):
         return self.global_data[label]
 
+    def doesGlobalDataExist(self, label):
+        return label in self.global_data
+
+
+def _interp_clamped(x, xs, ys):
+    """Piecewise-linear value at x, clamped to the end values (RadiationModel.cpp:3312-3366)."""
+    if x <= xs[0]:
+        return ys[0]
+    if x >= xs[-1]:
+        return ys[-1]
+    i = max(int(np.searchsorted(np.asarray(xs, np.float32), np.float32(x), side="left")), 1)
+    t = np.float32((np.float32(x) - np.float32(xs[i - 1])) / (np.float32(xs[i]) - np.float32(xs[i - 1])))
+    return float(np.float32(ys[i - 1]) + t * (np.float32(ys[i]) - np.float32(ys[i - 1])))
+
+
+def _weighted_average(wl, values, weights, response):
+    """Radiance-weighted mean of a unitless spectral parameter over a response curve:
+    sum p L R dl / sum L R dl by trapezoids over the response's segments
+    (RadiationModel::weightedAverageOverResponse, RadiationModel.cpp:3290-3380)."""
+    if not wl or not response:
+        return 0.0
+    num = den = 0.0
+    for (l1, r1), (l2, r2) in zip(response[:-1], response[1:]):
+        if l2 < wl[0] or l1 > wl[-1]:
+            continue
+        p1, p2 = _interp_clamped(l1, wl, values), _interp_clamped(l2, wl, values)
+        w1, w2 = _interp_clamped(l1, wl, weights), _interp_clamped(l2, wl, weights)
+        dl = l2 - l1
+        num += 0.5 * (p1 * w1 * r1 + p2 * w2 * r2) * dl
+        den += 0.5 * (w1 * r1 + w2 * r2) * dl
+    return float(np.float32(num / den)) if den > 1e-10 else 0.0
+
+
+def _angular_normalization(circ, width, horiz, N=50):
+    """1 / integral of the Prague pattern x cos(theta) over the hemisphere with the sun at the
+    zenith, midpoint rule on N x N cells in FP32 (RadiationModel::computeAngularNormalization,
+    RadiationModel.cpp:3382-3414)."""
+    f = np.float32
+    i = np.arange(N, dtype=np.float32)
+    theta = f(0.5) * f(math.pi) * (i + f(0.5)) / f(N)
+    cos_t = np.maximum(f(0.0), np.cos(theta).astype(np.float32))  # dir.z with the sun at the zenith
+    gamma = np.arccos(np.clip(cos_t, -1, 1)).astype(np.float32) * f(180.0) / f(math.pi)
+    pattern = (f(1.0) + f(circ) * np.exp(-gamma / f(width)).astype(np.float32)) * \
+        (f(1.0) + (f(horiz) - f(1.0)) * (f(1.0) - cos_t))
+    w = pattern * np.cos(theta).astype(np.float32) * np.sin(theta).astype(np.float32) * \
+        (f(math.pi) / (f(2.0) * f(N))) * (f(2.0) * f(math.pi) / f(N))
+    integral = f(0.0)
+    for _ in range(N):  # the azimuth loop adds the same column N times, in FP32
+        for v in w:
+            integral = f(integral + v)
+    return float(f(1.0) / max(integral, f(1e-10)))
+
 
 class _Band:
     def __init__(self):
@@ -319,6 +371,9 @@ class _Band:
         self.diffuseExtinction = 0.0
         self.diffusePeakDir = (0.0, 0.0, 1.0)
         self.diffuseDistNorm = 1.0
+        self.wavebandBounds = (0.0, 0.0)  # RadiationModel.h RadiationBand::wavebandBounds
+        self.diffuse_spectrum = []        # [(wavelength, value)]
+        self.diffusePragueParams = (0.0, 0.0, 0.0, 0.0)  # circumsolar strength, width (deg), horizon, norm
 
 
 class RadiationModel:
@@ -361,7 +416,11 @@ class RadiationModel:
         if label in self.bands:
             raise HeliosRuntimeError(f"ERROR (RadiationModel::addRadiationBand): Radiation band {label} has already "
                                      "been added.")
-        self.bands[label] = _Band()
+        band = _Band()
+        if wavelength_min is not None and wavelength_max is not None:
+            band.wavebandBounds = (float(wavelength_min), float(wavelength_max))
+        band.diffuse_spectrum = list(getattr(self, "_global_diffuse_spectrum", []))
+        self.bands[label] = band
         for s in self.sources:
             s["fluxes"].setdefault(label, -1.0)
 
@@ -507,6 +566,50 @@ class RadiationModel:
         b.diffuseExtinction = float(K)
         b.diffusePeakDir = tuple(d)
         b.diffuseDistNorm = 1.0 / norm
+
+    def setDiffuseSpectrum(self, spectrum_label):
+        """Diffuse spectrum of every band (and of bands added later) from global data of
+        (wavelength, value) pairs (RadiationModel.cpp:1287-1310).  A manual diffuse flux still
+        wins (getDiffuseFlux); the spectrum weights the Prague sky parameters."""
+        if not self.context.doesGlobalDataExist(spectrum_label):
+            raise HeliosRuntimeError(f"ERROR (RadiationModel::setDiffuseSpectrum): Global data '{spectrum_label}' "
+                                     "does not exist.")
+        spec = [(float(w), float(v)) for w, v in self.context.getGlobalData(spectrum_label)]
+        self._global_diffuse_spectrum = spec
+        for b in self.bands.values():
+            b.diffuse_spectrum = list(spec)
+
+    def _update_prague(self, band_labels):
+        """Prague sky parameters of the general diffuse radiation from the Context's global data
+        (RadiationModel::updatePragueParametersForGeneralDiffuse, RadiationModel.cpp:3145-3223):
+        with prague_sky_valid == 1, every band without a power-law sky gets the circumsolar
+        strength, circumsolar width and horizon brightness of prague_sky_spectral_params (6 values
+        per wavelength) averaged over its diffuse spectrum (or waveband) weighted by the zenith
+        radiance, the normalisation recomputed from them, and the sun direction as peak."""
+        g = self.context
+        if not g.doesGlobalDataExist("prague_sky_valid") or int(g.getGlobalData("prague_sky_valid")) != 1:
+            return
+        sp = np.asarray(g.getGlobalData("prague_sky_spectral_params"), np.float32).reshape(-1)
+        nw = sp.size // 6
+        sp = sp[:6 * nw].reshape(nw, 6)
+        wl, Lz = sp[:, 0].tolist(), sp[:, 1].tolist()
+        sun = tuple(float(x) for x in g.getGlobalData("prague_sky_sun_direction"))
+        for label in band_labels:
+            band = self.bands[label]
+            if band.diffuseExtinction > 0.0:
+                continue
+            spec = band.diffuse_spectrum
+            if not spec:
+                lo, hi = band.wavebandBounds
+                if lo > 0 and hi > lo:
+                    spec = [(lo, 1.0), (hi, 1.0)]
+            if not spec:
+                continue
+            circ = _weighted_average(wl, sp[:, 2].tolist(), Lz, spec)
+            width = _weighted_average(wl, sp[:, 3].tolist(), Lz, spec)
+            horiz = _weighted_average(wl, sp[:, 4].tolist(), Lz, spec)
+            band.diffusePragueParams = (circ, width, horiz, _angular_normalization(circ, width, horiz))
+            band.diffusePeakDir = sun
 
     def _add_source(self, src):
         if len(self.sources) >= 256:
@@ -679,6 +782,7 @@ class RadiationModel:
                                          "valid band. Use addRadiationBand() function to add the band.")
         all_bands = sorted(self.bands)  # std::map order (RadiationModel.cpp:3520-3527)
         band_labels = [b for b in all_bands if b in labels]
+        self._update_prague(band_labels)  # RadiationModel.cpp:3726-3729
         if not self.sources:
             self.addCollimatedRadiationSource()
         S = len(self.sources)
@@ -698,7 +802,7 @@ class RadiationModel:
             "diffuse_ext": np.array([x.diffuseExtinction for x in B], np.float32),
             "diffuse_norm": np.array([x.diffuseDistNorm for x in B], np.float32),
             "diffuse_peak": np.array([x.diffusePeakDir for x in B], np.float32),
-            "prague": np.zeros((len(B), 4), np.float32),
+            "prague": np.array([x.diffusePragueParams for x in B], np.float32).reshape(len(B), 4),
             "direct_rays": np.array([x.directRayCount for x in B], np.int32),
             "diffuse_rays": np.array([x.diffuseRayCount for x in B], np.int32),
             "depth": np.array([x.scatteringDepth for x in B], np.int32),

@@ -761,6 +761,75 @@ def eb_regressions(run_eb):
     return out
 
 
+def _sphere2cart(elevation, azimuth):
+    return (math.cos(elevation) * math.sin(azimuth), math.cos(elevation) * math.cos(azimuth), math.sin(elevation))
+
+
+def _sky_patch(rays):
+    ctx = Context()
+    p = ctx.addPatch((0, 0, 0), (1, 1))
+    ctx.setPrimitiveData(p, "twosided_flag", 0)
+    rad = RadiationModel(ctx)
+    rad.addRadiationBand("diffuse")
+    rad.disableEmission("diffuse")
+    rad.setDiffuseRayCount("diffuse", rays)
+    rad.setDiffuseRadiationFlux("diffuse", 1.0)
+    return ctx, rad
+
+
+def anisotropic_diffuse_patch(run, rays=50000):
+    """selfTest.cpp:1852-1891: a one-sided horizontal patch under power-law skies (K = 0,
+    0.25, 1; peak at the zenith and 45 degrees from it) of flux 1 receives 1: the sky
+    distribution is normalised over the hemisphere (RadiationModel.cpp:185-217)."""
+    ctx, rad = _sky_patch(rays)
+    out = []
+    for ti, theta in enumerate((0.0, 0.25 * math.pi)):
+        for K in (0.0, 0.25, 1.0):
+            rad.setDiffuseRadiationExtinctionCoeff("diffuse", K, _sphere2cart(0.5 * math.pi - theta, 0.0))
+            f = run(rad, ["diffuse"], 5 + 11 * ti + int(4 * K))
+            out.append((f"sky_powerlaw_K{K}_theta{ti}", float(f[0, 0]), 1.0, 0.01))
+    return out
+
+
+def _prague_globals(ctx, sun, circ, width, horiz, norm=0.0):
+    ctx.setGlobalData("prague_sky_valid", 1)
+    ctx.setGlobalData("prague_sky_sun_direction", sun)
+    ctx.setGlobalData("prague_sky_visibility_km", 50.0)
+    ctx.setGlobalData("prague_sky_ground_albedo", 0.2)
+    # one wavelength: 550 nm, zenith radiance 0.1, the three angular parameters, normalisation
+    ctx.setGlobalData("prague_sky_spectral_params", [550.0, 0.1, circ, width, horiz, norm])
+
+
+def prague_normalization(run, rays=100000):
+    """selfTest.cpp:1893-1995: Prague skies (clear, turbid, overcast) with the sun at 60
+    degrees elevation on a one-sided horizontal patch of diffuse flux 1 receive 1 within 3 %
+    (the normalisation is computed with the sun at the zenith, RadiationModel.cpp:3382-3414)."""
+    ctx, rad = _sky_patch(rays)
+    ctx.setGlobalData("prague_test_diffuse_spectrum", [(400.0, 1.0), (550.0, 1.0), (700.0, 1.0)])
+    rad.setDiffuseSpectrum("prague_test_diffuse_spectrum")
+    out = []
+    for k, (circ, width, horiz) in enumerate(((3.0, 15.0, 1.5), (8.0, 10.0, 2.5), (0.5, 30.0, 1.2))):
+        _prague_globals(ctx, (0.0, 0.5, 0.866), circ, width, horiz)
+        f = run(rad, ["diffuse"], 41 + k)
+        out.append((f"sky_prague_norm_{k}", float(f[0, 0]), 1.0, 0.03))
+    return out
+
+
+def prague_angular(run, rays=200000):
+    """selfTest.cpp:1997-2063: with the sun at 45 degrees and a strong, narrow circumsolar
+    peak (8, 10 degrees, no horizon brightening) the zenith-normalised Prague sky gives a
+    horizontal patch measurably less than the isotropic sky's 1: 0.70 < flux < 0.97."""
+    ctx, rad = _sky_patch(rays)
+    ctx.setGlobalData("prague_angular_test_spectrum", [(400.0, 1.0), (550.0, 1.0), (700.0, 1.0)])
+    rad.setDiffuseSpectrum("prague_angular_test_spectrum")
+    _prague_globals(ctx, (0.0, 0.707, 0.707), 8.0, 10.0, 1.0)
+    f = run(rad, ["diffuse"], 47)
+    return [("sky_prague_angular", float(f[0, 0]), 0.835, 0.135 / 0.835)]
+
+
+SKIES = ["anisotropic_diffuse_patch", "prague_normalization", "prague_angular"]
+
+
 ENERGY = ["eb_equilibrium", "eb_budget_closure", "eb_solution_checks", "eb_dynamic", "eb_regressions"]
 
 

@@ -18,7 +18,7 @@ def run(oracle_mod):
 
 @pytest.mark.parametrize("name", ["simple_direct", "black_parallel_rectangles", "gray_parallel_rectangles",
                                   "common_edge_squares", "launch_batching", "second_law_box",
-                                  "parallel_disks_masked"] + scenarios.GLASS)
+                                  "parallel_disks_masked"] + scenarios.GLASS + scenarios.SKIES)
 def test_known_answer(run, name):
     res = getattr(scenarios, name)(run)
     assert not scenarios.check(res), scenarios.check(res)
