@@ -33,10 +33,39 @@ sys.path.insert(0, ROOT)
 
 METRIC = "rays/s and solves/s (batched/served vs plain, 1 GB300) at <=1e-4 flux err; p50/p99"
 UNIT = "rays/s"
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the 4-wide persistent diffuse
-# kernel on the orchard (1 M triangles, 3 bands, 450 M rays per launch): mean of three
-# captured launches, 2.460 GB + 0.091 GB (profiles/k_diffuse_ps_wide4_orchard-1M_traffic.md)
-TRAFFIC_PER_LAUNCH = 2.551e9
+# Counters of the dominant kernel from ncu captures, valid only for the kernel sources they were
+# taken on: KERNEL_SOURCES hashed to `sources`.  When the sources change, the bench reports the
+# counters as stale (traffic null) until they are captured again.
+#   traffic_per_launch: dram__bytes_read.sum + dram__bytes_write.sum of one diffuse launch on
+#     this workload (1 M triangles, 3 bands, 450 M rays), mean of three captured launches;
+#   the rest: one --set full capture of the same kernel on a 100 k-triangle orchard (45 M rays).
+KERNEL_SOURCES = ["hrt_trace.cuh", "hrt_trace_w4.cuh", "hrt_device.cuh", "hrt_internal.h", "hrt_ps_w4.cu",
+                  "hrt_ps_accumulate.cu", "hrt_bvh4.cu", "hrt_bvh.cu"]
+PROFILE = {
+    "sources": None,
+    "kernel": None,
+    "traffic_per_launch": None,
+    "issue_active_pct": None,
+    "l1_hit_pct": None,
+    "l2_hit_pct": None,
+    "warps_active_pct": None,
+    "local_requests_per_ray": None,
+    "top_stall": None,
+}
+ACC_DIRECT_RAYS, ACC_DIFFUSE_RAYS = 4, 9  # the accuracy leg's reduced ray counts
+# diffuse-trace variants by the tuner's names (hrt_set_tuning(16 + v) forces one)
+VARIANTS = {"binary4": 1, "binary3": 2, "simple": 3, "wide4": 4, "wide4-3": 5, "lean4": 6, "lean5": 7,
+            "lean4-s16": 8, "lean4-b128": 9, "lean4-b512": 10}
+
+
+def kernel_sources_digest():
+    import hashlib
+
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, "helios_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:12]
 
 
 def peaks():
@@ -129,6 +158,43 @@ def cpu_sample(rad, seconds_hint=15.0, threads=0, prim_limit=None):
     _, st = sc.run_band(oracle_solve(desc), threads=cores, prim_limit=prim_limit)
     dt = time.perf_counter() - t0
     return st["rays"] / dt, cores, prim_limit, dt, st
+
+
+def accuracy_and_cpu(rad, ctx, desc, threads=0):
+    """The CPU-baseline leg, which is also the accuracy check of the timed kernels: the CPU
+    oracle (the reference algorithm restated, FP64, OpenMP on all host threads) solves the
+    whole orchard -- every primitive, all three bands, depth 5 -- at reduced ray counts
+    (ACC_DIRECT_RAYS direct, ACC_DIFFUSE_RAYS diffuse per primitive), timed as the CPU
+    baseline; the GPU solves the same seeded ray set with the benchmark's kernels; the
+    per-primitive flux error of the GPU against the oracle is reported per band."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle
+    from helpers import oracle_solve
+    from helios_gb300 import workloads
+
+    oracle.build()
+    red = dict(desc)
+    red["direct_rays"] = np.full_like(np.asarray(desc["direct_rays"]), ACC_DIRECT_RAYS)
+    red["diffuse_rays"] = np.full_like(np.asarray(desc["diffuse_rays"]), ACC_DIFFUSE_RAYS)
+    gpu = np.asarray(ctx.run_band(red, out=True), np.float64).reshape(desc["n"], -1)
+    gpu_rays = ctx.last_stats()["rays"]
+    T, ty, ts = rad.geometry_arrays()
+    sc = oracle.OracleScene(T, ty, ts)
+    cores = threads or os.cpu_count()
+    t0 = time.perf_counter()
+    ref, st = sc.run_band(oracle_solve(red), threads=cores)
+    dt = time.perf_counter() - t0
+    errs = {b: workloads.max_rel_err(gpu[:, i], ref[:, i]) for i, b in enumerate(BANDS)}
+    cpu = {"value": st["rays"] / dt, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"CPU oracle runBand over all {desc['n']} primitives, 3 bands, depth 5, at {ACC_DIRECT_RAYS} "
+                     f"direct / {ACC_DIFFUSE_RAYS} diffuse rays per primitive ({st['rays']} rays, {dt:.1f} s)"}
+    acc = {"max_rel_err": max(errs.values()), "per_band": errs, "primitives": int(desc["n"]),
+           "rays": int(st["rays"]), "same_rays": bool(gpu_rays == st["rays"]),
+           "against": "FP64 oracle on the same Philox ray set (values below 1e-3 x mean compared against that floor)",
+           "ray_counts": f"{ACC_DIRECT_RAYS} direct / {ACC_DIFFUSE_RAYS} diffuse per primitive; the timed solve uses "
+                         "100 / 225 with the same kernels"}
+    return cpu, acc
 
 
 def run_reference(args):
@@ -371,6 +437,8 @@ def run_gpu(args):
     rad, sc = orchard_model(nx=args.trees[0], ny=args.trees[1], device=local)
     stream = torch.cuda.Stream(device=local)
     rad.ctx.set_stream(stream.cuda_stream)
+    if args.variant:
+        rad.ctx.set_tuning(16 + VARIANTS[args.variant])  # profiling: one kernel, no tuner trials
     rad.setSeed(1234 + rank)
     t_setup = time.perf_counter()
     rad.updateGeometry()
@@ -402,6 +470,7 @@ def run_gpu(args):
         ev1.record(stream)
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1) / args.steps
+    kernels_per_step = int(ctx.last_stats()["kernels"])  # before other solves overwrite the statistics
     meas = ctx.get_measure()
     ctx.set_measure(0)
     ms_t = torch.tensor([ms], device=f"cuda:{local}")
@@ -429,7 +498,9 @@ def run_gpu(args):
     served = None
     if args.serve_requests > 0:
         served = run_served(args, device=local)
-    stress = None
+    stress = {"measured": False,
+              "why": "one solve of the 4 M-primitive + 64^3-voxel scene at depth 20 is ~72 G rays and takes minutes "
+                     "on one GB300, beyond the default run; bench.py --stress times it"}
     if args.stress:
         stress = run_stress(args, stream, device=local)
     if rank != 0:
@@ -447,15 +518,17 @@ def run_gpu(args):
     diff_share = meas["diffuse_ms"] / max(meas["diffuse_ms"] + meas["direct_ms"], 1e-9)
     bytes_per_launch = bytes_per_ray * rays_per_launch
     achieved = bytes_per_launch / (diff_ms * 1e-3) / 1e9
-    # DRAM bytes per launch of the same kernel on this workload, from one ncu capture
-    # (profiles/k_diffuse_ps_wide4_orchard-1M_traffic.md); the workload is fixed
-    traffic = TRAFFIC_PER_LAUNCH if sc.n == 1_000_000 else None
+    # ncu counters of the dominant kernel: used only while the kernel sources are the ones
+    # they were captured on, and the workload is the one they were captured for
+    digest = kernel_sources_digest()
+    fresh = PROFILE["sources"] == digest and sc.n == 1_000_000
+    traffic = PROFILE["traffic_per_launch"] if fresh else None
+    chosen = [x.rsplit("-> ", 1)[-1] for x in ctx.tuning_report().splitlines()
+              if x.startswith("accumulate") and "bands=3" in x]
     rps = rays_per_step * world / (ms * 1e-3)
-    cpu = None
+    cpu, accuracy = None, None
     if not args.no_cpu:
-        crps, cores, plim, dt, st = cpu_sample(rad, seconds_hint=args.ref_seconds)
-        cpu = {"value": crps, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"CPU oracle runBand, rays launched from the first {plim} of {sc.n} primitives, {dt:.1f} s"}
+        cpu, accuracy = accuracy_and_cpu(rad, ctx, desc)
     line = {
         "metric": METRIC, "value": rps, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -467,7 +540,12 @@ def run_gpu(args):
                    "l2": "working set (BVH 64 MB + records 128 MB + buffers) larger than the 129 MB L2; no flush",
                    "setup_s": setup_s},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_kind": peak_kind, "traffic": traffic, "kernel": "k_diffuse",
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "kernel": "k_diffuse_w4" if chosen and chosen[0].startswith("lean") else "k_diffuse_ps",
+                     "variant": chosen[0] if chosen else None,
+                     "limiter": "SM issue and L1/L2 hit latency of the node fetches, not DRAM: the algorithmic "
+                                "bytes are logical fetches, almost all served by L1/L2 (traffic = DRAM bytes)",
+                     "ncu": dict(PROFILE, sources_now=digest, stale=not fresh),
                      "kernel_ms": diff_ms, "kernel_share": diff_share, "bytes_per_launch": bytes_per_launch,
                      "rays_per_launch": rays_per_launch,
                      "node_visits_per_ray": stats["node_visits"] / max(rays_per_step, 1),
@@ -480,11 +558,12 @@ def run_gpu(args):
                 "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s},
         "gpu_launches": None,
         "cpu_baseline": cpu,
+        "accuracy": accuracy,
         "batched": batched,
         "served": served,
         "stress": stress,
     }
-    line["gpu_launches"] = int(ctx.last_stats()["kernels"]) * args.steps
+    line["gpu_launches"] = kernels_per_step * args.steps
     print(json.dumps(line))
 
 
@@ -496,13 +575,15 @@ def main():
     ap.add_argument("--impl", default="hrt", choices=["hrt", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the day-sweep measurement")
-    ap.add_argument("--serve-requests", type=int, default=100, help="served-stream requests (0 = skip)")
+    ap.add_argument("--serve-requests", type=int, default=2000, help="served-stream requests (0 = skip)")
     ap.add_argument("--serve-scenes", type=int, default=16, help="distinct scenes in the served stream")
-    ap.add_argument("--serve-plain", type=int, default=0,
+    ap.add_argument("--serve-plain", type=int, default=200,
                     help="requests timed on the plain per-solve path (0 = all of them)")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--trees", type=int, nargs=2, default=(20, 10), help="orchard grid (default 20 x 10 = 1M leaves)")
     ap.add_argument("--stress", action="store_true", help="also time the deep-scattering stress workload")
+    ap.add_argument("--variant", choices=sorted(VARIANTS), default=None,
+                    help="force one diffuse-trace variant instead of tuning (for profiling captures)")
     ap.add_argument("--stress-scale", type=float, default=1.0, help="primitive-count scale of the stress workload")
     args = ap.parse_args()
     if args.impl == "reference":

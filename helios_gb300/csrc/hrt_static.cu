@@ -2,7 +2,7 @@
 //
 // Some callers cannot call cudaMalloc: code that hands every byte of device
 // memory out of its own arena or framework allocator, and latency-critical loops
-// where a cudaMalloc/cudaFree would synchronise the device.  For them
+// where a cudaMalloc/cudaFree would synchronise the whole device.  For them
 // hrt_build_accel_static() builds the same LBVH as hrt_build_accel() from
 // caller-owned device buffers into caller-owned device buffers.  Its scratch
 // (sort buffers, boxes, parent links, arrival counters, the error word) lives in
@@ -11,8 +11,12 @@
 // array (about 5.6 MB) until the process exits.
 //
 // The first call on each device looks up the array's device address with
-// cudaGetSymbolAddress (with that device current) and caches it; make that first
-// call before any stream capture.
+// cudaGetSymbolAddress (with that device current) and caches it per device index;
+// make that first call before any stream capture.  A cudaDeviceReset of a device
+// invalidates its cached address: reload the library after one.
+//
+// Each call ends by reading the error word back on the caller's stream and waiting
+// for that stream; it never waits for the device or for other streams.
 //
 // All calls share the array and it keeps the last call's contents; the parts
 // that must start at zero (arrival counters, parent links, the error word) are

@@ -446,10 +446,12 @@ int hrt_get_measure(hrt_context *ctx, double *out, int count);
  * Scratch is a static device array sized for at most HRT_STATIC_MAX_PRIMS primitives
  * (about 5.6 MB held by every GPU that loads the library, until exit); larger n is
  * rejected with HRT_EINVAL.  The first call on a device looks the array's address up
- * and caches it: make it before any stream capture.  All calls share the array: calls
+ * and caches it per device index: make it before any stream capture, and reload the
+ * library after a cudaDeviceReset of that device.  All calls share the array: calls
  * whose GPU work overlaps (other streams or threads) race.  Work is queued on
- * `stream` (a cudaStream_t, NULL = legacy default stream) and the call returns after
- * it finished: HRT_OK, HRT_EINVAL, HRT_ECUDA or HRT_EDEVICE (device error word set). */
+ * `stream` (a cudaStream_t, NULL = legacy default stream); the call then reads the
+ * error word back and waits for that stream only (never the whole device) and returns
+ * HRT_OK, HRT_EINVAL, HRT_ECUDA or HRT_EDEVICE (device error word set). */
 #define HRT_STATIC_MAX_PRIMS 32768
 int hrt_build_accel_static(const float *d_transform, const uint32_t *d_type, int32_t n, void *d_records,
                            void *d_origins, void *d_nodes, uint64_t *d_codes, uint32_t *d_perm, void *stream);
