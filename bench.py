@@ -55,7 +55,7 @@ PROFILE = {
 ACC_DIRECT_RAYS, ACC_DIFFUSE_RAYS = 4, 9  # the accuracy leg's reduced ray counts
 # diffuse-trace variants by the tuner's names (hrt_set_tuning(16 + v) forces one)
 VARIANTS = {"binary4": 1, "binary3": 2, "simple": 3, "wide4": 4, "wide4-3": 5, "lean4": 6, "lean5": 7,
-            "lean4-s16": 8, "lean4-b128": 9, "lean4-b512": 10}
+            "lean4-s16": 8, "lean4-b128": 9, "lean4-b512": 10, "lean4-k4": 11, "lean4-k16": 12}
 
 
 def kernel_sources_digest():
@@ -334,6 +334,7 @@ def run_served(args, device=0):
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
             "wall_s": wall, "bvh_builds": st["builds"], "evictions": st["evictions"],
             "batches": st["batches"], "requests_per_batch": st["batched_requests"] / max(st["batches"], 1),
+            "multi_scene_groups": st["groups"], "batches_in_groups": st["grouped_batches"],
             "plain_solves_per_s": plain_sps, "plain_requests_timed": nplain,
             "speedup_solves_per_s": served_sps / plain_sps}
 

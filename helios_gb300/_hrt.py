@@ -30,7 +30,7 @@ EXPORTS = [
     "hrt_launch_pixel_labels", "hrt_zero_camera_pixel_buffers", "hrt_get_camera_results",
     "hrt_energy_balance", "hrt_run_coupled", "hrt_scene_load", "hrt_scene_last_error", "hrt_scene_count",
     "hrt_scene_arrays", "hrt_scene_data_labels", "hrt_scene_data", "hrt_scene_free",
-    "hrt_plan_launch_chunks", "hrt_set_launch_ray_limit", "hrt_set_visit_budget",
+    "hrt_plan_launch_chunks", "hrt_set_launch_ray_limit", "hrt_set_visit_budget", "hrt_run_sweep_multi",
 ]
 
 
@@ -296,6 +296,7 @@ def load(path: str | None = None):
         "hrt_get_measure": (C.c_int, [VP, VP, C.c_int]),
         "hrt_build_accel_static": (C.c_int, [VP, VP, C.c_int32, VP, VP, VP, VP, VP, VP]),
         "hrt_run_sweep": (C.c_int, [VP, C.POINTER(Sweep), VP]),
+        "hrt_run_sweep_multi": (C.c_int, [C.POINTER(VP), C.POINTER(Sweep), C.c_int32, C.POINTER(VP)]),
         "hrt_server_create": (C.c_int, [C.POINTER(VP), C.c_int, C.c_int, C.c_size_t]),
         "hrt_server_add_scene": (C.c_int, [VP, C.c_uint32, C.POINTER(Geometry), C.c_int32, VP, VP]),
         "hrt_server_submit": (C.c_int, [VP, C.POINTER(ServeRequest)]),
@@ -629,6 +630,16 @@ class Context:
         self.check(self.lib.hrt_run_sweep(self.h, C.byref(S), ptr(flux)))
         return flux
 
+    def _sweep_struct(self, sun_dir, direct_flux, diffuse_flux, rho, tau, direct_rays, diffuse_rays, depth, seed):
+        sd = f32(sun_dir).reshape(-1, 3)
+        nsun = sd.shape[0]
+        df = f32(direct_flux).reshape(nsun, -1)
+        nb = df.shape[1]
+        keep = [sd, df, f32(diffuse_flux).reshape(nsun, nb), f32(rho).reshape(self.n, nb), f32(tau).reshape(self.n, nb)]
+        S = Sweep(nsun, ptr(keep[0]), nb, ptr(keep[1]), ptr(keep[2]), ptr(keep[3]), ptr(keep[4]), int(direct_rays),
+                  int(diffuse_rays), int(depth), int(seed) & 0xFFFFFFFF)
+        return S, keep, (self.n, nsun, nb)
+
     def set_tuning(self, mode: int):
         """1: tune kernel variants per pass shape (default); 0: fixed default; 2: retune."""
         self.check(self.lib.hrt_set_tuning(self.h, int(mode)))
@@ -702,6 +713,27 @@ class Context:
         return st.value
 
 
+def run_sweep_multi(contexts, sweeps, out=True):
+    """Sweeps of several scenes in one launch graph (hrt_run_sweep_multi): contexts[k] holds scene
+    k, sweeps[k] a dict of Context.run_sweep's arguments (sun_dir, direct_flux, diffuse_flux,
+    rho, tau, direct_rays, diffuse_rays, depth, seed).  Returns one flux [n, nsun, nbands] per
+    scene; the graph runs on contexts[0]'s stream."""
+    lib = load()
+    k = len(contexts)
+    structs, keep, shapes = (Sweep * k)(), [], []
+    for i, (c, sw) in enumerate(zip(contexts, sweeps)):
+        S, kp, shape = c._sweep_struct(**sw)
+        structs[i] = S
+        keep.append(kp)
+        shapes.append(shape)
+    handles = (VP * k)(*[c.h for c in contexts])
+    flux = [np.zeros(sh, np.float32) for sh in shapes] if out else None
+    outs = (VP * k)(*[ptr(f) for f in flux]) if out else None
+    rc = lib.hrt_run_sweep_multi(handles, structs, k, outs)
+    contexts[0].check(rc)
+    return flux
+
+
 class Server:
     """Continuous-batching server over libhrt (hrt_server_*)."""
 
@@ -755,10 +787,11 @@ class Server:
                 "rays": rays.value, "flux": flux}
 
     def stats(self):
-        out = np.zeros(6, np.float64)
-        self.check(self.lib.hrt_server_stats(self.h, ptr(out), 6), "stats")
+        out = np.zeros(8, np.float64)
+        self.check(self.lib.hrt_server_stats(self.h, ptr(out), 8), "stats")
         return {"builds": int(out[0]), "evictions": int(out[1]), "resident_bytes": out[2], "budget": out[3],
-                "batches": int(out[4]), "batched_requests": int(out[5])}
+                "batches": int(out[4]), "batched_requests": int(out[5]), "groups": int(out[6]),
+                "grouped_batches": int(out[7])}
 
     def close(self):
         if getattr(self, "h", None):

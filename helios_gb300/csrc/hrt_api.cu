@@ -142,6 +142,12 @@ struct hrt_context {
     cudaGraphExec_t sw_exec = nullptr;
     std::string sw_key;
     int sw_kernels = 0;
+    // multi-scene sweeps this context leads: slot tables and the captured graph
+    DevBuf sw_slots;
+    cudaGraphExec_t mw_exec = nullptr;
+    std::string mw_key;
+    int mw_kernels = 0;
+    unsigned long long multi_rays = 0;
     // rays a lane of the persistent trace takes before its block retires (0: no limit)
     uint32_t lane_budget = 0;
     // rays one trace launch may carry (passes above it run as primitive chunks) and the
@@ -527,6 +533,8 @@ const char *variant_name(int v) {
         case DV_W4S4D16: return "lean4-s16";
         case DV_W4B128: return "lean4-b128";
         case DV_W4B512: return "lean4-b512";
+        case DV_W4K4: return "lean4-k4";
+        case DV_W4K16: return "lean4-k16";
         case DV_PS4: return "binary4";
         case DV_PS3: return "binary3";
         case DV_SIMPLE: return "simple";
@@ -557,11 +565,12 @@ int tuned_variant(hrt_context *ctx, const DiffuseParams &P0, bool record, int *v
     std::vector<int> cand;
     const bool w4 = P0.sc.nodes4 != nullptr;
     if (record)
-        cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_W4S4, DV_W4S5, DV_W4S4D16, DV_W4B128, DV_W4B512, DV_PS3, DV_PS4}
+        cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_W4S4, DV_W4S5, DV_W4S4D16, DV_W4B128, DV_W4B512, DV_W4K4,
+                                     DV_W4K16, DV_PS3, DV_PS4}
                   : std::vector<int>{DV_PS3, DV_PS4};
     else if (P0.sc.voxels) cand = w4 ? std::vector<int>{DV_W4, DV_PS4, DV_SIMPLE} : std::vector<int>{DV_PS4, DV_SIMPLE};
-    else cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_W4S4, DV_W4S5, DV_W4S4D16, DV_W4B128, DV_W4B512, DV_PS4, DV_PS3,
-                                      DV_SIMPLE}
+    else cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_W4S4, DV_W4S5, DV_W4S4D16, DV_W4B128, DV_W4B512, DV_W4K4,
+                                      DV_W4K16, DV_PS4, DV_PS3, DV_SIMPLE}
                    : std::vector<int>{DV_PS4, DV_PS3, DV_SIMPLE};
     DiffuseParams P = P0;
     P.count = std::min(P0.count, std::max(P0.count / 32u, 4096u));
@@ -881,6 +890,7 @@ int hrt_destroy(hrt_context *ctx) {
     cudaStream_t s = ctx->stream, own = ctx->own;
     cudaStreamSynchronize(s);
     if (ctx->sw_exec) cudaGraphExecDestroy(ctx->sw_exec);
+    if (ctx->mw_exec) cudaGraphExecDestroy(ctx->mw_exec);
     collect_timings(ctx);
     g_release_stream = s;  // buffers are released on the context's stream
     delete ctx;
@@ -1704,7 +1714,33 @@ int hrt_run_band(hrt_context *ctx, const hrt_band_solve *s, float *flux_out) {
 }
 
 // ------------------------------------------------------------ batched sweep --
-int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
+}  // extern "C"
+
+namespace {
+
+// A sweep of one scene, prepared for capture: inputs uploaded, buffers sized, the pass
+// sequence's flags and the recording kernel's variant chosen.
+struct SweepPlan {
+    hrt_context *ctx = nullptr;
+    int n = 0, nsun = 0, Bl = 0, C = 0;
+    size_t m = 0;
+    bool scattering = false, any_direct = false, any_diffuse = false, any_copy0 = false, any_active = false;
+    int dimx = 0, dimy = 0, ddx = 0, ddy = 0, Rd = 0, depth = 0;
+    uint32_t seed = 0, rec_per = 0;
+    int rec_variant = DV_W4;
+    float *d_sun = nullptr, *d_flux = nullptr, *d_sky = nullptr, *d_zero = nullptr;
+    uint8_t *m_all = nullptr, *m_fold = nullptr, *m_diff = nullptr, *m_copy0 = nullptr, *m_active = nullptr;
+    float *d_rho = nullptr, *d_tau = nullptr;
+    double *rin = nullptr, *stp = nullptr, *sbt = nullptr, *Gt = nullptr, *Gb = nullptr;
+    float *otop = nullptr, *obot = nullptr, *fin = nullptr;
+    uint32_t *hits = nullptr;
+    bool traces_diffuse() const { return Rd > 0 && any_diffuse; }
+    bool traces_scatter(int it) const { return Rd > 0 && scattering && any_active && it < depth; }
+};
+
+// Validates the sweep, uploads its inputs on the context's stream and sizes its buffers.
+// tune: time the recording kernel's variants (not allowed while another graph is captured).
+int sweep_prepare(hrt_context *ctx, const hrt_sweep *s, bool tune, SweepPlan *pl) {
     if (!ctx || !s) return HRT_EINVAL;
     int r = check_built(ctx);
     if (r) return r;
@@ -1717,37 +1753,45 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
     const int C = nsun * Bl;
     if (C > 256) return fail(ctx, HRT_EUNSUPPORTED, "a sweep holds at most 256 channels");
     if (s->direct_rays < 0 || s->diffuse_rays < 0 || s->scattering_depth < 0) return fail(ctx, HRT_EINVAL, "negative count");
-    const size_t m = (size_t)n * C;
+    SweepPlan P;
+    P.ctx = ctx;
+    P.n = n;
+    P.nsun = nsun;
+    P.Bl = Bl;
+    P.C = C;
+    P.m = (size_t)n * C;
+    P.depth = s->scattering_depth;
+    P.seed = s->seed;
     cudaStream_t st = ctx->stream;
     // per-channel pass-sequence flags of the plain runBand each channel stands for
-    const bool scattering = s->scattering_depth > 0;
+    P.scattering = s->scattering_depth > 0;
     std::vector<uint8_t> all(C, 1), rundirect(C), diffuse(C), fold(C), copy0(C), active(C);
-    bool any_direct = false, any_diffuse = false, any_copy0 = false, any_active = false;
     for (int c = 0; c < C; ++c) {
         rundirect[c] = s->direct_flux[c] > 0.f;
         diffuse[c] = s->diffuse_flux[c] > 0.f;
-        fold[c] = scattering && rundirect[c];
-        copy0[c] = scattering && diffuse[c] && !rundirect[c];
+        fold[c] = P.scattering && rundirect[c];
+        copy0[c] = P.scattering && diffuse[c] && !rundirect[c];
         active[c] = diffuse[c] || rundirect[c];
-        any_direct = any_direct || rundirect[c];
-        any_diffuse = any_diffuse || diffuse[c];
-        any_copy0 = any_copy0 || copy0[c];
-        any_active = any_active || active[c];
+        P.any_direct = P.any_direct || rundirect[c];
+        P.any_diffuse = P.any_diffuse || diffuse[c];
+        P.any_copy0 = P.any_copy0 || copy0[c];
+        P.any_active = P.any_active || active[c];
     }
-    int dimx, dimy;
-    strata((uint32_t)s->direct_rays, &dimx, &dimy);
+    strata((uint32_t)s->direct_rays, &P.dimx, &P.dimy);
     uint32_t rpp_d;
     {
         double c = std::ceil(std::sqrt((double)s->diffuse_rays));
         rpp_d = (uint32_t)(c * c);
     }
-    int ddx, ddy;
-    strata(rpp_d, &ddx, &ddy);
-    const int Rd = ddx * ddy;
+    strata(rpp_d, &P.ddx, &P.ddy);
+    P.Rd = P.ddx * P.ddy;
     // device inputs: [sun 3*nsun][flux C][sky C][zero C] floats, masks 6*C bytes, materials
     CU(ctx->sw_in.ensure(ctx->stream, (3 * (size_t)nsun + 3 * (size_t)C) * sizeof(float) + 6 * (size_t)C + 256));
-    float *d_sun = ctx->sw_in.as<float>(), *d_flux = d_sun + 3 * nsun, *d_sky = d_flux + C, *d_zero = d_sky + C;
-    uint8_t *d_masks = (uint8_t *)(d_zero + C);
+    P.d_sun = ctx->sw_in.as<float>();
+    P.d_flux = P.d_sun + 3 * nsun;
+    P.d_sky = P.d_flux + C;
+    P.d_zero = P.d_sky + C;
+    uint8_t *d_masks = (uint8_t *)(P.d_zero + C);
     {
         std::vector<float> h(3 * (size_t)nsun + 3 * (size_t)C, 0.f);
         std::copy(s->sun_dir, s->sun_dir + 3 * nsun, h.begin());
@@ -1755,36 +1799,48 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
         std::copy(s->diffuse_flux, s->diffuse_flux + C, h.begin() + 3 * nsun + C);
         std::vector<uint8_t> mk8;
         for (auto *v : {&all, &fold, &diffuse, &copy0, &active, &rundirect}) mk8.insert(mk8.end(), v->begin(), v->end());
-        CU(cudaMemcpyAsync(d_sun, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+        CU(cudaMemcpyAsync(P.d_sun, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, st));
         CU(cudaMemcpyAsync(d_masks, mk8.data(), mk8.size(), cudaMemcpyHostToDevice, st));
     }
-    uint8_t *m_all = d_masks, *m_fold = d_masks + C, *m_diff = d_masks + 2 * C, *m_copy0 = d_masks + 3 * C,
-            *m_active = d_masks + 4 * C;
+    P.m_all = d_masks;
+    P.m_fold = d_masks + C;
+    P.m_diff = d_masks + 2 * C;
+    P.m_copy0 = d_masks + 3 * C;
+    P.m_active = d_masks + 4 * C;
     CU(ctx->sw_mat.ensure(ctx->stream, 2 * (size_t)n * Bl * sizeof(float)));
-    float *d_rho = ctx->sw_mat.as<float>(), *d_tau = d_rho + (size_t)n * Bl;
-    CU(cudaMemcpyAsync(d_rho, s->rho, (size_t)n * Bl * sizeof(float), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(d_tau, s->tau, (size_t)n * Bl * sizeof(float), cudaMemcpyHostToDevice, st));
+    P.d_rho = ctx->sw_mat.as<float>();
+    P.d_tau = P.d_rho + (size_t)n * Bl;
+    CU(cudaMemcpyAsync(P.d_rho, s->rho, (size_t)n * Bl * sizeof(float), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P.d_tau, s->tau, (size_t)n * Bl * sizeof(float), cudaMemcpyHostToDevice, st));
     // buffers
+    const size_t m = P.m;
     CU(ctx->sw_acc.ensure(ctx->stream, 5 * m * sizeof(double)));
-    double *rin = ctx->sw_acc.as<double>(), *stp = rin + m, *sbt = stp + m, *Gt = sbt + m, *Gb = Gt + m;
+    P.rin = ctx->sw_acc.as<double>();
+    P.stp = P.rin + m;
+    P.sbt = P.stp + m;
+    P.Gt = P.sbt + m;
+    P.Gb = P.Gt + m;
     CU(ctx->sw_out.ensure(ctx->stream, 3 * m * sizeof(float)));
-    float *otop = ctx->sw_out.as<float>(), *obot = otop + m, *fin = obot + m;
-    const size_t nhits = 2 * (size_t)n * (size_t)std::max(Rd, 1);
+    P.otop = ctx->sw_out.as<float>();
+    P.obot = P.otop + m;
+    P.fin = P.obot + m;
+    const size_t nhits = 2 * (size_t)n * (size_t)std::max(P.Rd, 1);
     // recording launches over primitive chunks of at most rec_per primitives (32-bit ray ids)
-    const uint32_t rec_per = chunk_prims(ctx, 2ull * (uint64_t)std::max(Rd, 1));
-    if (rec_per == 0) return HRT_EUNSUPPORTED;
+    P.rec_per = chunk_prims(ctx, 2ull * (uint64_t)std::max(P.Rd, 1));
+    if (P.rec_per == 0) return HRT_EUNSUPPORTED;
     if ((uint64_t)n * (uint64_t)nsun >= 0xFFFFFFFFull)  // (primitive, sun) sum keys are 32-bit
         return fail(ctx, HRT_EUNSUPPORTED, "primitives x suns of a sweep must stay below 2^32");
     CU(ctx->sw_hits.ensure(ctx->stream, nhits * sizeof(uint32_t)));
+    P.hits = ctx->sw_hits.as<uint32_t>();
     CU(ctx->Gd.ensure(ctx->stream, std::max<size_t>((size_t)n * nsun * 2, 1) * sizeof(double)));
     CU(ctx->fetch.ensure(ctx->stream, sizeof(unsigned long long)));
     // choose the recording kernel's variant before capture (timing cannot run inside a capture)
-    int rec_variant = ctx->n4 > 0 ? DV_W4 : DV_PS3;
-    if (Rd > 0 && (any_diffuse || any_active)) {
+    P.rec_variant = ctx->n4 > 0 ? DV_W4 : DV_PS3;
+    if (tune && P.Rd > 0 && (P.any_diffuse || P.any_active)) {
         DiffuseParams T0{};
         T0.sc = scene_of(ctx);
-        T0.dimx = ddx;
-        T0.dimy = ddy;
+        T0.dimx = P.ddx;
+        T0.dimy = P.ddy;
         T0.seed = s->seed;
         T0.pass = 1;
         T0.count = (uint32_t)n;
@@ -1793,131 +1849,326 @@ int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
         T0.Bl = 1;
         T0.fetch = ctx->fetch.as<unsigned long long>();
         T0.lane_budget = ctx->lane_budget;
-        T0.hits = ctx->sw_hits.as<uint32_t>();
-        if ((r = tuned_variant(ctx, T0, true, &rec_variant))) return r;
+        T0.hits = P.hits;
+        if ((r = tuned_variant(ctx, T0, true, &P.rec_variant))) return r;
     }
-    // capture the pass sequence once per shape
-    char key[256];
-    std::snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%u/%d%d%d%d/%p/%p", n, nsun, Bl, s->direct_rays, s->diffuse_rays,
-                  s->scattering_depth, s->seed, (int)any_direct, (int)any_diffuse, (int)any_copy0, (int)any_active,
-                  ctx->sw_acc.p, ctx->sw_hits.p);
-    {
-        char more[128];
-        std::snprintf(more, sizeof more, "/%p/%p/%p/%p/%p/v%d/c%u", ctx->sw_in.p, ctx->sw_mat.p, ctx->sw_out.p,
-                      ctx->Gd.p, (void *)ctx->stream, rec_variant, rec_per);
-        std::strncat(key, more, sizeof key - std::strlen(key) - 1);
+    *pl = P;
+    return HRT_OK;
+}
+
+// Shape and buffers of a prepared sweep: a captured graph is valid while these stay the same.
+std::string sweep_key(const SweepPlan &P, const hrt_sweep *s) {
+    hrt_context *ctx = P.ctx;
+    char key[384];
+    std::snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%u/%d%d%d%d/%p/%p/%p/%p/%p/%p/%p/v%d/c%u", P.n, P.nsun, P.Bl,
+                  s->direct_rays, s->diffuse_rays, s->scattering_depth, s->seed, (int)P.any_direct,
+                  (int)P.any_diffuse, (int)P.any_copy0, (int)P.any_active, ctx->sw_acc.p, ctx->sw_hits.p,
+                  ctx->sw_in.p, ctx->sw_mat.p, ctx->sw_out.p, ctx->Gd.p, (void *)ctx->stream, P.rec_variant,
+                  P.rec_per);
+    return key;
+}
+
+// Capture-safe stages of a sweep, queued on st.
+struct SweepStages {
+    const SweepPlan &P;
+    cudaStream_t st;
+    int &nk;  // kernels queued
+
+    ChannelEpilogue epilogue() const {
+        ChannelEpilogue E{};
+        E.n = P.n;
+        E.C = P.C;
+        E.Bl = P.Bl;
+        E.rho = P.d_rho;
+        E.tau = P.d_tau;
+        E.rin = P.rin;
+        E.stop = P.stp;
+        E.sbot = P.sbt;
+        E.Gt = P.Gt;
+        E.Gb = P.Gb;
+        E.strength = 1.0 / (double)std::max(P.Rd, 1);
+        return E;
     }
-    if (!ctx->sw_exec || ctx->sw_key != key) {
-        if (ctx->sw_exec) {
-            cudaGraphExecDestroy(ctx->sw_exec);
-            ctx->sw_exec = nullptr;
-        }
-        CU(cudaStreamSynchronize(st));
-        CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        int nk = 0;
-        auto enqueue = [&]() -> cudaError_t {
-            cudaError_t e;
+    DiffuseParams record_params(uint32_t pass) const {
+        DiffuseParams D{};
+        TraceScene sc = scene_of(P.ctx);
+        sc.visits = nullptr;
+        D.sc = sc;
+        D.dimx = P.ddx;
+        D.dimy = P.ddy;
+        D.seed = P.seed;
+        D.pass = pass;
+        D.offset = 0;
+        D.count = (uint32_t)P.n;
+        D.faces = 3;
+        D.fetch = P.ctx->fetch.as<unsigned long long>();
+        D.lane_budget = P.ctx->lane_budget;
+        return D;
+    }
+    // accumulators and the ray counter to zero, the direct pass per sun, the one-sided fold
+    cudaError_t begin() {
+        cudaError_t e;
+        hrt_context *ctx = P.ctx;
+        if ((e = cudaMemsetAsync(P.rin, 0, 3 * P.m * sizeof(double), st)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), st)) != cudaSuccess) return e;
+        if (P.any_direct && P.dimx * P.dimy > 0) {
+            if ((e = cudaMemsetAsync(ctx->Gd.p, 0, (size_t)P.n * P.nsun * 2 * sizeof(double), st)) != cudaSuccess)
+                return e;
             TraceScene sc = scene_of(ctx);
             sc.visits = nullptr;
-            if ((e = cudaMemsetAsync(rin, 0, 3 * m * sizeof(double), st)) != cudaSuccess) return e;
-            if ((e = cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned long long), st)) != cudaSuccess) return e;
-            ChannelEpilogue E{};
-            E.n = n;
-            E.C = C;
-            E.Bl = Bl;
-            E.rho = d_rho;
-            E.tau = d_tau;
-            E.rin = rin;
-            E.stop = stp;
-            E.sbot = sbt;
-            if (any_direct && dimx * dimy > 0) {
-                if ((e = cudaMemsetAsync(ctx->Gd.p, 0, (size_t)n * nsun * 2 * sizeof(double), st)) != cudaSuccess) return e;
-                SweepDirectParams D{sc, d_sun, nsun, dimx, dimy, s->seed, ctx->Gd.as<double>()};
-                if ((e = launch_direct_sweep(D, max_blocks(ctx), st)) != cudaSuccess) return e;
-                E.flux = d_flux;
-                E.mask = m_all;
-                E.Gd = ctx->Gd.as<double>();
-                if ((e = launch_epilogue_direct_channels(E, st)) != cudaSuccess) return e;
-                nk += 2;
-            }
-            if ((e = launch_fold_channels(n, C, m_fold, sc.twosided, stp, sbt, otop, obot, st)) != cudaSuccess) return e;
-            ++nk;
-            DiffuseParams P{};
-            P.sc = sc;
-            P.dimx = ddx;
-            P.dimy = ddy;
-            P.seed = s->seed;
-            P.offset = 0;
-            P.count = (uint32_t)n;
-            P.faces = 3;
-            P.fetch = ctx->fetch.as<unsigned long long>();
-            P.lane_budget = ctx->lane_budget;
-            GatherParams Gp{n, C, Rd, 3, sc.twosided, ctx->sw_hits.as<uint32_t>(), otop, obot, d_sky, Gt, Gb};
-            E.Gt = Gt;
-            E.Gb = Gb;
-            E.strength = 1.0 / (double)std::max(Rd, 1);
-            auto pass = [&](uint32_t pass_id, const float *sky, const uint8_t *mask) -> cudaError_t {
-                cudaError_t e2;
-                DiffuseParams Q = P;
-                Q.pass = pass_id;
-                for (uint32_t done = 0; done < (uint32_t)n; done += Q.count) {
-                    Q.offset = done;
-                    Q.count = std::min(rec_per, (uint32_t)n - done);
-                    if ((e2 = launch_diffuse_record(Q, ctx->sw_hits.as<uint32_t>(), rec_variant, st)) != cudaSuccess)
-                        return e2;
-                    ++nk;
-                }
-                Gp.sky = sky;
-                if ((e2 = launch_gather(Gp, st)) != cudaSuccess) return e2;
-                E.mask = mask;
-                if ((e2 = launch_epilogue_diffuse_channels(E, st)) != cudaSuccess) return e2;
-                nk += 2;
-                return cudaSuccess;
-            };
-            if (any_diffuse && Rd > 0) {
-                if ((e = pass(1u, d_sky, m_diff)) != cudaSuccess) return e;
-            }
-            if (any_copy0) {
-                if ((e = launch_copy_channels(n, C, m_copy0, stp, sbt, otop, obot, 1, st)) != cudaSuccess) return e;
-                ++nk;
-            }
-            if (scattering && any_active && Rd > 0) {
-                for (int it = 0; it < s->scattering_depth; ++it) {
-                    if (it > 0) {
-                        if ((e = launch_copy_channels(n, C, m_all, stp, sbt, otop, obot, 0, st)) != cudaSuccess) return e;
-                        ++nk;
-                    }
-                    if ((e = cudaMemsetAsync(stp, 0, 2 * m * sizeof(double), st)) != cudaSuccess) return e;
-                    if ((e = pass(2u + (uint32_t)it, d_zero, m_active)) != cudaSuccess) return e;
-                }
-            }
-            if ((e = launch_final_flux(m, rin, stp, sbt, fin, st)) != cudaSuccess) return e;
-            ++nk;
-            return cudaSuccess;
-        };
-        cudaError_t ee = enqueue();
-        cudaGraph_t g = nullptr;
-        cudaError_t ec = cudaStreamEndCapture(st, &g);
-        if (ee != cudaSuccess || ec != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            return fail(ctx, HRT_ECUDA, std::string("sweep capture failed: ") +
-                                            cudaGetErrorString(ee != cudaSuccess ? ee : ec));
+            SweepDirectParams D{sc, P.d_sun, P.nsun, P.dimx, P.dimy, P.seed, ctx->Gd.as<double>()};
+            if ((e = launch_direct_sweep(D, max_blocks(ctx), st)) != cudaSuccess) return e;
+            ChannelEpilogue E = epilogue();
+            E.flux = P.d_flux;
+            E.mask = P.m_all;
+            E.Gd = ctx->Gd.as<double>();
+            if ((e = launch_epilogue_direct_channels(E, st)) != cudaSuccess) return e;
+            nk += 2;
         }
-        cudaError_t ei = cudaGraphInstantiate(&ctx->sw_exec, g, 0);
-        cudaGraphDestroy(g);
-        if (ei != cudaSuccess) return fail(ctx, HRT_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+        if ((e = launch_fold_channels(P.n, P.C, P.m_fold, scene_of(ctx).twosided, P.stp, P.sbt, P.otop, P.obot, st)) !=
+            cudaSuccess)
+            return e;
+        ++nk;
+        return cudaSuccess;
+    }
+    // this scene's recording launches of one pass (primitive chunks of the plan)
+    cudaError_t record(uint32_t pass) {
+        DiffuseParams Q = record_params(pass);
+        for (uint32_t done = 0; done < (uint32_t)P.n; done += Q.count) {
+            Q.offset = done;
+            Q.count = std::min(P.rec_per, (uint32_t)P.n - done);
+            cudaError_t e = launch_diffuse_record(Q, P.hits, P.rec_variant, st);
+            if (e != cudaSuccess) return e;
+            ++nk;
+        }
+        return cudaSuccess;
+    }
+    // channel gather of the recorded hits and the pass's epilogue
+    cudaError_t gather(const float *sky, const uint8_t *mask) {
+        cudaError_t e;
+        GatherParams Gp{P.n, P.C, P.Rd, 3, scene_of(P.ctx).twosided, P.hits, P.otop, P.obot, sky, P.Gt, P.Gb};
+        if ((e = launch_gather(Gp, st)) != cudaSuccess) return e;
+        ChannelEpilogue E = epilogue();
+        E.mask = mask;
+        if ((e = launch_epilogue_diffuse_channels(E, st)) != cudaSuccess) return e;
+        nk += 2;
+        return cudaSuccess;
+    }
+    cudaError_t after_primary() {
+        if (!P.any_copy0) return cudaSuccess;
+        ++nk;
+        return launch_copy_channels(P.n, P.C, P.m_copy0, P.stp, P.sbt, P.otop, P.obot, 1, st);
+    }
+    // before scattering iteration it: scatter -> radiation_out (it > 0), scatter sums to zero
+    cudaError_t before_scatter(int it) {
+        cudaError_t e;
+        if (it > 0) {
+            if ((e = launch_copy_channels(P.n, P.C, P.m_all, P.stp, P.sbt, P.otop, P.obot, 0, st)) != cudaSuccess)
+                return e;
+            ++nk;
+        }
+        return cudaMemsetAsync(P.stp, 0, 2 * P.m * sizeof(double), st);
+    }
+    cudaError_t finish() {
+        ++nk;
+        return launch_final_flux(P.m, P.rin, P.stp, P.sbt, P.fin, st);
+    }
+};
+
+// Capture `enqueue` on st into *exec (replacing the old graph).
+template <class F>
+int capture_graph(hrt_context *ctx, cudaStream_t st, cudaGraphExec_t *exec, F &&enqueue) {
+    if (*exec) {
+        cudaGraphExecDestroy(*exec);
+        *exec = nullptr;
+    }
+    CU(cudaStreamSynchronize(st));
+    CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ee = enqueue();
+    cudaGraph_t g = nullptr;
+    cudaError_t ec = cudaStreamEndCapture(st, &g);
+    if (ee != cudaSuccess || ec != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(ctx, HRT_ECUDA, std::string("sweep capture failed: ") + cudaGetErrorString(ee != cudaSuccess ? ee : ec));
+    }
+    cudaError_t ei = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return fail(ctx, HRT_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+    return HRT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out) {
+    SweepPlan P;
+    int r = sweep_prepare(ctx, s, true, &P);
+    if (r) return r;
+    cudaStream_t st = ctx->stream;
+    // capture the pass sequence once per shape
+    const std::string key = sweep_key(P, s);
+    if (!ctx->sw_exec || ctx->sw_key != key) {
+        int nk = 0;
+        SweepStages S{P, st, nk};
+        r = capture_graph(ctx, st, &ctx->sw_exec, [&]() -> cudaError_t {
+            cudaError_t e;
+            if ((e = S.begin()) != cudaSuccess) return e;
+            if (P.traces_diffuse()) {
+                if ((e = S.record(1u)) != cudaSuccess || (e = S.gather(P.d_sky, P.m_diff)) != cudaSuccess) return e;
+            }
+            if ((e = S.after_primary()) != cudaSuccess) return e;
+            for (int it = 0; P.traces_scatter(it); ++it) {
+                if ((e = S.before_scatter(it)) != cudaSuccess || (e = S.record(2u + (uint32_t)it)) != cudaSuccess ||
+                    (e = S.gather(P.d_zero, P.m_active)) != cudaSuccess)
+                    return e;
+            }
+            return S.finish();
+        });
+        if (r) return r;
         ctx->sw_key = key;
         ctx->sw_kernels = nk;
     }
     CU(cudaGraphLaunch(ctx->sw_exec, st));
     ctx->last_kernels = ctx->sw_kernels;
-    if (flux_out) CU(cudaMemcpyAsync(flux_out, fin, m * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (flux_out) CU(cudaMemcpyAsync(flux_out, P.fin, P.m * sizeof(float), cudaMemcpyDeviceToHost, st));
     unsigned long long rays = 0;
     CU(cudaMemcpyAsync(&rays, ctx->counter.p, sizeof(rays), cudaMemcpyDeviceToHost, st));
     r = sync_and_status(ctx);
     ctx->last_rays = rays;
     ctx->last_iters = (uint64_t)s->scattering_depth;
     return r;
+}
+
+int hrt_run_sweep_multi(hrt_context *const *ctxs, const hrt_sweep *sweeps, int32_t nscenes, float *const *flux_out) {
+    if (!ctxs || !sweeps || nscenes < 1 || !ctxs[0]) return HRT_EINVAL;
+    hrt_context *ctx = ctxs[0];  // owns the graph and the slot tables; its stream runs the graph
+    for (int k = 0; k < nscenes; ++k) {
+        if (!ctxs[k]) return fail(ctx, HRT_EINVAL, "null context in a multi-scene sweep");
+        if (ctxs[k]->device != ctx->device) return fail(ctx, HRT_EINVAL, "the scenes of a multi-scene sweep share one device");
+        for (int j = 0; j < k; ++j)
+            if (ctxs[j] == ctxs[k]) return fail(ctx, HRT_EINVAL, "a context appears twice in a multi-scene sweep");
+    }
+    std::vector<SweepPlan> plans(nscenes);
+    std::string key = "multi";
+    int r;
+    for (int k = 0; k < nscenes; ++k) {
+        if ((r = sweep_prepare(ctxs[k], &sweeps[k], false, &plans[k]))) {
+            if (k > 0) fail(ctx, r, std::string("scene ") + std::to_string(k) + ": " + ctxs[k]->err);
+            return r;
+        }
+        if (ctxs[k]->n4 <= 0) return fail(ctx, HRT_EUNSUPPORTED, "multi-scene sweeps trace 4-wide trees");
+        key += "|" + sweep_key(plans[k], &sweeps[k]);
+    }
+    for (int k = 1; k < nscenes; ++k) CU(cudaStreamSynchronize(ctxs[k]->stream));  // their uploads
+    cudaStream_t st = ctx->stream;
+    // slot tables of the recording passes: pass 0 = primary diffuse, pass 1 + it = scattering it;
+    // a pass lists the primitive chunks of every scene that traces it
+    int maxdepth = 0;
+    for (const auto &P : plans) maxdepth = std::max(maxdepth, P.depth);
+    std::vector<SceneSlot> slots;
+    std::vector<int> pass_first, pass_count;
+    std::vector<unsigned long long> pass_total;
+    for (int pass = 0; pass <= maxdepth; ++pass) {
+        pass_first.push_back((int)slots.size());
+        unsigned long long id = 0;
+        for (const auto &P : plans) {
+            if (!(pass == 0 ? P.traces_diffuse() : P.traces_scatter(pass - 1))) continue;
+            for (uint32_t done = 0; done < (uint32_t)P.n; done += P.rec_per) {
+                SceneSlot sl{};
+                sl.sc = scene_of(P.ctx);
+                sl.sc.visits = nullptr;
+                sl.dimx = P.ddx;
+                sl.dimy = P.ddy;
+                sl.seed = P.seed;
+                sl.pass = 1u + (uint32_t)pass;
+                sl.offset = done;
+                sl.count = std::min(P.rec_per, (uint32_t)P.n - done);
+                sl.id_begin = id;
+                sl.hits = P.hits;
+                id += (unsigned long long)sl.count * (unsigned long long)P.Rd * 2ull;
+                slots.push_back(sl);
+            }
+        }
+        pass_count.push_back((int)slots.size() - pass_first.back());
+        pass_total.push_back(id);
+        if (pass_count.back() > kMaxSlots)
+            return fail(ctx, HRT_EUNSUPPORTED, "a multi-scene pass holds at most 32 scene chunks");
+    }
+    CU(ctx->sw_slots.ensure(st, std::max<size_t>(slots.size(), 1) * sizeof(SceneSlot)));
+    CU(cudaMemcpyAsync(ctx->sw_slots.p, slots.data(), slots.size() * sizeof(SceneSlot), cudaMemcpyHostToDevice, st));
+    {
+        char more[64];
+        std::snprintf(more, sizeof more, "|slots %p %zu", ctx->sw_slots.p, slots.size());
+        key += more;
+    }
+    if (!ctx->mw_exec || ctx->mw_key != key) {
+        int nk = 0;
+        std::vector<SweepStages> S;
+        for (const auto &P : plans) S.push_back(SweepStages{P, st, nk});
+        auto multi_record = [&](int pass) -> cudaError_t {
+            if (pass_count[pass] == 0) return cudaSuccess;
+            DiffuseParams D{};
+            D.faces = 3;
+            D.fetch = ctx->fetch.as<unsigned long long>();
+            D.lane_budget = 0;
+            D.slots = ctx->sw_slots.as<SceneSlot>() + pass_first[pass];
+            D.nslots = pass_count[pass];
+            D.multi_total = pass_total[pass];
+            ++nk;
+            return launch_w4s_multi_record(D, st);
+        };
+        r = capture_graph(ctx, st, &ctx->mw_exec, [&]() -> cudaError_t {
+            cudaError_t e;
+            for (auto &s : S)
+                if ((e = s.begin()) != cudaSuccess) return e;
+            if ((e = multi_record(0)) != cudaSuccess) return e;
+            for (size_t k = 0; k < S.size(); ++k)
+                if (plans[k].traces_diffuse() && (e = S[k].gather(plans[k].d_sky, plans[k].m_diff)) != cudaSuccess)
+                    return e;
+            for (auto &s : S)
+                if ((e = s.after_primary()) != cudaSuccess) return e;
+            for (int it = 0; it < maxdepth; ++it) {
+                for (size_t k = 0; k < S.size(); ++k)
+                    if (plans[k].traces_scatter(it) && (e = S[k].before_scatter(it)) != cudaSuccess) return e;
+                if ((e = multi_record(1 + it)) != cudaSuccess) return e;
+                for (size_t k = 0; k < S.size(); ++k)
+                    if (plans[k].traces_scatter(it) && (e = S[k].gather(plans[k].d_zero, plans[k].m_active)) != cudaSuccess)
+                        return e;
+            }
+            for (auto &s : S)
+                if ((e = s.finish()) != cudaSuccess) return e;
+            return cudaSuccess;
+        });
+        if (r) return r;
+        ctx->mw_key = key;
+        ctx->mw_kernels = nk;
+    }
+    CU(cudaGraphLaunch(ctx->mw_exec, st));
+    std::vector<unsigned long long> rays(nscenes, 0);
+    for (int k = 0; k < nscenes; ++k) {
+        if (flux_out && flux_out[k])
+            CU(cudaMemcpyAsync(flux_out[k], plans[k].fin, plans[k].m * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(&rays[k], ctxs[k]->counter.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    }
+    CU(cudaStreamSynchronize(st));
+    int status = HRT_OK;
+    unsigned long long total = 0;
+    for (int k = 0; k < nscenes; ++k) {
+        ctxs[k]->last_rays = rays[k];
+        ctxs[k]->last_iters = (uint64_t)sweeps[k].scattering_depth;
+        ctxs[k]->last_kernels = ctx->mw_kernels;
+        total += rays[k];
+        uint32_t word = 0;  // each scene's device error word (the graph ran on ctx's stream)
+        CU(cudaMemcpy(&word, ctxs[k]->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        if (word && status == HRT_OK) {
+            int rk = sync_and_status(ctxs[k]);
+            status = rk;
+            if (k > 0) fail(ctx, rk, std::string("scene ") + std::to_string(k) + ": " + ctxs[k]->err);
+        }
+    }
+    ctx->multi_rays = total;
+    return status;
 }
 
 int hrt_set_launch_ray_limit(hrt_context *ctx, uint64_t max_rays) {

@@ -84,6 +84,19 @@ struct SkyParams {
     const float *prague;   // [Bc*4]
 };
 
+// One scene of a multi-scene recording launch (k_diffuse_w4 MULTI): its trace scene, the
+// primitive chunk and ray counts of its pass, and the launch's ray ids [id_begin, id_begin +
+// count * dimx * dimy * faces) that belong to it.
+struct SceneSlot {
+    TraceScene sc;
+    int dimx, dimy;
+    uint32_t seed, pass;
+    uint32_t offset, count;          // primitive chunk (count x rays x faces < 2^31)
+    unsigned long long id_begin;
+    uint32_t *hits;                  // [face][n][R] hit codes of this scene
+};
+constexpr int kMaxSlots = 32;        // scenes (chunks) one multi-scene launch carries
+
 struct DiffuseParams {
     TraceScene sc;
     int dimx, dimy;
@@ -103,6 +116,9 @@ struct DiffuseParams {
                                // rays when fewer than this many lanes are still in it (0: never);
                                // set by the launcher
     GlassParams gl;            // launches with covers (sc.cover non-null)
+    const SceneSlot *slots = nullptr;     // multi-scene recording: [nslots] device table
+    int nslots = 0;
+    unsigned long long multi_total = 0;   // ray ids of all slots
 };
 
 // ---------------------------------------------------------------- cameras
@@ -212,14 +228,18 @@ cudaError_t launch_diffuse(const DiffuseParams &p, int max_blocks, cudaStream_t 
 enum DiffuseVariant {
     DV_DEFAULT = 0, DV_PS4 = 1, DV_PS3 = 2, DV_SIMPLE = 3, DV_W4 = 4, DV_W43 = 5,
     // lean 4-wide trace (k_diffuse_w4): threads per block x resident blocks per SM, shared
-    // stack entries per lane -- 256 x 4, 8; 256 x 5, 8; 256 x 4, 16; 128 x 8, 8; 512 x 2, 8
-    DV_W4S4 = 6, DV_W4S5 = 7, DV_W4S4D16 = 8, DV_W4B128 = 9, DV_W4B512 = 10,
-    DV_LAST = DV_W4B512
+    // stack entries per lane, ray ids a warp takes per fetch (32 x batch) -- 256 x 4, 8, 1;
+    // 256 x 5, 8, 1; 256 x 4, 16, 1; 128 x 8, 8, 1; 512 x 2, 8, 1; 256 x 4, 8, 4; 256 x 4, 8, 16
+    DV_W4S4 = 6, DV_W4S5 = 7, DV_W4S4D16 = 8, DV_W4B128 = 9, DV_W4B512 = 10, DV_W4K4 = 11, DV_W4K16 = 12,
+    DV_LAST = DV_W4K16
 };
 bool is_w4s_variant(int v);
 cudaError_t launch_w4s(const DiffuseParams &p, int variant, cudaStream_t s);
 cudaError_t launch_w4s_record(const DiffuseParams &p, uint32_t *hits, int variant, cudaStream_t s);
 cudaError_t launch_w4s_stats(const DiffuseParams &p, int variant, cudaStream_t s);
+// Multi-scene recording launch: p.fetch, p.faces, p.slots / nslots / multi_total set; the
+// other scene fields of p are unused.
+cudaError_t launch_w4s_multi_record(const DiffuseParams &p, cudaStream_t s);
 cudaError_t launch_diffuse_variant(const DiffuseParams &p, int variant, int max_blocks, cudaStream_t s);
 // persistent-kernel launchers (hrt_ps_accumulate.cu, hrt_ps_special.cu)
 cudaError_t launch_ps_accumulate(const DiffuseParams &p, int variant, cudaStream_t s);

@@ -21,7 +21,7 @@ unsigned w4_grid(const DiffuseParams &p, int resident, int block) {
     return (unsigned)g;
 }
 
-template <int NB, bool RECORD, bool STATS, int MINB, int SD, int BLOCK>
+template <int NB, bool RECORD, bool STATS, int MINB, int SD, int BLOCK, int KB = 1, bool MULTI = false>
 cudaError_t w4_launch(const DiffuseParams &p, cudaStream_t s) {
     // resident blocks of one wave (SMs x blocks per SM); initialised once per instantiation,
     // thread-safe (the server launches from several threads)
@@ -29,20 +29,21 @@ cudaError_t w4_launch(const DiffuseParams &p, cudaStream_t s) {
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_diffuse_w4<NB, RECORD, STATS, MINB, SD, BLOCK>,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm,
+                                                      k_diffuse_w4<NB, RECORD, STATS, MINB, SD, BLOCK, KB, MULTI>,
                                                       BLOCK, 0);
         return (sms < 1 ? 1 : sms) * (per_sm < 1 ? 1 : per_sm);
     }();
     cudaError_t e = cudaMemsetAsync(p.fetch, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     DiffuseParams q = p;
-    q.refill = refill_threshold(false);
-    k_diffuse_w4<NB, RECORD, STATS, MINB, SD, BLOCK><<<w4_grid(q, resident, BLOCK), BLOCK, 0, s>>>(q);
+    q.refill = refill_threshold(false, true);
+    k_diffuse_w4<NB, RECORD, STATS, MINB, SD, BLOCK, KB, MULTI><<<w4_grid(q, resident, BLOCK), BLOCK, 0, s>>>(q);
     return cudaGetLastError();
 }
 
 // The tuner's shapes: threads per block x resident blocks per SM (all 64 registers a thread
-// but lean5, 48) and shared stack entries per lane.
+// but lean5, 48), shared stack entries per lane and the warp's ray-id batch.
 template <int NB, bool RECORD, bool STATS>
 cudaError_t w4_shape(const DiffuseParams &p, int variant, cudaStream_t s) {
     switch (variant) {
@@ -50,13 +51,15 @@ cudaError_t w4_shape(const DiffuseParams &p, int variant, cudaStream_t s) {
         case DV_W4S4D16: return w4_launch<NB, RECORD, STATS, 4, 16, 256>(p, s);
         case DV_W4B128: return w4_launch<NB, RECORD, STATS, 8, 8, 128>(p, s);
         case DV_W4B512: return w4_launch<NB, RECORD, STATS, 2, 8, 512>(p, s);
+        case DV_W4K4: return w4_launch<NB, RECORD, STATS, 4, 8, 256, 4>(p, s);
+        case DV_W4K16: return w4_launch<NB, RECORD, STATS, 4, 8, 256, 16>(p, s);
         default: return w4_launch<NB, RECORD, STATS, 4, 8, 256>(p, s);
     }
 }
 
 }  // namespace
 
-bool is_w4s_variant(int v) { return v >= DV_W4S4 && v <= DV_W4B512; }
+bool is_w4s_variant(int v) { return v >= DV_W4S4 && v <= DV_W4K16; }
 
 cudaError_t launch_w4s(const DiffuseParams &p, int variant, cudaStream_t s) {
     if (!p.sc.nodes4 || p.sc.voxels) return cudaErrorInvalidValue;
@@ -74,6 +77,14 @@ cudaError_t launch_w4s_record(const DiffuseParams &p, uint32_t *hits, int varian
     q.hits = hits;
     q.Bc = 1;
     return w4_shape<1, true, false>(q, variant, s);
+}
+
+cudaError_t launch_w4s_multi_record(const DiffuseParams &p, cudaStream_t s) {
+    if (!p.slots || p.nslots < 1 || p.nslots > kMaxSlots || p.lane_budget) return cudaErrorInvalidValue;
+    if (p.multi_total == 0) return cudaSuccess;
+    DiffuseParams q = p;
+    q.Bc = 1;
+    return w4_launch<1, true, false, 4, 8, 256, 1, true>(q, s);
 }
 
 cudaError_t launch_w4s_stats(const DiffuseParams &p, int variant, cudaStream_t s) {

@@ -18,10 +18,17 @@
 // and scattering passes once for the whole batch.  Each channel is the solve its
 // request would get alone (same Philox streams), so a result depends only on the
 // request -- the same alone as in the mix, up to the order of FP64 sums.
+//
+// Across scenes: the small batches that one dispatch scan admits (different scenes, each
+// below kGroupRays traced rays) form one work item, solved by hrt_run_sweep_multi: every
+// scene's direct pass and bookkeeping in one captured graph, and each diffuse or scattering
+// pass of all of them in one persistent launch (a lone request is a one-sun sweep, which is
+// its runBand).  HRT_SERVE_GROUP=0 turns this off.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <iterator>
@@ -63,6 +70,18 @@ constexpr uint32_t kRayBudget = 32; // rays per thread before a trace block reti
 // drops; small batches still run beside them (higher stream priority).
 constexpr double kLargeRays = 2e8;
 constexpr int kMaxBatch = 64;      // requests per batch
+// Batches of at most this many traced rays are grouped across scenes (small solves, where
+// per-launch and per-graph overheads weigh most), at most kMaxGroup scenes per group.
+constexpr double kGroupRays = 5e7;
+constexpr int kMaxGroup = 16;
+
+bool group_enabled() {
+    static const bool on = [] {  // initialised once, thread-safe
+        const char *e = std::getenv("HRT_SERVE_GROUP");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
 
 struct Request {
     uint64_t id = 0;
@@ -99,7 +118,9 @@ struct hrt_server {
     std::condition_variable cv_dispatch, cv_work, cv_done;
     std::map<uint32_t, std::unique_ptr<Scene>> scenes;
     std::deque<Request *> arrivals;   // sorted by arrival time when started
-    std::deque<std::vector<Request *>> ready;  // admitted batches, waiting for a worker
+    // admitted work, waiting for a worker: one batch, or small batches of different scenes
+    std::deque<std::vector<std::vector<Request *>>> ready;
+    size_t groups = 0, grouped_batches = 0;
     std::map<uint64_t, std::unique_ptr<Request>> requests;
     std::vector<std::thread> workers;
     std::thread dispatcher;
@@ -181,46 +202,75 @@ int solve_one(Scene *sc, Request *r, int Bl) {
     return HRT_OK;
 }
 
-// A batch of compatible requests: one sweep, channel c = request * Bl + band.
-int solve_batch(Scene *sc, const std::vector<Request *> &batch, int Bl) {
+int launched_bands(const Request *r) {
+    int Bl = 0;
+    for (uint8_t f : r->band_launch) Bl += f ? 1 : 0;
+    return Bl;
+}
+
+// Traced rays of a batch (direct rays per request, diffuse passes shared).
+double batch_rays(const Scene *sc, const std::vector<Request *> &batch) {
+    const Request *r0 = batch[0];
+    const double side = std::ceil(std::sqrt((double)r0->diffuse_rays));
+    return (double)sc->n * ((double)r0->direct_rays * (double)batch.size() + 2.0 * side * side * (1.0 + (double)r0->depth));
+}
+
+// The sweep of a batch of compatible requests: channel c = request * Bl + band.
+struct SweepInput {
+    std::vector<float> rho, tau, sun, dflux, sflux, out;
+    hrt_sweep w{};
+    int Bl = 0;
+};
+
+void make_sweep(const Scene *sc, const std::vector<Request *> &batch, SweepInput *in) {
+    const int Bl = launched_bands(batch[0]);
     const int nr = (int)batch.size(), C = nr * Bl;
     const size_t n = (size_t)sc->n;
     std::vector<int> cols;
     for (int b = 0; b < sc->nbands; ++b)
         if (batch[0]->band_launch[b]) cols.push_back(b);
-    std::vector<float> rho(n * Bl), tau(n * Bl), sun(3 * (size_t)nr), dflux(C), sflux(C);
+    in->Bl = Bl;
+    in->rho.assign(n * Bl, 0.f);
+    in->tau.assign(n * Bl, 0.f);
+    in->sun.assign(3 * (size_t)nr, 0.f);
+    in->dflux.assign(C, 0.f);
+    in->sflux.assign(C, 0.f);
+    in->out.assign(n * C, 0.f);
     for (size_t p = 0; p < n; ++p)
         for (int b = 0; b < Bl; ++b) {
-            rho[p * Bl + b] = sc->rho[p * sc->nbands + cols[b]];
-            tau[p * Bl + b] = sc->tau[p * sc->nbands + cols[b]];
+            in->rho[p * Bl + b] = sc->rho[p * sc->nbands + cols[b]];
+            in->tau[p * Bl + b] = sc->tau[p * sc->nbands + cols[b]];
         }
     for (int i = 0; i < nr; ++i) {
-        for (int k = 0; k < 3; ++k) sun[3 * i + k] = batch[i]->sun[k];
+        for (int k = 0; k < 3; ++k) in->sun[3 * i + k] = batch[i]->sun[k];
         for (int b = 0; b < Bl; ++b) {
-            dflux[i * Bl + b] = batch[i]->source_flux[b];
-            sflux[i * Bl + b] = batch[i]->diffuse_flux[b];
+            in->dflux[i * Bl + b] = batch[i]->source_flux[b];
+            in->sflux[i * Bl + b] = batch[i]->diffuse_flux[b];
         }
     }
-    hrt_sweep w{};
+    hrt_sweep &w = in->w;
+    w = hrt_sweep{};
     w.nsun = nr;
-    w.sun_dir = sun.data();
+    w.sun_dir = in->sun.data();
     w.nbands = Bl;
-    w.direct_flux = dflux.data();
-    w.diffuse_flux = sflux.data();
-    w.rho = rho.data();
-    w.tau = tau.data();
+    w.direct_flux = in->dflux.data();
+    w.diffuse_flux = in->sflux.data();
+    w.rho = in->rho.data();
+    w.tau = in->tau.data();
     w.direct_rays = batch[0]->direct_rays;
     w.diffuse_rays = batch[0]->diffuse_rays;
     w.scattering_depth = batch[0]->depth;
     w.seed = batch[0]->seed;
-    std::vector<float> out(n * C);
-    int rc = hrt_run_sweep(sc->ctx, &w, out.data());
-    if (rc != HRT_OK) return rc;
-    uint64_t st[2] = {0, 0};
-    hrt_last_stats(sc->ctx, st, 2);
+}
+
+// Results of a solved sweep back to its requests; rays of the batch shared evenly.
+void take_results(const Scene *sc, const std::vector<Request *> &batch, const SweepInput &in, uint64_t rays) {
+    const int nr = (int)batch.size(), Bl = in.Bl, C = nr * Bl;
+    const size_t n = (size_t)sc->n;
+    const std::vector<float> &out = in.out;
     for (int i = 0; i < nr; ++i) {
         Request *r = batch[i];
-        r->rays = st[0] / (uint64_t)nr;  // the batch's rays, shared evenly
+        r->rays = rays / (uint64_t)nr;
         std::vector<float> flux(n * Bl);
         double sum = 0.0;
         for (size_t p = 0; p < n; ++p)
@@ -232,61 +282,100 @@ int solve_batch(Scene *sc, const std::vector<Request *> &batch, int Bl) {
         r->checksum = sum;
         if (r->keep) r->flux.swap(flux);
     }
+}
+
+int solve_batch(Scene *sc, const std::vector<Request *> &batch) {
+    SweepInput in;
+    make_sweep(sc, batch, &in);
+    int rc = hrt_run_sweep(sc->ctx, &in.w, in.out.data());
+    if (rc != HRT_OK) return rc;
+    uint64_t st[2] = {0, 0};
+    hrt_last_stats(sc->ctx, st, 2);
+    take_results(sc, batch, in, st[0]);
     return HRT_OK;
+}
+
+// Small batches of different scenes: one multi-scene sweep.
+int solve_group(const std::vector<Scene *> &scs, const std::vector<std::vector<Request *>> &batches) {
+    const size_t k = scs.size();
+    std::vector<SweepInput> in(k);
+    std::vector<hrt_context *> ctxs(k);
+    std::vector<hrt_sweep> sweeps(k);
+    std::vector<float *> outs(k);
+    for (size_t i = 0; i < k; ++i) {
+        make_sweep(scs[i], batches[i], &in[i]);
+        ctxs[i] = scs[i]->ctx;
+        sweeps[i] = in[i].w;
+        outs[i] = in[i].out.data();
+    }
+    int rc = hrt_run_sweep_multi(ctxs.data(), sweeps.data(), (int32_t)k, outs.data());
+    if (rc != HRT_OK) return rc;
+    for (size_t i = 0; i < k; ++i) {
+        uint64_t st[2] = {0, 0};
+        hrt_last_stats(scs[i]->ctx, st, 2);
+        take_results(scs[i], batches[i], in[i], st[0]);
+    }
+    return HRT_OK;
+}
+
+// Device context of a scene: created, geometry uploaded, BVH built and materials set the
+// first time the scene is solved (or after an eviction).
+int prepare_scene(hrt_server *s, Scene *sc) {
+    if (sc->ctx) return HRT_OK;
+    int rc = hrt_create(&sc->ctx, s->device);
+    if (rc == HRT_OK) {
+        // Smaller scenes get higher stream priority and every trace block retires after
+        // kRayBudget rays per thread, so a small solve's blocks start as soon as SMs free up
+        // instead of waiting for a large solve to end.
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        double f = (std::log10((double)std::max(sc->n, 1)) - 3.0) / 3.5;  // 1e3 .. 3e6 prims
+        f = std::min(1.0, std::max(0.0, f));
+        const int prio = greatest + (int)std::lround(f * (double)(least - greatest));
+        if (cudaStreamCreateWithPriority(&sc->stream, cudaStreamNonBlocking, prio) == cudaSuccess)
+            rc = hrt_set_stream(sc->ctx, sc->stream);
+        if (rc == HRT_OK) rc = hrt_set_ray_budget(sc->ctx, kRayBudget);
+        // fixed default kernels: timing trials per scene would cost more than they save
+        if (rc == HRT_OK) rc = hrt_set_tuning(sc->ctx, 0);
+    }
+    if (rc == HRT_OK) {
+        hrt_geometry g{};
+        g.n = sc->n;
+        g.transform = sc->T.data();
+        g.type = sc->type.data();
+        g.twosided = sc->twosided.data();
+        rc = hrt_update_geometry(sc->ctx, &g);
+        if (rc == HRT_OK) rc = hrt_build_accel(sc->ctx);
+        if (rc == HRT_OK) rc = hrt_update_materials(sc->ctx, 1, sc->n, sc->nbands, sc->rho.data(), sc->tau.data());
+        std::lock_guard<std::mutex> lk(s->mu);
+        ++s->builds;
+    }
+    return rc;
 }
 
 void worker_loop(hrt_server *s) {
     for (;;) {
-        std::vector<Request *> batch;
-        Scene *sc = nullptr;
+        std::vector<std::vector<Request *>> item;
+        std::vector<Scene *> scs;
         {
             std::unique_lock<std::mutex> lk(s->mu);
             s->cv_work.wait(lk, [&] { return s->stopping || !s->ready.empty(); });
             if (s->stopping && s->ready.empty()) return;
-            batch.swap(s->ready.front());
+            item.swap(s->ready.front());
             s->ready.pop_front();
-            sc = s->scenes[batch[0]->scene].get();
+            for (const auto &b : item) scs.push_back(s->scenes[b[0]->scene].get());
         }
         int rc = HRT_OK;
-        if (!sc->ctx) {
-            rc = hrt_create(&sc->ctx, s->device);
-            if (rc == HRT_OK) {
-                // Smaller scenes get higher stream priority and every trace block retires
-                // after kRayBudget rays per thread, so a small solve's blocks start as soon as
-                // SMs free up instead of waiting for a large solve to end.
-                int least = 0, greatest = 0;
-                cudaDeviceGetStreamPriorityRange(&least, &greatest);
-                double f = (std::log10((double)std::max(sc->n, 1)) - 3.0) / 3.5;  // 1e3 .. 3e6 prims
-                f = std::min(1.0, std::max(0.0, f));
-                const int prio = greatest + (int)std::lround(f * (double)(least - greatest));
-                if (cudaStreamCreateWithPriority(&sc->stream, cudaStreamNonBlocking, prio) == cudaSuccess)
-                    rc = hrt_set_stream(sc->ctx, sc->stream);
-                if (rc == HRT_OK) rc = hrt_set_ray_budget(sc->ctx, kRayBudget);
-                // fixed default kernels: timing trials per scene would cost more than they save
-                if (rc == HRT_OK) rc = hrt_set_tuning(sc->ctx, 0);
-            }
-            if (rc == HRT_OK) {
-                hrt_geometry g{};
-                g.n = sc->n;
-                g.transform = sc->T.data();
-                g.type = sc->type.data();
-                g.twosided = sc->twosided.data();
-                rc = hrt_update_geometry(sc->ctx, &g);
-                if (rc == HRT_OK) rc = hrt_build_accel(sc->ctx);
-                if (rc == HRT_OK) rc = hrt_update_materials(sc->ctx, 1, sc->n, sc->nbands, sc->rho.data(), sc->tau.data());
-                std::lock_guard<std::mutex> lk(s->mu);
-                ++s->builds;
-            }
-        }
-        int Bl = 0;
-        for (uint8_t f : batch[0]->band_launch) Bl += f ? 1 : 0;
-        if (rc == HRT_OK) {
-            const Request *r0 = batch[0];
-            const double side = std::ceil(std::sqrt((double)r0->diffuse_rays));
-            const double rays = (double)sc->n * ((double)r0->direct_rays * (double)batch.size() +
-                                                 2.0 * side * side * (1.0 + (double)r0->depth));
+        for (Scene *sc : scs)
+            if (rc == HRT_OK) rc = prepare_scene(s, sc);
+        if (rc == HRT_OK && item.size() > 1) {
+            rc = solve_group(scs, item);
+        } else if (rc == HRT_OK) {
+            Scene *sc = scs[0];
+            std::vector<Request *> &batch = item[0];
+            const int Bl = launched_bands(batch[0]);
             std::unique_lock<std::mutex> gate(s->large, std::defer_lock);
-            if (rays > kLargeRays) {
+            if (batch_rays(sc, batch) > kLargeRays) {
                 gate.lock();
                 // requests of this scene that arrived while the batch waited for the GPU
                 // join it (the scene is busy, so they would otherwise wait for the next batch)
@@ -306,19 +395,25 @@ void worker_loop(hrt_server *s) {
                     }
                 }
             }
-            rc = batch.size() == 1 ? solve_one(sc, batch[0], Bl) : solve_batch(sc, batch, Bl);
+            rc = batch.size() == 1 ? solve_one(sc, batch[0], Bl) : solve_batch(sc, batch);
         }
         {
             std::lock_guard<std::mutex> lk(s->mu);
             const double t = s->now();
-            for (Request *r : batch) {
-                r->t_done = t;
-                r->status = rc;
-                --s->outstanding;
+            for (const auto &batch : item)
+                for (Request *r : batch) {
+                    r->t_done = t;
+                    r->status = rc;
+                    --s->outstanding;
+                }
+            if (rc != HRT_OK) {
+                for (Scene *sc : scs)
+                    if (sc->ctx && s->err.empty()) s->err = hrt_last_error(sc->ctx);
             }
-            if (rc != HRT_OK && sc->ctx) s->err = hrt_last_error(sc->ctx);
-            sc->busy = false;
-            sc->last_use = ++s->tick;
+            for (Scene *sc : scs) {
+                sc->busy = false;
+                sc->last_use = ++s->tick;
+            }
         }
         s->cv_dispatch.notify_all();
         s->cv_done.notify_all();
@@ -336,6 +431,7 @@ void dispatch_loop(hrt_server *s) {
         double t = s->now();
         bool admitted = false;
         double next_arrival = -1.0;
+        std::vector<std::vector<Request *>> small;  // this scan's small batches (different scenes)
         // scan requests that have arrived, in arrival order; admit every one whose scene
         // is idle and fits (continuous batching: later requests may pass a blocked one)
         for (auto it = s->arrivals.begin(); it != s->arrivals.end();) {
@@ -371,12 +467,27 @@ void dispatch_loop(hrt_server *s) {
                                   s->arrivals.end());
                 ++s->batches;
                 s->batched_requests += batch.size();
-                s->ready.push_back(std::move(batch));
+                if (group_enabled() && batch_rays(sc, batch) <= kGroupRays) {
+                    small.push_back(std::move(batch));
+                    if ((int)small.size() == kMaxGroup) {
+                        s->ready.push_back(std::move(small));
+                        small.clear();
+                    }
+                } else {
+                    s->ready.push_back({std::move(batch)});
+                }
                 admitted = true;
                 it = s->arrivals.begin();
             } else {
                 ++it;
             }
+        }
+        if (!small.empty()) {
+            if (small.size() > 1) {
+                ++s->groups;
+                s->grouped_batches += small.size();
+            }
+            s->ready.push_back(std::move(small));
         }
         if (admitted) {
             s->cv_work.notify_all();
@@ -504,9 +615,9 @@ int hrt_server_result(hrt_server *s, uint64_t request_id, float *flux_out, size_
 int hrt_server_stats(hrt_server *s, double *out, int count) {
     if (!s || !out) return HRT_EINVAL;
     std::lock_guard<std::mutex> lk(s->mu);
-    double v[6] = {(double)s->builds,  (double)s->evictions, (double)s->used,
-                   (double)s->budget,  (double)s->batches,   (double)s->batched_requests};
-    for (int i = 0; i < count && i < 6; ++i) out[i] = v[i];
+    double v[8] = {(double)s->builds,  (double)s->evictions, (double)s->used,           (double)s->budget,
+                   (double)s->batches, (double)s->batched_requests, (double)s->groups, (double)s->grouped_batches};
+    for (int i = 0; i < count && i < 8; ++i) out[i] = v[i];
     return HRT_OK;
 }
 

@@ -515,14 +515,19 @@ __device__ __forceinline__ double sky_fd(f3 dir, const SkyParams &sky, int b) {
 // 8 229 ms, 16 240 ms, 28 283 ms.  Scenes with voxels keep it off: on the deep-scatter scene the
 // 4-wide trace took 80.5 ms with it against 78.1 ms without.  HRT_REFILL overrides (0-32).
 constexpr int kRefillDefault = 8;
-inline int refill_threshold(bool voxels) {
+// The lean 4-wide trace (hrt_trace_w4.cuh) keeps fewer registers per lane and refills more
+// cheaply; on the same workload, per diffuse launch: 4 215 ms, 8 199.6 ms, 12 194.5 ms,
+// 16 192.0-194.2 ms, 20 191.9-192.4 ms, 24 200 ms, 28 229 ms, 32 390 ms.  16 sits in the flat
+// part of that curve.
+constexpr int kRefillLean = 16;
+inline int refill_threshold(bool voxels, bool lean = false) {
     static const int env = [] {  // initialised once, thread-safe; -1: not set
         const char *e = getenv("HRT_REFILL");
         const int v = e ? atoi(e) : -1;
         return (v < -1 || v > 32) ? -1 : v;
     }();
     if (env >= 0) return env;
-    return voxels ? 0 : kRefillDefault;
+    return voxels ? 0 : (lean ? kRefillLean : kRefillDefault);
 }
 
 // Blocks of a persistent launch: one resident wave; with a lane budget, enough blocks

@@ -44,14 +44,24 @@ struct RingStack {
 };
 
 // BLOCK: threads per block; MINB: resident blocks per SM the register allocation must allow.
-// SD: stack entries per lane in shared memory (a power of two).
-template <int NB, bool RECORD, bool STATS, int MINB, int SD, int BLOCK>
+// SD: stack entries per lane in shared memory (a power of two).  KB: ray-id batch -- a warp
+// takes 32 x KB consecutive ray ids from the global counter at a time and hands them to its
+// idle lanes from shared memory (KB = 1: every refill takes exactly the idle lanes' count).
+// MULTI (recording mode only): the launch traces several scenes -- P.slots[0..P.nslots) each
+// give a scene, a primitive chunk, ray counts, seed, pass and hit buffer, with consecutive
+// ranges of the launch's ray ids (id_begin) -- so one persistent launch covers the pass of
+// every scene of a multi-scene sweep.
+template <int NB, bool RECORD, bool STATS, int MINB, int SD, int BLOCK, int KB, bool MULTI = false>
 __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams P) {
+    static_assert(!MULTI || (RECORD && !STATS), "multi-scene launches record hits only");
     __shared__ double s_sum[RECORD ? 1 : NB][BLOCK];            // running sums of the lane's origin
     __shared__ float s_ray[6][BLOCK];                            // d.xyz, Sx, Sy, Sz
     __shared__ uint32_t s_lane[5][BLOCK];                        // see the L_* slots below
     __shared__ int32_t s_stack[SD][BLOCK];
     __shared__ unsigned long long s_rid[RECORD ? BLOCK : 1];     // record: hit-buffer index
+    __shared__ unsigned long long s_chunk[2][KB > 1 ? BLOCK / 32 : 1];  // per warp: next id, end
+    __shared__ SceneSlot s_slot[MULTI ? kMaxSlots : 1];          // multi-scene: the launch's scenes
+    __shared__ unsigned long long s_srays[MULTI ? kMaxSlots : 1];  // multi-scene: rays per scene
     constexpr int L_AXES = 0;  // kx | ky << 2 | kz << 4 | face << 6 | wraps << 8
     constexpr int L_P = 1;     // origin primitive
     constexpr int L_HIT = 2;   // best hit so far: prim << 1 | face, or kMissCode
@@ -59,13 +69,22 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
     constexpr int L_TAKEN = 4; // rays taken (lane budget)
     const int tid = threadIdx.x;
     const int lane = tid & 31;
-    const TraceScene &sc = P.sc;
     const uint32_t R = (uint32_t)(P.dimx * P.dimy);
     // count x R x faces < 2^31: the host splits larger passes into primitive chunks
     const uint32_t per_face = P.count * R;
     const int nf = ((P.faces & 1) ? 1 : 0) + ((P.faces & 2) ? 1 : 0);
-    const unsigned long long total = (unsigned long long)per_face * (unsigned long long)nf;
-    const uint32_t n4 = (uint32_t)sc.n4;
+    const unsigned long long total = MULTI ? P.multi_total : (unsigned long long)per_face * (unsigned long long)nf;
+    int lslot = 0;  // multi-scene: the scene slot of the lane's ray
+    // the scene of the lane's current ray
+#define SC (MULTI ? s_slot[lslot].sc : P.sc)
+    if (MULTI) {
+        const int words = P.nslots * (int)(sizeof(SceneSlot) / sizeof(uint32_t));
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(P.slots);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(s_slot);
+        for (int i = tid; i < words; i += BLOCK) dst[i] = src[i];
+        for (int i = tid; i < P.nslots; i += BLOCK) s_srays[i] = 0ull;
+        __syncthreads();
+    }
 
     RingStack<SD, BLOCK> stk;
     stk.ring = s_stack;
@@ -84,6 +103,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
     }
     s_lane[L_KEY][tid] = 0xFFFFFFFFu;
     s_lane[L_TAKEN][tid] = 0u;
+    // a lane budget retires lanes without drawing ids, so a warp could leave ids of its
+    // batch untraced: batched fetch only without one
+    const bool batched = KB > 1 && P.lane_budget == 0;
+    if (KB > 1 && lane == 0) {
+        s_chunk[0][tid >> 5] = 0ull;
+        s_chunk[1][tid >> 5] = 0ull;
+    }
+    __syncwarp();
 #define POP() (sp > 0 ? stk.pop(--sp) : kSentinel)
 
     for (;;) {
@@ -93,21 +120,65 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
         const unsigned m = __ballot_sync(0xffffffffu, need);
         if (m) {
             const int leader = __ffs(m) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(P.fetch, (unsigned long long)__popc(m));
-            base = __shfl_sync(0xffffffffu, base, leader);
+            const unsigned rank = __popc(m & ((1u << lane) - 1u));
+            unsigned long long id;
+            if (!batched) {
+                unsigned long long base = 0;
+                if (lane == leader) base = atomicAdd(P.fetch, (unsigned long long)__popc(m));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                id = base + rank;
+            } else {
+                // ids are handed out in increasing order, so every id below the end of the
+                // range is drawn before any lane of the warp draws one past it
+                const int w = tid >> 5;
+                const unsigned nneed = __popc(m);
+                const unsigned long long next = s_chunk[0][w], left = s_chunk[1][w] - next;
+                unsigned long long nb = 0;
+                if (left < nneed) {
+                    if (lane == leader) nb = atomicAdd(P.fetch, (unsigned long long)(32 * KB));
+                    nb = __shfl_sync(0xffffffffu, nb, leader);
+                }
+                id = rank < left ? next + rank : nb + (rank - left);
+                __syncwarp();
+                if (lane == leader) {
+                    if (left < nneed) {
+                        s_chunk[0][w] = nb + (nneed - left);
+                        s_chunk[1][w] = nb + 32ull * KB;
+                    } else {
+                        s_chunk[0][w] = next + nneed;
+                    }
+                }
+                __syncwarp();
+            }
             if (need) {
-                const unsigned long long id = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
                 if (id >= total) {
                     exhausted = true;
                 } else {
                     s_lane[L_TAKEN][tid] += 1u;
-                    const uint32_t fi = (uint32_t)(id / per_face);
-                    const uint32_t rem = (uint32_t)(id - (unsigned long long)fi * per_face);
+                    unsigned long long lid = id;
+                    uint32_t Rk = R, pfk = per_face, offk = P.offset, seedk = P.seed, passk = P.pass;
+                    int dxk = P.dimx, dyk = P.dimy;
+                    if (MULTI) {  // the slot whose id range holds id (ranges are consecutive)
+                        int k = 0;
+                        while (k + 1 < P.nslots && id >= s_slot[k + 1].id_begin) ++k;
+                        lslot = k;
+                        const SceneSlot &S = s_slot[k];
+                        lid = id - S.id_begin;
+                        dxk = S.dimx;
+                        dyk = S.dimy;
+                        Rk = (uint32_t)(dxk * dyk);
+                        pfk = S.count * Rk;
+                        offk = S.offset;
+                        seedk = S.seed;
+                        passk = S.pass;
+                    }
+                    const TraceScene &sc = SC;
+                    const uint32_t fi = (uint32_t)(lid / pfk);
+                    const uint32_t rem = (uint32_t)(lid - (unsigned long long)fi * pfk);
                     const int face = (nf == 2) ? (fi == 0 ? 1 : 0) : ((P.faces & 1) ? 1 : 0);
-                    const uint32_t p = P.offset + rem / R;
-                    const uint32_t r = rem % R;
-                    if (RECORD) s_rid[tid] = ((unsigned long long)fi * (unsigned long long)sc.n + p) * R + r;
+                    const uint32_t p = offk + rem / Rk;
+                    const uint32_t r = rem % Rk;
+                    if (RECORD) s_rid[tid] = ((unsigned long long)fi * (unsigned long long)sc.n + p) * Rk + r;
                     const int ts = sc.twosided[p];
                     const bool skip = (face == 1 && ts == 3) || (face == 0 && ts != 1);
                     if (!skip) {
@@ -115,7 +186,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                         load_rgen(sc, p, g);
                         const uint32_t type = __float_as_uint(g[0].w);
                         f3 d;
-                        diffuse_ray<false>(g, type, r, p, face, P.dimx, P.dimy, P.seed, P.pass, &o, &d, sc.masks);
+                        diffuse_ray<false>(g, type, r, p, face, dxk, dyk, seedk, passk, &o, &d, sc.masks);
                         const WT w = wt_setup(d);
                         s_ray[0][tid] = d.x;
                         s_ray[1][tid] = d.y;
@@ -133,7 +204,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                         sp = 0;
                         budget = sc.visit_budget;
                         live = true;
-                        ++nrays;
+                        if (MULTI) atomicAdd(&s_srays[lslot], 1ull);
+                        else ++nrays;
                     }
                 }
             }
@@ -144,6 +216,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
         if (!live) continue;
 
         // ---- internal nodes; leaves are postponed until every active lane has one
+        const TraceScene &sc = SC;
+        const uint32_t n4 = (uint32_t)sc.n4;
         while (cur >= 0 && cur != kSentinel) {
             if ((uint32_t)cur >= n4 || budget-- == 0u) {
                 raise(sc.status, budget == 0xFFFFFFFFu ? ERR_BUDGET : ERR_BOUNDS);
@@ -256,7 +330,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
         // ---- value of the finished ray, added to the lane's running sum
         live = false;
         if (RECORD) {
-            P.hits[s_rid[tid]] = lost ? kLostCode : bcode;
+            (MULTI ? s_slot[lslot].hits : P.hits)[s_rid[tid]] = lost ? kLostCode : bcode;
             continue;
         }
         if (lost) continue;
@@ -298,12 +372,19 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                 if (j < P.Bc && s_sum[j][tid] != 0.0) atomicAdd(dst + j, s_sum[j][tid]);
         }
     }
-    if (sc.rays && nrays) atomicAdd(sc.rays, (unsigned long long)nrays);
-    if (STATS && sc.visits) {
-        atomicAdd(sc.visits, (unsigned long long)nvis);
-        atomicAdd(sc.visits + 1, (unsigned long long)ntest);
+    if (MULTI) {  // every warp of the block is past its loop: count the rays per scene
+        __syncthreads();
+        for (int i = tid; i < P.nslots; i += BLOCK)
+            if (s_srays[i] && s_slot[i].sc.rays) atomicAdd(s_slot[i].sc.rays, s_srays[i]);
+    } else {
+        if (P.sc.rays && nrays) atomicAdd(P.sc.rays, (unsigned long long)nrays);
+    }
+    if (STATS && P.sc.visits) {
+        atomicAdd(P.sc.visits, (unsigned long long)nvis);
+        atomicAdd(P.sc.visits + 1, (unsigned long long)ntest);
     }
 #undef POP
+#undef SC
 }
 
 }  // namespace

@@ -332,6 +332,18 @@ typedef struct {
 } hrt_sweep;
 /* flux_out: host [n*nsun*nbands] (channel fastest), or NULL. */
 int hrt_run_sweep(hrt_context *ctx, const hrt_sweep *s, float *flux_out);
+/* ---- sweeps of several scenes in one launch graph (no counterpart in the reference).
+ * ctxs[k] holds scene k (its geometry and BVH, built as for any solve; all on one device,
+ * 4-wide trees); sweeps[k] is its sweep, as for hrt_run_sweep.  The recording launches run
+ * one resident wave (no per-thread ray budget applies).  The graph, on
+ * ctxs[0]'s stream, runs every scene's direct pass and channel bookkeeping, and traces each
+ * diffuse or scattering pass of ALL scenes in ONE persistent recording launch whose ray ids
+ * run over the scenes one after another (at most 32 scene chunks per pass).  Each scene's
+ * channels equal its hrt_run_sweep (the same Philox rays; sums in the same fixed order).
+ * flux_out[k]: host [n_k*nsun_k*nbands_k] or NULL (flux_out itself may be NULL).  Captured
+ * on the first call of a shape and replayed; the call returns after the graph finished;
+ * a device error of scene k is reported with its index. */
+int hrt_run_sweep_multi(hrt_context *const *ctxs, const hrt_sweep *sweeps, int32_t nscenes, float *const *flux_out);
 
 /* ---- continuous-batching server (no counterpart in the reference; a serving front end
  * for many radiation solves of uneven size).  Scenes are registered once (geometry and
@@ -368,7 +380,7 @@ int hrt_server_wait(hrt_server *s);
 int hrt_server_result(hrt_server *s, uint64_t request_id, float *flux_out, size_t count, double *timing,
                       double *checksum, uint64_t *rays);
 /* out: [0] BVH builds, [1] evictions, [2] bytes accounted resident, [3] budget,
- * [4] batches run, [5] requests in them. */
+ * [4] batches run, [5] requests in them, [6] multi-scene groups run, [7] batches in them. */
 int hrt_server_stats(hrt_server *s, double *out, int count);
 int hrt_server_destroy(hrt_server *s);
 

@@ -1,5 +1,6 @@
 """Served stream: continuous batching with device-resident scenes; every result equals the
-same solve run alone, whether it ran alone or in a batch of its scene's requests."""
+same solve run alone, whether it ran alone, in a batch of its scene's requests, or in a
+multi-scene group (small batches of different scenes traced by one persistent launch per pass)."""
 import numpy as np
 import pytest
 
@@ -56,6 +57,8 @@ def test_served_results_equal_alone(hrt_lib):
     assert st["builds"] >= 5
     # requests of a scene that were queued together ran as one batch
     assert st["batched_requests"] == len(reqs) and st["batches"] < len(reqs)
+    # small batches of different scenes admitted together ran as one multi-scene sweep
+    assert st["groups"] >= 1 and st["grouped_batches"] >= 2
     srv.close()
 
 

@@ -59,7 +59,7 @@ def test_sweep_channels_equal_plain_solves():
     np.testing.assert_allclose(again, sweep, rtol=1e-6, atol=1e-6)
 
 
-@pytest.mark.parametrize("variant", [4, 6, 7, 8, 9, 10])
+@pytest.mark.parametrize("variant", [4, 6, 7, 8, 9, 10, 11, 12])
 def test_sweep_recording_variants_agree(variant):
     """The recording trace of the sweep gives the same channels whichever 4-wide kernel
     records the hits (the generic persistent kernel or the lean one in each of its block
@@ -77,3 +77,55 @@ def test_sweep_recording_variants_agree(variant):
         rad.ctx.set_tuning(1)
     np.testing.assert_allclose(got, base, rtol=1e-6, atol=1e-9)
     assert rad.ctx.device_status() == 0
+
+
+def _scene_ctx(kind):
+    from helios_gb300 import _hrt
+
+    if kind == "orchard":
+        sc = scenes.orchard(nx=2, ny=2, leaves_per_tree=600, side=0.06, seed=11, ground=True)
+        bbox, per = None, (0.0, 0.0)
+    elif kind == "periodic":
+        sc = scenes.homogeneous_canopy(n_leaves=1500, leaf=0.1, domain=2.7386, seed=12)
+        ctx = Context()
+        ctx.addScene(sc)
+        rad = RadiationModel(ctx)
+        rad.enforcePeriodicBoundary("xy")
+        bbox, per = rad._bbox_faces(), rad.periodic  # the mirror's periodic walls
+    else:
+        sc = scenes.homogeneous_canopy(n_leaves=300, leaf=0.2, domain=2.0, seed=13)
+        bbox, per = None, (0.0, 0.0)
+    c = _hrt.Context(0)
+    c.update_geometry(sc.T, sc.ptype, sc.twosided, bbox, per)
+    c.build_accel()
+    return c, sc
+
+
+def test_multi_scene_sweep_equals_each_scene_alone():
+    """Three scenes of different sizes, suns, bands, ray counts and depths (one with periodic
+    walls) in one multi-scene graph: every pass of all scenes is one persistent launch, and each
+    scene's channels and ray count equal its own sweep's."""
+    specs = []
+    for kind, nsun, nb, dr, fr, depth, seed in (("orchard", 4, 2, 36, 49, 3, 5), ("periodic", 3, 1, 16, 64, 2, 6),
+                                                 ("small", 2, 3, 25, 36, 0, 7)):
+        c, sc = _scene_ctx(kind)
+        dirs, direct, diffuse, _ = scenes.day_sweep(n=nsun)
+        direct = np.repeat(direct[:, :1], nb, axis=1) * np.linspace(1.0, 0.6, nb)
+        diffuse = np.repeat(diffuse[:, :1], nb, axis=1) * np.linspace(1.0, 0.8, nb)
+        rng = np.random.default_rng(seed)
+        rho = rng.uniform(0.05, 0.45, (sc.n, nb)).astype(np.float32)
+        tau = (0.8 * rng.uniform(0.0, 1.0, (sc.n, nb)) * (1 - rho)).astype(np.float32)
+        specs.append((c, dict(sun_dir=dirs, direct_flux=direct, diffuse_flux=diffuse, rho=rho, tau=tau,
+                              direct_rays=dr, diffuse_rays=fr, depth=depth, seed=seed)))
+    alone, rays = [], []
+    for c, sw in specs:
+        alone.append(c.run_sweep(**sw).astype(np.float64))
+        rays.append(c.last_stats()["rays"])
+    from helios_gb300 import _hrt
+
+    for _ in range(2):  # capture, then replay
+        multi = _hrt.run_sweep_multi([c for c, _ in specs], [sw for _, sw in specs])
+        for k, (c, _) in enumerate(specs):
+            np.testing.assert_allclose(multi[k], alone[k], rtol=1e-6, atol=1e-9)
+            assert c.last_stats()["rays"] == rays[k]
+            assert c.device_status() == 0
