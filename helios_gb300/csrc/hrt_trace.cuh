@@ -42,9 +42,9 @@ constexpr int kStack4 = 128;               // a 4-wide node pushes up to three c
 
 // The four child boxes of a compressed 4-wide node (q0..q3, format in hrt_device.cuh) against
 // a ray (origin o, inverse direction inv) within [tmin, tmax]: entry distances tk (INFINITY:
-// missed) and child references ck (kSentinel: missed), sorted nearest first.
-__device__ __forceinline__ void node4_test(const float4 q0, const float4 q1, const float4 q2, const float4 q3, f3 o,
-                                           f3 inv, float tmin, float tmax, float tk[4], int32_t ck[4]) {
+// missed) and child references ck (kSentinel: missed), in slot order.
+__device__ __forceinline__ void node4_children(const float4 q0, const float4 q1, const float4 q2, const float4 q3,
+                                               f3 o, f3 inv, float tmin, float tmax, float tk[4], int32_t ck[4]) {
     const uint32_t eb = __float_as_uint(q0.w);
     const float sx = q_step(eb & 0xFFu), sy = q_step((eb >> 8) & 0xFFu), sz = q_step((eb >> 16) & 0xFFu);
     // near / far plane bytes per axis from the sign of the ray direction: with inv >= 0 the
@@ -79,6 +79,10 @@ __device__ __forceinline__ void node4_test(const float4 q0, const float4 q1, con
         tk[k] = hit ? tn : INFINITY;
         ck[k] = hit ? cref[k] : kSentinel;
     }
+}
+
+// The children of node4_children sorted nearest first (a five-comparator network).
+__device__ __forceinline__ void node4_sort(float tk[4], int32_t ck[4]) {
 #define HRT_CSWAP(a, b)                                  \
     if (tk[b] < tk[a]) {                                 \
         const float tt = tk[a];                          \
@@ -94,6 +98,13 @@ __device__ __forceinline__ void node4_test(const float4 q0, const float4 q1, con
     HRT_CSWAP(1, 3)
     HRT_CSWAP(1, 2)
 #undef HRT_CSWAP
+}
+
+// node4_children, sorted nearest first.
+__device__ __forceinline__ void node4_test(const float4 q0, const float4 q1, const float4 q2, const float4 q3, f3 o,
+                                           f3 inv, float tmin, float tmax, float tk[4], int32_t ck[4]) {
+    node4_children(q0, q1, q2, q3, o, inv, tmin, tmax, tk, ck);
+    node4_sort(tk, ck);
 }
 
 // Closest (or any) hit over the BVH.  Visiting order: both child boxes are
