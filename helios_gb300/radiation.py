@@ -246,6 +246,13 @@ class Context:
 
     # --------------------------------------------------------------- data
     def setPrimitiveData(self, uuid, label, value):
+        if np.ndim(uuid) > 0 and np.asarray(value).dtype.kind in "US":  # strings: one entry per primitive
+            uuids = np.asarray(uuid).ravel()
+            vals = np.broadcast_to(np.asarray(value), uuids.shape)
+            d = self.primitive_data.setdefault(label, {})
+            for u, v in zip(uuids.tolist(), vals.tolist()):
+                d[int(u)] = str(v)
+            return
         if np.ndim(uuid) > 0:
             uuids = np.asarray(uuid).ravel()
             vals = np.broadcast_to(np.asarray(value), uuids.shape)
@@ -321,6 +328,43 @@ def _interp_clamped(x, xs, ys):
     i = max(int(np.searchsorted(np.asarray(xs, np.float32), np.float32(x), side="left")), 1)
     t = np.float32((np.float32(x) - np.float32(xs[i - 1])) / (np.float32(xs[i]) - np.float32(xs[i - 1])))
     return float(np.float32(ys[i - 1]) + t * (np.float32(ys[i]) - np.float32(ys[i - 1])))
+
+
+def _spectrum_over_band(spec, w1, w2, source=None):
+    """Band value of an object spectrum [(wavelength, value)] over [w1, w2]
+    (RadiationModel::integrateSpectrum, RadiationModel.cpp:1463-1538), in FP32: the trapezoids
+    run over the object's own wavelengths from the segment holding w1 to the one holding w2.
+    With a source spectrum: sum value x source / sum source, the source interpolated at the
+    object's wavelengths (clamped at its ends).  Without one the source is taken as flat: the
+    integral divided by (w2 - w1), which the caller does (RadiationModel.cpp:2450)."""
+    f = np.float32
+    n = len(spec)
+    if n < 2 or not w1 < w2:
+        raise HeliosRuntimeError("ERROR (RadiationModel::integrateSpectrum): Radiation spectrum must have at least 2 "
+                                 "wavelengths and the lower wavelength bound must be less than the upper one.")
+    xs = [f(x) for x, _ in spec]
+    ys = [f(y) for _, y in spec]
+    istart, iend = (0 if source is not None else 1), n - 1
+    for i in range(n - 1):
+        if xs[i] <= w1 < xs[i + 1]:
+            istart = i
+        if xs[i] <= w2 < xs[i + 1]:
+            iend = i + 1
+            break
+    if source is None:
+        E = f(0.0)
+        for i in range(istart, iend):
+            E = f(E + f(f(f(ys[i] + ys[i + 1]) * f(xs[i + 1] - xs[i])) * f(0.5)))
+        return float(E)
+    sx = [w for w, _ in source]
+    sy = [v for _, v in source]
+    E = Etot = f(0.0)
+    for i in range(istart, iend):
+        s0, s1 = f(_interp_clamped(xs[i], sx, sy)), f(_interp_clamped(xs[i + 1], sx, sy))
+        dx = f(xs[i + 1] - xs[i])
+        E = f(E + f(f(f(0.5) * f(f(ys[i] * s0) + f(ys[i + 1] * s1))) * dx))
+        Etot = f(Etot + f(f(f(0.5) * f(s1 + s0)) * dx))
+    return float(f(E / Etot))
 
 
 def _weighted_average(wl, values, weights, response):
@@ -579,6 +623,49 @@ class RadiationModel:
         for b in self.bands.values():
             b.diffuse_spectrum = list(spec)
 
+    def setSourceSpectrum(self, source, spectrum_label):
+        """Spectrum of one or more sources from global data of (wavelength, value) pairs
+        (RadiationModel::setSourceSpectrum); it weights the band averages of primitive spectra."""
+        if not self.context.doesGlobalDataExist(spectrum_label):
+            raise HeliosRuntimeError(f"ERROR (RadiationModel::setSourceSpectrum): Global data '{spectrum_label}' "
+                                     "does not exist.")
+        spec = [(float(w), float(v)) for w, v in self.context.getGlobalData(spectrum_label)]
+        for sid in (np.atleast_1d(source).tolist()):
+            if sid >= len(self.sources):
+                raise HeliosRuntimeError("ERROR (RadiationModel::setSourceSpectrum): Source ID out of bounds.")
+            self.sources[int(sid)]["spectrum"] = spec
+
+    def _spectral_property(self, kind, bands, S):
+        """[S][n][Bg] values of primitives whose `<kind>_spectrum` names global spectral data, NaN
+        elsewhere (RadiationModel.cpp:2400-2470, 2625-2700): per band with waveband bounds and
+        per source, the spectrum averaged over the band, weighted by the source's spectrum if it
+        has one, else flat; NaN for bands without bounds (the constant value applies)."""
+        labels = self.context.primitive_data.get(kind + "_spectrum", {})
+        n = self.context.getPrimitiveCount()
+        out = np.full((S, n, len(bands)), np.nan)
+        if not labels:
+            return out
+        cache = {}
+        ptype = self.context.arrays()[1]
+        for uuid, lab in labels.items():
+            if not isinstance(lab, str) or not self.context.doesGlobalDataExist(lab):
+                continue
+            if ptype[uuid] == scenes.VOXEL:  # voxels take no spectra (RadiationModel.cpp:2626)
+                continue
+            for bi, b in enumerate(bands):
+                w1, w2 = self.bands[b].wavebandBounds
+                if w1 == 0 or w2 == 0:
+                    continue
+                for si in range(S):
+                    src = self.sources[si].get("spectrum")
+                    key = (lab, b, si if src else -1)
+                    if key not in cache:
+                        spec = [(float(w), float(v)) for w, v in self.context.getGlobalData(lab)]
+                        cache[key] = (_spectrum_over_band(spec, w1, w2, src) if src else
+                                      _spectrum_over_band(spec, w1, w2) / (w2 - w1))
+                    out[si, uuid, bi] = cache[key]
+        return out
+
     def _update_prague(self, band_labels):
         """Prague sky parameters of the general diffuse radiation from the Context's global data
         (RadiationModel::updatePragueParametersForGeneralDiffuse, RadiationModel.cpp:3145-3223):
@@ -727,15 +814,22 @@ class RadiationModel:
         n = self.context.getPrimitiveCount()
         all_bands = sorted(self.bands)
         Bg = len(all_bands)
-        rho = np.zeros((n, Bg))
-        tau = np.zeros((n, Bg))
+        rho = np.zeros((S, n, Bg))
+        tau = np.zeros((S, n, Bg))
         eps_l = np.ones((n, len(band_labels)))
         self._glass = None
+        # spectral reflectivity / transmissivity: used where no constant (other than the default)
+        # is set for the band (RadiationModel.cpp:2640-2660), clamped to [0, 1]
+        rho_spec = self._spectral_property("reflectivity", all_bands, S)
+        tau_spec = self._spectral_property("transmissivity", all_bands, S)
         for bi, b in enumerate(all_bands):
             band = self.bands[b]
-            r = self.context.primitive_array("reflectivity_" + b, self.rho_default)
-            t = self.context.primitive_array("transmissivity_" + b, self.tau_default)
+            r0 = self.context.primitive_array("reflectivity_" + b, self.rho_default)
+            t0 = self.context.primitive_array("transmissivity_" + b, self.tau_default)
             e = self.context.primitive_array("emissivity_" + b, self.eps_default)
+            r_s = np.clip(np.where((r0 == self.rho_default) & ~np.isnan(rho_spec[:, :, bi]), rho_spec[:, :, bi], r0), 0, 1)
+            t_s = np.clip(np.where((t0 == self.tau_default) & ~np.isnan(tau_spec[:, :, bi]), tau_spec[:, :, bi], t0), 0, 1)
+            r, t = r_s[0], t_s[0]
             # translucent cover: glass_n_<band> >= 1 activates the sheet model, glass_KL_<band>
             # (default 0, negative clamped) its absorption (RadiationModel.cpp:2759-2807); the
             # constant rho/tau of a glass entry are kept as set and not checked (:2844-2846)
@@ -764,13 +858,14 @@ class RadiationModel:
             elif (~g & (t + r > 1.0 + 1e-6)).any():
                 raise HeliosRuntimeError("ERROR (RadiationModel): transmissivity and reflectivity cannot sum to "
                                          "greater than 1 ensure energy conservation.")
-            rho[:, bi] = r
-            tau[:, bi] = t
+            # the emissivity rules above act on source 0's values; sources with their own spectra
+            # keep their spectral values where the rules left a primitive unchanged
+            same_r, same_t = r == r_s[0], t == t_s[0]
+            rho[:, :, bi] = np.where(same_r[None, :], r_s, r[None, :])
+            tau[:, :, bi] = np.where(same_t[None, :], t_s, t[None, :])
             if b in band_labels:
                 eps_l[:, band_labels.index(b)] = e
-        rho = np.broadcast_to(rho, (S, n, Bg)).astype(np.float32)
-        tau = np.broadcast_to(tau, (S, n, Bg)).astype(np.float32)
-        return rho, tau, eps_l.astype(np.float32)
+        return rho.astype(np.float32), tau.astype(np.float32), eps_l.astype(np.float32)
 
     def solve_description(self, labels, seed=None):
         """The band set of one runBand call as plain arrays (shared with the oracle)."""

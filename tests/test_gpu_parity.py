@@ -273,6 +273,50 @@ def test_anisotropic_sky_canopy_vs_oracle(oracle_mod, sky):
     assert np.abs(np.asarray(iso.runBand("SW"), np.float64) - got).max() > 1e-3 * np.abs(got).max()
 
 
+def test_spectral_materials_per_source_vs_oracle(oracle_mod):
+    """Leaves whose reflectivity and transmissivity are spectra (global data named by primitive
+    data), two suns with different spectra: each source sees its own band-averaged materials
+    ([source][primitive][band], RadiationModel.cpp:2400-2470), which the direct pass reads per
+    source and the diffuse passes from source 0 (OptiX8DeviceCode.cu:1612).  GPU vs the FP64
+    oracle within 1e-4 per primitive, over two bands."""
+    rad = _canopy_model(n_leaves=2000, depth=2, periodic=True)
+    ctx = rad.context
+    lv = np.arange(1, ctx.getPrimitiveCount())
+    ctx.setGlobalData("leaf_rho", [(400, 0.05), (500, 0.10), (600, 0.08), (700, 0.45), (800, 0.50), (900, 0.48)])
+    ctx.setGlobalData("leaf_tau", [(400, 0.02), (500, 0.05), (600, 0.04), (700, 0.40), (800, 0.45), (900, 0.44)])
+    ctx.setGlobalData("sun_a", [(400, 1.5), (500, 2.0), (600, 1.8), (700, 1.2), (800, 1.0), (900, 0.8)])
+    ctx.setGlobalData("sun_b", [(400, 0.2), (600, 1.0), (900, 2.0)])
+    ctx.setPrimitiveData(lv, "reflectivity_spectrum", "leaf_rho")
+    ctx.setPrimitiveData(lv, "transmissivity_spectrum", "leaf_tau")
+    for b in ("reflectivity_SW", "transmissivity_SW"):  # leave the band constants at their defaults
+        ctx.primitive_data.pop(b, None)
+        ctx.bulk_data.pop(b, None)
+    rad.bands.pop("SW")
+    for b, lo, hi in (("VIS", 400, 700), ("NIR", 700, 900)):
+        rad.addRadiationBand(b, lo, hi)
+        rad.disableEmission(b)
+        rad.setDirectRayCount(b, 64)
+        rad.setDiffuseRayCount(b, 100)
+        rad.setScatteringDepth(b, 2)
+        rad.setDiffuseRadiationFlux(b, 60.0)
+    rad.sources.clear()
+    a = rad.addCollimatedRadiationSource(scenes.sun_direction(30, 0))
+    c = rad.addCollimatedRadiationSource(scenes.sun_direction(55, 140))
+    rad.setSourceSpectrum(a, "sun_a")
+    rad.setSourceSpectrum(c, "sun_b")
+    for b, fa, fc in (("VIS", 500.0, 200.0), ("NIR", 450.0, 300.0)):
+        rad.setSourceFlux(a, b, fa)
+        rad.setSourceFlux(c, b, fc)
+    desc = rad.solve_description(["NIR", "VIS"])
+    assert not np.allclose(desc["rho"][0], desc["rho"][1])  # the sources see different materials
+    rad.setSeed(41)
+    got = rad.runBand(["NIR", "VIS"])
+    ref, st = run_oracle(rad, ["NIR", "VIS"], oracle_mod, seed=41)
+    worst, _ = _flux_close(got, ref)
+    assert worst <= FLUX_RTOL, worst
+    assert rad.last_stats["rays"] == st["rays"]
+
+
 def test_canopy_beer_reference_size():
     """The reference's periodic canopy test at its own size: 20 x 20 m, LAI 2, 5 cm
     leaves (160,000 patches), 1000 direct / 5000 diffuse rays (selfTest.cpp:1625-1717)."""

@@ -57,8 +57,49 @@ def test_served_results_equal_alone(hrt_lib):
     assert st["builds"] >= 5
     # requests of a scene that were queued together ran as one batch
     assert st["batched_requests"] == len(reqs) and st["batches"] < len(reqs)
-    # small batches of different scenes admitted together ran as one multi-scene sweep
-    assert st["groups"] >= 1 and st["grouped_batches"] >= 2
+    srv.close()
+
+
+def test_small_requests_of_different_scenes_share_one_sweep(hrt_lib):
+    """Four small scenes, one request each, all arrived when the server starts: the first
+    dispatch scan admits all four, and they run as one multi-scene sweep (each pass of all four
+    scenes in one persistent launch); every result equals its solve alone."""
+    built = [scenes.mixed_canopy(n, lai, seed=20 + k) for k, (n, lai) in
+             enumerate(((2500, 1.5), (4000, 3.0), (6000, 0.8), (3000, 4.5)))]
+    srv = _hrt.Server(device=0, workers=2, hbm_budget=2 << 30)
+    for k, sc in enumerate(built):
+        rho, tau = _materials(sc)
+        srv.add_scene(k, sc.T, sc.ptype, sc.twosided, rho, tau)
+    rng = np.random.default_rng(9)
+    reqs = []
+    for k in range(4):
+        bands = np.array([1, k % 2, 1, 0], np.uint8)
+        bl = int(bands.sum())
+        r = {"id": k, "scene": k, "bands": bands, "sun": scenes.sun_direction(20 + 10 * k, 40 * k),
+             "direct": rng.uniform(200, 900, bl), "diffuse": rng.uniform(20, 120, bl), "rays": 49 + 15 * k,
+             "seed": 100 + k}
+        srv.submit(r["id"], k, 0.0, bands, r["sun"], r["direct"], r["diffuse"], 36, r["rays"], 2, r["seed"], keep=True)
+        reqs.append(r)
+    srv.start()
+    srv.wait()
+    st = srv.stats()
+    assert st["groups"] == 1 and st["grouped_batches"] == 4, st
+    alone = _hrt.Context(0)
+    for r in reqs:
+        sc = built[r["scene"]]
+        bl = int(r["bands"].sum())
+        res = srv.result(r["id"], sc.n * bl)
+        alone.update_geometry(sc.T, sc.ptype, sc.twosided)
+        alone.build_accel()
+        rho, tau = _materials(sc)
+        desc = {"band_launch": r["bands"], "sources": [{"type": 0, "position": tuple(r["sun"])}],
+                "source_flux": r["direct"], "rho": rho, "tau": tau, "diffuse_flux": r["diffuse"],
+                "direct_rays": np.full(bl, 36), "diffuse_rays": np.full(bl, r["rays"]),
+                "depth": np.full(bl, 2), "emission": np.zeros(bl, np.uint8), "seed": r["seed"]}
+        ref = alone.run_band(desc).reshape(-1)
+        floor = 1e-3 * max(float(np.abs(ref).mean()), 1e-30)
+        err = np.abs(res["flux"].astype(np.float64) - ref) / np.maximum(np.abs(ref), floor)
+        assert err.max() <= 1e-5, (r["id"], err.max())
     srv.close()
 
 
