@@ -55,7 +55,8 @@ PROFILE = {
 ACC_DIRECT_RAYS, ACC_DIFFUSE_RAYS = 4, 9  # the accuracy leg's reduced ray counts
 # diffuse-trace variants by the tuner's names (hrt_set_tuning(16 + v) forces one)
 VARIANTS = {"binary4": 1, "binary3": 2, "simple": 3, "wide4": 4, "wide4-3": 5, "lean4": 6, "lean5": 7,
-            "lean4-s16": 8, "lean4-b128": 9, "lean4-b512": 10, "lean4-k4": 11, "lean4-k16": 12}
+            "lean4-s16": 8, "lean4-b128": 9, "lean4-b512": 10, "lean4-k4": 11, "lean4-k16": 12,
+            "lean4-s32": 13}
 
 
 def kernel_sources_digest():

@@ -535,6 +535,7 @@ const char *variant_name(int v) {
         case DV_W4B512: return "lean4-b512";
         case DV_W4K4: return "lean4-k4";
         case DV_W4K16: return "lean4-k16";
+        case DV_W4S4D32: return "lean4-s32";
         case DV_PS4: return "binary4";
         case DV_PS3: return "binary3";
         case DV_SIMPLE: return "simple";
@@ -565,12 +566,12 @@ int tuned_variant(hrt_context *ctx, const DiffuseParams &P0, bool record, int *v
     std::vector<int> cand;
     const bool w4 = P0.sc.nodes4 != nullptr;
     if (record)
-        cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_W4S4, DV_W4S5, DV_W4S4D16, DV_W4B128, DV_W4B512, DV_W4K4,
-                                     DV_W4K16, DV_PS3, DV_PS4}
+        cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_W4S4, DV_W4S5, DV_W4S4D16, DV_W4S4D32, DV_W4B128, DV_W4B512,
+                                     DV_W4K4, DV_W4K16, DV_PS3, DV_PS4}
                   : std::vector<int>{DV_PS3, DV_PS4};
     else if (P0.sc.voxels) cand = w4 ? std::vector<int>{DV_W4, DV_PS4, DV_SIMPLE} : std::vector<int>{DV_PS4, DV_SIMPLE};
-    else cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_W4S4, DV_W4S5, DV_W4S4D16, DV_W4B128, DV_W4B512, DV_W4K4,
-                                      DV_W4K16, DV_PS4, DV_PS3, DV_SIMPLE}
+    else cand = w4 ? std::vector<int>{DV_W4, DV_W43, DV_W4S4, DV_W4S5, DV_W4S4D16, DV_W4S4D32, DV_W4B128, DV_W4B512,
+                                      DV_W4K4, DV_W4K16, DV_PS4, DV_PS3, DV_SIMPLE}
                    : std::vector<int>{DV_PS4, DV_PS3, DV_SIMPLE};
     DiffuseParams P = P0;
     P.count = std::min(P0.count, std::max(P0.count / 32u, 4096u));
@@ -1036,6 +1037,9 @@ int hrt_build_accel(hrt_context *ctx) {
     // compressed 4-wide nodes for the persistent diffuse trace (scratch reuses the build's)
     ctx->n4 = 0;
     CU(ctx->nodes4.ensure(ctx->stream, bvh4_node_capacity(n) * 4 * sizeof(float4)));
+    // the traces fetch a node in two 256-bit loads, which need 32-byte aligned addresses
+    if (((uintptr_t)ctx->nodes.p | (uintptr_t)ctx->nodes4.p) & 63u)
+        return fail(ctx, HRT_ECUDA, "node arrays are not 64-byte aligned");
     if (bvh4_scratch_bytes(n) > ctx->bvh_scratch.cap) CU(ctx->bvh_scratch.ensure(ctx->stream, bvh4_scratch_bytes(n)));
     int n4 = 0;
     // the 4-wide nodes come from the clustered binary tree (fewer node visits than the

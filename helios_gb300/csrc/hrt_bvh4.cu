@@ -122,12 +122,8 @@ __global__ void __launch_bounds__(kThreads4) k_collapse(int n2count, const float
     if (!(lo[0] <= hi[0])) {  // no child: cannot happen for a built tree
         for (int a = 0; a < 3; ++a) lo[a] = hi[a] = 0.f;
     }
-    uint32_t e[3];
     float s[3];
-    for (int a = 0; a < 3; ++a) {
-        e[a] = pick_exponent(lo[a], hi[a]);
-        s[a] = q_step(e[a]);
-    }
+    for (int a = 0; a < 3; ++a) s[a] = q_step(pick_exponent(lo[a], hi[a]));
     uint32_t wlo[3] = {0, 0, 0}, whi[3] = {0, 0, 0};
     int32_t outref[4] = {kEmptyChild, kEmptyChild, kEmptyChild, kEmptyChild};
     // The internal children of a node get consecutive indices from one allocation, padded to
@@ -165,12 +161,12 @@ __global__ void __launch_bounds__(kThreads4) k_collapse(int n2count, const float
         }
     }
     float4 *o = n4 + 4 * (size_t)q;
-    o[0] = make_float4(lo[0], lo[1], lo[2], __uint_as_float(e[0] | (e[1] << 8) | (e[2] << 16)));
+    o[0] = make_float4(lo[0], lo[1], lo[2], s[0]);
     o[1] = make_float4(__uint_as_float(wlo[0]), __uint_as_float(wlo[1]), __uint_as_float(wlo[2]),
                        __uint_as_float(whi[0]));
     o[2] = make_float4(__uint_as_float(whi[1]), __uint_as_float(whi[2]), __int_as_float(outref[0]),
                        __int_as_float(outref[1]));
-    o[3] = make_float4(__int_as_float(outref[2]), __int_as_float(outref[3]), 0.f, 0.f);
+    o[3] = make_float4(__int_as_float(outref[2]), __int_as_float(outref[3]), s[1], s[2]);
 }
 
 }  // namespace

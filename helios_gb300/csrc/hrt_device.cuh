@@ -310,12 +310,13 @@ __device__ __forceinline__ f3 sample_point(const float4 g[4], uint32_t type, flo
 }
 
 // ------------------------------------------------------- compressed 4-wide BVH ---
-// Node (64 B, one 4 x float4 load):
-//   q0 = (px, py, pz, ebits)    origin p (the node box's lower corner), ebits = ex | ey << 8 |
-//                               ez << 16 with s_k = 2^(e_k - 127) the per-axis step
+// Node (64 B, two 256-bit loads):
+//   q0 = (px, py, pz, sx)       origin p (the node box's lower corner) and the x step
 //   q1 = (lox, loy, loz, hix)   quantised child boxes, byte k = child k (0 <= q <= 255)
 //   q2 = (hiy, hiz, c0, c1)     child refs c_k: >= 0 node, ~slot leaf, kEmptyChild none
-//   q3 = (c2, c3, 0, 0)
+//   q3 = (c2, c3, sy, sz)       the y and z steps
+// Each step s = 2^(e - 127) is a power of two (e in [1, 254]), stored as a float so that the
+// test reads it without decoding.
 // An empty child slot has lo bytes 255 and hi bytes 0: an inverted box that no ray enters.
 // On every axis the slab slope a = inv * s is nonzero (|inv| >= 1 for a unit direction,
 // s >= 2^-126), so the near plane lies beyond the far plane; an infinite slope gives a NaN
@@ -326,6 +327,18 @@ __device__ __forceinline__ f3 sample_point(const float4 g[4], uint32_t type, flo
 // Karras, Laine, "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs",
 // HPG 2017, with 4 children per node).
 __device__ __forceinline__ float q_step(uint32_t e) { return __uint_as_float(e << 23); }
+// The four float4 of a 64-byte node (binary or 4-wide) in two 256-bit read-only loads; node
+// arrays start on a 256-byte boundary, so every node is 64-byte aligned.
+__device__ __forceinline__ void load_node64(const float4 *nodes, int32_t i, float4 &q0, float4 &q1, float4 &q2,
+                                           float4 &q3) {
+    const float4 *a = nodes + 4 * (size_t)i;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(q0.x), "=f"(q0.y), "=f"(q0.z), "=f"(q0.w), "=f"(q1.x), "=f"(q1.y), "=f"(q1.z), "=f"(q1.w)
+        : "l"(a));
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(q2.x), "=f"(q2.y), "=f"(q2.z), "=f"(q2.w), "=f"(q3.x), "=f"(q3.y), "=f"(q3.z), "=f"(q3.w)
+        : "l"(a + 2));
+}
 __device__ __forceinline__ float q_decode(float p, uint32_t q, float s) { return p + (float)q * s; }
 __device__ __forceinline__ uint32_t q_byte(uint32_t w, int k) { return (w >> (8 * k)) & 0xFFu; }
 // Three-input minimum / maximum (PTX min.f32 / max.f32 with three sources; a NaN input

@@ -228,10 +228,11 @@ cudaError_t launch_diffuse(const DiffuseParams &p, int max_blocks, cudaStream_t 
 enum DiffuseVariant {
     DV_DEFAULT = 0, DV_PS4 = 1, DV_PS3 = 2, DV_SIMPLE = 3, DV_W4 = 4, DV_W43 = 5,
     // lean 4-wide trace (k_diffuse_w4): threads per block x resident blocks per SM, shared
-    // stack entries per lane, ray ids a warp takes per fetch (32 x batch) -- 256 x 4, 8, 1;
-    // 256 x 5, 8, 1; 256 x 4, 16, 1; 128 x 8, 8, 1; 512 x 2, 8, 1; 256 x 4, 8, 4; 256 x 4, 8, 16
+    // stack entries per lane (r: a ring over local memory, l: the bottom entries), ray ids a
+    // warp takes per fetch (32 x batch) -- 256 x 4, 8r, 1; 256 x 5, 8r, 1; 256 x 4, 16l, 1;
+    // 128 x 8, 8r, 1; 512 x 2, 8r, 1; 256 x 4, 8r, 4; 256 x 4, 8r, 16; 256 x 4, 32l, 1
     DV_W4S4 = 6, DV_W4S5 = 7, DV_W4S4D16 = 8, DV_W4B128 = 9, DV_W4B512 = 10, DV_W4K4 = 11, DV_W4K16 = 12,
-    DV_LAST = DV_W4K16
+    DV_W4S4D32 = 13, DV_LAST = DV_W4S4D32
 };
 bool is_w4s_variant(int v);
 cudaError_t launch_w4s(const DiffuseParams &p, int variant, cudaStream_t s);

@@ -21,7 +21,7 @@ unsigned w4_grid(const DiffuseParams &p, int resident, int block) {
     return (unsigned)g;
 }
 
-template <int NB, bool RECORD, bool STATS, int MINB, int SD, int BLOCK, int KB = 1, bool MULTI = false>
+template <int NB, bool RECORD, bool STATS, int MINB, int SD, int BLOCK, int KB = 1, bool MULTI = false, bool LIN = false>
 cudaError_t w4_launch(const DiffuseParams &p, cudaStream_t s) {
     // resident blocks of one wave (SMs x blocks per SM); initialised once per instantiation,
     // thread-safe (the server launches from several threads)
@@ -30,7 +30,7 @@ cudaError_t w4_launch(const DiffuseParams &p, cudaStream_t s) {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm,
-                                                      k_diffuse_w4<NB, RECORD, STATS, MINB, SD, BLOCK, KB, MULTI>,
+                                                      k_diffuse_w4<NB, RECORD, STATS, MINB, SD, BLOCK, KB, MULTI, LIN>,
                                                       BLOCK, 0);
         return (sms < 1 ? 1 : sms) * (per_sm < 1 ? 1 : per_sm);
     }();
@@ -38,17 +38,19 @@ cudaError_t w4_launch(const DiffuseParams &p, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     DiffuseParams q = p;
     q.refill = refill_threshold(false, true);
-    k_diffuse_w4<NB, RECORD, STATS, MINB, SD, BLOCK, KB, MULTI><<<w4_grid(q, resident, BLOCK), BLOCK, 0, s>>>(q);
+    k_diffuse_w4<NB, RECORD, STATS, MINB, SD, BLOCK, KB, MULTI, LIN><<<w4_grid(q, resident, BLOCK), BLOCK, 0, s>>>(q);
     return cudaGetLastError();
 }
 
 // The tuner's shapes: threads per block x resident blocks per SM (all 64 registers a thread
-// but lean5, 48), shared stack entries per lane and the warp's ray-id batch.
+// but lean5, 48), shared stack entries per lane (a ring over local memory, or with LIN the
+// bottom entries) and the warp's ray-id batch.
 template <int NB, bool RECORD, bool STATS>
 cudaError_t w4_shape(const DiffuseParams &p, int variant, cudaStream_t s) {
     switch (variant) {
         case DV_W4S5: return w4_launch<NB, RECORD, STATS, 5, 8, 256>(p, s);
-        case DV_W4S4D16: return w4_launch<NB, RECORD, STATS, 4, 16, 256>(p, s);
+        case DV_W4S4D16: return w4_launch<NB, RECORD, STATS, 4, 16, 256, 1, false, true>(p, s);
+        case DV_W4S4D32: return w4_launch<NB, RECORD, STATS, 4, 32, 256, 1, false, true>(p, s);
         case DV_W4B128: return w4_launch<NB, RECORD, STATS, 8, 8, 128>(p, s);
         case DV_W4B512: return w4_launch<NB, RECORD, STATS, 2, 8, 512>(p, s);
         case DV_W4K4: return w4_launch<NB, RECORD, STATS, 4, 8, 256, 4>(p, s);
@@ -59,7 +61,7 @@ cudaError_t w4_shape(const DiffuseParams &p, int variant, cudaStream_t s) {
 
 }  // namespace
 
-bool is_w4s_variant(int v) { return v >= DV_W4S4 && v <= DV_W4K16; }
+bool is_w4s_variant(int v) { return v >= DV_W4S4 && v <= DV_W4S4D32; }
 
 cudaError_t launch_w4s(const DiffuseParams &p, int variant, cudaStream_t s) {
     if (!p.sc.nodes4 || p.sc.voxels) return cudaErrorInvalidValue;

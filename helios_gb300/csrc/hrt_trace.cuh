@@ -40,13 +40,26 @@ constexpr int kMaxCovers = 16;  // covers taken per periodic segment of a ray
 constexpr int32_t kSentinel = 0x7FFFFFF0;  // no node (empty stack, missed child)
 constexpr int kStack4 = 128;               // a 4-wide node pushes up to three children
 
+// Slab offsets of a compressed 4-wide node for a ray: b = (p - o) * inv per axis, p the
+// node's lower corner (q0.xyz).
+__device__ __forceinline__ f3 node4_offset(const float4 q0, f3 o, f3 inv) {
+    return mk((q0.x - o.x) * inv.x, (q0.y - o.y) * inv.y, (q0.z - o.z) * inv.z);
+}
+// The same from the origin premultiplied (ooi = o * inv), one fused multiply-add per axis:
+// b = p * inv - ooi.  Its rounding (of ooi, |o| 2^-24 in space) is of the order of the other
+// form's and far inside the leaf-box padding ((|x| + extent) 2^-20) for rays that start in the
+// scene, as diffuse rays do.
+__device__ __forceinline__ f3 node4_offset_ooi(const float4 q0, f3 ooi, f3 inv) {
+    return mk(__fmaf_rn(q0.x, inv.x, -ooi.x), __fmaf_rn(q0.y, inv.y, -ooi.y), __fmaf_rn(q0.z, inv.z, -ooi.z));
+}
+
 // The four child boxes of a compressed 4-wide node (q0..q3, format in hrt_device.cuh) against
-// a ray (origin o, inverse direction inv) within [tmin, tmax]: entry distances tk (INFINITY:
-// missed) and child references ck (kSentinel: missed), in slot order.
+// a ray (inverse direction inv, node offsets b from node4_offset) within [tmin, tmax]: entry
+// distances tk (INFINITY: missed) and child references ck in slot order -- kSentinel for a
+// missed child when MARK, else every slot's reference (a hit always has tk <= tmax < INFINITY).
+template <bool MARK = true>
 __device__ __forceinline__ void node4_children(const float4 q0, const float4 q1, const float4 q2, const float4 q3,
-                                               f3 o, f3 inv, float tmin, float tmax, float tk[4], int32_t ck[4]) {
-    const uint32_t eb = __float_as_uint(q0.w);
-    const float sx = q_step(eb & 0xFFu), sy = q_step((eb >> 8) & 0xFFu), sz = q_step((eb >> 16) & 0xFFu);
+                                               f3 b, f3 inv, float tmin, float tmax, float tk[4], int32_t ck[4]) {
     // near / far plane bytes per axis from the sign of the ray direction: with inv >= 0 the
     // lower plane is entered first (q_lo <= q_hi, fma is monotone)
     const uint32_t nx = inv.x >= 0.f ? __float_as_uint(q1.x) : __float_as_uint(q1.w);
@@ -56,17 +69,16 @@ __device__ __forceinline__ void node4_children(const float4 q0, const float4 q1,
     const uint32_t nz = inv.z >= 0.f ? __float_as_uint(q1.z) : __float_as_uint(q2.y);
     const uint32_t fz = inv.z >= 0.f ? __float_as_uint(q2.y) : __float_as_uint(q1.z);
     const int32_t cref[4] = {__float_as_int(q2.z), __float_as_int(q2.w), __float_as_int(q3.x), __float_as_int(q3.y)};
-    // slab planes in the node's quantised frame: t = q * (inv s) + (p - o) inv, one fused
-    // multiply-add per plane (inv s is exact: s is a power of two).  The rounding is of the
-    // same order as the binary test's and is covered by the leaf-box padding, so no box
-    // holding an accepted hit is culled.
-    const float ax = inv.x * sx, ay = inv.y * sy, az = inv.z * sz;
-    const float bx = (q0.x - o.x) * inv.x, by = (q0.y - o.y) * inv.y, bz = (q0.z - o.z) * inv.z;
+    // slab planes in the node's quantised frame: t = q * (inv s) + b, one fused multiply-add
+    // per plane (inv s is exact: s is a power of two).  The rounding is of the same order as
+    // the binary test's and is covered by the leaf-box padding, so no box holding an accepted
+    // hit is culled.
+    const float ax = inv.x * q0.w, ay = inv.y * q3.z, az = inv.z * q3.w;
     // near and far plane of one axis as one packed pair: the same two subtractions (exact)
     // and fused multiply-adds as the scalar form, in half the instructions
     const unsigned long long bias = f2_pack(8388608.0f, 8388608.0f);
     const unsigned long long ax2 = f2_pack(ax, ax), ay2 = f2_pack(ay, ay), az2 = f2_pack(az, az);
-    const unsigned long long bx2 = f2_pack(bx, bx), by2 = f2_pack(by, by), bz2 = f2_pack(bz, bz);
+    const unsigned long long bx2 = f2_pack(b.x, b.x), by2 = f2_pack(b.y, b.y), bz2 = f2_pack(b.z, b.z);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         float tnx, tfx, tny, tfy, tnz, tfz;
@@ -77,7 +89,7 @@ __device__ __forceinline__ void node4_children(const float4 q0, const float4 q1,
         const float tf = fmin3(tfx, tfy, fminf(tfz, tmax));
         const bool hit = tn <= tf;  // empty slots hold inverted boxes
         tk[k] = hit ? tn : INFINITY;
-        ck[k] = hit ? cref[k] : kSentinel;
+        ck[k] = (hit || !MARK) ? cref[k] : kSentinel;
     }
 }
 
@@ -103,7 +115,7 @@ __device__ __forceinline__ void node4_sort(float tk[4], int32_t ck[4]) {
 // node4_children, sorted nearest first.
 __device__ __forceinline__ void node4_test(const float4 q0, const float4 q1, const float4 q2, const float4 q3, f3 o,
                                            f3 inv, float tmin, float tmax, float tk[4], int32_t ck[4]) {
-    node4_children(q0, q1, q2, q3, o, inv, tmin, tmax, tk, ck);
+    node4_children(q0, q1, q2, q3, node4_offset(q0, o, inv), inv, tmin, tmax, tk, ck);
     node4_sort(tk, ck);
 }
 
@@ -131,8 +143,8 @@ __device__ Hit trace_bvh(const TraceScene &sc, f3 o, f3 d, float tmin, float tma
             return h;
         }
         if (STATS) ++*nv;
-        const float4 *nd = sc.nodes + 4 * (size_t)cur;
-        float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
+        float4 n0, n1, n2, n3;
+        load_node64(sc.nodes, cur, n0, n1, n2, n3);
         int32_t c[2] = {__float_as_int(n3.x), __float_as_int(n3.y)};
         float tn0, tn1;
         bool hb[2];
@@ -218,10 +230,11 @@ __device__ Hit trace_bvh4(const TraceScene &sc, f3 o, f3 d, float tmin, float tm
             return h;
         }
         if (STATS) ++*nv;
-        const float4 *nd = sc.nodes4 + 4 * (size_t)cur;
+        float4 q0, q1, q2, q3;
+        load_node64(sc.nodes4, cur, q0, q1, q2, q3);
         float tk[4];
         int32_t ck[4];
-        node4_test(__ldg(nd), __ldg(nd + 1), __ldg(nd + 2), __ldg(nd + 3), o, inv, tmin, best, tk, ck);
+        node4_test(q0, q1, q2, q3, o, inv, tmin, best, tk, ck);
         int32_t inner[4];
         int ni = 0;
 #pragma unroll
@@ -676,8 +689,8 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
                     break;
                 }
                 if (STATS) ++nvis;
-                const float4 *nd = sc.nodes4 + 4 * (size_t)cur;
-                const float4 q0 = __ldg(nd), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2), q3 = __ldg(nd + 3);
+                float4 q0, q1, q2, q3;
+                load_node64(sc.nodes4, cur, q0, q1, q2, q3);
                 float tk[4];
                 int32_t ck[4];
                 node4_test(q0, q1, q2, q3, o, inv, 1e-4f, best, tk, ck);
@@ -711,8 +724,8 @@ __global__ void __launch_bounds__(kBlock, MINB) k_diffuse_ps(const DiffuseParams
                     break;
                 }
                 if (STATS) ++nvis;
-                const float4 *nd = sc.nodes + 4 * (size_t)cur;
-                const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
+                float4 n0, n1, n2, n3;
+                load_node64(sc.nodes, cur, n0, n1, n2, n3);
                 int32_t c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
                 float tn0, tn1;
                 const bool h0 = c0 != kEmptyChild &&

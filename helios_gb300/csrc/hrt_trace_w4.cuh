@@ -3,20 +3,28 @@
 //
 // The trace is bound by the latency of node fetches (L1/L2 hits) and by issue slots, not by
 // DRAM.  More resident warps hide more of that latency, so this kernel keeps only the state
-// of the node loop in registers -- ray origin, inverse direction, best distance, current
-// node, postponed leaf, stack pointer and visit budget -- and moves the rest of each lane's
-// state to shared memory, where it is touched only when a ray starts, reaches a leaf or
-// ends: the direction and the watertight-test set-up (kx, ky, kz, Sx, Sy, Sz), the best hit
-// so far, the origin primitive and face, the wrap count, the running-sum key and sums.
-// The traversal stack is a ring of SD entries per lane in shared memory (indexed
-// [entry][lane], so the 32 lanes of a warp always hit 32 different banks) over a local
-// overflow array: entries deeper than SD below the top are moved to local memory on push
-// and brought back on pop, so local memory is touched only by rays whose stack is deeper
-// than SD.
+// of the node loop in registers -- the ray origin premultiplied by the inverse direction
+// (ooi), the inverse direction, best distance, current node, postponed leaf, stack pointer
+// and visit budget -- and moves the rest of each lane's state to shared memory, where it is
+// touched only when a ray starts, reaches a leaf or ends: the origin, the direction and the
+// watertight-test set-up (kx, ky, kz, Sx, Sy, Sz), the best hit so far, the origin primitive
+// and face, the wrap count, the running-sum key and sums.  A node visit computes each slab
+// offset in one fused multiply-add from ooi (node4_offset_ooi) and reads the node in two
+// 256-bit loads.
+// The traversal stack keeps SD entries per lane in shared memory (indexed [entry][lane], so
+// the 32 lanes of a warp always hit 32 different banks) over a local overflow array, in one
+// of two layouts.  RingStack: the top SD entries in a ring, entries deeper than SD below the
+// top moved to local memory on push and brought back on pop.  LinStack (LIN): the bottom SD
+// entries in shared memory, deeper ones in local memory, and a visit whose pushes all stay
+// below SD writes them with no overflow test.  Local memory is touched only by rays whose
+// stack is deeper than SD.  On the 1 M-triangle orchard LinStack with SD = 16 is the faster
+// (180 against 184 ms per diffuse launch for the ring at SD = 16, 186-189 at SD = 8).
 //
 // Hits equal those of trace_bvh / k_diffuse_ps: the same node and primitive tests, the same
 // tie rule (closest, then smaller original index); only the order of work differs.
 #pragma once
+#include <type_traits>
+
 #include "hrt_trace.cuh"
 
 namespace hrt {
@@ -43,6 +51,19 @@ struct RingStack {
     }
 };
 
+// The bottom SD entries in shared memory ([entry][lane]), deeper ones in local memory.
+template <int SD, int BLOCK>
+struct LinStack {
+    int32_t (*ring)[BLOCK];   // [SD][BLOCK] in shared memory (not a ring: entry i at row i)
+    int tid;
+    int32_t spill[kStack4];
+    __device__ __forceinline__ void push(int sp, int32_t v) {
+        if (sp < SD) ring[sp][tid] = v;
+        else spill[sp - SD] = v;
+    }
+    __device__ __forceinline__ int32_t pop(int sp) { return sp < SD ? ring[sp][tid] : spill[sp - SD]; }
+};
+
 // BLOCK: threads per block; MINB: resident blocks per SM the register allocation must allow.
 // SD: stack entries per lane in shared memory (a power of two).  KB: ray-id batch -- a warp
 // takes 32 x KB consecutive ray ids from the global counter at a time and hands them to its
@@ -50,12 +71,12 @@ struct RingStack {
 // MULTI (recording mode only): the launch traces several scenes -- P.slots[0..P.nslots) each
 // give a scene, a primitive chunk, ray counts, seed, pass and hit buffer, with consecutive
 // ranges of the launch's ray ids (id_begin) -- so one persistent launch covers the pass of
-// every scene of a multi-scene sweep.
-template <int NB, bool RECORD, bool STATS, int MINB, int SD, int BLOCK, int KB, bool MULTI = false>
+// every scene of a multi-scene sweep.  LIN: the LinStack layout, else RingStack.
+template <int NB, bool RECORD, bool STATS, int MINB, int SD, int BLOCK, int KB, bool MULTI = false, bool LIN = false>
 __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams P) {
     static_assert(!MULTI || (RECORD && !STATS), "multi-scene launches record hits only");
     __shared__ double s_sum[RECORD ? 1 : NB][BLOCK];            // running sums of the lane's origin
-    __shared__ float s_ray[6][BLOCK];                            // d.xyz, Sx, Sy, Sz
+    __shared__ float s_ray[9][BLOCK];                            // d.xyz, Sx, Sy, Sz, o.xyz
     __shared__ uint32_t s_lane[5][BLOCK];                        // see the L_* slots below
     __shared__ int32_t s_stack[SD][BLOCK];
     __shared__ unsigned long long s_rid[RECORD ? BLOCK : 1];     // record: hit-buffer index
@@ -86,13 +107,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
         __syncthreads();
     }
 
-    RingStack<SD, BLOCK> stk;
+    typename std::conditional<LIN, LinStack<SD, BLOCK>, RingStack<SD, BLOCK>>::type stk;
     stk.ring = s_stack;
     stk.tid = tid;
     uint32_t nvis = 0, ntest = 0;  // statistics builds only
     uint32_t nrays = 0;
     bool live = false, exhausted = false;
-    f3 o = mk(0.f, 0.f, 0.f), inv = o;
+    f3 ooi = mk(0.f, 0.f, 0.f), inv = ooi;
     float best = 1e38f;
     int32_t cur = kSentinel, leaf = 0;
     int sp = 0;
@@ -185,7 +206,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                         float4 g[4];
                         load_rgen(sc, p, g);
                         const uint32_t type = __float_as_uint(g[0].w);
-                        f3 d;
+                        f3 o, d;
                         diffuse_ray<false>(g, type, r, p, face, dxk, dyk, seedk, passk, &o, &d, sc.masks);
                         const WT w = wt_setup(d);
                         s_ray[0][tid] = d.x;
@@ -194,10 +215,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                         s_ray[3][tid] = w.Sx;
                         s_ray[4][tid] = w.Sy;
                         s_ray[5][tid] = w.Sz;
+                        s_ray[6][tid] = o.x;
+                        s_ray[7][tid] = o.y;
+                        s_ray[8][tid] = o.z;
                         s_lane[L_AXES][tid] = (uint32_t)(w.kx | (w.ky << 2) | (w.kz << 4) | (face << 6));
                         s_lane[L_P][tid] = p;
                         s_lane[L_HIT][tid] = kMissCode;
                         inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+                        ooi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
                         best = 1e38f;
                         cur = (sc.n > 0) ? 0 : kSentinel;
                         leaf = 0;
@@ -227,24 +252,31 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                 break;
             }
             if (STATS) ++nvis;
-            const float4 *nd = sc.nodes4 + 4 * (size_t)cur;
-            const float4 q0 = __ldg(nd), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2), q3 = __ldg(nd + 3);
+            float4 q0, q1, q2, q3;
+            load_node64(sc.nodes4, cur, q0, q1, q2, q3);
             float tk[4];
-            int32_t ck[4];
-            node4_test(q0, q1, q2, q3, o, inv, 1e-4f, best, tk, ck);
-            if (ck[0] == kSentinel) {
+            int32_t ck[4];  // every slot's reference: a child is hit when its tk < INFINITY
+            node4_children<false>(q0, q1, q2, q3, node4_offset_ooi(q0, ooi, inv), inv, 1e-4f, best, tk, ck);
+            node4_sort(tk, ck);
+            if (!(tk[0] < INFINITY)) {
                 cur = POP();
             } else {
-                if (sp + 3 > SD + kStack4) {
-                    raise(sc.status, ERR_STACK);
-                    cur = kSentinel;
-                    leaf = 0;
-                    sp = 0;
-                    break;
-                }
+                if (LIN && sp + 3 <= SD) {  // the whole push in shared memory
 #pragma unroll
-                for (int k = 3; k >= 1; --k)
-                    if (ck[k] != kSentinel) stk.push(sp++, ck[k]);
+                    for (int k = 3; k >= 1; --k)
+                        if (tk[k] < INFINITY) s_stack[sp++][tid] = ck[k];
+                } else {
+                    if (sp + 3 > SD + kStack4) {
+                        raise(sc.status, ERR_STACK);
+                        cur = kSentinel;
+                        leaf = 0;
+                        sp = 0;
+                        break;
+                    }
+#pragma unroll
+                    for (int k = 3; k >= 1; --k)
+                        if (tk[k] < INFINITY) stk.push(sp++, ck[k]);
+                }
                 cur = ck[0];
             }
             if (cur < 0 && leaf == 0) {
@@ -254,8 +286,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
             const unsigned am = __activemask();
             if (__all_sync(am, leaf != 0) || __popc(am) < P.refill) break;
         }
-        // ---- primitive tests (direction and watertight set-up come back from shared memory)
+        // ---- primitive tests (origin, direction and watertight set-up come back from shared memory)
         if (leaf != 0) {
+            const f3 o = mk(s_ray[6][tid], s_ray[7][tid], s_ray[8][tid]);
             const f3 d = mk(s_ray[0][tid], s_ray[1][tid], s_ray[2][tid]);
             const uint32_t ax = s_lane[L_AXES][tid];
             WT w;
@@ -297,6 +330,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
         const uint32_t bcode = s_lane[L_HIT][tid];
         bool lost = false;
         if (sc.nbbox > 0) {
+            const f3 o = mk(s_ray[6][tid], s_ray[7][tid], s_ray[8][tid]);
             const f3 d = mk(s_ray[0][tid], s_ray[1][tid], s_ray[2][tid]);
             float tb;
             int which = -1;
@@ -316,7 +350,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                         const float width = sc.bbox[4 * (yb + 1)].y - sc.bbox[4 * yb].y;
                         hp.y = hp.y + ((which == yb) ? width : -width);
                     }
-                    o = hp;
+                    s_ray[6][tid] = hp.x;
+                    s_ray[7][tid] = hp.y;
+                    s_ray[8][tid] = hp.z;
+                    ooi = mk(hp.x * inv.x, hp.y * inv.y, hp.z * inv.z);
                     best = 1e38f;
                     s_lane[L_HIT][tid] = kMissCode;
                     s_lane[L_AXES][tid] = (ax & 0xFFu) | ((wraps + 1u) << 8);

@@ -408,7 +408,7 @@ def test_traversal_counts_match_oracle(gpu, oracle_mod):
     assert 0 < m["diffuse_prim_tests"] <= m["prim_tests"]
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13])
 def test_traversal_variants_agree(oracle_mod, variant):
     """Every diffuse-kernel variant (binary or compressed 4-wide nodes, persistent or one
     ray per thread) gives the oracle's fluxes and ray count: hits do not depend on the

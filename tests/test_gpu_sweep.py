@@ -59,7 +59,7 @@ def test_sweep_channels_equal_plain_solves():
     np.testing.assert_allclose(again, sweep, rtol=1e-6, atol=1e-6)
 
 
-@pytest.mark.parametrize("variant", [4, 6, 7, 8, 9, 10, 11, 12])
+@pytest.mark.parametrize("variant", [4, 6, 7, 8, 9, 10, 11, 12, 13])
 def test_sweep_recording_variants_agree(variant):
     """The recording trace of the sweep gives the same channels whichever 4-wide kernel
     records the hits (the generic persistent kernel or the lean one in each of its block
