@@ -244,13 +244,15 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
         const TraceScene &sc = SC;
         const uint32_t n4 = (uint32_t)sc.n4;
         while (cur >= 0 && cur != kSentinel) {
-            if ((uint32_t)cur >= n4 || budget-- == 0u) {
-                raise(sc.status, budget == 0xFFFFFFFFu ? ERR_BUDGET : ERR_BOUNDS);
+            // both tests evaluated (no short-circuit branch), then the visit is counted
+            if (((uint32_t)cur >= n4) | (budget == 0u)) {
+                raise(sc.status, (uint32_t)cur >= n4 ? ERR_BOUNDS : ERR_BUDGET);
                 cur = kSentinel;
                 leaf = 0;
                 sp = 0;
                 break;
             }
+            --budget;
             if (STATS) ++nvis;
             float4 q0, q1, q2, q3;
             load_node64(sc.nodes4, cur, q0, q1, q2, q3);
@@ -258,15 +260,17 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
             int32_t ck[4];  // every slot's reference: a child is hit when its tk < INFINITY
             node4_children<false>(q0, q1, q2, q3, node4_offset_ooi(q0, ooi, inv), inv, 1e-4f, best, tk, ck);
             node4_sort(tk, ck);
-            if (!(tk[0] < INFINITY)) {
-                cur = POP();
-            } else {
-                if (LIN && sp + 3 <= SD) {  // the whole push in shared memory
+            if (LIN) {
+                // hit children other than the nearest pushed farthest first (predicated: a
+                // visit that hits nothing pushes nothing), then the nearest entered or, with
+                // no hit, the top of the stack taken -- no branch between the two cases
+                const bool any = tk[0] < INFINITY;
+                if (sp + 3 <= SD) {  // the whole push in shared memory
 #pragma unroll
                     for (int k = 3; k >= 1; --k)
                         if (tk[k] < INFINITY) s_stack[sp++][tid] = ck[k];
                 } else {
-                    if (sp + 3 > SD + kStack4) {
+                    if (any && sp + 3 > SD + kStack4) {
                         raise(sc.status, ERR_STACK);
                         cur = kSentinel;
                         leaf = 0;
@@ -277,6 +281,22 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                     for (int k = 3; k >= 1; --k)
                         if (tk[k] < INFINITY) stk.push(sp++, ck[k]);
                 }
+                int32_t nxt = ck[0];
+                if (!any) nxt = POP();
+                cur = nxt;
+            } else if (!(tk[0] < INFINITY)) {
+                cur = POP();
+            } else {
+                if (sp + 3 > SD + kStack4) {
+                    raise(sc.status, ERR_STACK);
+                    cur = kSentinel;
+                    leaf = 0;
+                    sp = 0;
+                    break;
+                }
+#pragma unroll
+                for (int k = 3; k >= 1; --k)
+                    if (tk[k] < INFINITY) stk.push(sp++, ck[k]);
                 cur = ck[0];
             }
             if (cur < 0 && leaf == 0) {
