@@ -93,8 +93,6 @@ __device__ __forceinline__ void node4_children(const float4 q0, const float4 q1,
     }
 }
 
-// The children of node4_children sorted nearest first (a five-comparator network).
-__device__ __forceinline__ void node4_sort(float tk[4], int32_t ck[4]) {
 #define HRT_CSWAP(a, b)                                  \
     if (tk[b] < tk[a]) {                                 \
         const float tt = tk[a];                          \
@@ -104,13 +102,24 @@ __device__ __forceinline__ void node4_sort(float tk[4], int32_t ck[4]) {
         ck[a] = ck[b];                                   \
         ck[b] = cc;                                      \
     }
+// The children of node4_children sorted nearest first (a five-comparator network).
+__device__ __forceinline__ void node4_sort(float tk[4], int32_t ck[4]) {
     HRT_CSWAP(0, 1)
     HRT_CSWAP(2, 3)
     HRT_CSWAP(0, 2)
     HRT_CSWAP(1, 3)
     HRT_CSWAP(1, 2)
-#undef HRT_CSWAP
 }
+// The nearest child of node4_children moved to slot 0 (a three-comparator tournament); the
+// others keep the tournament's order.  The lean trace enters the nearest child and pushes the
+// rest: ordering them too (node4_sort) saved 0.4 % of the node visits on the 1 M-triangle
+// orchard and cost 2.6 % of the time per diffuse launch.
+__device__ __forceinline__ void node4_nearest(float tk[4], int32_t ck[4]) {
+    HRT_CSWAP(0, 1)
+    HRT_CSWAP(2, 3)
+    HRT_CSWAP(0, 2)
+}
+#undef HRT_CSWAP
 
 // node4_children, sorted nearest first.
 __device__ __forceinline__ void node4_test(const float4 q0, const float4 q1, const float4 q2, const float4 q3, f3 o,

@@ -259,11 +259,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
             float tk[4];
             int32_t ck[4];  // every slot's reference: a child is hit when its tk < INFINITY
             node4_children<false>(q0, q1, q2, q3, node4_offset_ooi(q0, ooi, inv), inv, 1e-4f, best, tk, ck);
-            node4_sort(tk, ck);
+            node4_nearest(tk, ck);
             if (LIN) {
-                // hit children other than the nearest pushed farthest first (predicated: a
-                // visit that hits nothing pushes nothing), then the nearest entered or, with
-                // no hit, the top of the stack taken -- no branch between the two cases
+                // hit children other than the nearest pushed (predicated: a visit that hits
+                // nothing pushes nothing), then the nearest entered or, with no hit, the top of
+                // the stack taken -- no branch between the two cases
                 const bool any = tk[0] < INFINITY;
                 if (sp + 3 <= SD) {  // the whole push in shared memory
 #pragma unroll
