@@ -327,6 +327,28 @@ __device__ __forceinline__ f3 sample_point(const float4 g[4], uint32_t type, flo
 // Karras, Laine, "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs",
 // HPG 2017, with 4 children per node).
 __device__ __forceinline__ float q_step(uint32_t e) { return __uint_as_float(e << 23); }
+
+// Unsigned 32-bit division by a divisor fixed for a launch, by multiplication (Granlund and
+// Montgomery, "Division by invariant integers using multiplication", PLDI 1994, the round-up
+// method with a 32-bit multiplier): with l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1,
+// n / d = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0) for t = umulhi(m, n), exactly for every
+// 32-bit n and 1 <= d < 2^32.
+struct FastDiv {
+    uint32_t m, s1, s2;
+};
+__host__ __device__ __forceinline__ FastDiv make_fastdiv(uint32_t d) {
+    uint32_t l = 0;
+    while (l < 32 && (1ull << l) < d) ++l;
+    FastDiv f;
+    f.m = (uint32_t)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    f.s1 = l < 1 ? l : 1;
+    f.s2 = l > 1 ? l - 1 : 0;
+    return f;
+}
+__host__ __device__ __forceinline__ uint32_t fast_div(uint32_t n, const FastDiv &f) {
+    const uint32_t t = (uint32_t)(((uint64_t)f.m * n) >> 32);  // umulhi
+    return (t + ((n - t) >> f.s1)) >> f.s2;
+}
 // The four float4 of a 64-byte node (binary or 4-wide) in two 256-bit read-only loads; node
 // arrays start on a 256-byte boundary, so every node is 64-byte aligned.
 __device__ __forceinline__ void load_node64(const float4 *nodes, int32_t i, float4 &q0, float4 &q1, float4 &q2,

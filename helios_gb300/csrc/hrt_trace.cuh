@@ -504,11 +504,11 @@ __device__ __forceinline__ f3 direct_origin(const float4 g[4], uint32_t type, ui
 // bottom).  Surfaces: cosine-weighted about the normal, counter (r, p, face, 0).  Voxels
 // (VOX builds only): both faces share the sample of counter (r, p, 1, 0), the third
 // coordinate comes from (r, p, 2, 0), and the bottom face flips the direction.
+// diffuse_ray with the ray's stratum given: ti = r % dimx, pi = r / dimx.
 template <bool VOX>
-__device__ __forceinline__ void diffuse_ray(const float4 g[4], uint32_t type, uint32_t r, uint32_t p, int face,
-                                            int dimx, int dimy, uint32_t seed, uint32_t pass, f3 *org, f3 *dir,
-                                            const MaskSet &ms) {
-    const int ti = (int)(r % (uint32_t)dimx), pi = (int)(r / (uint32_t)dimx);
+__device__ __forceinline__ void diffuse_ray_cell(const float4 g[4], uint32_t type, uint32_t r, uint32_t p, int face,
+                                                 int ti, int pi, int dimx, int dimy, uint32_t seed, uint32_t pass,
+                                                 f3 *org, f3 *dir, const MaskSet &ms) {
     f3 dd;
     if (VOX && type == PT_VOXEL) {
         const u4 u = philox(r, p, 1u, 0u, seed, pass);
@@ -523,6 +523,13 @@ __device__ __forceinline__ void diffuse_ray(const float4 g[4], uint32_t type, ui
         *org = sample_point(g, type, uu, vv, 0.f);
     }
     *dir = (face == 0) ? mk(-dd.x, -dd.y, -dd.z) : dd;
+}
+template <bool VOX>
+__device__ __forceinline__ void diffuse_ray(const float4 g[4], uint32_t type, uint32_t r, uint32_t p, int face,
+                                            int dimx, int dimy, uint32_t seed, uint32_t pass, f3 *org, f3 *dir,
+                                            const MaskSet &ms) {
+    diffuse_ray_cell<VOX>(g, type, r, p, face, (int)(r % (uint32_t)dimx), (int)(r / (uint32_t)dimx), dimx, dimy,
+                          seed, pass, org, dir, ms);
 }
 
 // ------------------------------------------------------------------ diffuse --
