@@ -4,8 +4,8 @@
 // The trace is bound by the latency of node fetches (L1/L2 hits) and by issue slots, not by
 // DRAM.  More resident warps hide more of that latency, so this kernel keeps only the state
 // of the node loop in registers -- the ray origin premultiplied by the inverse direction
-// (ooi), the inverse direction, best distance, current node, postponed leaf, stack pointer
-// and visit budget -- and moves the rest of each lane's state to shared memory, where it is
+// (ooi), the inverse direction, best distance, current node, two postponed leaves, stack
+// pointer and visit budget -- and moves the rest of each lane's state to shared memory, where it is
 // touched only when a ray starts, reaches a leaf or ends: the origin, the direction and the
 // watertight-test set-up (kx, ky, kz, Sx, Sy, Sz), the best hit so far, the origin primitive
 // and face, the wrap count, the running-sum key and sums.  A node visit computes each slab
@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
     bool live = false, exhausted = false;
     f3 ooi = mk(0.f, 0.f, 0.f), inv = ooi;
     float best = 1e38f;
-    int32_t cur = kSentinel, leaf = 0;
+    int32_t cur = kSentinel, leaf = 0, leaf2 = 0;  // current node, up to two postponed leaves
     // LIN: entry 0 of the shared stack holds kSentinel for good and a ray starts with sp = 1, so a
     // pop needs no empty-stack test: popping the sentinel ends the ray's traversal (168.7 against
     // 173.2 ms per diffuse launch of the 1 M-triangle orchard)
@@ -254,6 +254,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                         best = 1e38f;
                         cur = (sc.n > 0) ? 0 : kSentinel;
                         leaf = 0;
+                        leaf2 = 0;
                         sp = kSp0;
                         budget = sc.visit_budget;
                         live = true;
@@ -279,6 +280,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                 raise(sc.status, (uint32_t)cur >= n4 ? ERR_BOUNDS : ERR_BUDGET);
                 cur = kSentinel;
                 leaf = 0;
+                leaf2 = 0;
                 sp = kSp0;
                 break;
             }
@@ -304,6 +306,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                         raise(sc.status, ERR_STACK);
                         cur = kSentinel;
                         leaf = 0;
+                        leaf2 = 0;
                         sp = kSp0;
                         break;
                     }
@@ -321,6 +324,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                     raise(sc.status, ERR_STACK);
                     cur = kSentinel;
                     leaf = 0;
+                    leaf2 = 0;
                     sp = kSp0;
                     break;
                 }
@@ -329,12 +333,16 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                     if (tk[k] < INFINITY) stk.push(sp++, ck[k]);
                 cur = ck[0];
             }
-            if (cur < 0 && leaf == 0) {
-                leaf = cur;
+            // a leaf is postponed while one of the two slots is free; a lane with both full stops
+            // at its third leaf.  The warp leaves the loop only when fewer than P.refill lanes
+            // remain in it (no vote on the leaves): 162.7 against 167.4 ms per diffuse launch of
+            // the 1 M-triangle orchard with one slot and a leave-when-all-have-a-leaf vote
+            if (cur < 0 && leaf2 == 0) {
+                if (leaf == 0) leaf = cur;
+                else leaf2 = cur;
                 cur = POP();
             }
-            const unsigned am = __activemask();
-            if (__all_sync(am, leaf != 0) || __popc(am) < P.refill) break;
+            if (__popc(__activemask()) < P.refill) break;
         }
         // ---- primitive tests (origin, direction and watertight set-up come back from shared memory)
         if (leaf != 0) {
@@ -366,8 +374,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
                 } else {
                     raise(sc.status, ERR_BOUNDS);
                 }
-                leaf = 0;
-                if (cur < 0) {
+                leaf = leaf2;
+                leaf2 = 0;
+                if (leaf == 0 && cur < 0) {
                     leaf = cur;
                     cur = POP();
                 }
