@@ -561,10 +561,10 @@ __device__ __forceinline__ double sky_fd(f3 dir, const SkyParams &sky, int b) {
 // 4-wide trace took 80.5 ms with it against 78.1 ms without.  HRT_REFILL overrides (0-32).
 constexpr int kRefillDefault = 8;
 // The lean 4-wide trace (hrt_trace_w4.cuh) keeps fewer registers per lane and refills more
-// cheaply; on the same workload, per diffuse launch: 4 215 ms, 8 199.6 ms, 12 194.5 ms,
-// 16 192.0-194.2 ms, 20 191.9-192.4 ms, 24 200 ms, 28 229 ms, 32 390 ms.  16 sits in the flat
-// part of that curve.
-constexpr int kRefillLean = 16;
+// cheaply; on the same workload, per diffuse launch, with two postponed leaves and no leaf
+// vote: 8 162.5 ms, 10 160.4 ms, 12 160.2 ms, 14 161.2 ms, 16 162.7 ms, 18 161.8 ms, 20 161.1 ms,
+// 24 170.6 ms (run to run on one box within 0.02 ms).
+constexpr int kRefillLean = 12;
 inline int refill_threshold(bool voxels, bool lean = false) {
     static const int env = [] {  // initialised once, thread-safe; -1: not set
         const char *e = getenv("HRT_REFILL");
