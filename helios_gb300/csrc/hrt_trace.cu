@@ -575,13 +575,25 @@ __global__ void __launch_bounds__(kBlock, 3) k_direct_sweep(const SweepDirectPar
 
 // One warp per (face, primitive): lanes run over channels, the R recorded hits of the
 // primitive are read in order, so every sum is deterministic.  A hit reads the row
-// radiation_out[hit][0..C) (coalesced); a miss adds the channel's sky flux.
+// radiation_out[hit][0..C) (coalesced); a miss adds the channel's sky flux.  The hit codes come
+// 32 at a time in one coalesced load and are broadcast by shuffles, so the row loads of
+// consecutive hits do not wait on one another.  Sums are compensated FP32 (Kahan: each add
+// carries its rounding error into the next), converted to FP64 once per channel: GB300 runs
+// FP32 adds at many times its FP64 rate, and the FP64 form of this gather (an F2F and a DADD
+// per channel and hit) was FP64-bound at 0.37 s per pass of the 1 M-triangle orchard's day
+// sweep.  The compensated sum's error is about 2^-23 of the sum of the values (all >= 0).
 template <int CPL>
 __global__ void __launch_bounds__(256) k_gather(const GatherParams P) {
     const int lane = threadIdx.x & 31;
     const int nf = ((P.faces & 1) ? 1 : 0) + ((P.faces & 2) ? 1 : 0);
     const long long items = (long long)nf * P.n;
     const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+    float sky[CPL];
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) {
+        const int c = lane + 32 * k;
+        sky[k] = c < P.C ? __ldg(P.sky + c) : 0.f;
+    }
     for (long long item = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < items; item += warps) {
         const int fi = (int)(item / P.n);
         const int p = (int)(item % P.n);
@@ -592,25 +604,29 @@ __global__ void __launch_bounds__(256) k_gather(const GatherParams P) {
             for (int c = lane; c < P.C; c += 32) G[c] = 0.0;
             continue;
         }
-        double acc[CPL];
+        float sum[CPL], err[CPL];
 #pragma unroll
-        for (int k = 0; k < CPL; ++k) acc[k] = 0.0;
+        for (int k = 0; k < CPL; ++k) sum[k] = err[k] = 0.f;
         const uint32_t *row = P.hits + ((size_t)fi * P.n + p) * P.R;
-        for (int r = 0; r < P.R; ++r) {
-            const uint32_t h = __ldg(row + r);
-            if (h == kLostCode) continue;
-            if (h == kMissCode) {
+        for (int r0 = 0; r0 < P.R; r0 += 32) {
+            const uint32_t mine = (r0 + lane < P.R) ? __ldg(row + r0 + lane) : kLostCode;
+            const int nr = min(32, P.R - r0);
+#pragma unroll 4
+            for (int j = 0; j < nr; ++j) {
+                const uint32_t h = __shfl_sync(0xffffffffu, mine, j);  // the same code in every lane
+                if (h == kLostCode) continue;
+                const bool miss = h == kMissCode;
+                const uint32_t hc = miss ? 0u : h;  // a miss reads the sky; its row pointer stays in bounds
+                const float *src = ((hc & 1u) ? P.otop : P.obot) + (size_t)(hc >> 1) * P.C;
 #pragma unroll
                 for (int k = 0; k < CPL; ++k) {
                     const int c = lane + 32 * k;
-                    if (c < P.C) acc[k] += (double)__ldg(P.sky + c);
-                }
-            } else {
-                const float *src = ((h & 1u) ? P.otop : P.obot) + (size_t)(h >> 1) * P.C;
-#pragma unroll
-                for (int k = 0; k < CPL; ++k) {
-                    const int c = lane + 32 * k;
-                    if (c < P.C) acc[k] += (double)__ldg(src + c);
+                    if (c < P.C) {
+                        const float x = miss ? sky[k] : __ldg(src + c);
+                        const float y = x - err[k], t = sum[k] + y;
+                        err[k] = (t - sum[k]) - y;
+                        sum[k] = t;
+                    }
                 }
             }
         }
@@ -618,7 +634,7 @@ __global__ void __launch_bounds__(256) k_gather(const GatherParams P) {
 #pragma unroll
         for (int k = 0; k < CPL; ++k) {
             const int c = lane + 32 * k;
-            if (c < P.C) G[c] = acc[k];
+            if (c < P.C) G[c] = (double)sum[k] - (double)err[k];
         }
     }
 }
@@ -916,6 +932,7 @@ cudaError_t launch_gather(const GatherParams &p, cudaStream_t s) {
     if (cpl <= 1) k_gather<1><<<(unsigned)blocks, 256, 0, s>>>(p);
     else if (cpl <= 2) k_gather<2><<<(unsigned)blocks, 256, 0, s>>>(p);
     else if (cpl <= 4) k_gather<4><<<(unsigned)blocks, 256, 0, s>>>(p);
+    else if (cpl <= 6) k_gather<6><<<(unsigned)blocks, 256, 0, s>>>(p);
     else if (cpl <= 8) k_gather<8><<<(unsigned)blocks, 256, 0, s>>>(p);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
