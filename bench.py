@@ -42,15 +42,15 @@ UNIT = "rays/s"
 KERNEL_SOURCES = ["hrt_trace.cuh", "hrt_trace_w4.cuh", "hrt_device.cuh", "hrt_internal.h", "hrt_ps_w4.cu",
                   "hrt_ps_accumulate.cu", "hrt_bvh4.cu", "hrt_bvh.cu"]
 PROFILE = {
-    "sources": "aae51a4c404f",
+    "sources": "b95fea6c6a52",
     "kernel": "k_diffuse_w4<4,0,0,4,16,256,1,0,1> (lean4-s16; lean4-s32 is within 1 %)",
-    "traffic_per_launch": 2.428e9,   # 2.374 GB read + 0.054 GB written, mean of 3 launches at 1 M
+    "traffic_per_launch": 2.425e9,   # 2.371 GB read + 0.054 GB written, mean of 3 launches at 1 M
     "issue_active_pct": 83.5,
-    "l1_hit_pct": 51.9,   # sector hit rate of 32-byte node loads (no second 16-byte load per sector)
+    "l1_hit_pct": 51.4,   # sector hit rate of 32-byte node loads (no second 16-byte load per sector)
     "l2_hit_pct": 92.9,
-    "warps_active_pct": 49.7,
+    "warps_active_pct": 49.8,
     "local_requests_per_ray": 0.232,  # (6.42 M + 4.02 M) / 45 M rays
-    "top_stall": "not_selected 2.28, wait 2.11, long_scoreboard 1.65 per issued instruction",
+    "top_stall": "not_selected 2.27, wait 2.11, long_scoreboard 1.65 per issued instruction",
 }
 ACC_DIRECT_RAYS, ACC_DIFFUSE_RAYS = 4, 9  # the accuracy leg's reduced ray counts
 # diffuse-trace variants by the tuner's names (hrt_set_tuning(16 + v) forces one)
