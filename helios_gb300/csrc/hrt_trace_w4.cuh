@@ -5,12 +5,17 @@
 // DRAM.  More resident warps hide more of that latency, so this kernel keeps only the state
 // of the node loop in registers -- the ray origin premultiplied by the inverse direction
 // (ooi), the inverse direction, best distance, current node, two postponed leaves, stack
-// pointer and visit budget -- and moves the rest of each lane's state to shared memory, where it is
-// touched only when a ray starts, reaches a leaf or ends: the origin, the direction and the
-// watertight-test set-up (kx, ky, kz, Sx, Sy, Sz), the best hit so far, the origin primitive
-// and face, the wrap count, the running-sum key and sums.  A node visit computes each slab
-// offset in one fused multiply-add from ooi (node4_offset_ooi) and reads the node in two
-// 256-bit loads.
+// pointer and visit budget -- and moves the rest of each lane's state to shared memory, where
+// it is touched only when a ray starts, reaches a leaf or ends: the origin, the direction and
+// the watertight-test set-up (kx, ky, kz, Sx, Sy, Sz), the best hit so far, the origin
+// primitive and face, the wrap count, the running-sum key and sums.
+// A node visit is kept short because the kernel is issue-bound: two 256-bit node loads, each
+// slab offset in one fused multiply-add from ooi (node4_offset_ooi), the nearest hit child
+// found by a three-comparator tournament (node4_nearest) and entered, the other hit children
+// pushed without a branch between the hit and no-hit cases, pops with no empty-stack test (a
+// sentinel at the bottom of the stack), leaves postponed two per lane, and the loop left only
+// when fewer than P.refill lanes remain; ray ids are split into face, primitive, ray and
+// stratum by multiplication (FastDiv).
 // The traversal stack keeps SD entries per lane in shared memory (indexed [entry][lane], so
 // the 32 lanes of a warp always hit 32 different banks) over a local overflow array, in one
 // of two layouts.  RingStack: the top SD entries in a ring, entries deeper than SD below the

@@ -28,3 +28,18 @@ def test_reference_arm_json_line():
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_counter_digest_ignores_comments(tmp_path):
+    """The ncu counters in the bench line are tied to a digest of the kernel code: a comment
+    edit keeps it, a code edit changes it."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    a, b, c = tmp_path / "a.cuh", tmp_path / "b.cuh", tmp_path / "c.cuh"
+    a.write_text("int f(int x) {\n    return x + 1;  // one\n}\n")
+    b.write_text("// header\nint f(int x) {\n\n    /* the sum */ return x + 1;   // plus one\n}\n")
+    c.write_text("int f(int x) {\n    return x + 2;\n}\n")
+    assert bench.code_digest([a]) == bench.code_digest([b])
+    assert bench.code_digest([a]) != bench.code_digest([c])
+    assert len(bench.kernel_sources_digest()) == 12
