@@ -10,8 +10,9 @@ passes) over the resident scene.
 
 Arms:
   (default)          libhrt on cuda:0; `value` = device-resident rays/s, `e2e` =
-                     rays/s through the C ABI with host buffers (geometry upload,
-                     BVH build, material upload, solve, flux download every step).
+                     rays/s through the C ABI with pinned host buffers (geometry
+                     upload, BVH build, material upload, solve, flux download every
+                     step).
   --impl reference   the reference algorithm on the host cores (the CPU oracle,
                      OpenMP, all threads) on a bounded sample of the same workload.
 """
@@ -490,19 +491,31 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
     ms = float(ms_t.item())
-    # end to end through the C ABI with host buffers
-    T, ty, ts = rad.geometry_arrays()
+    # end to end through the C ABI with host buffers in pinned memory: every step uploads the
+    # geometry and the materials, builds the trees, solves and reads the fluxes back
+    keep = []
+
+    def pinned(a):
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+        keep.append(t)
+        v = t.numpy().view(a.dtype).reshape(a.shape)
+        v[...] = a
+        return v
+
+    T, ty, ts = (pinned(np.ascontiguousarray(a)) for a in rad.geometry_arrays())
     full = dict(desc)
-    h2d = T.nbytes + ty.nbytes + ts.nbytes + desc["rho"].nbytes + desc["tau"].nbytes + desc["eps"].nbytes + \
-        desc["temperature"].nbytes
-    d2h = sc.n * len(BANDS) * 4
+    for k in ("rho", "tau", "eps", "temperature"):
+        full[k] = pinned(np.ascontiguousarray(desc[k]))
+    h2d = T.nbytes + ty.nbytes + ts.nbytes + sum(full[k].nbytes for k in ("rho", "tau", "eps", "temperature"))
+    flux_out = pinned(np.zeros((sc.n, len(BANDS)), np.float32))
+    d2h = flux_out.nbytes
     e2e_steps = max(1, min(args.steps, 3))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         ctx.update_geometry(T, ty, ts)
         ctx.build_accel()
-        flux = ctx.run_band(full, out=True)
+        flux = ctx.run_band(full, out=True, flux_out=flux_out)
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     batched = None

@@ -606,11 +606,21 @@ class Context:
         self.check(self.lib.hrt_get_camera_results(self.h, ptr(pix), ptr(lab), ptr(dep), int(width), int(height)))
         return pix, lab, dep
 
-    def run_band(self, solve: dict, out: bool = True):
+    def run_band(self, solve: dict, out: bool = True, flux_out=None):
+        """Device-resident runBand; returns the [n, launched bands] FP32 flux (out=True), written
+        into flux_out when given (a C-contiguous float32 array of that shape, e.g. pinned)."""
         self.update_glass(solve.get("is_glass"), solve.get("glass_n"), solve.get("glass_kl"))
         s, keep = self.band_solve(solve)
         bl = int(np.count_nonzero(np.asarray(solve["band_launch"])))
-        flux = np.zeros((self.n, bl), np.float32) if out else None
+        flux = None
+        if out:
+            if flux_out is not None:
+                if (flux_out.shape != (self.n, bl) or flux_out.dtype != np.float32
+                        or not flux_out.flags["C_CONTIGUOUS"]):
+                    raise ValueError(f"flux_out must be C-contiguous float32 of shape {(self.n, bl)}")
+                flux = flux_out
+            else:
+                flux = np.zeros((self.n, bl), np.float32)
         self.check(self.lib.hrt_run_band(self.h, C.byref(s), ptr(flux)))
         return flux
 
