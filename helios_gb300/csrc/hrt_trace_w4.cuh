@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_diffuse_w4(const DiffuseParams 
         if (__all_sync(0xffffffffu, exhausted && !live)) break;
         if (!live) continue;
 
-        // ---- internal nodes; leaves are postponed until every active lane has one
+        // ---- internal nodes; up to two leaves per lane are postponed to the primitive tests below
         const TraceScene &sc = SC;
         const uint32_t n4 = (uint32_t)sc.n4;
         // cur is an internal node: 0 <= cur < kSentinel in one unsigned compare (leaves are
