@@ -216,9 +216,10 @@ __device__ Hit trace_bvh(const TraceScene &sc, f3 o, f3 d, float tmin, float tma
 }
 
 // Closest (or any) hit over the compressed 4-wide nodes (sc.nodes4).  Each visit tests the four
-// child boxes against the current best distance; leaf children are intersected at once, nearest
-// first; of the internal children the nearest is entered and the others pushed farthest first
-// (an any-hit trace orders only the nearest child of a node first).
+// child boxes against the current best distance and orders them (sorted nearest first, or for an
+// any-hit trace only the nearest moved first); leaf children are intersected at once; of the
+// internal children the first in that order is entered and the others are pushed, the next in
+// order on top.
 // The closest hit (ties to the smaller original index) is the binary trace's; an any-hit trace
 // may report another occluder.
 template <bool STATS>
